@@ -1,0 +1,370 @@
+"""Benchmark: Richardson-Lucy light-field deconvolution volumes/s on one GB300.
+
+Workload (default "fullfield"): Nnum 15, 67 x 67 lenslets (1005 x 1005 px),
+41 z planes at -100..+100 um (step 5), one frame; synthetic seeded inputs
+(2000 Gaussian beads + 50 random-walk filaments, forward projected, +100
+background, Poisson noise) and a synthetic PSF set with the shapes of that
+optical configuration.  One step = one deconvolved volume at the accuracy of
+8 plain-RL iterations: back projection Htf of the image, a uniform start
+volume, 8 Prevedel RL iterations (the reference's default update).
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the reference's
+CPU algorithm (the oracle port, numpy/scipy on all host cores) on bounded
+samples of the same workload instead.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fast-light-field_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "volumes/s to plain-RL(8 it) accuracy: learned warm-start vs plain RL, 1 GB300"
+UNIT = "volumes/s"
+
+WORKLOADS = {
+    # name: (Nnum, lenslets, z_min, z_max, z_step, psf size ref (lenslets at z_max), beads, filaments)
+    "fullfield": dict(Nnum=15, lenslets=67, z=(-100, 100, 5), img_size_ref=28, beads=2000, filaments=50,
+                      label="full-field 1005x1005 px, Nnum 15, 41 planes -100..100 um, plain RL"),
+    "small": dict(Nnum=15, lenslets=30, z=(-25, 25, 5), img_size_ref=7, beads=200, filaments=0,
+                  label="450x450 px, Nnum 15, 11 planes -25..25 um, plain RL"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="fullfield", choices=sorted(WORKLOADS))
+    ap.add_argument("--iters", type=int, default=8)
+    ap.add_argument("--frames", type=int, default=1)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-planes", type=int, default=2)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_problem(wl, seed=1234):
+    import psfmatrix
+    import synthetic
+    N = wl["Nnum"]
+    z0, z1, dz = wl["z"]
+    z = np.arange(z0, z1 + dz / 2, dz)
+    H, Ht = synthetic.synthetic_psf(N, z, wl["img_size_ref"])
+    hm = psfmatrix.HMatrixArrays(H, Ht, name="bench-%s" % wl["label"])
+    Y = X = wl["lenslets"] * N
+    gt, _ = synthetic.bead_volume((len(z), Y, X), wl["beads"], seed=seed, sigma=1.0,
+                                  amp_range=(500.0, 1000.0))
+    if wl["filaments"]:
+        gt = gt + synthetic.filament_volume((len(z), Y, X), wl["filaments"], seed=seed + 1, width=1.5,
+                                            intensity=500.0)
+    return hm, H, Ht, z, gt.astype(np.float32), Y, X
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(hm, H, Ht, z, Y, X, N, iters, nplanes_sample, cores):
+    """Reference CPU algorithm (oracle port) on a bounded sample, extrapolated to one volume."""
+    from oracle import lf_oracle as O
+    rng = np.random.default_rng(7)
+    img = rng.random((1, Y, X)).astype(np.float32)
+    Z = len(z)
+    # sample planes spanning the PSF sizes: largest and smallest support
+    hs = np.array([h.shape[-1] for h in Ht])
+    order = np.argsort(hs)
+    picks = sorted(set([int(order[-1]), int(order[0])] + [int(order[len(order) // 2])][: max(0, nplanes_sample - 2)]))
+    times = {}
+    t_all = time.time()
+    for zi in picks:
+        t0 = time.time()
+        O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
+        times[zi] = time.time() - t0
+    sample_s = time.time() - t_all
+    # cost per plane ~ F_z * RX_z (the spectral multiply-accumulate and FFT sizes)
+
+    def cost(zi):
+        (FY, FX), _ = O.convolution_shape((Y, X), (hs[zi], hs[zi]), N, True)
+        return FY * (FX // 2 + 1)
+
+    xs = np.array([cost(p) for p in picks], dtype=np.float64)
+    ys = np.array([times[p] for p in picks])
+    if len(picks) >= 2 and xs.max() > xs.min():
+        a, b = np.polyfit(xs, ys, 1)
+    else:
+        a, b = ys[0] / xs[0], 0.0
+    per_projection = float(sum(max(a * cost(zi) + b, 0.0) for zi in range(Z)))
+    projections = 1 + 2 * iters
+    vol_s = per_projection * projections
+    return {
+        "value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": "port",
+        "sample": "back projection of planes %s (PSF sizes %s) of the workload on %d threads in %.1f s; "
+                  "one volume = %d projections x %d planes, extrapolated linearly in the per-plane "
+                  "spectrum size" % (picks, [int(hs[p]) for p in picks], cores, sample_s, projections, Z),
+        "seconds_per_volume": vol_s,
+    }
+
+
+def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
+    """Each step back-projects one sample plane (cycling largest / smallest / middle PSF);
+    the timed samples fit the per-plane cost model that extrapolates one volume."""
+    from oracle import lf_oracle as O
+    rng = np.random.default_rng(7)
+    img = rng.random((1, Y, X)).astype(np.float32)
+    hs = np.array([h.shape[-1] for h in Ht])
+    order = np.argsort(hs)
+    cycle = [int(order[-1]), int(order[0]), int(order[len(order) // 2])]
+
+    def cost(zi):
+        (FY, FX), _ = O.convolution_shape((Y, X), (hs[zi], hs[zi]), N, True)
+        return FY * (FX // 2 + 1)
+
+    xs, ys = [], []
+    t_all = time.time()
+    for i in range(warmup + steps):
+        zi = cycle[i % len(cycle)]
+        t0 = time.time()
+        O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
+        dt = time.time() - t0
+        if i >= warmup:
+            xs.append(cost(zi))
+            ys.append(dt)
+    xs, ys = np.array(xs, float), np.array(ys, float)
+    if len(set(xs)) >= 2:
+        a, b = np.polyfit(xs, ys, 1)
+    else:
+        a, b = float(np.mean(ys / xs)), 0.0
+    per_projection = float(sum(max(a * cost(zi) + b, 0.0) for zi in range(len(z))))
+    vol_s = per_projection * (1 + 2 * iters)
+    return {"value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d timed single-plane back projections (PSF sizes %s) on %d threads, %.1f s total; "
+                      "one volume = %d projections x %d planes, extrapolated linearly in the per-plane "
+                      "spectrum size" % (steps, sorted(set(int(hs[c]) for c in cycle)), cores,
+                                         time.time() - t_all, 1 + 2 * iters, len(z)),
+            "seconds_per_volume": vol_s}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    N = wl["Nnum"]
+    hm, H, Ht, z, gt, Y, X = build_problem(wl)
+    cores = os.cpu_count() or 1
+    cb = reference_steps(Ht, z, Y, X, N, args.iters, cores, args.warmup, args.steps)
+    v = cb["value"]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl["label"], "rl_iterations": args.iters, "frames": 1,
+                       "implementation": "reference CPU algorithm, numpy/scipy port (oracle)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world, local):
+    import torch
+    import lfdeconv
+    import projector
+    import _flf
+    import build_lib
+    build_lib.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    wl = WORKLOADS[args.workload]
+    N = wl["Nnum"]
+    T = args.frames
+    t_setup = time.time()
+    hm, H, Ht, z, gt, Y, X = build_problem(wl, seed=1234 + rank)
+    Z = len(z)
+    p = projector.Projector_gb300(device=local)
+    p.storeVolumesOnGPU = True
+    gt_d = torch.as_tensor(gt[:, None], device=dev).repeat(1, T, 1, 1).contiguous()
+    clean = p.ForwardProjectACC(hm, gt_d, None)
+    gen = torch.Generator(device="cpu").manual_seed(99 + rank)
+    img_h = torch.poisson((clean.cpu().double() + 100.0).clamp_min(0), generator=gen).float().numpy()
+    ctx = p.context(hm)
+    geo = ctx.geometry()
+    setup_s = time.time() - t_setup
+    stream = torch.cuda.current_stream(dev)
+    img_d = torch.as_tensor(img_h, device=dev)
+    htf = torch.empty((Z, T, Y, X), dtype=torch.float32, device=dev)
+    x = torch.empty((Z, T, Y, X), dtype=torch.float32, device=dev)
+
+    def step():
+        ctx.backward(img_d, htf, T, Y, X, None, stream=stream.cuda_stream)
+        x.fill_(1.0)
+        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ctx.profile(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * T / (ms / 1000.0)
+
+    # end to end through the public API: host image and start volume in, host volume out
+    e2e = None
+    if not args.no_e2e:
+        p.storeVolumesOnGPU = False
+        x0_h = np.ones((Z, T, Y, X), np.float32)
+        r = lfdeconv.DeconvRL(hm, None, args.iters, x0_h, logPrint=False, projector=p, im=img_h)
+        torch.cuda.synchronize()
+        ne = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            r = lfdeconv.DeconvRL(hm, None, args.iters, x0_h, logPrint=False, projector=p, im=img_h)
+        e2e_s = (time.perf_counter() - t0) / ne
+        e2e = {"value": world * T / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(img_h.nbytes + x0_h.nbytes),
+               "d2h_bytes_per_step": int(r.nbytes), "ms_per_step": e2e_s * 1000.0}
+
+    # roofline of the dominant kernel (the spectral multiply-accumulate)
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    mac = {k: v for k, v in prof.items() if k.startswith("k_mac")}
+    tot_ms = sum(v["ms"] for v in mac.values())
+    tot_bytes = sum(v["bytes"] for v in mac.values())
+    n_mac = sum(v["launches"] for v in mac.values())
+    achieved = tot_bytes / (tot_ms / 1000.0) / 1e9 if tot_ms > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_mac_fwd+k_mac_bwd",
+            "peak_source": peak_kind, "launches": n_mac,
+            "bytes_per_launch": tot_bytes / max(n_mac, 1), "avg_launch_ms": tot_ms / max(n_mac, 1),
+            "kernel_share": {k: round(v["ms"] / sum(w["ms"] for w in prof.values()), 4) for k, v in prof.items()}}
+    launches = sum(v["launches"] for v in prof.values()) // args.steps
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(hm, H, Ht, z, Y, X, N, args.iters, args.cpu_sample_planes, os.cpu_count() or 1)
+
+    if rank == 0:
+        gb = ctx.memory_usage() / 1e9
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "frames": T,
+                           "rl_iterations": args.iters, "rl_variant": "prevedel", "start": "uniform",
+                           "projections_per_step": 1 + 2 * args.iters,
+                           "transform_size": geo["f"], "kernel_radius_lenslets": geo["R"],
+                           "precompute_fp64": geo["fp64"], "device_gb": round(gb, 2),
+                           "setup_s": round(setup_s, 1),
+                           "l2": "inputs larger than L2: %.1f GB of transfer matrices streamed per "
+                                 "projection pair, %.0f MB volume" % (tot_bytes / max(n_mac, 1) * 2 / 1e9,
+                                                                     Z * T * Y * X * 4 / 1e6),
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cb,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,187 @@
+"""ctypes binding of libflf.so (C ABI in include/flf.h).
+
+The GB300 counterpart of the reference's compiled extension ``py_light_field``
+(imported as ``plf`` by projector.py / lfdeconv.py).  There is no CPU fallback:
+importing works without a GPU, but creating a context raises ``FlfError`` when
+the library or a CUDA device is missing.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libflf.so")
+
+FLF_OK = 0
+FLF_DIR_FORWARD = 0
+FLF_DIR_BACKWARD = 1
+FLF_RL_PREVEDEL = 0
+FLF_RL_STANDARD = 1
+
+_ERRNAMES = {-1: "FLF_E_ARG", -2: "FLF_E_CUDA", -3: "FLF_E_NOMEM", -4: "FLF_E_STATE", -5: "FLF_E_TIMEOUT"}
+
+# name -> (restype, argtypes); mirrors include/flf.h
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_SIGS = {
+    "flf_ctx_create": (_I, [ctypes.POINTER(_P), _I, _I, _I]),
+    "flf_ctx_destroy": (_I, [_P]),
+    "flf_last_error": (_I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "flf_psf_upload": (_I, [_P, _I, _I, _P, _I, _I]),
+    "flf_prepare": (_I, [_P, _I, _I, _I, _I]),
+    "flf_forward": (_I, [_P, _P, _P, _I, _I, _I, _P, _I, _P]),
+    "flf_backward": (_I, [_P, _P, _P, _I, _I, _I, _P, _I, _P]),
+    "flf_rl_iterate": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_memory_usage": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "flf_clear_cache": (_I, [_P]),
+    "flf_geometry": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "flf_version": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
+    "flf_profile": (_I, [_P, _I]),
+    "flf_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+}
+
+_lib = None
+
+
+class FlfError(RuntimeError):
+    """Failure reported by libflf (status code and message)."""
+
+    def __init__(self, code, message):
+        super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "FLF_E?"), code, message))
+        self.code = code
+
+
+def load_library(path=LIB_PATH):
+    """Load libflf.so and declare every entry point of include/flf.h."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FlfError(-4, "libflf.so not found at %s: run __graft_entry__.build() or "
+                           "python fast-light-field_gb300/build_lib.py" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def version():
+    lib = load_library()
+    buf = ctypes.create_string_buffer(256)
+    lib.flf_version(buf, 256)
+    return buf.value.decode()
+
+
+def _ptr(x):
+    """Raw pointer of a torch tensor / numpy array / int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError("cannot take a pointer of %r" % type(x))
+
+
+class Context:
+    """One libflf context: PSFs of one Nnum / plane count on one device."""
+
+    def __init__(self, nnum, num_planes, device=0):
+        self._lib = load_library()
+        self._h = _P()
+        rc = self._lib.flf_ctx_create(ctypes.byref(self._h), int(device), int(nnum), int(num_planes))
+        if rc != FLF_OK:
+            raise FlfError(rc, self._msg(None))
+        self.nnum = int(nnum)
+        self.num_planes = int(num_planes)
+        self.device = int(device)
+
+    def _msg(self, h):
+        buf = ctypes.create_string_buffer(1024)
+        self._lib.flf_last_error(h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc):
+        if rc != FLF_OK:
+            raise FlfError(rc, self._msg(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.flf_ctx_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_psf(self, plane, direction, H):
+        H = np.ascontiguousarray(H, dtype=np.float32)
+        if H.ndim != 4 or H.shape[2] != H.shape[3]:
+            raise ValueError("PSF array must be [n_h, n_h, h, h], got %s" % (H.shape,))
+        self._check(self._lib.flf_psf_upload(self._h, int(plane), int(direction), H.ctypes.data,
+                                             int(H.shape[0]), int(H.shape[2])))
+
+    def prepare(self, Y, X, fft_size=0, fp64=False):
+        self._check(self._lib.flf_prepare(self._h, int(Y), int(X), int(fft_size), int(bool(fp64))))
+
+    @staticmethod
+    def _planes_arg(planes, nz):
+        if planes is None:
+            return None, nz, None
+        arr = np.ascontiguousarray(np.asarray(list(planes), dtype=np.int32))
+        return arr.ctypes.data, int(arr.size), arr
+
+    def forward(self, vol, img, T, Y, X, planes=None, stream=None):
+        p, n, keep = self._planes_arg(planes, self.num_planes)
+        self._check(self._lib.flf_forward(self._h, _ptr(vol), _ptr(img), int(T), int(Y), int(X),
+                                          p, n, _ptr(stream)))
+        del keep
+
+    def backward(self, img, vol, T, Y, X, planes=None, stream=None):
+        p, n, keep = self._planes_arg(planes, self.num_planes)
+        self._check(self._lib.flf_backward(self._h, _ptr(img), _ptr(vol), int(T), int(Y), int(X),
+                                           p, n, _ptr(stream)))
+        del keep
+
+    def rl_iterate(self, x, ref, norm, variant, iters, T, Y, X, stream=None):
+        self._check(self._lib.flf_rl_iterate(self._h, _ptr(x), _ptr(ref), _ptr(norm), int(variant),
+                                             int(iters), int(T), int(Y), int(X), _ptr(stream)))
+
+    def memory_usage(self):
+        v = ctypes.c_size_t(0)
+        self._check(self._lib.flf_memory_usage(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def clear_cache(self):
+        self._check(self._lib.flf_clear_cache(self._h))
+
+    def profile(self, enable):
+        self._check(self._lib.flf_profile(self._h, int(bool(enable))))
+
+    def profile_read(self):
+        """{kernel: {"launches", "ms", "bytes"}} since the last profile() call."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._lib.flf_profile_read(self._h, buf, 1 << 16))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms, b = line.split()
+            out[name] = {"launches": int(n), "ms": float(ms), "bytes": float(b)}
+        return out
+
+    def geometry(self):
+        out = (ctypes.c_int * 4)()
+        self._check(self._lib.flf_geometry(self._h, out))
+        return {"f": out[0], "R": out[1], "fp64": bool(out[2]), "freq_pairs": out[3]}

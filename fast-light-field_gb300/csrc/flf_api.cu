@@ -1,0 +1,788 @@
+// C ABI of libflf.so (declared in include/flf.h): context, PSF upload,
+// transfer-matrix precompute, and the forward / back projection and
+// Richardson-Lucy sequences built from the kernels in flf_kernels.cu.
+#include "flf_internal.cuh"
+#include "../../include/flf.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+using namespace flf;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct Workspace {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Geometry {
+  bool valid = false;
+  int Y = 0, X = 0, Ly = 0, Lx = 0, f = 0, fh = 0, fq = 0, nkp = 0, R = 0, fp64 = 0;
+  FftPlan plan{};
+  float2 *tw = nullptr;       // float twiddles [f]
+  double2 *tw64 = nullptr;    // double twiddles [f]
+  float2 *P[2] = {nullptr, nullptr};
+  bool built[2] = {false, false};
+};
+
+}  // namespace
+
+struct flf_ctx {
+  int device = 0, N = 0, nz = 0;
+  Layout L{};
+  std::vector<float *> dH[2];
+  std::vector<int> h[2];
+  Geometry geo;
+  // index tables (device)
+  short4 *d_rowS = nullptr;
+  short *d_slotcol = nullptr, *d_colslot = nullptr;
+  int *d_rep_ch = nullptr, *d_rep_row = nullptr, *d_rep_kind = nullptr;
+  int *d_planes_all = nullptr;
+  int *d_planes_user = nullptr;
+  int planes_user_cap = 0;
+  int *d_zero = nullptr;
+  std::vector<int> rep_ch, rep_row, rep_kind;
+  Workspace wsS, wsO, wsImg;
+  int num_sms = 0;
+  int req_f = 0, req_fp64 = 0;   // transform size / precision asked for by flf_prepare
+  // per-kernel launch statistics; event timing when profiling is on
+  struct KStat { long long launches = 0; double ms = 0, bytes = 0; };
+  struct Pending { std::string name; cudaEvent_t a, b; };
+  std::map<std::string, KStat> kstats;
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> evpool;
+  bool profiling = false;
+  std::string err;
+};
+
+namespace {
+
+int fail(flf_ctx *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                   \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(ctx, FLF_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),   \
+                  __FILE__, __LINE__);                                                        \
+  } while (0)
+
+cudaEvent_t get_event(flf_ctx *ctx) {
+  if (!ctx->evpool.empty()) {
+    cudaEvent_t e = ctx->evpool.back();
+    ctx->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void resolve_pending(flf_ctx *ctx) {
+  for (auto &p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+      ctx->kstats[p.name].ms += ms;
+    ctx->evpool.push_back(p.a);
+    ctx->evpool.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
+
+// Launches `fn` (returning cudaError_t), counts it under `name` with its
+// algorithmic bytes, and brackets it with events on `s` when profiling.
+template <typename F>
+int counted_launch(flf_ctx *ctx, const char *name, double bytes, cudaStream_t s, F &&fn) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->profiling) {
+    if (ctx->pending.size() > 8192) resolve_pending(ctx);
+    a = get_event(ctx);
+    b = get_event(ctx);
+    cudaEventRecord(a, s);
+  }
+  cudaError_t e = fn();
+  if (e != cudaSuccess)
+    return fail(ctx, FLF_E_CUDA, "launch of %s failed: %s", name, cudaGetErrorString(e));
+  if (ctx->profiling) {
+    cudaEventRecord(b, s);
+    ctx->pending.push_back({name, a, b});
+  }
+  auto &k = ctx->kstats[name];
+  k.launches++;
+  k.bytes += bytes;
+  return FLF_OK;
+}
+
+#define LAUNCH(ctx, name, bytes, s, expr)                                  \
+  do {                                                                     \
+    int rc_ = counted_launch(ctx, name, (double)(bytes), s, [&]() { return (expr); }); \
+    if (rc_ != FLF_OK) return rc_;                                         \
+  } while (0)
+
+bool is_smooth_even(int n) {
+  if (n < 2 || (n & 1)) return false;
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+FftPlan make_plan(int n) {
+  FftPlan pl{};
+  pl.n = n;
+  int m = n, k = 0;
+  while (m % 4 == 0) { pl.rad[k++] = 4; m /= 4; }
+  while (m % 2 == 0) { pl.rad[k++] = 2; m /= 2; }
+  for (int p : {3, 5, 7})
+    while (m % p == 0) { pl.rad[k++] = p; m /= p; }
+  pl.nst = k;
+  return pl;
+}
+
+int ensure_ws(flf_ctx *ctx, Workspace &w, size_t bytes) {
+  if (w.bytes >= bytes) return FLF_OK;
+  if (w.p) cudaFree(w.p);
+  w.p = nullptr;
+  w.bytes = 0;
+  cudaError_t e = cudaMalloc(&w.p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, FLF_E_NOMEM, "cudaMalloc(%zu bytes) for workspace failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  w.bytes = bytes;
+  return FLF_OK;
+}
+
+void free_geometry(Geometry &g) {
+  if (g.tw) cudaFree(g.tw);
+  if (g.tw64) cudaFree(g.tw64);
+  for (int d = 0; d < 2; d++)
+    if (g.P[d]) cudaFree(g.P[d]);
+  g = Geometry();
+}
+
+// Host-side index tables of the packed layout (see flf_internal.cuh).
+int build_tables(flf_ctx *ctx) {
+  const int N = ctx->N, NN = N * N, c = N / 2;
+  const Layout &L = ctx->L;
+  auto My = [&](int i) { return (N - 1 - i / N) * N + i % N; };
+  auto Mx = [&](int i) { return (i / N) * N + (N - 1 - i % N); };
+  auto Mxy = [&](int i) { return NN - 1 - i; };
+  std::vector<short> slotcol;
+  for (int be = 0; be < c; be++)
+    for (int al = 0; al < c; al++) {
+      int q = be * N + al;
+      slotcol.push_back(q); slotcol.push_back(My(q)); slotcol.push_back(Mx(q)); slotcol.push_back(Mxy(q));
+    }
+  for (int be = 0; be < c; be++) { int q = be * N + c; slotcol.push_back(q); slotcol.push_back(My(q)); }
+  for (int al = 0; al < c; al++) { int q = c * N + al; slotcol.push_back(q); slotcol.push_back(Mx(q)); }
+  slotcol.push_back(c * N + c);
+  if ((int)slotcol.size() != NN) return fail(ctx, FLF_E_STATE, "internal: slot table size");
+  std::vector<short> colslot(NN, -1);
+  for (int s = 0; s < NN; s++) colslot[slotcol[s]] = s;
+
+  std::vector<short4> rowS;
+  ctx->rep_ch.clear(); ctx->rep_row.clear(); ctx->rep_kind.clear();
+  int row = 0;
+  for (int b = 0; b < c; b++)
+    for (int a = 0; a < N; a++) {
+      if (a == c) continue;
+      int i = b * N + a;
+      rowS.push_back(make_short4(i, Mxy(i), NN + My(i), NN + Mx(i)));
+      ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row++); ctx->rep_kind.push_back(0);
+    }
+  for (int k = 0; k < L.nrep; k++) {
+    int i, kind;
+    if (k < c) { i = k * N + c; kind = 1; }
+    else if (k < 2 * c) { i = c * N + (k - c); kind = 2; }
+    else { i = c * N + c; kind = 3; }
+    short4 s;
+    if (kind == 1) s = make_short4(i, NN + i, NN + My(i), My(i));
+    else if (kind == 2) s = make_short4(i, NN + i, NN + Mx(i), Mx(i));
+    else s = make_short4(i, NN + i, 0, 0);
+    rowS.push_back(s);
+    ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row); ctx->rep_kind.push_back(kind);
+    row += 2;
+  }
+  if (row != L.nrow) return fail(ctx, FLF_E_STATE, "internal: row table size");
+  const int nrepAll = (int)ctx->rep_ch.size();
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_rowS, sizeof(short4) * rowS.size()));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_rowS, rowS.data(), sizeof(short4) * rowS.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_slotcol, sizeof(short) * NN));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_slotcol, slotcol.data(), sizeof(short) * NN, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_colslot, sizeof(short) * NN));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_colslot, colslot.data(), sizeof(short) * NN, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_rep_ch, sizeof(int) * nrepAll));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_rep_ch, ctx->rep_ch.data(), sizeof(int) * nrepAll, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_rep_row, sizeof(int) * nrepAll));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_rep_row, ctx->rep_row.data(), sizeof(int) * nrepAll, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_rep_kind, sizeof(int) * nrepAll));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_rep_kind, ctx->rep_kind.data(), sizeof(int) * nrepAll, cudaMemcpyHostToDevice));
+  std::vector<int> all(ctx->nz);
+  for (int z = 0; z < ctx->nz; z++) all[z] = z;
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_planes_all, sizeof(int) * std::max(1, ctx->nz)));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_planes_all, all.data(), sizeof(int) * ctx->nz, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_zero, sizeof(int)));
+  CUDA_TRY(ctx, cudaMemset(ctx->d_zero, 0, sizeof(int)));
+  return FLF_OK;
+}
+
+int kernel_radius(const flf_ctx *ctx, int hh) { return ((hh - 1) / 2 + ctx->N - 1) / ctx->N; }
+
+int imgs_per_cta(int f, int fp64, size_t budget) {
+  int b = 1;
+  while (b < 16 && rfft2_smem_bytes(f, b + 1, fp64) <= budget) b++;
+  return b;
+}
+
+// Transfer matrices of one direction for all uploaded planes.
+int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
+  Geometry &G = ctx->geo;
+  const Layout &L = ctx->L;
+  const int NN = L.NN, f = G.f, fh = G.fh;
+  for (int z = 0; z < ctx->nz; z++)
+    if (!ctx->dH[dir][z])
+      return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, dir);
+  const size_t plane_elems = (size_t)G.nkp * L.nrow * L.RS;
+  const size_t bytes = plane_elems * ctx->nz * sizeof(float2);
+  if (!G.P[dir]) {
+    cudaError_t e = cudaMalloc(&G.P[dir], bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, FLF_E_NOMEM,
+                  "cudaMalloc(%zu bytes) for the transfer matrices of direction %d failed: %s",
+                  bytes, dir, cudaGetErrorString(e));
+    }
+  }
+  CUDA_TRY(ctx, cudaMemsetAsync(G.P[dir], 0, bytes, s));
+  const int fp64 = G.fp64;
+  const size_t rsz = fp64 ? sizeof(double) : sizeof(float);
+  const size_t per_rep = (size_t)NN * ((size_t)f * f * rsz + (size_t)f * fh * 2 * rsz);
+  const int nrepAll = (int)ctx->rep_ch.size();
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>(nrepAll, (size_t)(512u << 20) / per_rep));
+  Workspace wk, wspec;
+  int rc = ensure_ws(ctx, wk, (size_t)chunk * NN * f * f * rsz);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, wspec, (size_t)chunk * NN * f * fh * 2 * rsz);
+  if (rc != FLF_OK) {
+    if (wk.p) cudaFree(wk.p);
+    if (wspec.p) cudaFree(wspec.p);
+    return rc;
+  }
+  const int ipc = imgs_per_cta(f, fp64, 200 * 1024);
+  for (int z = 0; z < ctx->nz && rc == FLF_OK; z++) {
+    const int hh = ctx->h[dir][z];
+    for (int r0 = 0; r0 < nrepAll && rc == FLF_OK; r0 += chunk) {
+      const int nr = std::min(chunk, nrepAll - r0);
+      BuildKParams bk{};
+      bk.N = ctx->N; bk.h = hh; bk.ch = (hh - 1) / 2; bk.R = kernel_radius(ctx, hh); bk.f = f;
+      bk.H = ctx->dH[dir][z]; bk.rep_ch = ctx->d_rep_ch; bk.rep0 = r0; bk.nrep_chunk = nr;
+      bk.dst = wk.p; bk.fp64 = fp64;
+      cudaError_t e = launch_build_k(bk, nr * NN, s);
+      if (e == cudaSuccess) {
+        Rfft2Params rp{};
+        rp.plan = G.plan; rp.N = ctx->N; rp.nimg = nr * NN; rp.mode = 1;
+        rp.src_img = wk.p; rp.dst = wspec.p;
+        rp.twiddle = fp64 ? (const void *)G.tw64 : (const void *)G.tw;
+        rp.imgs_per_cta = ipc; rp.nq_rows = f / 2;
+        e = launch_rfft2(rp, fp64, s);
+      }
+      if (e == cudaSuccess) {
+        PackParams pp{};
+        pp.L = L; pp.f = f; pp.fh = fh; pp.fq = G.fq; pp.nkp = G.nkp;
+        pp.spec = wspec.p; pp.rep0 = r0; pp.nrep_chunk = nr;
+        pp.rep_row = ctx->d_rep_row; pp.rep_kind = ctx->d_rep_kind; pp.rep_ch = ctx->d_rep_ch;
+        pp.col_slot = ctx->d_colslot;
+        pp.P = G.P[dir] + plane_elems * z;
+        pp.scale = 1.0 / ((double)f * (double)f);
+        pp.fp64 = fp64;
+        // pack writes rows of the chunk's representatives only
+        e = launch_pack(pp, s);
+      }
+      if (e != cudaSuccess)
+        rc = fail(ctx, FLF_E_CUDA, "precompute launch failed: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t es = cudaStreamSynchronize(s);
+  if (wk.p) cudaFree(wk.p);
+  if (wspec.p) cudaFree(wspec.p);
+  if (rc != FLF_OK) return rc;
+  if (es != cudaSuccess) return fail(ctx, FLF_E_CUDA, "precompute failed: %s", cudaGetErrorString(es));
+  G.built[dir] = true;
+  return FLF_OK;
+}
+
+int prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
+  if (Y <= 0 || X <= 0) return fail(ctx, FLF_E_ARG, "image shape must be positive (got %d x %d)", Y, X);
+  const int N = ctx->N;
+  const int Ly = (Y + N - 1) / N, Lx = (X + N - 1) / N;
+  int R = 0;
+  for (int d = 0; d < 2; d++)
+    for (int z = 0; z < ctx->nz; z++)
+      if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
+  int f;
+  if (fft_size > 0) {
+    f = fft_size;
+    if (!is_smooth_even(f))
+      return fail(ctx, FLF_E_ARG, "fft_size %d must be even with prime factors in {2,3,5,7}", f);
+    if (f < std::max(Ly, Lx) + R || f < 2 * R + 1)
+      return fail(ctx, FLF_E_ARG, "fft_size %d too small: need >= %d", f, std::max(std::max(Ly, Lx) + R, 2 * R + 1));
+  } else {
+    f = std::max(std::max(Ly, Lx) + R, 2 * R + 1);
+    while (!is_smooth_even(f)) f++;
+  }
+  if (f > kMaxF)
+    return fail(ctx, FLF_E_ARG, "lenslet-grid transform size %d exceeds the supported maximum %d "
+                "(image %d x %d, Nnum %d, kernel radius %d lenslets)", f, kMaxF, Y, X, N, R);
+  if (fp64 && f > kMaxF64) fp64 = 0;   // double buffers do not fit shared memory
+  Geometry &G = ctx->geo;
+  if (G.valid && G.f == f && G.Ly == Ly && G.Lx == Lx && G.R == R && G.fp64 == fp64) {
+    G.Y = Y; G.X = X;
+    return FLF_OK;
+  }
+  free_geometry(G);
+  G.Y = Y; G.X = X; G.Ly = Ly; G.Lx = Lx; G.R = R; G.f = f; G.fh = f / 2 + 1; G.fq = f / 2 + 1;
+  G.nkp = G.fq * G.fq; G.fp64 = fp64;
+  G.plan = make_plan(f);
+  std::vector<float2> tw(f);
+  std::vector<double2> tw64(f);
+  for (int k = 0; k < f; k++) {
+    // exp(-2 pi i k / f) in double, rounded once
+    const double ang = -2.0 * M_PI * (double)k / (double)f;
+    tw64[k] = make_double2(std::cos(ang), std::sin(ang));
+    tw[k] = make_float2((float)tw64[k].x, (float)tw64[k].y);
+  }
+  CUDA_TRY(ctx, cudaMalloc(&G.tw, sizeof(float2) * f));
+  CUDA_TRY(ctx, cudaMemcpy(G.tw, tw.data(), sizeof(float2) * f, cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&G.tw64, sizeof(double2) * f));
+  CUDA_TRY(ctx, cudaMemcpy(G.tw64, tw64.data(), sizeof(double2) * f, cudaMemcpyHostToDevice));
+  G.valid = true;
+  return FLF_OK;
+}
+
+int set_user_planes(flf_ctx *ctx, const int *planes, int nplanes, cudaStream_t s, const int **out) {
+  if (!planes) {
+    if (nplanes != ctx->nz) return fail(ctx, FLF_E_ARG, "planes == NULL requires nplanes == num_planes");
+    *out = ctx->d_planes_all;
+    return FLF_OK;
+  }
+  if (nplanes <= 0 || nplanes > ctx->nz) return fail(ctx, FLF_E_ARG, "nplanes %d out of range", nplanes);
+  std::vector<char> seen(ctx->nz, 0);
+  for (int i = 0; i < nplanes; i++) {
+    if (planes[i] < 0 || planes[i] >= ctx->nz)
+      return fail(ctx, FLF_E_ARG, "plane id %d out of range [0, %d)", planes[i], ctx->nz);
+    if (seen[planes[i]]) return fail(ctx, FLF_E_ARG, "plane id %d listed twice", planes[i]);
+    seen[planes[i]] = 1;
+  }
+  if (ctx->planes_user_cap < nplanes) {
+    if (ctx->d_planes_user) cudaFree(ctx->d_planes_user);
+    ctx->d_planes_user = nullptr;
+    CUDA_TRY(ctx, cudaMalloc(&ctx->d_planes_user, sizeof(int) * ctx->nz));
+    ctx->planes_user_cap = ctx->nz;
+  }
+  // the synchronous copy orders against earlier work on every stream
+  CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_planes_user, planes, sizeof(int) * nplanes, cudaMemcpyHostToDevice));
+  *out = ctx->d_planes_user;
+  return FLF_OK;
+}
+
+int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
+  if (!ctx) return FLF_E_ARG;
+  if (T <= 0) return fail(ctx, FLF_E_ARG, "frame count must be positive (got %d)", T);
+  int f_req = ctx->req_f;
+  if (f_req > 0) {
+    const int N = ctx->N, Ly = (Y + N - 1) / N, Lx = (X + N - 1) / N;
+    int R = 0;
+    for (int d = 0; d < 2; d++)
+      for (int z = 0; z < ctx->nz; z++)
+        if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
+    if (f_req < std::max(Ly, Lx) + R || f_req < 2 * R + 1) f_req = 0;   // not valid for this shape
+  }
+  int rc = prepare(ctx, Y, X, f_req, ctx->req_fp64);
+  if (rc != FLF_OK) return rc;
+  if (!ctx->geo.built[dir]) rc = build_direction(ctx, dir, s);
+  return rc;
+}
+
+int zgroup_for(const flf_ctx *ctx, int nz) {
+  const int target = 4 * std::max(1, ctx->num_sms);
+  const int nzg_needed = std::max(1, (target + ctx->geo.nkp - 1) / ctx->geo.nkp);
+  const int zg = (nz + nzg_needed - 1) / nzg_needed;
+  return std::max(1, zg);
+}
+
+int mac_groups(const Layout &L) {
+  int G = std::max(1, 512 / L.nthr);
+  G = std::min(G, std::max(1, L.nrowG));
+  return G;
+}
+
+// Forward projection of frames [t0, t0+nt) of vol into out (epilogue epi).
+int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const int *d_planes, int nplanes,
+                  int t0, int nt, Strided out, Strided aux, int epi, cudaStream_t s) {
+  Geometry &G = ctx->geo;
+  const Layout &L = ctx->L;
+  const int NN = L.NN, ffh = G.f * G.fh;
+  const int Y = G.Y, X = G.X;
+  const int zgroup = zgroup_for(ctx, nplanes);
+  const int nzg = (nplanes + zgroup - 1) / zgroup;
+  int rc = ensure_ws(ctx, ctx->wsS, sizeof(float2) * (size_t)nt * nplanes * NN * ffh);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sizeof(float2) * (size_t)nzg * nt * NN * ffh);
+  if (rc != FLF_OK) return rc;
+
+  Rfft2Params rp{};
+  rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
+  rp.nimg = nt * nplanes * NN; rp.nz = nplanes; rp.mode = 0;
+  rp.src = vol + (long long)t0 * Y * X; rp.src_sz = vol_sz; rp.src_st = (long long)Y * X;
+  rp.planes = d_planes; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
+  rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
+  LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * G.Ly * G.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
+
+  const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
+  MacParams mp{};
+  mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
+  mp.P = G.P[FLF_DIR_FORWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = zgroup;
+  mp.S = (const float2 *)ctx->wsS.p; mp.nzS = nplanes; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nzg;
+  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol; mp.G = mac_groups(L);
+  LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
+
+  Irfft2Params ip{};
+  ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
+  ip.nimg = nt * NN; ip.nzo = 1; ip.src = (const float2 *)ctx->wsO.p;
+  ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg; ip.planes = nullptr;
+  ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = Strided{nullptr, 0, 0};
+  ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+  LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh * nzg + 4.0 * G.Ly * G.Lx * (epi == EPI_DIVIDE ? 2 : 1)), s,
+         launch_irfft2(ip, s));
+  return FLF_OK;
+}
+
+// Back projection of frames [t0, t0+nt) of img; out/aux/norm address volumes.
+int backward_chunk(flf_ctx *ctx, const float *img, const int *d_planes, int nplanes, int t0, int nt,
+                   Strided out, Strided aux, Strided norm, int epi, cudaStream_t s) {
+  Geometry &G = ctx->geo;
+  const Layout &L = ctx->L;
+  const int NN = L.NN, ffh = G.f * G.fh;
+  const int Y = G.Y, X = G.X;
+  int rc = ensure_ws(ctx, ctx->wsS, sizeof(float2) * (size_t)nt * NN * ffh);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sizeof(float2) * (size_t)nt * nplanes * NN * ffh);
+  if (rc != FLF_OK) return rc;
+
+  Rfft2Params rp{};
+  rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
+  rp.nimg = nt * NN; rp.nz = 1; rp.mode = 0;
+  rp.src = img + (long long)t0 * Y * X; rp.src_sz = 0; rp.src_st = (long long)Y * X;
+  rp.planes = ctx->d_zero; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
+  rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
+  LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * G.Ly * G.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
+
+  const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
+  MacParams mp{};
+  mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
+  mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = 1;
+  mp.S = (const float2 *)ctx->wsS.p; mp.nzS = 1; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nplanes;
+  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol; mp.G = mac_groups(L);
+  LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
+
+  Irfft2Params ip{};
+  ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
+  ip.nimg = nt * nplanes * NN; ip.nzo = nplanes; ip.src = (const float2 *)ctx->wsO.p;
+  ip.sum_stride = 0; ip.nsum = 1; ip.planes = d_planes;
+  ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = norm;
+  ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+  const double px = 4.0 * G.Ly * G.Lx * (epi == EPI_STORE ? 1 : (epi == EPI_RL_STANDARD && norm.p ? 4 : 3));
+  LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh + px), s, launch_irfft2(ip, s));
+  return FLF_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int flf_ctx_create(flf_ctx **out, int device, int nnum, int num_planes) {
+  if (!out) return fail(nullptr, FLF_E_ARG, "out pointer is NULL");
+  *out = nullptr;
+  if (nnum < 3 || (nnum % 2) == 0 || nnum > 31)
+    return fail(nullptr, FLF_E_ARG, "Nnum must be odd and in [3, 31] (got %d)", nnum);
+  if (num_planes <= 0 || num_planes > 4096)
+    return fail(nullptr, FLF_E_ARG, "num_planes out of range (got %d)", num_planes);
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, FLF_E_CUDA, "no CUDA device available: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= ndev) return fail(nullptr, FLF_E_ARG, "device %d out of range", device);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  flf_ctx *ctx = new flf_ctx();
+  ctx->device = device;
+  ctx->N = nnum;
+  ctx->nz = num_planes;
+  ctx->L = make_layout(nnum);
+  for (int d = 0; d < 2; d++) {
+    ctx->dH[d].assign(num_planes, nullptr);
+    ctx->h[d].assign(num_planes, 0);
+  }
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  int rc = build_tables(ctx);
+  if (rc != FLF_OK) {
+    g_create_error = ctx->err;
+    flf_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return FLF_OK;
+}
+
+int flf_ctx_destroy(flf_ctx *ctx) {
+  if (!ctx) return FLF_OK;
+  cudaSetDevice(ctx->device);
+  for (int d = 0; d < 2; d++)
+    for (float *p : ctx->dH[d])
+      if (p) cudaFree(p);
+  resolve_pending(ctx);
+  for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+  free_geometry(ctx->geo);
+  void *ptrs[] = {ctx->d_rowS, ctx->d_slotcol, ctx->d_colslot, ctx->d_rep_ch, ctx->d_rep_row,
+                  ctx->d_rep_kind, ctx->d_planes_all, ctx->d_planes_user, ctx->d_zero,
+                  ctx->wsS.p, ctx->wsO.p, ctx->wsImg.p};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete ctx;
+  return FLF_OK;
+}
+
+int flf_last_error(const flf_ctx *ctx, char *buf, size_t len) {
+  if (!buf || len == 0) return FLF_E_ARG;
+  const std::string &s = ctx ? ctx->err : g_create_error;
+  const size_t n = std::min(len - 1, s.size());
+  memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return FLF_OK;
+}
+
+int flf_psf_upload(flf_ctx *ctx, int plane, int direction, const float *H_host, int n_h, int h) {
+  if (!ctx) return FLF_E_ARG;
+  if (plane < 0 || plane >= ctx->nz) return fail(ctx, FLF_E_ARG, "plane %d out of range [0, %d)", plane, ctx->nz);
+  if (direction != FLF_DIR_FORWARD && direction != FLF_DIR_BACKWARD)
+    return fail(ctx, FLF_E_ARG, "direction must be 0 (H) or 1 (Ht), got %d", direction);
+  if (!H_host) return fail(ctx, FLF_E_ARG, "H pointer is NULL");
+  if (n_h != ctx->L.nh) return fail(ctx, FLF_E_ARG, "n_h %d does not match Nnum %d (expected %d)", n_h, ctx->N, ctx->L.nh);
+  if (h <= 0 || (h % 2) == 0) return fail(ctx, FLF_E_ARG, "PSF size h must be odd and positive (got %d)", h);
+  cudaSetDevice(ctx->device);
+  float *&dst = ctx->dH[direction][plane];
+  if (dst && ctx->h[direction][plane] != h) { cudaFree(dst); dst = nullptr; }
+  const size_t bytes = sizeof(float) * (size_t)n_h * n_h * h * h;
+  if (!dst) {
+    cudaError_t e = cudaMalloc(&dst, bytes);
+    if (e != cudaSuccess) { cudaGetLastError(); dst = nullptr; return fail(ctx, FLF_E_NOMEM, "cudaMalloc for PSF failed: %s", cudaGetErrorString(e)); }
+  }
+  CUDA_TRY(ctx, cudaMemcpy(dst, H_host, bytes, cudaMemcpyHostToDevice));
+  ctx->h[direction][plane] = h;
+  // transfer matrices depend on the PSF and on the kernel radius
+  ctx->geo.built[0] = ctx->geo.built[1] = false;
+  ctx->geo.valid = false;
+  return FLF_OK;
+}
+
+int flf_prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
+  if (!ctx) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  for (int d = 0; d < 2; d++)
+    for (int z = 0; z < ctx->nz; z++)
+      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+  int rc = prepare(ctx, Y, X, fft_size, fp64);
+  if (rc != FLF_OK) return rc;
+  ctx->req_f = fft_size;
+  ctx->req_fp64 = fp64;
+  for (int d = 0; d < 2 && rc == FLF_OK; d++)
+    if (!ctx->geo.built[d]) rc = build_direction(ctx, d, 0);
+  return rc;
+}
+
+int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y, int X,
+                const int *planes, int nplanes, void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  if (!vol_dev || !img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int z = 0; z < ctx->nz; z++)
+    if (!ctx->dH[FLF_DIR_FORWARD][z]) return fail(ctx, FLF_E_STATE, "forward PSF for plane %d was not uploaded", z);
+  const int *d_planes;
+  int rc = set_user_planes(ctx, planes, nplanes, s, &d_planes);
+  if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
+  if (rc != FLF_OK) return rc;
+  const int TF = mac_max_frames();
+  const long long vol_sz = (long long)T * Y * X;
+  for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
+    const int nt = std::min(TF, T - t0);
+    Strided out{img_dev + (long long)t0 * Y * X, 0, (long long)Y * X};
+    rc = forward_chunk(ctx, vol_dev, vol_sz, d_planes, nplanes, t0, nt, out, Strided{nullptr, 0, 0}, EPI_STORE, s);
+  }
+  return rc;
+}
+
+int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X,
+                 const int *planes, int nplanes, void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  if (!vol_dev || !img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int z = 0; z < ctx->nz; z++)
+    if (!ctx->dH[FLF_DIR_BACKWARD][z]) return fail(ctx, FLF_E_STATE, "backward PSF for plane %d was not uploaded", z);
+  const int *d_planes;
+  int rc = set_user_planes(ctx, planes, nplanes, s, &d_planes);
+  if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
+  if (rc != FLF_OK) return rc;
+  const int TF = mac_max_frames();
+  for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
+    const int nt = std::min(TF, T - t0);
+    Strided out{vol_dev + (long long)t0 * Y * X, (long long)T * Y * X, (long long)Y * X};
+    rc = backward_chunk(ctx, img_dev, d_planes, nplanes, t0, nt, out, Strided{nullptr, 0, 0},
+                        Strided{nullptr, 0, 0}, EPI_STORE, s);
+  }
+  return rc;
+}
+
+int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev,
+                   int variant, int iters, int T, int Y, int X, void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  if (!x_dev || !ref_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
+  if (variant != FLF_RL_PREVEDEL && variant != FLF_RL_STANDARD)
+    return fail(ctx, FLF_E_ARG, "unknown RL variant %d", variant);
+  if (iters < 0) return fail(ctx, FLF_E_ARG, "iters must be >= 0");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int d = 0; d < 2; d++)
+    for (int z = 0; z < ctx->nz; z++)
+      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+  int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
+  if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
+  if (rc != FLF_OK) return rc;
+  const int TF = mac_max_frames();
+  const int nz = ctx->nz;
+  const long long YX = (long long)Y * X;
+  rc = ensure_ws(ctx, ctx->wsImg, sizeof(float) * (size_t)TF * YX);
+  if (rc != FLF_OK) return rc;
+  float *hx = (float *)ctx->wsImg.p;
+  for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
+    const int nt = std::min(TF, T - t0);
+    const Strided xs{x_dev + t0 * YX, (long long)T * YX, YX};
+    for (int it = 0; it < iters && rc == FLF_OK; it++) {
+      // H x  (standard variant: y / H x fused into the store)
+      const Strided hxo{hx, 0, YX};
+      if (variant == FLF_RL_PREVEDEL) {
+        rc = forward_chunk(ctx, x_dev, (long long)T * YX, ctx->d_planes_all, nz, t0, nt, hxo,
+                           Strided{nullptr, 0, 0}, EPI_STORE, s);
+      } else {
+        rc = forward_chunk(ctx, x_dev, (long long)T * YX, ctx->d_planes_all, nz, t0, nt, hxo,
+                           Strided{const_cast<float *>(ref_dev) + t0 * YX, 0, YX}, EPI_DIVIDE, s);
+      }
+      if (rc != FLF_OK) break;
+      if (variant == FLF_RL_PREVEDEL) {
+        const Strided htf{const_cast<float *>(ref_dev) + t0 * YX, (long long)T * YX, YX};
+        rc = backward_chunk(ctx, hx, ctx->d_planes_all, nz, 0, nt, xs, htf, Strided{nullptr, 0, 0},
+                            EPI_RL_PREVEDEL, s);
+      } else {
+        const Strided nrm{const_cast<float *>(norm_dev), YX, 0};
+        rc = backward_chunk(ctx, hx, ctx->d_planes_all, nz, 0, nt, xs, Strided{nullptr, 0, 0}, nrm,
+                            EPI_RL_STANDARD, s);
+      }
+    }
+  }
+  return rc;
+}
+
+int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {
+  if (!ctx || !bytes) return FLF_E_ARG;
+  size_t b = 0;
+  for (int d = 0; d < 2; d++)
+    for (int z = 0; z < ctx->nz; z++)
+      if (ctx->dH[d][z]) b += sizeof(float) * (size_t)ctx->L.nh * ctx->L.nh * ctx->h[d][z] * ctx->h[d][z];
+  const Geometry &G = ctx->geo;
+  if (G.valid) {
+    const size_t pe = (size_t)G.nkp * ctx->L.nrow * ctx->L.RS * ctx->nz * sizeof(float2);
+    for (int d = 0; d < 2; d++)
+      if (G.P[d]) b += pe;
+  }
+  b += ctx->wsS.bytes + ctx->wsO.bytes + ctx->wsImg.bytes;
+  *bytes = b;
+  return FLF_OK;
+}
+
+int flf_clear_cache(flf_ctx *ctx) {
+  if (!ctx) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  free_geometry(ctx->geo);
+  Workspace *ws[] = {&ctx->wsS, &ctx->wsO, &ctx->wsImg};
+  for (Workspace *w : ws) {
+    if (w->p) cudaFree(w->p);
+    *w = Workspace();
+  }
+  return FLF_OK;
+}
+
+int flf_geometry(const flf_ctx *ctx, int *out4) {
+  if (!ctx || !out4) return FLF_E_ARG;
+  const Geometry &G = ctx->geo;
+  out4[0] = G.valid ? G.f : 0;
+  out4[1] = G.valid ? G.R : 0;
+  out4[2] = G.valid ? G.fp64 : 0;
+  out4[3] = G.valid ? G.nkp : 0;
+  return FLF_OK;
+}
+
+int flf_profile(flf_ctx *ctx, int enable) {
+  if (!ctx) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  resolve_pending(ctx);
+  ctx->kstats.clear();
+  ctx->profiling = enable != 0;
+  return FLF_OK;
+}
+
+int flf_profile_read(flf_ctx *ctx, char *buf, size_t len) {
+  if (!ctx || !buf || len == 0) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  resolve_pending(ctx);
+  std::string out;
+  char line[256];
+  for (auto &kv : ctx->kstats) {
+    snprintf(line, sizeof(line), "%s %lld %.6f %.0f\n", kv.first.c_str(), kv.second.launches, kv.second.ms,
+             kv.second.bytes);
+    out += line;
+  }
+  const size_t n = std::min(len - 1, out.size());
+  memcpy(buf, out.data(), n);
+  buf[n] = 0;
+  return out.size() < len ? FLF_OK : FLF_E_ARG;
+}
+
+int flf_version(char *buf, size_t len) {
+  if (!buf || len == 0) return FLF_E_ARG;
+  snprintf(buf, len, "libflf 0.1 sm_103a kernels: k_rfft2 k_mac k_irfft2 k_build_k k_pack");
+  return FLF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+// Internal declarations shared by the CUDA translation units of libflf.so.
+//
+// Data model (lenslet-grid / polyphase form of the reference's projection):
+//  * An image of Y x X pixels is split into N*N "channels", one per pixel
+//    offset (b, a) inside a lenslet: s_{ba}(p, q) = img(p*N + b, q*N + a),
+//    each an Ly x Lx image (Ly = ceil(Y/N)).  Channel index i = b*N + a.
+//  * One z plane of the reference's projection (sum over offsets of masked
+//    'same' convolutions, projector.py:1084-1126) is, per output channel
+//    j = (beta, alpha), out_j = sum_i K_ij (*) s_i with the lenslet-grid
+//    kernel K_ij(m, n) = Hfull_i(m*N + beta - b + ch, n*N + alpha - a + ch),
+//    |m|,|n| <= R = floor((ch + N - 1)/N), ch = (h-1)/2.
+//  * With an f x f circular transform (f >= max(Ly, Lx) + R) this is, for
+//    every frequency u, a complex matrix-vector product
+//    out_j[u] = sum_i T_ij[u] S_i[u], T = rfft2(K) / f^2.
+//  * The PSF symmetries of the reference (projector.py:159-189) give
+//    T_{My i, My j}[u] = T_ij[u*]           (b != c), u* = (-uy, ux)
+//    T_{Mx i, Mx j}[u] = conj T_ij[u*]      (a != c)
+//    T_{Mxy i, Mxy j}[u] = conj T_ij[u]     (b != c and a != c)
+//    so the stored matrices cover a quarter of the frequencies and about
+//    half of the rows; see the packed layout below.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace flf {
+
+constexpr int kMaxStages = 12;
+constexpr int kMaxF = 160;          // largest lenslet-grid FFT size (float)
+constexpr int kMaxF64 = 112;        // largest size for the fp64 precompute
+
+struct FftPlan {
+  int n;                 // transform length (f)
+  int nst;               // number of radix stages
+  int rad[kMaxStages];   // radices, each in {2,3,4,5,7}
+};
+
+// Packed transfer-matrix layout for one (plane, direction):
+//   P[kpair][row][slot], kpair = uy*fq + ux over uy, ux in [0, f/2],
+//   fq = f/2 + 1; rows = 2*n_h^2; slot stride RS = N*N rounded up to even.
+// Rows: 2c^2 "generic" input channels (b < c, a != c) stored at u, then for
+// each of the 2c+1 centre-cross channels (b < c, a = c), (b = c, a < c),
+// (c, c) a pair of rows holding u and u*.  Slots: output channels grouped by
+// mirror orbit: c^2 generic orbits [q, My q, Mx q, Mxy q], c orbits
+// [q, My q] (alpha = c), c orbits [q, Mx q] (beta = c), then the centre.
+struct Layout {
+  int N, NN, c, nh;
+  int nrowG;      // 2c^2
+  int nrep;       // 2c+1
+  int nrow;       // 2 nh^2
+  int RS;         // row stride in complex elements
+  int nthr;       // nh^2: threads (orbits) per row group
+};
+
+inline Layout make_layout(int N) {
+  Layout L;
+  L.N = N; L.NN = N * N; L.c = N / 2; L.nh = L.c + 1;
+  L.nrowG = 2 * L.c * L.c;
+  L.nrep = 2 * L.c + 1;
+  L.nrow = 2 * L.nh * L.nh;
+  L.RS = (L.NN + 1) & ~1;
+  L.nthr = L.nh * L.nh;
+  return L;
+}
+
+// Epilogue modes of the inverse transform kernel.
+enum Epilogue : int {
+  EPI_STORE = 0,         // out = value
+  EPI_DIVIDE = 1,        // out = aux / value           (y / Hx)
+  EPI_RL_PREVEDEL = 2,   // x = x * (aux / value), NaN -> 0
+  EPI_RL_STANDARD = 3,   // x = x * value [/ norm], NaN -> 0
+};
+
+struct Strided {         // base + plane*sz + frame*st + y*X + x
+  float *p;
+  long long sz, st;
+};
+
+// ----------------------------------------------------------------------------
+// Kernel parameter blocks
+// ----------------------------------------------------------------------------
+
+struct Rfft2Params {
+  FftPlan plan;
+  int N, Y, X, Ly, Lx;
+  int nimg;                 // total images
+  int nz;                   // planes per frame in this launch
+  int mode;                 // 0: channel gather from [Z][T][Y][X]; 1: contiguous f*f images
+  const float *src;         // mode 0 (float input)
+  long long src_sz, src_st; // mode 0 strides (plane, frame)
+  const int *planes;        // mode 0: plane id per z index (device)
+  const void *src_img;      // mode 1: Real images [nimg][f][f]
+  void *dst;                // Complex<Real> [nimg][f][fh]
+  const void *twiddle;      // Complex<Real> [f]
+  int imgs_per_cta;
+  int nq_rows;              // row pairs carrying data (<= f/2)
+};
+
+struct Irfft2Params {
+  FftPlan plan;
+  int N, Y, X, Ly, Lx;
+  int nimg;                 // images: (t*nzo + zo)*NN + j
+  int nzo;                  // output planes per frame
+  const float2 *src;        // spectra [nsum][nimg][f][fh]
+  long long sum_stride;     // elements between partial sums
+  int nsum;
+  const int *planes;        // plane id per zo (device); NULL -> zo
+  int epi;
+  Strided out;              // destination (or x for RL updates)
+  Strided aux;              // y (EPI_DIVIDE) or Htf (EPI_RL_PREVEDEL)
+  Strided norm;             // EPI_RL_STANDARD normaliser (p may be NULL)
+  const float2 *twiddle;
+  int imgs_per_cta;
+};
+
+struct MacParams {
+  Layout L;
+  int f, fh, fq, nkp;       // transform size, f/2+1, f/2+1, fq*fq
+  int T;                    // frames in this launch (<= template TF)
+  const float2 *P;          // packed matrices [plane][nkp][nrow][RS]
+  const int *planes;        // plane id per z index
+  int nz;                   // planes in the list
+  int zgroup;               // forward: planes per CTA group
+  const float2 *S;          // input spectra [T][nzS][NN][f][fh]
+  int nzS;                  // planes in S (forward nz, backward 1)
+  float2 *O;                // output spectra
+  int nzo;                  // forward: number of z groups; backward: nz
+  const short4 *rowS;       // per-row S gather indices into [su | ss]
+  const short *slotcol;     // slot -> output channel
+  int G;                    // row groups per CTA
+};
+
+struct BuildKParams {       // lenslet-grid kernels K_iq for the precompute
+  int N, h, ch, R, f;
+  const float *H;           // reduced PSF [nh][nh][h][h] (device)
+  const int *rep_ch;        // input channel of each row representative
+  int rep0, nrep_chunk;     // representatives in this chunk
+  void *dst;                // Real [nrep_chunk][NN][f][f]
+  int fp64;
+};
+
+struct PackParams {
+  Layout L;
+  int f, fh, fq, nkp;
+  const void *spec;         // Complex<Real> [nrep_chunk][NN][f][fh]
+  int rep0, nrep_chunk;
+  const int *rep_row;       // packed row of representative (first row)
+  const int *rep_kind;      // 0 generic, 1 cc, 2 cr, 3 ctr
+  const int *rep_ch;
+  const short *col_slot;    // channel -> slot
+  float2 *P;                // this plane's packed block [nkp][nrow][RS]
+  double scale;             // 1/f^2
+  int fp64;
+};
+
+// Launchers (flf_kernels.cu)
+cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s);
+cudaError_t launch_irfft2(const Irfft2Params &p, cudaStream_t s);
+cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
+cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);
+cudaError_t launch_pack(const PackParams &p, cudaStream_t s);
+size_t rfft2_smem_bytes(int f, int imgs, int fp64);
+size_t irfft2_smem_bytes(int f, int imgs);
+int mac_max_frames();
+
+}  // namespace flf

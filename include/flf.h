@@ -1,0 +1,135 @@
+/*
+ * flf.h - C ABI of the GB300 light-field projection library (libflf.so).
+ *
+ * This is the native boundary that replaces the reference's CPython extension
+ * `py_light_field` for the Richardson-Lucy hot path of jmtayloruk/fast-light-field.
+ * The reference binds that extension from Python (method table
+ * py_light_field/py_light_field.cpp:1956-1973); a Python host binds this file
+ * with ctypes (fast-light-field_gb300/_flf.py).
+ *
+ * Conventions
+ *  - Every call returns an int status: FLF_OK (0) or a negative FLF_E_* code.
+ *    The message of the last failure on a context is read with
+ *    flf_last_error(); failures of flf_ctx_create() are read with
+ *    flf_last_error(NULL, ...).
+ *  - Array arguments named *_dev are CUDA device pointers owned by the caller
+ *    (float32, C-contiguous).  Host arrays are plain float pointers.
+ *  - Volumes are laid out [Z][T][Y][X] (plane, frame, row, column), images
+ *    [T][Y][X], exactly as the reference's numpy arrays
+ *    (lfdeconv.py:27-70).  `planes` lists the plane ids taking part, as the
+ *    reference's `planes` argument (projector.py:806, 851).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    stream-ordered and not thread-safe for one context.
+ *  - The context owns the PSFs, the precomputed transfer matrices (the GB300
+ *    form of the reference's FH cache) and all workspaces.
+ */
+#ifndef FLF_H
+#define FLF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLF_OK 0
+#define FLF_E_ARG (-1)      /* bad argument: shape, range, null pointer   */
+#define FLF_E_CUDA (-2)     /* a CUDA runtime call failed                  */
+#define FLF_E_NOMEM (-3)    /* device or host allocation failed            */
+#define FLF_E_STATE (-4)    /* call out of order (e.g. PSF not uploaded)   */
+#define FLF_E_TIMEOUT (-5)  /* a bounded device wait gave up               */
+
+/* Projection direction / PSF set selector. */
+#define FLF_DIR_FORWARD 0   /* H:  volume -> image  (reference useHt=False) */
+#define FLF_DIR_BACKWARD 1  /* Ht: image  -> volume (reference useHt=True)  */
+
+/* Richardson-Lucy update variants (lfdeconv.py:112-183). */
+#define FLF_RL_PREVEDEL 0   /* x <- x * Htf / Ht(H x); NaN -> 0             */
+#define FLF_RL_STANDARD 1   /* x <- x * Ht(y / H x) [/ norm]; NaN -> 0       */
+
+typedef struct flf_ctx flf_ctx;
+
+/* Create a context on CUDA device `device` for a PSF with lenslet size
+ * `nnum` (odd) and `num_planes` z planes.  Replaces the module-level state
+ * of py_light_field (gFHCache, gNumThreadsToUse; py_light_field.cpp:15-32,
+ * 1319-1385). */
+int flf_ctx_create(flf_ctx **out, int device, int nnum, int num_planes);
+
+/* Free every device allocation of the context. */
+int flf_ctx_destroy(flf_ctx *ctx);
+
+/* Copy the last error message (NUL-terminated, truncated to len) of `ctx`,
+ * or of the calling thread's last flf_ctx_create when ctx is NULL.
+ * Replaces the PyErr_* exceptions of py_light_field.cpp:1425-1493. */
+int flf_last_error(const flf_ctx *ctx, char *buf, size_t len);
+
+/* Upload the stored PSF quadrant of one plane and direction: host array
+ * [n_h][n_h][h][h] float32 with n_h = (nnum+1)/2 and h odd.  This is the
+ * per-plane `hMatrix.Hcc(cc, useHt)` array the reference passes to
+ * ProjectForZList (projector.py:813-815, 855-857; psfmatrix.py:46-66).
+ * Invalidates transfer matrices built from an earlier upload. */
+int flf_psf_upload(flf_ctx *ctx, int plane, int direction, const float *H_host,
+                   int n_h, int h);
+
+/* Build (or reuse) the transfer matrices for images of Y x X pixels:
+ * the PSF spectrum precompute that the reference redoes on every call in
+ * FHWorkItem::Run (py_light_field.cpp:781-812, 829-867) unless cacheFH.
+ * `fft_size` 0 picks the transform size automatically; `fp64` nonzero
+ * runs the precompute in double precision.  Optional: projections call it
+ * themselves when the shape changes. */
+int flf_prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64);
+
+/* Forward projection H x: vol_dev [Z][T][Y][X] -> img_dev [T][Y][X]
+ * (sum over `planes`).  Replaces Projector_allC.ForwardProjectACC's
+ * ProjectForZList + InverseRFFTList + CropAfterFFT + plane sum
+ * (projector.py:851-896; py_light_field.cpp:1417-1635, 1663-1740). */
+int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y,
+                int X, const int *planes, int nplanes, void *stream);
+
+/* Back projection Ht y: img_dev [T][Y][X] -> vol_dev [Z][T][Y][X]; only the
+ * listed planes are written.  Replaces Projector_allC.BackwardProjectACC
+ * (projector.py:806-849). */
+int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y,
+                 int X, const int *planes, int nplanes, void *stream);
+
+/* `iters` Richardson-Lucy iterations in place on x_dev [Z][T][Y][X] over all
+ * planes of the context (the loop of DeconvRL, lfdeconv.py:185-196).
+ *  FLF_RL_PREVEDEL: ref_dev = Htf [Z][T][Y][X]; norm_dev ignored.
+ *  FLF_RL_STANDARD: ref_dev = camera image [T][Y][X]; norm_dev = Ht(mask)
+ *    [Z][1][Y][X] or NULL (no normaliser). */
+int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev,
+                   const float *norm_dev, int variant, int iters, int T, int Y,
+                   int X, void *stream);
+
+/* Bytes of device memory the context holds (PSFs, transfer matrices,
+ * workspaces).  Counterpart of gMemoryUsage (py_light_field.cpp:654-670). */
+int flf_memory_usage(const flf_ctx *ctx, size_t *bytes);
+
+/* Drop the transfer matrices and workspaces (keeps the uploaded PSFs).
+ * Counterpart of ClearFHCache (py_light_field.cpp:1370-1385). */
+int flf_clear_cache(flf_ctx *ctx);
+
+/* Transform size and precompute precision chosen by the last prepare:
+ * out[0] = f (lenslet-grid FFT size), out[1] = R (kernel radius in
+ * lenslets), out[2] = fp64 flag, out[3] = number of frequency pairs. */
+int flf_geometry(const flf_ctx *ctx, int *out4);
+
+/* Per-kernel statistics.  flf_profile(ctx, 1) clears the counters and
+ * brackets every subsequent kernel launch with CUDA events on its stream;
+ * flf_profile(ctx, 0) clears them and stops the event timing (launch counts
+ * are always kept).  flf_profile_read writes one line per kernel:
+ * "<name> <launches> <total_ms> <algorithmic_bytes>".  The reference's
+ * counterparts are its per-work-item timeline and stats files
+ * (SetThreadFileName / SetStatsFile, py_light_field.cpp:171-282). */
+int flf_profile(flf_ctx *ctx, int enable);
+int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
+
+/* Library self-description for diagnostics: writes a short text (build
+ * arch, kernel list) into buf. */
+int flf_version(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLF_H */

@@ -1,0 +1,203 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the reference's
+golden vectors and the CPU oracle.
+
+Tolerances: projections are FP32 arithmetic; they must agree with the FP64
+oracle / the reference's FP32 output to 2e-5 of the output's maximum
+(the reference's own self-test accepts 1e-4 absolute on O(1) outputs,
+projector.py:1212).  Richardson-Lucy results must agree to 1e-4 relative
+(max abs error / max abs value).
+"""
+
+import numpy as np
+import pytest
+
+from golden_inputs import CASES, case_inputs
+from oracle import lf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PROJ_TOL = 2e-5
+RL_TOL = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def mods(built_lib):
+    import lfdeconv
+    import projector
+    import psfmatrix
+    import _flf
+    _flf.load_library()
+    return projector, lfdeconv, psfmatrix
+
+
+def gold():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.npz"))
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if CASES[n]["kind"] == "project"])
+@pytest.mark.parametrize("fp64", [True, False])
+def test_projection_matches_reference_vectors(mods, name, fp64):
+    projector, lfdeconv, psfmatrix = mods
+    c = case_inputs(name)
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    p = projector.Projector_gb300()
+    p.fp64_precompute = fp64
+    bk = lfdeconv.BackwardProjectACC(hm, c["img"], projector=p, logPrint=False)
+    fw = lfdeconv.ForwardProjectACC(hm, c["vol"], projector=p, logPrint=False)
+    g = gold()
+    assert bk.shape == g[name + "/backward"].shape and bk.dtype == np.float32
+    assert fw.shape == g[name + "/forward"].shape and fw.dtype == np.float32
+    assert rel(bk, g[name + "/backward"]) < PROJ_TOL
+    assert rel(fw, g[name + "/forward"]) < PROJ_TOL
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if CASES[n]["kind"] == "rl"])
+def test_rl_matches_reference_vectors(mods, name):
+    projector, lfdeconv, psfmatrix = mods
+    c = case_inputs(name)
+    Z = len(c["hs"])
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    p = projector.Projector_gb300()
+    x0 = None if c["prevedel"] else np.ones((Z,) + c["img"].shape, np.float32)
+    r = lfdeconv.DeconvRL(hm, None, c["iters"], x0, logPrint=False, projector=p, im=c["img"],
+                          prevedel=c["prevedel"])
+    assert rel(r, gold()[name + "/rl"]) < RL_TOL
+
+
+@pytest.mark.parametrize("N,hs,T,Y,X", [
+    (3, [7, 9, 5], 1, 18, 21),
+    (5, [21, 11, 31], 3, 40, 35),     # ragged image (not a multiple of Nnum)
+    (7, [43, 15], 6, 49, 56),         # T > 4 exercises frame chunking
+    (15, [61, 91], 2, 150, 120),
+    (19, [77], 1, 95, 114),
+])
+def test_projection_matches_fp64_oracle(mods, N, hs, T, Y, X):
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    H, Ht = synthetic.random_psf(N, hs, seed=N * 7 + T)
+    rng = np.random.default_rng(N + Y)
+    img = rng.random((T, Y, X)).astype(np.float32)
+    vol = rng.random((len(hs), T, Y, X)).astype(np.float32)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    p = projector.Projector_gb300()
+    bk = p.BackwardProjectACC(hm, img, None)
+    fw = p.ForwardProjectACC(hm, vol, None)
+    meth = "direct" if N <= 7 else "special"
+    bo = O.backward_project(Ht, img, N, method=meth, dtype=np.float64)
+    fo = O.forward_project(H, vol, N, method=meth, dtype=np.float64)
+    assert rel(bk, bo) < PROJ_TOL
+    assert rel(fw, fo) < PROJ_TOL
+
+
+def test_plane_subsets(mods):
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    N = 5
+    H, Ht = synthetic.random_psf(N, [21, 11, 31, 15], seed=3)
+    rng = np.random.default_rng(5)
+    img = rng.random((2, 30, 35)).astype(np.float32)
+    vol = rng.random((4, 2, 30, 35)).astype(np.float32)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    p = projector.Projector_gb300()
+    full_bk = O.backward_project(Ht, img, N, method="direct", dtype=np.float64)
+    for planes in ([2], [3, 1], [0, 2, 3]):
+        bk = p.BackwardProjectACC(hm, img, planes)
+        for z in range(4):
+            if z in planes:
+                assert rel(bk[z], full_bk[z]) < PROJ_TOL
+            else:
+                assert np.all(bk[z] == 0)
+        fw = p.ForwardProjectACC(hm, vol, planes)
+        fo = O.forward_project(H, vol, N, planes=planes, method="direct", dtype=np.float64)
+        assert rel(fw, fo) < PROJ_TOL
+
+
+def test_standard_rl_with_trust_mask(mods):
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    N = 5
+    H, Ht = synthetic.synthetic_psf(N, [-10, 0, 10], 2)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(9)
+    img = (rng.random((1, 40, 40)) * 500 + 100).astype(np.float32)
+    mask = np.ones((40, 40), np.float32)
+    mask[:5] = 0
+    img[:, :5] = 0
+    x0 = np.ones((3, 1, 40, 40), np.float32)
+    p = projector.Projector_gb300()
+    r = lfdeconv.DeconvRL(hm, None, 3, x0, logPrint=False, projector=p, im=img, prevedel=False,
+                          trustMask=mask)
+    with np.errstate(all="ignore"):
+        o = O.deconv_rl(H, Ht, N, 3, im=img, x0=x0, prevedel=False, trust_mask=mask, method="direct",
+                        dtype=np.float64)
+    assert rel(r, o) < RL_TOL
+
+
+def test_zero_image_rl_gives_zero(mods):
+    projector, lfdeconv, psfmatrix = mods
+    c = case_inputs("rl_prevedel")
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    p = projector.Projector_gb300()
+    img = np.zeros_like(c["img"])
+    r = lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=img)
+    assert np.all(r == 0)
+
+
+def test_full_size_linearity_and_adjointness(mods):
+    """Config-0 sizes (450x450, Nnum 15, 11 planes): size-independent properties."""
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    z = np.arange(-25, 26, 5)
+    H, Ht = synthetic.synthetic_psf(15, z, 7)
+    assert max(h.shape[-1] for h in H) == 211
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    p = projector.Projector_gb300()
+    rng = np.random.default_rng(1)
+    x1 = rng.random((11, 1, 450, 450)).astype(np.float32)
+    x2 = rng.random((11, 1, 450, 450)).astype(np.float32)
+    y = rng.random((1, 450, 450)).astype(np.float32)
+    h1 = p.ForwardProjectACC(hm, x1, None).astype(np.float64)
+    h2 = p.ForwardProjectACC(hm, x2, None).astype(np.float64)
+    h12 = p.ForwardProjectACC(hm, (2.0 * x1 - 0.5 * x2).astype(np.float32), None).astype(np.float64)
+    assert rel(h12, 2.0 * h1 - 0.5 * h2) < 1e-5
+    bt = p.BackwardProjectACC(hm, y, None).astype(np.float64)
+    lhs = np.sum(h1 * y)
+    rhs = np.sum(x1.astype(np.float64) * bt)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # flux: each forward PSF sums to 1, so a uniform volume far from the border
+    # projects to Z per pixel in the image centre
+    u = np.ones((11, 1, 450, 450), np.float32)
+    hu = p.ForwardProjectACC(hm, u, None)
+    assert abs(float(hu[0, 225, 225]) - 11.0) < 1e-3
+
+
+def test_planes_validation(mods):
+    projector, lfdeconv, psfmatrix = mods
+    c = case_inputs("planes_n7")
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    p = projector.Projector_gb300()
+    with pytest.raises(IndexError):
+        p.BackwardProjectACC(hm, c["img"], [5])
+    with pytest.raises(ValueError):
+        p.BackwardProjectACC(hm, c["img"], [1, 1])
+    with pytest.raises(ValueError):
+        p.BackwardProjectACC(hm, c["img"][0], None)
+
+
+def test_context_errors(mods):
+    import _flf
+    with pytest.raises(_flf.FlfError):
+        _flf.Context(4, 3)          # even Nnum
+    ctx = _flf.Context(5, 2)
+    with pytest.raises(_flf.FlfError):
+        ctx.upload_psf(0, 0, np.zeros((3, 3, 10, 10), np.float32))   # even h
+    with pytest.raises(_flf.FlfError):
+        ctx.prepare(30, 30)          # PSFs not uploaded
+    ctx.close()
