@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-planes", type=int, default=2)
+    ap.add_argument("--cpu-sample-planes", type=int, default=5)
     return ap.parse_args()
 
 
@@ -143,17 +143,23 @@ def cpu_baseline(hm, H, Ht, z, Y, X, N, iters, nplanes_sample, cores):
     rng = np.random.default_rng(7)
     img = rng.random((1, Y, X)).astype(np.float32)
     Z = len(z)
-    # sample planes spanning the PSF sizes: largest and smallest support
+    # sample planes spanning the PSF sizes (evenly spaced in support size),
+    # repeated until the sample holds about 10 s of CPU work
     hs = np.array([h.shape[-1] for h in Ht])
     order = np.argsort(hs)
-    picks = sorted(set([int(order[-1]), int(order[0])] + [int(order[len(order) // 2])][: max(0, nplanes_sample - 2)]))
-    times = {}
+    k = max(2, min(nplanes_sample, len(order)))
+    picks = sorted(set(int(order[int(round(i * (len(order) - 1) / (k - 1)))]) for i in range(k)))
+    times = {zi: [] for zi in picks}
     t_all = time.time()
-    for zi in picks:
-        t0 = time.time()
-        O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
-        times[zi] = time.time() - t0
+    while True:
+        for zi in picks:
+            t0 = time.time()
+            O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
+            times[zi].append(time.time() - t0)
+        if time.time() - t_all > 10.0 or len(times[picks[0]]) >= 5:
+            break
     sample_s = time.time() - t_all
+    times = {zi: float(np.median(v)) for zi, v in times.items()}
     # cost per plane ~ F_z * RX_z (the spectral multiply-accumulate and FFT sizes)
 
     def cost(zi):
@@ -171,7 +177,7 @@ def cpu_baseline(hm, H, Ht, z, Y, X, N, iters, nplanes_sample, cores):
     vol_s = per_projection * projections
     return {
         "value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": "port",
-        "sample": "back projection of planes %s (PSF sizes %s) of the workload on %d threads in %.1f s; "
+        "sample": "back projections of planes %s (PSF sizes %s) of the workload on %d threads, %.1f s in total; "
                   "one volume = %d projections x %d planes, extrapolated linearly in the per-plane "
                   "spectrum size" % (picks, [int(hs[p]) for p in picks], cores, sample_s, projections, Z),
         "seconds_per_volume": vol_s,

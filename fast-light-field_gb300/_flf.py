@@ -40,6 +40,8 @@ _SIGS = {
     "flf_version": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
     "flf_profile": (_I, [_P, _I]),
     "flf_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "flf_set_option": (_I, [_P, ctypes.c_char_p, ctypes.c_longlong]),
+    "flf_synchronize": (_I, [_P, _P]),
 }
 
 _lib = None
@@ -167,6 +169,12 @@ class Context:
 
     def clear_cache(self):
         self._check(self._lib.flf_clear_cache(self._h))
+
+    def set_option(self, name, value):
+        self._check(self._lib.flf_set_option(self._h, name.encode(), int(value)))
+
+    def synchronize(self, stream=None):
+        self._check(self._lib.flf_synchronize(self._h, _ptr(stream)))
 
     def profile(self, enable):
         self._check(self._lib.flf_profile(self._h, int(bool(enable))))

@@ -54,6 +54,11 @@ struct flf_ctx {
   Workspace wsS, wsO, wsImg;
   int num_sms = 0;
   int req_f = 0, req_fp64 = 0;   // transform size / precision asked for by flf_prepare
+  int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
+  int opt_chunk_rows = 8;        // tunable: stored rows per pipeline stage
+  int opt_split = 2;             // tunable: threads sharing one orbit's rows
+  int *h_err = nullptr;          // host-mapped flag set by bounded device waits
+  int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
   struct KStat { long long launches = 0; double ms = 0, bytes = 0; };
   struct Pending { std::string name; cudaEvent_t a, b; };
@@ -136,6 +141,16 @@ int counted_launch(flf_ctx *ctx, const char *name, double bytes, cudaStream_t s,
     int rc_ = counted_launch(ctx, name, (double)(bytes), s, [&]() { return (expr); }); \
     if (rc_ != FLF_OK) return rc_;                                         \
   } while (0)
+
+// Report a bounded device wait that gave up in an earlier launch.
+int check_device_flag(flf_ctx *ctx) {
+  if (ctx->h_err && *(volatile int *)ctx->h_err) {
+    const int code = *(volatile int *)ctx->h_err;
+    *(volatile int *)ctx->h_err = 0;
+    return fail(ctx, FLF_E_TIMEOUT, "a bounded wait in the multiply-accumulate pipeline gave up (code %d)", code);
+  }
+  return FLF_OK;
+}
 
 bool is_smooth_even(int n) {
   if (n < 2 || (n & 1)) return false;
@@ -406,6 +421,7 @@ int set_user_planes(flf_ctx *ctx, const int *planes, int nplanes, cudaStream_t s
 
 int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
   if (!ctx) return FLF_E_ARG;
+  if (int rc0 = check_device_flag(ctx)) return rc0;
   if (T <= 0) return fail(ctx, FLF_E_ARG, "frame count must be positive (got %d)", T);
   int f_req = ctx->req_f;
   if (f_req > 0) {
@@ -422,17 +438,12 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
   return rc;
 }
 
+// Planes per CTA of the multiply-accumulate: enough CTAs for about 32 per SM
+// (a few waves at the kernel's occupancy), as few plane groups as that allows.
 int zgroup_for(const flf_ctx *ctx, int nz) {
-  const int target = 4 * std::max(1, ctx->num_sms);
-  const int nzg_needed = std::max(1, (target + ctx->geo.nkp - 1) / ctx->geo.nkp);
-  const int zg = (nz + nzg_needed - 1) / nzg_needed;
-  return std::max(1, zg);
-}
-
-int mac_groups(const Layout &L) {
-  int G = std::max(1, 512 / L.nthr);
-  G = std::min(G, std::max(1, L.nrowG));
-  return G;
+  const int target = 32 * std::max(1, ctx->num_sms);
+  const int nzg_needed = std::min(nz, std::max(1, (target + ctx->geo.nkp - 1) / ctx->geo.nkp));
+  return std::max(1, (nz + nzg_needed - 1) / nzg_needed);
 }
 
 // Forward projection of frames [t0, t0+nt) of vol into out (epilogue epi).
@@ -461,7 +472,8 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const int *d
   mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
   mp.P = G.P[FLF_DIR_FORWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = zgroup;
   mp.S = (const float2 *)ctx->wsS.p; mp.nzS = nplanes; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nzg;
-  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol; mp.G = mac_groups(L);
+  mp.nzo_grid = nzg; mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
+  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split; mp.err = ctx->d_err;
   LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
 
   Irfft2Params ip{};
@@ -497,9 +509,11 @@ int backward_chunk(flf_ctx *ctx, const float *img, const int *d_planes, int npla
   const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
   MacParams mp{};
   mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
-  mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = 1;
+  const int zgb = zgroup_for(ctx, nplanes);
+  mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = zgb;
   mp.S = (const float2 *)ctx->wsS.p; mp.nzS = 1; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nplanes;
-  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol; mp.G = mac_groups(L);
+  mp.nzo_grid = (nplanes + zgb - 1) / zgb; mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
+  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split; mp.err = ctx->d_err;
   LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
 
   Irfft2Params ip{};
@@ -544,7 +558,15 @@ int flf_ctx_create(flf_ctx **out, int device, int nnum, int num_planes) {
     ctx->h[d].assign(num_planes, 0);
   }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-  int rc = build_tables(ctx);
+  int rc = FLF_OK;
+  if (cudaHostAlloc((void **)&ctx->h_err, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void **)&ctx->d_err, ctx->h_err, 0) != cudaSuccess) {
+    cudaGetLastError();
+    rc = fail(ctx, FLF_E_CUDA, "mapped host allocation for the error flag failed");
+  } else {
+    *ctx->h_err = 0;
+  }
+  if (rc == FLF_OK) rc = build_tables(ctx);
   if (rc != FLF_OK) {
     g_create_error = ctx->err;
     flf_ctx_destroy(ctx);
@@ -568,6 +590,7 @@ int flf_ctx_destroy(flf_ctx *ctx) {
                   ctx->wsS.p, ctx->wsO.p, ctx->wsImg.p};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (ctx->h_err) cudaFreeHost(ctx->h_err);
   delete ctx;
   return FLF_OK;
 }
@@ -777,6 +800,34 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len) {
   memcpy(buf, out.data(), n);
   buf[n] = 0;
   return out.size() < len ? FLF_OK : FLF_E_ARG;
+}
+
+int flf_synchronize(flf_ctx *ctx, void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  CUDA_TRY(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+  return check_device_flag(ctx);
+}
+
+int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
+  if (!ctx || !name) return FLF_E_ARG;
+  if (!strcmp(name, "mac_stages") || !strcmp(name, "mac_chunk_rows") || !strcmp(name, "mac_split")) {
+    const int st = !strcmp(name, "mac_stages") ? (int)value : ctx->opt_stages;
+    const int cr = !strcmp(name, "mac_chunk_rows") ? (int)value : ctx->opt_chunk_rows;
+    const int sp = !strcmp(name, "mac_split") ? (int)value : ctx->opt_split;
+    if (st < 2 || st > 16) return fail(ctx, FLF_E_ARG, "mac_stages must be in [2, 16]");
+    if (cr < 2 || cr > 64 || (cr & 1)) return fail(ctx, FLF_E_ARG, "mac_chunk_rows must be even, in [2, 64]");
+    const int ntp = (ctx->L.nthr + 31) / 32 * 32;
+    if (sp < 1 || sp > 4 || sp * ntp > 256)
+      return fail(ctx, FLF_E_ARG, "mac_split must be in [1, 4] with at most 256 threads per block");
+    if (mac_smem_bytes(ctx->L, mac_max_frames(), st, cr, sp, true) > 227 * 1024)
+      return fail(ctx, FLF_E_ARG, "pipeline of %d stages x %d rows exceeds shared memory", st, cr);
+    ctx->opt_stages = st;
+    ctx->opt_chunk_rows = cr;
+    ctx->opt_split = sp;
+    return FLF_OK;
+  }
+  return fail(ctx, FLF_E_ARG, "unknown option '%s'", name);
 }
 
 int flf_version(char *buf, size_t len) {

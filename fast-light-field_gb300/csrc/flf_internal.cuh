@@ -124,10 +124,14 @@ struct MacParams {
   const float2 *S;          // input spectra [T][nzS][NN][f][fh]
   int nzS;                  // planes in S (forward nz, backward 1)
   float2 *O;                // output spectra
-  int nzo;                  // forward: number of z groups; backward: nz
+  int nzo;                  // forward: number of z groups (output sets); backward: nz
+  int nzo_grid;             // grid.y: number of z groups of this launch
   const short4 *rowS;       // per-row S gather indices into [su | ss]
   const short *slotcol;     // slot -> output channel
-  int G;                    // row groups per CTA
+  int stages;               // shared-memory ring stages of the bulk-copy pipeline
+  int chunk_rows;           // stored rows per stage (even)
+  int split;                // threads sharing one orbit's rows (1..4)
+  int *err;                 // set nonzero when a bounded wait gives up
 };
 
 struct BuildKParams {       // lenslet-grid kernels K_iq for the precompute
@@ -162,5 +166,6 @@ cudaError_t launch_pack(const PackParams &p, cudaStream_t s);
 size_t rfft2_smem_bytes(int f, int imgs, int fp64);
 size_t irfft2_smem_bytes(int f, int imgs);
 int mac_max_frames();
+size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int split, bool fwd);
 
 }  // namespace flf

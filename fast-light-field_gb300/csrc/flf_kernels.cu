@@ -322,229 +322,471 @@ __global__ void __launch_bounds__(256) k_irfft2(Irfft2Params p) {
 // CalculateRow/CalculateRowBoth (py_light_field.cpp:303-341), which read and
 // wrote the accumulator once per lenslet offset.
 // ----------------------------------------------------------------------------
-template <int K> struct Orb;
-template <> struct Orb<0> {  // generic orbit [q, My q, Mx q, Mxy q]
-  static constexpr int NS = 4;
-  __device__ static constexpr int sy(int k) { return k ^ 1; }
-  __device__ static constexpr int sx(int k) { return k ^ 2; }
-  __device__ static constexpr int sxy(int k) { return 3 - k; }
-};
-template <> struct Orb<1> {  // alpha = c: [q, My q]
-  static constexpr int NS = 2;
-  __device__ static constexpr int sy(int k) { return k ^ 1; }
-  __device__ static constexpr int sx(int k) { return k; }
-  __device__ static constexpr int sxy(int k) { return k ^ 1; }
-};
-template <> struct Orb<2> {  // beta = c: [q, Mx q]
-  static constexpr int NS = 2;
-  __device__ static constexpr int sy(int k) { return k; }
-  __device__ static constexpr int sx(int k) { return k ^ 1; }
-  __device__ static constexpr int sxy(int k) { return k ^ 1; }
-};
-template <> struct Orb<3> {  // centre
-  static constexpr int NS = 1;
-  __device__ static constexpr int sy(int) { return 0; }
-  __device__ static constexpr int sx(int) { return 0; }
-  __device__ static constexpr int sxy(int) { return 0; }
-};
+// ---------------------------------------------------------------------------
+// Bulk-copy pipeline primitives (sm_90+ PTX: mbarrier, cp.async.bulk).
+// Every wait is bounded by a wall-clock limit read from %globaltimer.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *ptr) {
+  return (unsigned)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Wait for phase `parity` of `bar`; false after `limit_ns` nanoseconds.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+// Global -> shared bulk copy completing `bytes` of transaction count on `bar`.
+__device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned bytes,
+                                         unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(sdst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
 
-template <int NS>
-__device__ __forceinline__ void load_slots(const float2 *__restrict__ ptr, float2 (&t)[4]) {
-  if (NS == 4) {
-    const float4 a = __ldcs(reinterpret_cast<const float4 *>(ptr));
-    const float4 b = __ldcs(reinterpret_cast<const float4 *>(ptr) + 1);
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // 1 s per wait
+
+// Loads the four virtual slots [q, My q, Mx q, Mxy q] of this thread's orbit
+// from one staged row.  Degenerate orbits repeat their stored entries:
+// alpha = c: [q, My q, q, My q]; beta = c: [q, q, Mx q, Mx q]; centre: [q]x4.
+// With that padding every thread runs the same 4-slot update (the padded
+// slots compute duplicates that are never written), so warps do not diverge.
+__device__ __forceinline__ void load_orbit(const float2 *ptr, int kind, float2 (&t)[4]) {
+  if (kind == 0) {
+    const float4 a = reinterpret_cast<const float4 *>(ptr)[0];
+    const float4 b = reinterpret_cast<const float4 *>(ptr)[1];
     t[0] = make_float2(a.x, a.y); t[1] = make_float2(a.z, a.w);
     t[2] = make_float2(b.x, b.y); t[3] = make_float2(b.z, b.w);
-  } else if (NS == 2) {
-    const float4 a = __ldcs(reinterpret_cast<const float4 *>(ptr));
-    t[0] = make_float2(a.x, a.y); t[1] = make_float2(a.z, a.w);
+  } else if (kind == 3) {
+    const float2 a = ptr[0];
+    t[0] = a; t[1] = a; t[2] = a; t[3] = a;
   } else {
-    t[0] = __ldcs(ptr);
+    const float4 a = reinterpret_cast<const float4 *>(ptr)[0];
+    const float2 x = make_float2(a.x, a.y), y = make_float2(a.z, a.w);
+    t[0] = x;
+    t[1] = (kind == 1) ? y : x;
+    t[2] = (kind == 1) ? x : y;
+    t[3] = y;
   }
 }
 
-template <int TF, int K>
-__device__ __forceinline__ void mac_rows(const float2 *__restrict__ Pk, const float2 *comb,
-                                         const short4 *rowS, const Layout &L, int g, int G,
-                                         float2 (&U)[TF][4], float2 (&V)[TF][4]) {
-  typedef Orb<K> O;
-  constexpr int NS = O::NS;
-  const int RS = L.RS, NN2 = 2 * L.NN;
-  // generic rows: each stored element t feeds channel i at u, Mxy i at u,
-  // My i at u*, Mx i at u*.
-  constexpr int UNR = 4;
-  int r = g;
-  for (; r + (UNR - 1) * G < L.nrowG; r += UNR * G) {
-    float2 t[UNR][4];
-#pragma unroll
-    for (int w = 0; w < UNR; w++) load_slots<NS>(Pk + (long long)(r + w * G) * RS, t[w]);
-#pragma unroll
-    for (int w = 0; w < UNR; w++) {
-      const short4 si = rowS[r + w * G];
-#pragma unroll
-      for (int tf = 0; tf < TF; tf++) {
-        const float2 *cb = comb + tf * NN2;
-        const float2 s0 = cb[si.x], s1 = cb[si.y], s2 = cb[si.z], s3 = cb[si.w];
-#pragma unroll
-        for (int k = 0; k < NS; k++) {
-          cmac(U[tf][k], t[w][k], s0);
-          cmacc(U[tf][k], t[w][O::sxy(k)], s1);
-          cmac(V[tf][O::sy(k)], t[w][k], s2);
-          cmacc(V[tf][O::sx(k)], t[w][k], s3);
-        }
-      }
-    }
-  }
-  for (; r < L.nrowG; r += G) {
-    float2 t[4];
-    load_slots<NS>(Pk + (long long)r * RS, t);
+// Slot permutations of the orbit [q, My q, Mx q, Mxy q].
+__device__ __forceinline__ constexpr int sy(int k) { return k ^ 1; }
+__device__ __forceinline__ constexpr int sx(int k) { return k ^ 2; }
+__device__ __forceinline__ constexpr int sxy(int k) { return 3 - k; }
+
+// Packed two-lane FP32 arithmetic (sm_100+): one fma.rn.f32x2 performs two
+// independent IEEE fused multiply-adds, halving the issue slots of the
+// complex multiply-accumulate.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};\n" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 unpk(f2x v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;\n" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ void ffma2(f2x &acc, f2x a, f2x b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;\n" : "+l"(acc) : "l"(a), "l"(b));
+}
+
+// Per stored row, the input spectra enter as four packed operand pairs
+// (A_j, B_j), j = 0..3, so that with Tn = (t.x, t.y), Ts = (t.y, t.x)
+//   acc += t * s        is  acc = fma2(Tn, (s.x, s.x)) ; fma2(Ts, (-s.y, s.y))
+//   acc += conj(t) * s  is  acc = fma2(Tn, (s.x,-s.x)) ; fma2(Ts, ( s.y, s.y))
+// sv[tf][row][j] = float4(A_j, B_j); built from comb once per plane.
+__device__ void build_sv(float4 *sv, const float2 *comb, const short4 *rowS, const Layout &L, int TF) {
+  const int nrowT = L.nrowG + L.nrep, NN2 = 2 * L.NN;
+  for (int idx = threadIdx.x; idx < TF * nrowT * 4; idx += blockDim.x) {
+    const int j = idx & 3;
+    const int r = (idx >> 2) % nrowT;
+    const int tf = (idx >> 2) / nrowT;
     const short4 si = rowS[r];
+    const int ci = (j == 0) ? si.x : (j == 1) ? si.y : (j == 2) ? si.z : si.w;
+    bool conj = false, zero = false;
+    if (r < L.nrowG) {
+      conj = (j & 1);                          // s1, s3 multiply conjugated rows
+    } else {
+      const int k2 = r - L.nrowG;
+      const int rk = (k2 < L.c) ? 1 : ((k2 < 2 * L.c) ? 2 : 3);
+      if (rk == 2) conj = (j >= 2);
+      if (rk == 3 && j >= 2) zero = true;
+    }
+    const float2 sc = zero ? make_float2(0.f, 0.f) : comb[tf * NN2 + ci];
+    sv[idx] = conj ? make_float4(sc.x, -sc.x, sc.y, sc.y) : make_float4(sc.x, sc.x, -sc.y, sc.y);
+  }
+}
+
+// One generic stored row t (input channel i at u): feeds channel i at u,
+// Mxy i at u, My i at u*, Mx i at u*.
+template <int TF>
+__device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const float4 *svr, int svstride,
+                                                f2x (&U)[TF][4], f2x (&V)[TF][4]) {
+  f2x Tn[4], Ts[4];
 #pragma unroll
-    for (int tf = 0; tf < TF; tf++) {
-      const float2 *cb = comb + tf * NN2;
-      const float2 s0 = cb[si.x], s1 = cb[si.y], s2 = cb[si.z], s3 = cb[si.w];
+  for (int k = 0; k < 4; k++) { Tn[k] = pk(t[k].x, t[k].y); Ts[k] = pk(t[k].y, t[k].x); }
 #pragma unroll
-      for (int k = 0; k < NS; k++) {
-        cmac(U[tf][k], t[k], s0);
-        cmacc(U[tf][k], t[O::sxy(k)], s1);
-        cmac(V[tf][O::sy(k)], t[k], s2);
-        cmacc(V[tf][O::sx(k)], t[k], s3);
-      }
+  for (int tf = 0; tf < TF; tf++) {
+    const float4 q0 = svr[tf * svstride + 0], q1 = svr[tf * svstride + 1];
+    const float4 q2 = svr[tf * svstride + 2], q3 = svr[tf * svstride + 3];
+    const f2x A0 = pk(q0.x, q0.y), B0 = pk(q0.z, q0.w), A1 = pk(q1.x, q1.y), B1 = pk(q1.z, q1.w);
+    const f2x A2 = pk(q2.x, q2.y), B2 = pk(q2.z, q2.w), A3 = pk(q3.x, q3.y), B3 = pk(q3.z, q3.w);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      ffma2(U[tf][k], Tn[k], A0);
+      ffma2(U[tf][k], Ts[k], B0);
+      ffma2(U[tf][k], Tn[sxy(k)], A1);
+      ffma2(U[tf][k], Ts[sxy(k)], B1);
+      ffma2(V[tf][sy(k)], Tn[k], A2);
+      ffma2(V[tf][sy(k)], Ts[k], B2);
+      ffma2(V[tf][sx(k)], Tn[k], A3);
+      ffma2(V[tf][sx(k)], Ts[k], B3);
     }
   }
-  // centre-cross representatives: rows (u, u*) pairs
-  for (int k2 = g; k2 < L.nrep; k2 += G) {
-    const int rr = L.nrowG + 2 * k2;
-    float2 t[4], s[4];
-    load_slots<NS>(Pk + (long long)rr * RS, t);
-    load_slots<NS>(Pk + (long long)(rr + 1) * RS, s);
-    const short4 si = rowS[L.nrowG + k2];
-    const int rk = (k2 < L.c) ? 1 : ((k2 < 2 * L.c) ? 2 : 3);
+}
+
+// A centre-cross row pair (t at u, s at u*) of representative kind rk.
+template <int TF>
+__device__ __forceinline__ void mac_pair_rows(const float2 (&t)[4], const float2 (&s)[4], int rk,
+                                              const float4 *svr, int svstride, f2x (&U)[TF][4],
+                                              f2x (&V)[TF][4]) {
+  f2x Tn[4], Ts[4], Sn[4], Ss[4];
 #pragma unroll
-    for (int tf = 0; tf < TF; tf++) {
-      const float2 *cb = comb + tf * NN2;
-      const float2 s0 = cb[si.x], s1 = cb[si.y], s2 = cb[si.z], s3 = cb[si.w];
+  for (int k = 0; k < 4; k++) {
+    Tn[k] = pk(t[k].x, t[k].y); Ts[k] = pk(t[k].y, t[k].x);
+    Sn[k] = pk(s[k].x, s[k].y); Ss[k] = pk(s[k].y, s[k].x);
+  }
 #pragma unroll
-      for (int k = 0; k < NS; k++) {
-        cmac(U[tf][k], t[k], s0);
-        cmac(V[tf][k], s[k], s1);
-      }
+  for (int tf = 0; tf < TF; tf++) {
+    const float4 q0 = svr[tf * svstride + 0], q1 = svr[tf * svstride + 1];
+    const f2x A0 = pk(q0.x, q0.y), B0 = pk(q0.z, q0.w), A1 = pk(q1.x, q1.y), B1 = pk(q1.z, q1.w);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      ffma2(U[tf][k], Tn[k], A0);
+      ffma2(U[tf][k], Ts[k], B0);
+      ffma2(V[tf][k], Sn[k], A1);
+      ffma2(V[tf][k], Ss[k], B1);
+    }
+    if (rk != 3) {
+      const float4 q2 = svr[tf * svstride + 2], q3 = svr[tf * svstride + 3];
+      const f2x A2 = pk(q2.x, q2.y), B2 = pk(q2.z, q2.w), A3 = pk(q3.x, q3.y), B3 = pk(q3.z, q3.w);
       if (rk == 1) {
 #pragma unroll
-        for (int k = 0; k < NS; k++) {
-          cmac(V[tf][O::sy(k)], t[k], s2);
-          cmac(U[tf][O::sy(k)], s[k], s3);
+        for (int k = 0; k < 4; k++) {
+          ffma2(V[tf][sy(k)], Tn[k], A2);
+          ffma2(V[tf][sy(k)], Ts[k], B2);
+          ffma2(U[tf][sy(k)], Sn[k], A3);
+          ffma2(U[tf][sy(k)], Ss[k], B3);
         }
-      } else if (rk == 2) {
+      } else {
 #pragma unroll
-        for (int k = 0; k < NS; k++) {
-          cmacc(V[tf][O::sx(k)], t[k], s2);
-          cmacc(U[tf][O::sx(k)], s[k], s3);
+        for (int k = 0; k < 4; k++) {
+          ffma2(V[tf][sx(k)], Tn[k], A2);
+          ffma2(V[tf][sx(k)], Ts[k], B2);
+          ffma2(U[tf][sx(k)], Sn[k], A3);
+          ffma2(U[tf][sx(k)], Ss[k], B3);
         }
       }
     }
   }
 }
 
+// Asynchronous 8-byte global -> shared copy (completes at cp.async.wait_all).
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Stage the input spectra of plane slot `zs` at frequencies u and u* into
+// shared memory: comb[t][i] = S_i[u], comb[t][NN + i] = S_i[u*].
+__device__ __forceinline__ void stage_comb(float2 *comb, const MacParams &p, int TF, int zs, int uy,
+                                           int us, int ux) {
+  const int NN = p.L.NN, ffh = p.f * p.fh;
+  for (int idx = threadIdx.x; idx < TF * NN; idx += blockDim.x) {
+    const int t = idx / NN, i = idx % NN;
+    if (t < p.T) {
+      const float2 *sb = p.S + ((long long)(t * p.nzS + zs) * NN + i) * ffh;
+      cp_async8(comb + t * 2 * NN + i, sb + uy * p.fh + ux);
+      cp_async8(comb + t * 2 * NN + NN + i, sb + us * p.fh + ux);
+    } else {
+      comb[t * 2 * NN + i] = make_float2(0.f, 0.f);
+      comb[t * 2 * NN + NN + i] = make_float2(0.f, 0.f);
+    }
+  }
+  cp_async_commit();
+}
+
+// Shared memory of k_mac: ring | sv | scratch (comb staging, later the
+// row-split reduction) | rowS | mbarriers.
+__host__ __device__ inline size_t mac_scratch_elems(const Layout &L, int TF, int split, bool fwd) {
+  const size_t comb = (size_t)(fwd ? 2 : 1) * TF * 2 * L.NN;               // float2
+  const size_t red = (size_t)(split - 1) * ((L.nthr + 31) / 32 * 32) * 8 * TF;  // f2x = 8 B
+  return comb > red ? comb : red;
+}
+
+size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int split, bool fwd) {
+  return sizeof(float2) * ((size_t)stages * chunk_rows * L.RS + mac_scratch_elems(L, TF, split, fwd)) +
+         sizeof(float4) * (size_t)TF * (L.nrowG + L.nrep) * 4 + sizeof(short4) * (L.nrowG + L.nrep) +
+         2 * sizeof(unsigned long long) * stages + 16;
+}
+
+template <int TF> struct MacOcc { static constexpr int v = 2; };
+template <> struct MacOcc<4> { static constexpr int v = 1; };
+
+// One CTA = one frequency pair and a group of planes.  Thread (h, o) owns the
+// mirror orbit o of output channels for the rows of its share h (rows are
+// dealt round-robin to the `split` threads of an orbit; their partial sums
+// are added through shared memory when a plane's output is due), so there is
+// no atomic and every output is written by exactly one thread.
+// The stored rows stream through a ring of shared-memory stages filled by
+// bulk copies (thread 0 issues them `stages-1` chunks ahead, crossing plane
+// boundaries); consumers read their orbit's slots with shared loads.
+// Forward projection accumulates the planes of the group (the group sums are
+// added by the inverse transform); back projection writes each plane's
+// spectra when the plane is done.  The spectra of the next plane are staged
+// with cp.async while the current plane streams.
 template <int TF, bool FWD>
-__global__ void __launch_bounds__(512) k_mac(MacParams p) {
+__global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_abort;
+  volatile int *abortf = &s_abort;
   const Layout &L = p.L;
-  const int NN = L.NN, NT = L.nthr, c = L.c, c2 = c * c;
-  float2 *comb = reinterpret_cast<float2 *>(smraw);                 // [TF][2 NN]
-  short4 *rowS = reinterpret_cast<short4 *>(comb + TF * 2 * NN);   // [nrowG + nrep]
-  float *red = reinterpret_cast<float *>(rowS + (L.nrowG + L.nrep));  // [G][NT][16]
-  for (int i = threadIdx.x; i < L.nrowG + L.nrep; i += blockDim.x) rowS[i] = p.rowS[i];
+  const int NN = L.NN, NT = L.nthr, c = L.c, c2 = c * c, RS = L.RS, NN2 = 2 * L.NN;
+  const int CH = p.chunk_rows, NST = p.stages, H = p.split;
+  const int NTP = (NT + 31) / 32 * 32;
+  const int nrowT = L.nrowG + L.nrep;
+  float2 *ring = reinterpret_cast<float2 *>(smraw);                          // [NST][CH*RS]
+  float4 *sv = reinterpret_cast<float4 *>(ring + (size_t)NST * CH * RS);     // [TF][nrowT][4]
+  float2 *scratch = reinterpret_cast<float2 *>(sv + TF * nrowT * 4);        // comb [1|2][TF][2NN] / red
+  f2x *red = reinterpret_cast<f2x *>(scratch);                              // [H-1][NTP][TF][8]
+  short4 *rowS = reinterpret_cast<short4 *>(scratch + mac_scratch_elems(L, TF, H, FWD));
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(rowS + nrowT);
+  unsigned long long *empty = full + NST;
+
+  const int tid = threadIdx.x;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  if (tid == 0) {
+    for (int i = 0; i < NST; i++) {
+      mbar_init(full + i, 1);
+      mbar_init(empty + i, nwarps);
+    }
+    *abortf = 0;
+    fence_mbar_init();
+  }
+  for (int i = tid; i < nrowT; i += blockDim.x) rowS[i] = p.rowS[i];
 
   const int kp = blockIdx.x;
   const int uy = kp / p.fq, ux = kp % p.fq;
   const int us = uy ? p.f - uy : 0;
   const bool selfp = (us == uy);
   const int ffh = p.f * p.fh;
-  const int tid = threadIdx.x;
-  const int g = tid / NT, o = tid % NT;
-  const bool active = g < p.G;
+  const int h = tid / NTP, o = tid - h * NTP;
+  const bool active = o < NT;
   const int kind = (o < c2) ? 0 : ((o < c2 + c) ? 1 : ((o < c2 + 2 * c) ? 2 : 3));
-  const int slotbase = (kind == 0) ? 4 * o
+  const int slotbase = !active ? 0
+                      : (kind == 0) ? 4 * o
                       : (kind == 1) ? 4 * c2 + 2 * (o - c2)
                       : (kind == 2) ? 4 * c2 + 2 * c + 2 * (o - c2 - c)
                                     : NN - 1;
+  const int ns = (kind == 0) ? 4 : ((kind == 3) ? 1 : 2);
+  const int z0 = blockIdx.y * p.zgroup;
+  const int z1 = min(z0 + p.zgroup, p.nz);
+  const int cpb = (L.nrow + CH - 1) / CH;            // chunks per (frequency pair, plane) block
+  const int total = (z1 - z0) * cpb;
+  const size_t blockElems = (size_t)L.nrow * RS;
 
-  float2 U[TF][4], V[TF][4];
+  f2x U[TF][4], V[TF][4];
 #pragma unroll
   for (int tf = 0; tf < TF; tf++)
 #pragma unroll
-    for (int k = 0; k < 4; k++) { U[tf][k] = make_float2(0.f, 0.f); V[tf][k] = make_float2(0.f, 0.f); }
+    for (int k = 0; k < 4; k++) { U[tf][k] = 0ull; V[tf][k] = 0ull; }
 
-  int z0, z1;
-  if (FWD) { z0 = blockIdx.y * p.zgroup; z1 = min(z0 + p.zgroup, p.nz); }
-  else { z0 = blockIdx.y; z1 = z0 + 1; }
+  stage_comb(scratch, p, TF, FWD ? z0 : 0, uy, us, ux);
+  cp_async_wait_all();
+  __syncthreads();   // barriers initialised, rowS and first spectra staged
+  build_sv(sv, scratch, rowS, L, TF);
+  __syncthreads();   // (back projection: the staging area is free for the reduction)
 
-  for (int zi = z0; zi < z1; zi++) {
-    __syncthreads();
-    const int zs = FWD ? zi : 0;
-    for (int idx = tid; idx < TF * NN; idx += blockDim.x) {
-      const int t = idx / NN, i = idx % NN;
-      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-      if (t < p.T) {
-        const float2 *sb = p.S + ((long long)(t * p.nzS + zs) * NN + i) * ffh;
-        a = sb[uy * p.fh + ux];
-        b = sb[us * p.fh + ux];
-      }
-      comb[t * 2 * NN + i] = a;
-      comb[t * 2 * NN + NN + i] = b;
-    }
-    __syncthreads();
-    if (active) {
-      const int plane = p.planes[zi];
-      const float2 *Pk = p.P + ((long long)plane * p.nkp + kp) * (long long)L.nrow * L.RS + slotbase;
-      switch (kind) {
-        case 0: mac_rows<TF, 0>(Pk, comb, rowS, L, g, p.G, U, V); break;
-        case 1: mac_rows<TF, 1>(Pk, comb, rowS, L, g, p.G, U, V); break;
-        case 2: mac_rows<TF, 2>(Pk, comb, rowS, L, g, p.G, U, V); break;
-        default: mac_rows<TF, 3>(Pk, comb, rowS, L, g, p.G, U, V); break;
-      }
-    }
+  // producer: chunk g -> ring slot g % NST
+  int issued = 0;
+  auto issue = [&](int g) {
+    const int zl = g / cpb, ch = g - zl * cpb;
+    const int plane = p.planes[z0 + zl];
+    const int r0 = ch * CH;
+    const int nr = min(CH, L.nrow - r0);
+    const float2 *src = p.P + ((long long)plane * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
+    const int slot = g % NST;
+    const unsigned bytes = (unsigned)(nr * RS * sizeof(float2));
+    mbar_arrive_expect_tx(full + slot, bytes);
+    bulk_g2s(ring + (size_t)slot * CH * RS, src, bytes, full + slot);
+  };
+  if (tid == 0) {
+    const int pre = min(NST - 1, total);
+    for (int g = 0; g < pre; g++) issue(g);
+    issued = pre;
   }
 
-  const int ns = (kind == 0) ? 4 : ((kind == 3) ? 1 : 2);
-  const int zo = FWD ? blockIdx.y : z0;
-#pragma unroll
-  for (int tf = 0; tf < TF; tf++) {
-    __syncthreads();
-    if (active) {
-      float *rp = red + (g * NT + o) * 16;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        rp[2 * k] = U[tf][k].x; rp[2 * k + 1] = U[tf][k].y;
-        rp[8 + 2 * k] = V[tf][k].x; rp[8 + 2 * k + 1] = V[tf][k].y;
+  bool dead = false;
+  for (int g = 0; g < total; g++) {
+    const int zl = g / cpb, ch = g - zl * cpb;
+    const int zi = z0 + zl;
+    if (FWD && ch == 0) {
+      if (zl > 0) {
+        cp_async_wait_all();
+        __syncthreads();   // spectra of plane zi staged; all threads done with plane zi-1
+        build_sv(sv, scratch + (zl & 1) * TF * NN2, rowS, L, TF);
+        __syncthreads();
       }
+      if (zi + 1 < z1) stage_comb(scratch + ((zl + 1) & 1) * TF * NN2, p, TF, zi + 1, uy, us, ux);
     }
-    __syncthreads();
-    if (g == 0 && tf < p.T) {
-      float s[16];
-#pragma unroll
-      for (int e = 0; e < 16; e++) s[e] = 0.f;
-      for (int gg = 0; gg < p.G; gg++) {
-        const float *rp = red + (gg * NT + o) * 16;
-#pragma unroll
-        for (int e = 0; e < 16; e++) s[e] += rp[e];
-      }
-      long long obase;
-      if (FWD) obase = ((long long)(zo * p.T + tf) * NN) * ffh;
-      else obase = ((long long)(tf * p.nzo + zo) * NN) * ffh;
-      for (int k = 0; k < ns; k++) {
-        const int q = p.slotcol[slotbase + k];
-        float2 *op = p.O + obase + (long long)q * ffh;
-        if (selfp) {
-          op[uy * p.fh + ux] = make_float2(s[2 * k] + s[8 + 2 * k], s[2 * k + 1] + s[8 + 2 * k + 1]);
-        } else {
-          op[uy * p.fh + ux] = make_float2(s[2 * k], s[2 * k + 1]);
-          op[us * p.fh + ux] = make_float2(s[8 + 2 * k], s[8 + 2 * k + 1]);
+    if (*abortf) dead = true;
+    // producer step: refill the slot freed by chunk g-1 with chunk g+NST-1
+    if (tid == 0 && !dead && issued < total) {
+      const int gn = issued;
+      if (gn >= NST) {
+        const int slot = gn % NST;
+        if (!mbar_wait(empty + slot, ((gn / NST) - 1) & 1, kWaitLimitNs)) {
+          dead = true;
+          *abortf = 1;
+          atomicExch(p.err, 1);
         }
       }
+      if (!dead) { issue(gn); issued = gn + 1; }
+    }
+    const int slot = g % NST;
+    if (!dead && !mbar_wait(full + slot, (g / NST) & 1, kWaitLimitNs)) {
+      dead = true;
+      *abortf = 1;
+      atomicExch(p.err, 2);
+    }
+    if (!dead && active) {
+      const int r0 = ch * CH;
+      const int r1 = min(L.nrow, r0 + CH);
+      const float2 *stage = ring + (size_t)slot * CH * RS + slotbase;
+      const int rg = min(r1, L.nrowG);
+      const int svs = nrowT * 4;
+#pragma unroll 2
+      for (int r = r0 + h; r < rg; r += H) {
+        float2 t[4];
+        load_orbit(stage + (size_t)(r - r0) * RS, kind, t);
+        mac_generic_row<TF>(t, sv + r * 4, svs, U, V);
+      }
+      // centre-cross row pairs of this chunk, dealt round-robin over the split
+      const int pr0 = max(r0, L.nrowG);
+      for (int r = pr0 + 2 * h; r < r1; r += 2 * H) {
+        const int k2 = (r - L.nrowG) >> 1;
+        float2 t[4], s2[4];
+        load_orbit(stage + (size_t)(r - r0) * RS, kind, t);
+        load_orbit(stage + (size_t)(r + 1 - r0) * RS, kind, s2);
+        const int rk = (k2 < c) ? 1 : ((k2 < 2 * c) ? 2 : 3);
+        mac_pair_rows<TF>(t, s2, rk, sv + (L.nrowG + k2) * 4, svs, U, V);
+      }
+    }
+    __syncwarp();
+    if ((tid & 31) == 0 && !dead) mbar_arrive(empty + slot);
+
+    const bool out_due = (ch == cpb - 1) && (!FWD || zi + 1 == z1);
+    if (out_due) {
+      if (H > 1) {
+        // add the partial sums of the other row shares into share 0
+        if (FWD) cp_async_wait_all();   // the staging area doubles as reduction buffer
+        __syncthreads();
+        if (h > 0 && active) {
+          f2x *rp = red + ((size_t)(h - 1) * NTP + o) * TF * 8;
+#pragma unroll
+          for (int tf = 0; tf < TF; tf++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) { rp[tf * 8 + k] = U[tf][k]; rp[tf * 8 + 4 + k] = V[tf][k]; }
+        }
+        __syncthreads();
+        if (h == 0 && active) {
+          for (int hh = 1; hh < H; hh++) {
+            const f2x *rp = red + ((size_t)(hh - 1) * NTP + o) * TF * 8;
+#pragma unroll
+            for (int tf = 0; tf < TF; tf++)
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                const float2 a = unpk(U[tf][k]), b = unpk(rp[tf * 8 + k]);
+                const float2 cc2 = unpk(V[tf][k]), d = unpk(rp[tf * 8 + 4 + k]);
+                U[tf][k] = pk(a.x + b.x, a.y + b.y);
+                V[tf][k] = pk(cc2.x + d.x, cc2.y + d.y);
+              }
+          }
+        }
+      }
+      if (h == 0 && active && !dead) {
+#pragma unroll
+        for (int tf = 0; tf < TF; tf++) {
+          if (tf >= p.T) break;
+          const long long obase = FWD ? ((long long)(blockIdx.y * p.T + tf) * NN) * ffh
+                                      : ((long long)(tf * p.nzo + zi) * NN) * ffh;
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const int vk = (kind == 2) ? ((k & 1) ? 2 : 0) : k;   // stored slot k -> virtual slot
+            if (k < ns) {
+              const int q = p.slotcol[slotbase + k];
+              float2 *op = p.O + obase + (long long)q * ffh;
+              float2 u = unpk(U[tf][0]), v = unpk(V[tf][0]);
+#pragma unroll
+              for (int m = 1; m < 4; m++)
+                if (m == vk) { u = unpk(U[tf][m]); v = unpk(V[tf][m]); }
+              if (selfp) {
+                op[uy * p.fh + ux] = make_float2(u.x + v.x, u.y + v.y);
+              } else {
+                op[uy * p.fh + ux] = u;
+                op[us * p.fh + ux] = v;
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int tf = 0; tf < TF; tf++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) { U[tf][k] = 0ull; V[tf][k] = 0ull; }
+      if (H > 1) __syncthreads();   // the reduction buffer is free again
     }
   }
+  // Never leave a bulk copy in flight into this CTA's shared memory.
+  if (tid == 0 && dead) {
+    for (int g = max(0, issued - NST); g < issued; g++) mbar_wait(full + (g % NST), (g / NST) & 1, kWaitLimitNs / 10);
+  }
+  cp_async_wait_all();
 }
 
 // ----------------------------------------------------------------------------
@@ -661,11 +903,9 @@ int mac_max_frames() { return 4; }
 
 template <int TF>
 static cudaError_t launch_mac_tf(const MacParams &p, bool fwd, cudaStream_t s) {
-  const Layout &L = p.L;
-  const size_t sm = sizeof(float2) * TF * 2 * L.NN + sizeof(short4) * (L.nrowG + L.nrep) +
-                    sizeof(float) * (size_t)p.G * L.nthr * 16;
-  dim3 grid(p.nkp, p.nzo);
-  const int block = p.G * L.nthr;
+  const size_t sm = mac_smem_bytes(p.L, TF, p.stages, p.chunk_rows, p.split, fwd);
+  dim3 grid(p.nkp, p.nzo_grid);
+  const int block = p.split * (((p.L.nthr + 31) / 32) * 32);
   cudaError_t e;
   if (fwd) {
     if ((e = set_smem((const void *)k_mac<TF, true>, sm)) != cudaSuccess) return e;

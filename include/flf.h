@@ -124,6 +124,18 @@ int flf_geometry(const flf_ctx *ctx, int *out4);
 int flf_profile(flf_ctx *ctx, int enable);
 int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
 
+/* Tunable launch parameters (the GB300 counterpart of the reference's
+ * block-shape knobs gBlockSelection / gCalculateRowsBlocks,
+ * projector.py:26-36).  Options: "mac_stages" (shared-memory pipeline
+ * stages of the multiply-accumulate, 2..16) and "mac_chunk_rows" (stored
+ * rows per stage, even, 2..64).  Results do not depend on them. */
+int flf_set_option(flf_ctx *ctx, const char *name, long long value);
+
+/* Wait for `stream` and report any failure of earlier launches, including a
+ * bounded device-side wait that gave up (FLF_E_TIMEOUT).  Counterpart of the
+ * reference's synchronous return from ProjectForZList. */
+int flf_synchronize(flf_ctx *ctx, void *stream);
+
 /* Library self-description for diagnostics: writes a short text (build
  * arch, kernel list) into buf. */
 int flf_version(char *buf, size_t len);
