@@ -42,7 +42,9 @@ _SIGS = {
     "flf_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "flf_set_option": (_I, [_P, ctypes.c_char_p, ctypes.c_longlong]),
     "flf_synchronize": (_I, [_P, _P]),
+    "flf_backward_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
 }
+NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 
 _lib = None
 
@@ -157,6 +159,11 @@ class Context:
         self._check(self._lib.flf_backward(self._h, _ptr(img), _ptr(vol), int(T), int(Y), int(X),
                                            p, n, _ptr(stream)))
         del keep
+
+    def backward_noalloc(self, img, vol, T, Y, X, stream=None):
+        """Back projection over all planes that allocates no device memory (see include/flf.h)."""
+        self._check(self._lib.flf_backward_noalloc(self._h, _ptr(img), _ptr(vol), int(T), int(Y), int(X),
+                                                   _ptr(stream)))
 
     def rl_iterate(self, x, ref, norm, variant, iters, T, Y, X, stream=None):
         self._check(self._lib.flf_rl_iterate(self._h, _ptr(x), _ptr(ref), _ptr(norm), int(variant),

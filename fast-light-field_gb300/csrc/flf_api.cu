@@ -527,6 +527,33 @@ int backward_chunk(flf_ctx *ctx, const float *img, const int *d_planes, int npla
   return FLF_OK;
 }
 
+// ----------------------------------------------------------------------------
+// Fixed scratch for flf_backward_noalloc: a file-scope device array, so that
+// entry point never asks the driver for memory.  Every GPU that loads this
+// library holds FLF_NOALLOC_SCRATCH_BYTES of it until the process exits.
+// ----------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FLF_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+void *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (`device`).
+// The host-side symbol is only a stand-in and must never reach a kernel; the
+// real address is looked up once per device, with that device current.
+int noalloc_scratch(flf_ctx *ctx, int device, void **out) {
+  if (device < 0 || device >= kMaxDevices)
+    return fail(ctx, FLF_E_ARG, "device %d beyond the %d devices the fixed scratch supports", device, kMaxDevices);
+  if (!g_noalloc_ptr[device]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(ctx, FLF_E_CUDA, "cudaGetSymbolAddress of the fixed scratch failed: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[device] = ptr;
+  }
+  *out = g_noalloc_ptr[device];
+  return FLF_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -685,6 +712,68 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
                         Strided{nullptr, 0, 0}, EPI_STORE, s);
   }
   return rc;
+}
+
+int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X,
+                         void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  if (!vol_dev || !img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
+  if (T <= 0) return fail(ctx, FLF_E_ARG, "frame count must be positive (got %d)", T);
+  cudaSetDevice(ctx->device);
+  if (int rc0 = check_device_flag(ctx)) return rc0;
+  Geometry &G = ctx->geo;
+  if (!G.valid || G.Y != Y || G.X != X || !G.built[FLF_DIR_BACKWARD])
+    return fail(ctx, FLF_E_STATE,
+                "flf_backward_noalloc needs transfer matrices for %d x %d built beforehand: call flf_prepare "
+                "with this image shape first", Y, X);
+  const Layout &L = ctx->L;
+  const int NN = L.NN, ffh = G.f * G.fh, nz = ctx->nz;
+  const size_t spec = sizeof(float2) * (size_t)NN * ffh;   // one frame (or one plane) of spectra
+  if (2 * spec > FLF_NOALLOC_SCRATCH_BYTES)
+    return fail(ctx, FLF_E_ARG,
+                "flf_backward_noalloc needs %zu bytes of scratch for this geometry (Nnum %d, transform %d), "
+                "more than its fixed %u bytes; use flf_backward", 2 * spec, ctx->N, G.f,
+                (unsigned)FLF_NOALLOC_SCRATCH_BYTES);
+  void *scratch = nullptr;
+  int rc = noalloc_scratch(ctx, ctx->device, &scratch);
+  if (rc != FLF_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  float2 *S = (float2 *)scratch;                       // channel spectra of the current frame
+  float2 *O = (float2 *)((char *)scratch + spec);      // output spectra of a group of planes
+  const int zb = std::max(1, std::min(nz, (int)((FLF_NOALLOC_SCRATCH_BYTES - spec) / spec)));
+  const long long YX = (long long)Y * X;
+  for (int t = 0; t < T; t++) {
+    Rfft2Params rp{};
+    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
+    rp.nimg = NN; rp.nz = 1; rp.mode = 0;
+    rp.src = img_dev + t * YX; rp.src_sz = 0; rp.src_st = YX;
+    rp.planes = ctx->d_zero; rp.dst = S; rp.twiddle = G.tw;
+    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
+    cudaError_t e = launch_rfft2(rp, 0, s);
+    for (int z0 = 0; z0 < nz && e == cudaSuccess; z0 += zb) {
+      const int nzl = std::min(zb, nz - z0);
+      const int zg = zgroup_for(ctx, nzl);
+      MacParams mp{};
+      mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = 1;
+      mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = ctx->d_planes_all + z0; mp.nz = nzl; mp.zgroup = zg;
+      mp.S = S; mp.nzS = 1; mp.O = O; mp.nzo = nzl; mp.nzo_grid = (nzl + zg - 1) / zg;
+      mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
+      mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split;
+      mp.err = ctx->d_err;
+      e = launch_mac(mp, false, s);
+      if (e != cudaSuccess) break;
+      Irfft2Params ip{};
+      ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
+      ip.nimg = nzl * NN; ip.nzo = nzl; ip.src = O; ip.sum_stride = 0; ip.nsum = 1;
+      ip.planes = ctx->d_planes_all + z0; ip.epi = EPI_STORE;
+      ip.out = Strided{vol_dev + t * YX, (long long)T * YX, YX};
+      ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
+      ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+      e = launch_irfft2(ip, s);
+    }
+    if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "flf_backward_noalloc launch failed: %s", cudaGetErrorString(e));
+  }
+  return FLF_OK;
 }
 
 int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev,

@@ -92,6 +92,33 @@ int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y
 int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y,
                  int X, const int *planes, int nplanes, void *stream);
 
+/* Size of the fixed device scratch used by flf_backward_noalloc. */
+#define FLF_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* Back projection that allocates nothing: the same result as flf_backward
+ * over all planes, for callers that cannot ask the CUDA driver for memory
+ * while they run - for example a real-time acquisition loop that must never
+ * wait on the device allocator, or a plug-in whose host application hands
+ * out all device memory from its own pool and forbids cudaMalloc.  This entry
+ * point has no counterpart in the reference.
+ *  - The caller passes the image and the output volume; the transfer matrices
+ *    must already exist for this Y x X (call flf_prepare earlier), otherwise
+ *    FLF_E_STATE is returned instead of building them.
+ *  - The intermediate spectra live in one fixed device array of
+ *    FLF_NOALLOC_SCRATCH_BYTES (16 MiB) inside the library: one frame of
+ *    channel spectra plus the output spectra of as many planes as fit.  Every
+ *    GPU that loads the library holds this array until the process exits.
+ *    Geometries that need more (2 * Nnum^2 * f * (f/2+1) * 8 bytes, e.g. the
+ *    1005 x 1005 full field) are rejected with FLF_E_ARG; use flf_backward.
+ *  - The first call on each device looks up the array's device address (a
+ *    one-time set-up with that device current); make that first call before
+ *    any stream capture.
+ *  - All calls share the one array and nothing in it needs to start at zero
+ *    (every element read is written first by the same call); calls whose
+ *    work overlaps on the GPU, on any stream or context, race on it. */
+int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y,
+                         int X, void *stream);
+
 /* `iters` Richardson-Lucy iterations in place on x_dev [Z][T][Y][X] over all
  * planes of the context (the loop of DeconvRL, lfdeconv.py:185-196).
  *  FLF_RL_PREVEDEL: ref_dev = Htf [Z][T][Y][X]; norm_dev ignored.
