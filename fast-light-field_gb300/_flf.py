@@ -199,4 +199,4 @@ class Context:
     def geometry(self):
         out = (ctypes.c_int * 4)()
         self._check(self._lib.flf_geometry(self._h, out))
-        return {"f": out[0], "R": out[1], "fp64": bool(out[2]), "freq_pairs": out[3]}
+        return {"f": out[0], "R": out[1], "fp64": bool(out[2]), "groups": out[3]}

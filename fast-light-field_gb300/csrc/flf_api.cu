@@ -24,14 +24,36 @@ struct Workspace {
   size_t bytes = 0;
 };
 
-struct Geometry {
-  bool valid = false;
-  int Y = 0, X = 0, Ly = 0, Lx = 0, f = 0, fh = 0, fq = 0, nkp = 0, R = 0, fp64 = 0;
+// Planes sharing one lenslet-grid transform size.  Every plane uses the
+// smallest size its own kernel radius allows; planes with equal sizes share
+// one group (one set of launches per projection).
+struct Group {
+  int f = 0, fh = 0, fq = 0, nkp = 0, R = 0;
   FftPlan plan{};
   float2 *tw = nullptr;       // float twiddles [f]
   double2 *tw64 = nullptr;    // double twiddles [f]
-  float2 *P[2] = {nullptr, nullptr};
+  float2 *P[2] = {nullptr, nullptr};   // packed matrices [slot][nkp][nrow][RS]
   bool built[2] = {false, false};
+  std::vector<int> planes;    // plane ids of the group, ascending (slot = index)
+  int *d_ids = nullptr;       // device copy of `planes`
+  int *d_slots = nullptr;     // 0..n-1
+};
+
+struct Geometry {
+  bool valid = false;
+  int Y = 0, X = 0, Ly = 0, Lx = 0, fp64 = 0, uniform_f = 0;
+  std::vector<Group> groups;
+  std::vector<int> plane_group, plane_slot;
+  bool built(int dir) const {
+    for (const Group &g : groups)
+      if (!g.built[dir]) return false;
+    return !groups.empty();
+  }
+  int max_f() const {
+    int m = 0;
+    for (const Group &g : groups) m = std::max(m, g.f);
+    return m;
+  }
 };
 
 }  // namespace
@@ -47,7 +69,7 @@ struct flf_ctx {
   short *d_slotcol = nullptr, *d_colslot = nullptr;
   int *d_rep_ch = nullptr, *d_rep_row = nullptr, *d_rep_kind = nullptr;
   int *d_planes_all = nullptr;
-  int *d_planes_user = nullptr;
+  int *d_planes_user = nullptr;   // per-call plane subsets: ids then slots, per group
   int planes_user_cap = 0;
   int *d_zero = nullptr;
   std::vector<int> rep_ch, rep_row, rep_kind;
@@ -57,6 +79,7 @@ struct flf_ctx {
   int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
   int opt_chunk_rows = 8;        // tunable: stored rows per pipeline stage
   int opt_split = 2;             // tunable: threads sharing one orbit's rows
+  int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
   int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
@@ -186,12 +209,13 @@ int ensure_ws(flf_ctx *ctx, Workspace &w, size_t bytes) {
   return FLF_OK;
 }
 
-void free_geometry(Geometry &g) {
-  if (g.tw) cudaFree(g.tw);
-  if (g.tw64) cudaFree(g.tw64);
-  for (int d = 0; d < 2; d++)
-    if (g.P[d]) cudaFree(g.P[d]);
-  g = Geometry();
+void free_geometry(Geometry &G) {
+  for (Group &g : G.groups) {
+    void *ptrs[] = {g.tw, g.tw64, g.P[0], g.P[1], g.d_ids, g.d_slots};
+    for (void *p : ptrs)
+      if (p) cudaFree(p);
+  }
+  G = Geometry();
 }
 
 // Host-side index tables of the packed layout (see flf_internal.cuh).
@@ -268,16 +292,12 @@ int imgs_per_cta(int f, int fp64, size_t budget) {
   return b;
 }
 
-// Transfer matrices of one direction for all uploaded planes.
-int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
-  Geometry &G = ctx->geo;
+// Transfer matrices of one direction for the planes of one group.
+int build_group(flf_ctx *ctx, Group &G, int fp64, int dir, cudaStream_t s) {
   const Layout &L = ctx->L;
-  const int NN = L.NN, f = G.f, fh = G.fh;
-  for (int z = 0; z < ctx->nz; z++)
-    if (!ctx->dH[dir][z])
-      return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, dir);
+  const int NN = L.NN, f = G.f, fh = G.fh, ng = (int)G.planes.size();
   const size_t plane_elems = (size_t)G.nkp * L.nrow * L.RS;
-  const size_t bytes = plane_elems * ctx->nz * sizeof(float2);
+  const size_t bytes = plane_elems * ng * sizeof(float2);
   if (!G.P[dir]) {
     cudaError_t e = cudaMalloc(&G.P[dir], bytes);
     if (e != cudaSuccess) {
@@ -288,7 +308,6 @@ int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
     }
   }
   CUDA_TRY(ctx, cudaMemsetAsync(G.P[dir], 0, bytes, s));
-  const int fp64 = G.fp64;
   const size_t rsz = fp64 ? sizeof(double) : sizeof(float);
   const size_t per_rep = (size_t)NN * ((size_t)f * f * rsz + (size_t)f * fh * 2 * rsz);
   const int nrepAll = (int)ctx->rep_ch.size();
@@ -302,7 +321,8 @@ int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
     return rc;
   }
   const int ipc = imgs_per_cta(f, fp64, 200 * 1024);
-  for (int z = 0; z < ctx->nz && rc == FLF_OK; z++) {
+  for (int sl = 0; sl < ng && rc == FLF_OK; sl++) {
+    const int z = G.planes[sl];
     const int hh = ctx->h[dir][z];
     for (int r0 = 0; r0 < nrepAll && rc == FLF_OK; r0 += chunk) {
       const int nr = std::min(chunk, nrepAll - r0);
@@ -325,10 +345,9 @@ int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
         pp.spec = wspec.p; pp.rep0 = r0; pp.nrep_chunk = nr;
         pp.rep_row = ctx->d_rep_row; pp.rep_kind = ctx->d_rep_kind; pp.rep_ch = ctx->d_rep_ch;
         pp.col_slot = ctx->d_colslot;
-        pp.P = G.P[dir] + plane_elems * z;
+        pp.P = G.P[dir] + plane_elems * sl;
         pp.scale = 1.0 / ((double)f * (double)f);
         pp.fp64 = fp64;
-        // pack writes rows of the chunk's representatives only
         e = launch_pack(pp, s);
       }
       if (e != cudaSuccess)
@@ -344,58 +363,121 @@ int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
   return FLF_OK;
 }
 
-int prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
-  if (Y <= 0 || X <= 0) return fail(ctx, FLF_E_ARG, "image shape must be positive (got %d x %d)", Y, X);
-  const int N = ctx->N;
-  const int Ly = (Y + N - 1) / N, Lx = (X + N - 1) / N;
+// Transfer matrices of one direction for all uploaded planes.
+int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
+  for (int z = 0; z < ctx->nz; z++)
+    if (!ctx->dH[dir][z])
+      return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, dir);
+  for (Group &g : ctx->geo.groups)
+    if (!g.built[dir])
+      if (int rc = build_group(ctx, g, ctx->geo.fp64, dir, s)) return rc;
+  return FLF_OK;
+}
+
+int smooth_at_least(int n) {
+  int f = std::max(n, 2);
+  while (!is_smooth_even(f)) f++;
+  return f;
+}
+
+int plane_radius(const flf_ctx *ctx, int z) {
   int R = 0;
   for (int d = 0; d < 2; d++)
-    for (int z = 0; z < ctx->nz; z++)
-      if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
-  int f;
+    if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
+  return R;
+}
+
+int prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
+  if (Y <= 0 || X <= 0) return fail(ctx, FLF_E_ARG, "image shape must be positive (got %d x %d)", Y, X);
+  const int N = ctx->N, nz = ctx->nz;
+  const int Ly = (Y + N - 1) / N, Lx = (X + N - 1) / N, Lm = std::max(Ly, Lx);
+  int Rmax = 0;
+  for (int z = 0; z < nz; z++) Rmax = std::max(Rmax, plane_radius(ctx, z));
+  std::vector<int> fz(nz);
   if (fft_size > 0) {
-    f = fft_size;
-    if (!is_smooth_even(f))
-      return fail(ctx, FLF_E_ARG, "fft_size %d must be even with prime factors in {2,3,5,7}", f);
-    if (f < std::max(Ly, Lx) + R || f < 2 * R + 1)
-      return fail(ctx, FLF_E_ARG, "fft_size %d too small: need >= %d", f, std::max(std::max(Ly, Lx) + R, 2 * R + 1));
+    if (!is_smooth_even(fft_size))
+      return fail(ctx, FLF_E_ARG, "fft_size %d must be even with prime factors in {2,3,5,7}", fft_size);
+    const int need = std::max(Lm + Rmax, 2 * Rmax + 1);
+    if (fft_size < need) return fail(ctx, FLF_E_ARG, "fft_size %d too small: need >= %d", fft_size, need);
+    std::fill(fz.begin(), fz.end(), fft_size);
+  } else if (!ctx->opt_plane_sizes) {
+    std::fill(fz.begin(), fz.end(), smooth_at_least(std::max(Lm + Rmax, 2 * Rmax + 1)));
   } else {
-    f = std::max(std::max(Ly, Lx) + R, 2 * R + 1);
-    while (!is_smooth_even(f)) f++;
+    for (int z = 0; z < nz; z++) {
+      const int R = plane_radius(ctx, z);
+      fz[z] = smooth_at_least(std::max(Lm + R, 2 * R + 1));
+    }
   }
-  if (f > kMaxF)
+  const int fmax = *std::max_element(fz.begin(), fz.end());
+  if (fmax > kMaxF)
     return fail(ctx, FLF_E_ARG, "lenslet-grid transform size %d exceeds the supported maximum %d "
-                "(image %d x %d, Nnum %d, kernel radius %d lenslets)", f, kMaxF, Y, X, N, R);
-  if (fp64 && f > kMaxF64) fp64 = 0;   // double buffers do not fit shared memory
+                "(image %d x %d, Nnum %d, kernel radius %d lenslets)", fmax, kMaxF, Y, X, N, Rmax);
+  if (fp64 && fmax > kMaxF64) fp64 = 0;   // double buffers do not fit shared memory
   Geometry &G = ctx->geo;
-  if (G.valid && G.f == f && G.Ly == Ly && G.Lx == Lx && G.R == R && G.fp64 == fp64) {
-    G.Y = Y; G.X = X;
-    return FLF_OK;
+  if (G.valid && G.Ly == Ly && G.Lx == Lx && G.fp64 == fp64 && (int)G.plane_group.size() == nz) {
+    bool same = true;
+    for (int z = 0; z < nz && same; z++) same = (G.groups[G.plane_group[z]].f == fz[z]);
+    if (same) {
+      G.Y = Y; G.X = X;
+      return FLF_OK;
+    }
   }
   free_geometry(G);
-  G.Y = Y; G.X = X; G.Ly = Ly; G.Lx = Lx; G.R = R; G.f = f; G.fh = f / 2 + 1; G.fq = f / 2 + 1;
-  G.nkp = G.fq * G.fq; G.fp64 = fp64;
-  G.plan = make_plan(f);
-  std::vector<float2> tw(f);
-  std::vector<double2> tw64(f);
-  for (int k = 0; k < f; k++) {
-    // exp(-2 pi i k / f) in double, rounded once
-    const double ang = -2.0 * M_PI * (double)k / (double)f;
-    tw64[k] = make_double2(std::cos(ang), std::sin(ang));
-    tw[k] = make_float2((float)tw64[k].x, (float)tw64[k].y);
+  G.Y = Y; G.X = X; G.Ly = Ly; G.Lx = Lx; G.fp64 = fp64; G.uniform_f = fft_size;
+  G.plane_group.assign(nz, -1);
+  G.plane_slot.assign(nz, -1);
+  std::vector<int> sizes(fz);
+  std::sort(sizes.begin(), sizes.end());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  for (int f : sizes) {
+    Group g;
+    g.f = f; g.fh = f / 2 + 1; g.fq = f / 2 + 1; g.nkp = g.fq * g.fq;
+    g.plan = make_plan(f);
+    for (int z = 0; z < nz; z++)
+      if (fz[z] == f) {
+        G.plane_group[z] = (int)G.groups.size();
+        G.plane_slot[z] = (int)g.planes.size();
+        g.planes.push_back(z);
+        g.R = std::max(g.R, plane_radius(ctx, z));
+      }
+    G.groups.push_back(g);
   }
-  CUDA_TRY(ctx, cudaMalloc(&G.tw, sizeof(float2) * f));
-  CUDA_TRY(ctx, cudaMemcpy(G.tw, tw.data(), sizeof(float2) * f, cudaMemcpyHostToDevice));
-  CUDA_TRY(ctx, cudaMalloc(&G.tw64, sizeof(double2) * f));
-  CUDA_TRY(ctx, cudaMemcpy(G.tw64, tw64.data(), sizeof(double2) * f, cudaMemcpyHostToDevice));
+  for (Group &g : G.groups) {
+    const int f = g.f;
+    std::vector<float2> tw(f);
+    std::vector<double2> tw64(f);
+    for (int k = 0; k < f; k++) {
+      // exp(-2 pi i k / f) in double, rounded once
+      const double ang = -2.0 * M_PI * (double)k / (double)f;
+      tw64[k] = make_double2(std::cos(ang), std::sin(ang));
+      tw[k] = make_float2((float)tw64[k].x, (float)tw64[k].y);
+    }
+    std::vector<int> slots(g.planes.size());
+    for (size_t i = 0; i < slots.size(); i++) slots[i] = (int)i;
+    CUDA_TRY(ctx, cudaMalloc(&g.tw, sizeof(float2) * f));
+    CUDA_TRY(ctx, cudaMemcpy(g.tw, tw.data(), sizeof(float2) * f, cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMalloc(&g.tw64, sizeof(double2) * f));
+    CUDA_TRY(ctx, cudaMemcpy(g.tw64, tw64.data(), sizeof(double2) * f, cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMalloc(&g.d_ids, sizeof(int) * g.planes.size()));
+    CUDA_TRY(ctx, cudaMemcpy(g.d_ids, g.planes.data(), sizeof(int) * g.planes.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMalloc(&g.d_slots, sizeof(int) * slots.size()));
+    CUDA_TRY(ctx, cudaMemcpy(g.d_slots, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice));
+  }
   G.valid = true;
   return FLF_OK;
 }
 
-int set_user_planes(flf_ctx *ctx, const int *planes, int nplanes, cudaStream_t s, const int **out) {
+// The planes one projection call works on, split by transform group:
+// for group g, n[g] planes with ids ids[g] (volume addressing) and slots
+// slots[g] (rows of the group's packed matrices), both device arrays.
+struct PlaneSet {
+  std::vector<int> n;
+  std::vector<const int *> ids, slots;
+};
+
+int check_planes_arg(flf_ctx *ctx, const int *planes, int nplanes) {
   if (!planes) {
     if (nplanes != ctx->nz) return fail(ctx, FLF_E_ARG, "planes == NULL requires nplanes == num_planes");
-    *out = ctx->d_planes_all;
     return FLF_OK;
   }
   if (nplanes <= 0 || nplanes > ctx->nz) return fail(ctx, FLF_E_ARG, "nplanes %d out of range", nplanes);
@@ -406,16 +488,51 @@ int set_user_planes(flf_ctx *ctx, const int *planes, int nplanes, cudaStream_t s
     if (seen[planes[i]]) return fail(ctx, FLF_E_ARG, "plane id %d listed twice", planes[i]);
     seen[planes[i]] = 1;
   }
-  if (ctx->planes_user_cap < nplanes) {
+  return FLF_OK;
+}
+
+// Requires a valid geometry.  planes == NULL: every plane.
+int make_plane_set(flf_ctx *ctx, const int *planes, int nplanes, cudaStream_t s, PlaneSet &ps) {
+  const Geometry &G = ctx->geo;
+  const int ng = (int)G.groups.size();
+  ps.n.assign(ng, 0);
+  ps.ids.assign(ng, nullptr);
+  ps.slots.assign(ng, nullptr);
+  if (!planes) {
+    for (int g = 0; g < ng; g++) {
+      ps.n[g] = (int)G.groups[g].planes.size();
+      ps.ids[g] = G.groups[g].d_ids;
+      ps.slots[g] = G.groups[g].d_slots;
+    }
+    return FLF_OK;
+  }
+  std::vector<std::vector<int>> ids(ng), slots(ng);
+  for (int i = 0; i < nplanes; i++) {
+    const int z = planes[i], g = G.plane_group[z];
+    ids[g].push_back(z);
+    slots[g].push_back(G.plane_slot[z]);
+  }
+  std::vector<int> host;   // per group: ids then slots
+  std::vector<int> off(ng);
+  for (int g = 0; g < ng; g++) {
+    off[g] = (int)host.size();
+    host.insert(host.end(), ids[g].begin(), ids[g].end());
+    host.insert(host.end(), slots[g].begin(), slots[g].end());
+  }
+  if (ctx->planes_user_cap < (int)host.size()) {
     if (ctx->d_planes_user) cudaFree(ctx->d_planes_user);
     ctx->d_planes_user = nullptr;
-    CUDA_TRY(ctx, cudaMalloc(&ctx->d_planes_user, sizeof(int) * ctx->nz));
-    ctx->planes_user_cap = ctx->nz;
+    CUDA_TRY(ctx, cudaMalloc(&ctx->d_planes_user, sizeof(int) * 2 * ctx->nz));
+    ctx->planes_user_cap = 2 * ctx->nz;
   }
   // the synchronous copy orders against earlier work on every stream
   CUDA_TRY(ctx, cudaStreamSynchronize(s));
-  CUDA_TRY(ctx, cudaMemcpy(ctx->d_planes_user, planes, sizeof(int) * nplanes, cudaMemcpyHostToDevice));
-  *out = ctx->d_planes_user;
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_planes_user, host.data(), sizeof(int) * host.size(), cudaMemcpyHostToDevice));
+  for (int g = 0; g < ng; g++) {
+    ps.n[g] = (int)ids[g].size();
+    ps.ids[g] = ctx->d_planes_user + off[g];
+    ps.slots[g] = ctx->d_planes_user + off[g] + ps.n[g];
+  }
   return FLF_OK;
 }
 
@@ -427,103 +544,149 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
   if (f_req > 0) {
     const int N = ctx->N, Ly = (Y + N - 1) / N, Lx = (X + N - 1) / N;
     int R = 0;
-    for (int d = 0; d < 2; d++)
-      for (int z = 0; z < ctx->nz; z++)
-        if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
+    for (int z = 0; z < ctx->nz; z++) R = std::max(R, plane_radius(ctx, z));
     if (f_req < std::max(Ly, Lx) + R || f_req < 2 * R + 1) f_req = 0;   // not valid for this shape
   }
   int rc = prepare(ctx, Y, X, f_req, ctx->req_fp64);
   if (rc != FLF_OK) return rc;
-  if (!ctx->geo.built[dir]) rc = build_direction(ctx, dir, s);
+  if (!ctx->geo.built(dir)) rc = build_direction(ctx, dir, s);
   return rc;
 }
 
 // Planes per CTA of the multiply-accumulate: enough CTAs for about 32 per SM
 // (a few waves at the kernel's occupancy), as few plane groups as that allows.
-int zgroup_for(const flf_ctx *ctx, int nz) {
+int zgroup_for(const flf_ctx *ctx, int nz, int nkp) {
   const int target = 32 * std::max(1, ctx->num_sms);
-  const int nzg_needed = std::min(nz, std::max(1, (target + ctx->geo.nkp - 1) / ctx->geo.nkp));
+  const int nzg_needed = std::min(nz, std::max(1, (target + nkp - 1) / nkp));
   return std::max(1, (nz + nzg_needed - 1) / nzg_needed);
 }
 
-// Forward projection of frames [t0, t0+nt) of vol into out (epilogue epi).
-int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const int *d_planes, int nplanes,
-                  int t0, int nt, Strided out, Strided aux, int epi, cudaStream_t s) {
-  Geometry &G = ctx->geo;
-  const Layout &L = ctx->L;
-  const int NN = L.NN, ffh = G.f * G.fh;
-  const int Y = G.Y, X = G.X;
-  const int zgroup = zgroup_for(ctx, nplanes);
-  const int nzg = (nplanes + zgroup - 1) / zgroup;
-  int rc = ensure_ws(ctx, ctx->wsS, sizeof(float2) * (size_t)nt * nplanes * NN * ffh);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sizeof(float2) * (size_t)nzg * nt * NN * ffh);
-  if (rc != FLF_OK) return rc;
+// Workspace needs of one projection over plane set ps (bytes of S and O).
+void ws_needs(const flf_ctx *ctx, const PlaneSet &ps, int nt, bool fwd, size_t &sS, size_t &sO) {
+  const Geometry &G = ctx->geo;
+  const int NN = ctx->L.NN;
+  sS = sO = 0;
+  for (size_t g = 0; g < G.groups.size(); g++) {
+    if (!ps.n[g]) continue;
+    const size_t spec = sizeof(float2) * (size_t)NN * G.groups[g].f * G.groups[g].fh;
+    const int n = ps.n[g];
+    if (fwd) {
+      const int zg = zgroup_for(ctx, n, G.groups[g].nkp);
+      sS = std::max(sS, spec * nt * n);
+      sO = std::max(sO, spec * nt * ((n + zg - 1) / zg));
+    } else {
+      sS = std::max(sS, spec * nt);
+      sO = std::max(sO, spec * nt * n);
+    }
+  }
+}
 
-  Rfft2Params rp{};
-  rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
-  rp.nimg = nt * nplanes * NN; rp.nz = nplanes; rp.mode = 0;
-  rp.src = vol + (long long)t0 * Y * X; rp.src_sz = vol_sz; rp.src_st = (long long)Y * X;
-  rp.planes = d_planes; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
-  rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
-  LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * G.Ly * G.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
-
-  const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
+MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   MacParams mp{};
-  mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
-  mp.P = G.P[FLF_DIR_FORWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = zgroup;
-  mp.S = (const float2 *)ctx->wsS.p; mp.nzS = nplanes; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nzg;
-  mp.nzo_grid = nzg; mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
-  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split; mp.err = ctx->d_err;
-  LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
+  mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
+  mp.P = G.P[dir];
+  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
+  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split;
+  mp.err = ctx->d_err;
+  return mp;
+}
 
-  Irfft2Params ip{};
-  ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
-  ip.nimg = nt * NN; ip.nzo = 1; ip.src = (const float2 *)ctx->wsO.p;
-  ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg; ip.planes = nullptr;
-  ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = Strided{nullptr, 0, 0};
-  ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
-  LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh * nzg + 4.0 * G.Ly * G.Lx * (epi == EPI_DIVIDE ? 2 : 1)), s,
-         launch_irfft2(ip, s));
+// Forward projection of frames [t0, t0+nt) of vol into out: each transform
+// group is projected and summed in Fourier space over its planes; the groups
+// are added in pixel space (the first stores, the others add).
+int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneSet &ps, int t0, int nt,
+                  Strided out, cudaStream_t s) {
+  Geometry &Gm = ctx->geo;
+  const Layout &L = ctx->L;
+  const int NN = L.NN, Y = Gm.Y, X = Gm.X;
+  size_t sS, sO;
+  ws_needs(ctx, ps, nt, true, sS, sO);
+  int rc = ensure_ws(ctx, ctx->wsS, sS);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
+  if (rc != FLF_OK) return rc;
+  bool first = true;
+  for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
+    const int nplanes = ps.n[gi];
+    if (!nplanes) continue;
+    const Group &G = Gm.groups[gi];
+    const int ffh = G.f * G.fh;
+    const int zgroup = zgroup_for(ctx, nplanes, G.nkp);
+    const int nzg = (nplanes + zgroup - 1) / zgroup;
+
+    Rfft2Params rp{};
+    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
+    rp.nimg = nt * nplanes * NN; rp.nz = nplanes; rp.mode = 0;
+    rp.src = vol + (long long)t0 * Y * X; rp.src_sz = vol_sz; rp.src_st = (long long)Y * X;
+    rp.planes = ps.ids[gi]; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
+    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
+    LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * Gm.Ly * Gm.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
+
+    const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
+    MacParams mp = mac_params(ctx, G, FLF_DIR_FORWARD, nt);
+    mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zgroup;
+    mp.S = (const float2 *)ctx->wsS.p; mp.nzS = nplanes; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nzg;
+    mp.nzo_grid = nzg;
+    LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
+
+    Irfft2Params ip{};
+    ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
+    ip.nimg = nt * NN; ip.nzo = 1; ip.src = (const float2 *)ctx->wsO.p;
+    ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg; ip.planes = nullptr;
+    ip.epi = first ? EPI_STORE : EPI_ADD; ip.out = out;
+    ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
+    ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+    LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh * nzg + 4.0 * Gm.Ly * Gm.Lx * (first ? 1 : 2)), s,
+           launch_irfft2(ip, s));
+    first = false;
+  }
   return FLF_OK;
 }
 
-// Back projection of frames [t0, t0+nt) of img; out/aux/norm address volumes.
-int backward_chunk(flf_ctx *ctx, const float *img, const int *d_planes, int nplanes, int t0, int nt,
+// Back projection of frames [t0, t0+nt) of img (or of num / img when num is
+// given: the standard RL error image); out/aux/norm address volumes.
+int backward_chunk(flf_ctx *ctx, const float *img, const float *num, const PlaneSet &ps, int t0, int nt,
                    Strided out, Strided aux, Strided norm, int epi, cudaStream_t s) {
-  Geometry &G = ctx->geo;
+  Geometry &Gm = ctx->geo;
   const Layout &L = ctx->L;
-  const int NN = L.NN, ffh = G.f * G.fh;
-  const int Y = G.Y, X = G.X;
-  int rc = ensure_ws(ctx, ctx->wsS, sizeof(float2) * (size_t)nt * NN * ffh);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sizeof(float2) * (size_t)nt * nplanes * NN * ffh);
+  const int NN = L.NN, Y = Gm.Y, X = Gm.X;
+  size_t sS, sO;
+  ws_needs(ctx, ps, nt, false, sS, sO);
+  int rc = ensure_ws(ctx, ctx->wsS, sS);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
   if (rc != FLF_OK) return rc;
+  for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
+    const int nplanes = ps.n[gi];
+    if (!nplanes) continue;
+    const Group &G = Gm.groups[gi];
+    const int ffh = G.f * G.fh;
 
-  Rfft2Params rp{};
-  rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
-  rp.nimg = nt * NN; rp.nz = 1; rp.mode = 0;
-  rp.src = img + (long long)t0 * Y * X; rp.src_sz = 0; rp.src_st = (long long)Y * X;
-  rp.planes = ctx->d_zero; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
-  rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
-  LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * G.Ly * G.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
+    Rfft2Params rp{};
+    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
+    rp.nimg = nt * NN; rp.nz = 1; rp.mode = 0;
+    rp.src = img + (long long)t0 * Y * X; rp.src_sz = 0; rp.src_st = (long long)Y * X;
+    rp.num = num ? num + (long long)t0 * Y * X : nullptr;
+    rp.planes = ctx->d_zero; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
+    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
+    LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * Gm.Ly * Gm.Lx * (num ? 2 : 1) + 8.0 * ffh), s,
+           launch_rfft2(rp, 0, s));
 
-  const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
-  MacParams mp{};
-  mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
-  const int zgb = zgroup_for(ctx, nplanes);
-  mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = d_planes; mp.nz = nplanes; mp.zgroup = zgb;
-  mp.S = (const float2 *)ctx->wsS.p; mp.nzS = 1; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nplanes;
-  mp.nzo_grid = (nplanes + zgb - 1) / zgb; mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
-  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split; mp.err = ctx->d_err;
-  LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
+    const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
+    const int zgb = zgroup_for(ctx, nplanes, G.nkp);
+    MacParams mp = mac_params(ctx, G, FLF_DIR_BACKWARD, nt);
+    mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zgb;
+    mp.S = (const float2 *)ctx->wsS.p; mp.nzS = 1; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nplanes;
+    mp.nzo_grid = (nplanes + zgb - 1) / zgb;
+    LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
 
-  Irfft2Params ip{};
-  ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
-  ip.nimg = nt * nplanes * NN; ip.nzo = nplanes; ip.src = (const float2 *)ctx->wsO.p;
-  ip.sum_stride = 0; ip.nsum = 1; ip.planes = d_planes;
-  ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = norm;
-  ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
-  const double px = 4.0 * G.Ly * G.Lx * (epi == EPI_STORE ? 1 : (epi == EPI_RL_STANDARD && norm.p ? 4 : 3));
-  LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh + px), s, launch_irfft2(ip, s));
+    Irfft2Params ip{};
+    ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
+    ip.nimg = nt * nplanes * NN; ip.nzo = nplanes; ip.src = (const float2 *)ctx->wsO.p;
+    ip.sum_stride = 0; ip.nsum = 1; ip.planes = ps.ids[gi];
+    ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = norm;
+    ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+    const double px = 4.0 * Gm.Ly * Gm.Lx * (epi == EPI_STORE ? 1 : (epi == EPI_RL_STANDARD && norm.p ? 4 : 3));
+    LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh + px), s, launch_irfft2(ip, s));
+  }
   return FLF_OK;
 }
 
@@ -650,8 +813,7 @@ int flf_psf_upload(flf_ctx *ctx, int plane, int direction, const float *H_host, 
   CUDA_TRY(ctx, cudaMemcpy(dst, H_host, bytes, cudaMemcpyHostToDevice));
   ctx->h[direction][plane] = h;
   // transfer matrices depend on the PSF and on the kernel radius
-  ctx->geo.built[0] = ctx->geo.built[1] = false;
-  ctx->geo.valid = false;
+  free_geometry(ctx->geo);
   return FLF_OK;
 }
 
@@ -666,7 +828,7 @@ int flf_prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
   ctx->req_f = fft_size;
   ctx->req_fp64 = fp64;
   for (int d = 0; d < 2 && rc == FLF_OK; d++)
-    if (!ctx->geo.built[d]) rc = build_direction(ctx, d, 0);
+    if (!ctx->geo.built(d)) rc = build_direction(ctx, d, 0);
   return rc;
 }
 
@@ -678,16 +840,17 @@ int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y
   cudaStream_t s = (cudaStream_t)stream;
   for (int z = 0; z < ctx->nz; z++)
     if (!ctx->dH[FLF_DIR_FORWARD][z]) return fail(ctx, FLF_E_STATE, "forward PSF for plane %d was not uploaded", z);
-  const int *d_planes;
-  int rc = set_user_planes(ctx, planes, nplanes, s, &d_planes);
+  int rc = check_planes_arg(ctx, planes, nplanes);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
+  PlaneSet ps;
+  if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
   const long long vol_sz = (long long)T * Y * X;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
     Strided out{img_dev + (long long)t0 * Y * X, 0, (long long)Y * X};
-    rc = forward_chunk(ctx, vol_dev, vol_sz, d_planes, nplanes, t0, nt, out, Strided{nullptr, 0, 0}, EPI_STORE, s);
+    rc = forward_chunk(ctx, vol_dev, vol_sz, ps, t0, nt, out, s);
   }
   return rc;
 }
@@ -700,15 +863,16 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
   cudaStream_t s = (cudaStream_t)stream;
   for (int z = 0; z < ctx->nz; z++)
     if (!ctx->dH[FLF_DIR_BACKWARD][z]) return fail(ctx, FLF_E_STATE, "backward PSF for plane %d was not uploaded", z);
-  const int *d_planes;
-  int rc = set_user_planes(ctx, planes, nplanes, s, &d_planes);
+  int rc = check_planes_arg(ctx, planes, nplanes);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
+  PlaneSet ps;
+  if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
     Strided out{vol_dev + (long long)t0 * Y * X, (long long)T * Y * X, (long long)Y * X};
-    rc = backward_chunk(ctx, img_dev, d_planes, nplanes, t0, nt, out, Strided{nullptr, 0, 0},
+    rc = backward_chunk(ctx, img_dev, nullptr, ps, t0, nt, out, Strided{nullptr, 0, 0},
                         Strided{nullptr, 0, 0}, EPI_STORE, s);
   }
   return rc;
@@ -721,57 +885,58 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
   if (T <= 0) return fail(ctx, FLF_E_ARG, "frame count must be positive (got %d)", T);
   cudaSetDevice(ctx->device);
   if (int rc0 = check_device_flag(ctx)) return rc0;
-  Geometry &G = ctx->geo;
-  if (!G.valid || G.Y != Y || G.X != X || !G.built[FLF_DIR_BACKWARD])
+  Geometry &Gm = ctx->geo;
+  if (!Gm.valid || Gm.Y != Y || Gm.X != X || !Gm.built(FLF_DIR_BACKWARD))
     return fail(ctx, FLF_E_STATE,
                 "flf_backward_noalloc needs transfer matrices for %d x %d built beforehand: call flf_prepare "
                 "with this image shape first", Y, X);
   const Layout &L = ctx->L;
-  const int NN = L.NN, ffh = G.f * G.fh, nz = ctx->nz;
-  const size_t spec = sizeof(float2) * (size_t)NN * ffh;   // one frame (or one plane) of spectra
-  if (2 * spec > FLF_NOALLOC_SCRATCH_BYTES)
+  const int NN = L.NN;
+  size_t need = 0;
+  for (const Group &G : Gm.groups) need = std::max(need, 2 * sizeof(float2) * (size_t)NN * G.f * G.fh);
+  if (need > FLF_NOALLOC_SCRATCH_BYTES)
     return fail(ctx, FLF_E_ARG,
                 "flf_backward_noalloc needs %zu bytes of scratch for this geometry (Nnum %d, transform %d), "
-                "more than its fixed %u bytes; use flf_backward", 2 * spec, ctx->N, G.f,
+                "more than its fixed %u bytes; use flf_backward", need, ctx->N, Gm.max_f(),
                 (unsigned)FLF_NOALLOC_SCRATCH_BYTES);
   void *scratch = nullptr;
   int rc = noalloc_scratch(ctx, ctx->device, &scratch);
   if (rc != FLF_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  float2 *S = (float2 *)scratch;                       // channel spectra of the current frame
-  float2 *O = (float2 *)((char *)scratch + spec);      // output spectra of a group of planes
-  const int zb = std::max(1, std::min(nz, (int)((FLF_NOALLOC_SCRATCH_BYTES - spec) / spec)));
   const long long YX = (long long)Y * X;
   for (int t = 0; t < T; t++) {
-    Rfft2Params rp{};
-    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = G.Ly; rp.Lx = G.Lx;
-    rp.nimg = NN; rp.nz = 1; rp.mode = 0;
-    rp.src = img_dev + t * YX; rp.src_sz = 0; rp.src_st = YX;
-    rp.planes = ctx->d_zero; rp.dst = S; rp.twiddle = G.tw;
-    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (G.Ly + 1) / 2;
-    cudaError_t e = launch_rfft2(rp, 0, s);
-    for (int z0 = 0; z0 < nz && e == cudaSuccess; z0 += zb) {
-      const int nzl = std::min(zb, nz - z0);
-      const int zg = zgroup_for(ctx, nzl);
-      MacParams mp{};
-      mp.L = L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = 1;
-      mp.P = G.P[FLF_DIR_BACKWARD]; mp.planes = ctx->d_planes_all + z0; mp.nz = nzl; mp.zgroup = zg;
-      mp.S = S; mp.nzS = 1; mp.O = O; mp.nzo = nzl; mp.nzo_grid = (nzl + zg - 1) / zg;
-      mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
-      mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split;
-      mp.err = ctx->d_err;
-      e = launch_mac(mp, false, s);
-      if (e != cudaSuccess) break;
-      Irfft2Params ip{};
-      ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = G.Ly; ip.Lx = G.Lx;
-      ip.nimg = nzl * NN; ip.nzo = nzl; ip.src = O; ip.sum_stride = 0; ip.nsum = 1;
-      ip.planes = ctx->d_planes_all + z0; ip.epi = EPI_STORE;
-      ip.out = Strided{vol_dev + t * YX, (long long)T * YX, YX};
-      ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
-      ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
-      e = launch_irfft2(ip, s);
+    for (const Group &G : Gm.groups) {
+      const size_t spec = sizeof(float2) * (size_t)NN * G.f * G.fh;   // one frame or one plane
+      float2 *S = (float2 *)scratch;                        // channel spectra of the frame
+      float2 *O = (float2 *)((char *)scratch + spec);       // output spectra of a group of planes
+      const int ng = (int)G.planes.size();
+      const int zb = std::max(1, std::min(ng, (int)((FLF_NOALLOC_SCRATCH_BYTES - spec) / spec)));
+      Rfft2Params rp{};
+      rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
+      rp.nimg = NN; rp.nz = 1; rp.mode = 0;
+      rp.src = img_dev + t * YX; rp.src_sz = 0; rp.src_st = YX;
+      rp.planes = ctx->d_zero; rp.dst = S; rp.twiddle = G.tw;
+      rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
+      cudaError_t e = launch_rfft2(rp, 0, s);
+      for (int z0 = 0; z0 < ng && e == cudaSuccess; z0 += zb) {
+        const int nzl = std::min(zb, ng - z0);
+        const int zg = zgroup_for(ctx, nzl, G.nkp);
+        MacParams mp = mac_params(ctx, G, FLF_DIR_BACKWARD, 1);
+        mp.planes = G.d_slots + z0; mp.nz = nzl; mp.zgroup = zg;
+        mp.S = S; mp.nzS = 1; mp.O = O; mp.nzo = nzl; mp.nzo_grid = (nzl + zg - 1) / zg;
+        e = launch_mac(mp, false, s);
+        if (e != cudaSuccess) break;
+        Irfft2Params ip{};
+        ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
+        ip.nimg = nzl * NN; ip.nzo = nzl; ip.src = O; ip.sum_stride = 0; ip.nsum = 1;
+        ip.planes = G.d_ids + z0; ip.epi = EPI_STORE;
+        ip.out = Strided{vol_dev + t * YX, (long long)T * YX, YX};
+        ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
+        ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+        e = launch_irfft2(ip, s);
+      }
+      if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "flf_backward_noalloc launch failed: %s", cudaGetErrorString(e));
     }
-    if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "flf_backward_noalloc launch failed: %s", cudaGetErrorString(e));
   }
   return FLF_OK;
 }
@@ -792,32 +957,25 @@ int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
-  const int nz = ctx->nz;
   const long long YX = (long long)Y * X;
   rc = ensure_ws(ctx, ctx->wsImg, sizeof(float) * (size_t)TF * YX);
+  PlaneSet ps;
+  if (rc == FLF_OK) rc = make_plane_set(ctx, nullptr, ctx->nz, s, ps);
   if (rc != FLF_OK) return rc;
   float *hx = (float *)ctx->wsImg.p;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
     const Strided xs{x_dev + t0 * YX, (long long)T * YX, YX};
     for (int it = 0; it < iters && rc == FLF_OK; it++) {
-      // H x  (standard variant: y / H x fused into the store)
-      const Strided hxo{hx, 0, YX};
-      if (variant == FLF_RL_PREVEDEL) {
-        rc = forward_chunk(ctx, x_dev, (long long)T * YX, ctx->d_planes_all, nz, t0, nt, hxo,
-                           Strided{nullptr, 0, 0}, EPI_STORE, s);
-      } else {
-        rc = forward_chunk(ctx, x_dev, (long long)T * YX, ctx->d_planes_all, nz, t0, nt, hxo,
-                           Strided{const_cast<float *>(ref_dev) + t0 * YX, 0, YX}, EPI_DIVIDE, s);
-      }
+      // H x, then Ht of (Htf update) or of y / H x (the division is fused into the gather)
+      rc = forward_chunk(ctx, x_dev, (long long)T * YX, ps, t0, nt, Strided{hx, 0, YX}, s);
       if (rc != FLF_OK) break;
       if (variant == FLF_RL_PREVEDEL) {
         const Strided htf{const_cast<float *>(ref_dev) + t0 * YX, (long long)T * YX, YX};
-        rc = backward_chunk(ctx, hx, ctx->d_planes_all, nz, 0, nt, xs, htf, Strided{nullptr, 0, 0},
-                            EPI_RL_PREVEDEL, s);
+        rc = backward_chunk(ctx, hx, nullptr, ps, 0, nt, xs, htf, Strided{nullptr, 0, 0}, EPI_RL_PREVEDEL, s);
       } else {
         const Strided nrm{const_cast<float *>(norm_dev), YX, 0};
-        rc = backward_chunk(ctx, hx, ctx->d_planes_all, nz, 0, nt, xs, Strided{nullptr, 0, 0}, nrm,
+        rc = backward_chunk(ctx, hx, ref_dev + t0 * YX, ps, 0, nt, xs, Strided{nullptr, 0, 0}, nrm,
                             EPI_RL_STANDARD, s);
       }
     }
@@ -831,9 +989,9 @@ int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {
   for (int d = 0; d < 2; d++)
     for (int z = 0; z < ctx->nz; z++)
       if (ctx->dH[d][z]) b += sizeof(float) * (size_t)ctx->L.nh * ctx->L.nh * ctx->h[d][z] * ctx->h[d][z];
-  const Geometry &G = ctx->geo;
-  if (G.valid) {
-    const size_t pe = (size_t)G.nkp * ctx->L.nrow * ctx->L.RS * ctx->nz * sizeof(float2);
+  const Geometry &Gm = ctx->geo;
+  for (const Group &G : Gm.groups) {
+    const size_t pe = (size_t)G.nkp * ctx->L.nrow * ctx->L.RS * G.planes.size() * sizeof(float2);
     for (int d = 0; d < 2; d++)
       if (G.P[d]) b += pe;
   }
@@ -858,10 +1016,12 @@ int flf_clear_cache(flf_ctx *ctx) {
 int flf_geometry(const flf_ctx *ctx, int *out4) {
   if (!ctx || !out4) return FLF_E_ARG;
   const Geometry &G = ctx->geo;
-  out4[0] = G.valid ? G.f : 0;
-  out4[1] = G.valid ? G.R : 0;
+  int R = 0;
+  for (const Group &g : G.groups) R = std::max(R, g.R);
+  out4[0] = G.valid ? G.max_f() : 0;
+  out4[1] = G.valid ? R : 0;
   out4[2] = G.valid ? G.fp64 : 0;
-  out4[3] = G.valid ? G.nkp : 0;
+  out4[3] = G.valid ? (int)G.groups.size() : 0;
   return FLF_OK;
 }
 
@@ -900,6 +1060,15 @@ int flf_synchronize(flf_ctx *ctx, void *stream) {
 
 int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
   if (!ctx || !name) return FLF_E_ARG;
+  if (!strcmp(name, "plane_transform_sizes")) {
+    if (value != 0 && value != 1) return fail(ctx, FLF_E_ARG, "plane_transform_sizes must be 0 or 1");
+    if (ctx->opt_plane_sizes != (int)value) {
+      ctx->opt_plane_sizes = (int)value;
+      cudaDeviceSynchronize();
+      free_geometry(ctx->geo);   // rebuilt on the next call
+    }
+    return FLF_OK;
+  }
   if (!strcmp(name, "mac_stages") || !strcmp(name, "mac_chunk_rows") || !strcmp(name, "mac_split")) {
     const int st = !strcmp(name, "mac_stages") ? (int)value : ctx->opt_stages;
     const int cr = !strcmp(name, "mac_chunk_rows") ? (int)value : ctx->opt_chunk_rows;

@@ -69,6 +69,7 @@ enum Epilogue : int {
   EPI_DIVIDE = 1,        // out = aux / value           (y / Hx)
   EPI_RL_PREVEDEL = 2,   // x = x * (aux / value), NaN -> 0
   EPI_RL_STANDARD = 3,   // x = x * value [/ norm], NaN -> 0
+  EPI_ADD = 4,           // out += value                 (sum over transform groups)
 };
 
 struct Strided {         // base + plane*sz + frame*st + y*X + x
@@ -89,6 +90,7 @@ struct Rfft2Params {
   const float *src;         // mode 0 (float input)
   long long src_sz, src_st; // mode 0 strides (plane, frame)
   const int *planes;        // mode 0: plane id per z index (device)
+  const float *num;         // mode 0, optional: gather num / src instead of src (same layout)
   const void *src_img;      // mode 1: Real images [nimg][f][f]
   void *dst;                // Complex<Real> [nimg][f][fh]
   const void *twiddle;      // Complex<Real> [f]

@@ -172,8 +172,20 @@ __global__ void __launch_bounds__(256) k_rfft2(Rfft2Params p) {
       const int x = c * N + a;
       if (c < p.Lx && x < p.X) {
         const int y0 = r0 * N + b, y1 = r1 * N + b;
-        if (r0 < p.Ly && y0 < p.Y) v0 = (R)base[(long long)y0 * p.X + x];
-        if (r1 < p.Ly && y1 < p.Y) v1 = (R)base[(long long)y1 * p.X + x];
+        if (p.num) {   // the standard RL error image num / src (lfdeconv.py:192)
+          const float *nb = p.num + t * p.src_st;
+          if (r0 < p.Ly && y0 < p.Y) {
+            const long long o = (long long)y0 * p.X + x;
+            v0 = (R)__fdiv_rn(nb[o], base[o]);
+          }
+          if (r1 < p.Ly && y1 < p.Y) {
+            const long long o = (long long)y1 * p.X + x;
+            v1 = (R)__fdiv_rn(nb[o], base[o]);
+          }
+        } else {
+          if (r0 < p.Ly && y0 < p.Y) v0 = (R)base[(long long)y0 * p.X + x];
+          if (r1 < p.Ly && y1 < p.Y) v1 = (R)base[(long long)y1 * p.X + x];
+        }
       }
     } else {
       const R *im = reinterpret_cast<const R *>(p.src_img) + (long long)g * f * f;
@@ -285,6 +297,7 @@ __global__ void __launch_bounds__(256) k_irfft2(Irfft2Params p) {
     float *o = p.out.p + plane * p.out.sz + t * p.out.st + pix;
     switch (p.epi) {
       case EPI_STORE: *o = val; break;
+      case EPI_ADD: *o += val; break;
       case EPI_DIVIDE: {
         const float yv = p.aux.p[plane * p.aux.sz + t * p.aux.st + pix];
         *o = __fdiv_rn(yv, val);

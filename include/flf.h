@@ -136,9 +136,10 @@ int flf_memory_usage(const flf_ctx *ctx, size_t *bytes);
  * Counterpart of ClearFHCache (py_light_field.cpp:1370-1385). */
 int flf_clear_cache(flf_ctx *ctx);
 
-/* Transform size and precompute precision chosen by the last prepare:
- * out[0] = f (lenslet-grid FFT size), out[1] = R (kernel radius in
- * lenslets), out[2] = fp64 flag, out[3] = number of frequency pairs. */
+/* Transform sizes and precompute precision chosen by the last prepare:
+ * out[0] = largest lenslet-grid FFT size f, out[1] = largest kernel radius R
+ * (lenslets), out[2] = fp64 flag, out[3] = number of transform groups
+ * (planes with equal f share one). */
 int flf_geometry(const flf_ctx *ctx, int *out4);
 
 /* Per-kernel statistics.  flf_profile(ctx, 1) clears the counters and
@@ -154,8 +155,11 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
 /* Tunable launch parameters (the GB300 counterpart of the reference's
  * block-shape knobs gBlockSelection / gCalculateRowsBlocks,
  * projector.py:26-36).  Options: "mac_stages" (shared-memory pipeline
- * stages of the multiply-accumulate, 2..16) and "mac_chunk_rows" (stored
- * rows per stage, even, 2..64).  Results do not depend on them. */
+ * stages of the multiply-accumulate, 2..16), "mac_chunk_rows" (stored rows
+ * per stage, even, 2..64), "mac_split" (threads sharing an orbit's rows,
+ * 1..4) and "plane_transform_sizes" (1: each plane uses the smallest
+ * transform its PSF allows, planes grouped by size - the default; 0: one
+ * size for all planes).  Results agree to rounding whatever the values. */
 int flf_set_option(flf_ctx *ctx, const char *name, long long value);
 
 /* Wait for `stream` and report any failure of earlier launches, including a

@@ -178,6 +178,31 @@ def test_full_size_linearity_and_adjointness(mods):
     assert abs(hu[0, 150:300, 150:300].mean() - 11.0) < 1e-4
 
 
+def test_transform_groups_match_uniform_transform(mods):
+    """Per-plane transform sizes (grouped) and one size for all planes agree."""
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    N = 7
+    H, Ht = synthetic.random_psf(N, [43, 15, 29, 15, 57], seed=11)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(2)
+    img = rng.random((2, 56, 63)).astype(np.float32)
+    vol = rng.random((5, 2, 56, 63)).astype(np.float32)
+    p = projector.Projector_gb300()
+    bk = p.BackwardProjectACC(hm, img, None)
+    fw = p.ForwardProjectACC(hm, vol, None)
+    geo = p.geometry()
+    assert geo["groups"] >= 3
+    p.context(hm).set_option("plane_transform_sizes", 0)
+    p._shape_key = None
+    bku = p.BackwardProjectACC(hm, img, None)
+    fwu = p.ForwardProjectACC(hm, vol, None)
+    assert p.geometry()["groups"] == 1
+    assert rel(bk, bku) < PROJ_TOL and rel(fw, fwu) < PROJ_TOL
+    bo = O.backward_project(Ht, img, N, method="direct", dtype=np.float64)
+    assert rel(bk, bo) < PROJ_TOL
+
+
 def test_planes_validation(mods):
     projector, lfdeconv, psfmatrix = mods
     c = case_inputs("planes_n7")
