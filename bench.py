@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-planes", type=int, default=5)
+    ap.add_argument("--planes", default=None,
+                    help="comma-separated z indices of the workload to keep (smaller cases for profiling)")
     return ap.parse_args()
 
 
@@ -63,12 +65,14 @@ def dist_env():
     return rank, world, local
 
 
-def build_problem(wl, seed=1234):
+def build_problem(wl, seed=1234, keep=None):
     import psfmatrix
     import synthetic
     N = wl["Nnum"]
     z0, z1, dz = wl["z"]
     z = np.arange(z0, z1 + dz / 2, dz)
+    if keep is not None:
+        z = z[keep]
     H, Ht = synthetic.synthetic_psf(N, z, wl["img_size_ref"])
     hm = psfmatrix.HMatrixArrays(H, Ht, name="bench-%s" % wl["label"])
     Y = X = wl["lenslets"] * N
@@ -259,7 +263,8 @@ def run_gb300(args, rank, world, local):
     N = wl["Nnum"]
     T = args.frames
     t_setup = time.time()
-    hm, H, Ht, z, gt, Y, X = build_problem(wl, seed=1234 + rank)
+    keep = [int(v) for v in args.planes.split(",")] if args.planes else None
+    hm, H, Ht, z, gt, Y, X = build_problem(wl, seed=1234 + rank, keep=keep)
     Z = len(z)
     p = projector.Projector_gb300(device=local)
     p.storeVolumesOnGPU = True
@@ -346,15 +351,16 @@ def run_gb300(args, rank, world, local):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "frames": T,
+                "config": {"workload": wl["label"] + (" (planes %s only)" % args.planes if keep else ""),
+                           "image": [Y, X], "planes": Z, "nnum": N, "frames": T,
                            "rl_iterations": args.iters, "rl_variant": "prevedel", "start": "uniform",
                            "projections_per_step": 1 + 2 * args.iters,
                            "transform_size": geo["f"], "kernel_radius_lenslets": geo["R"],
                            "precompute_fp64": geo["fp64"], "device_gb": round(gb, 2),
                            "setup_s": round(setup_s, 1),
                            "l2": "inputs larger than L2: %.1f GB of transfer matrices streamed per "
-                                 "projection pair, %.0f MB volume" % (tot_bytes / max(n_mac, 1) * 2 / 1e9,
-                                                                     Z * T * Y * X * 4 / 1e6),
+                                 "projection, %.0f MB volume" % (tot_bytes / args.steps / (1 + 2 * args.iters) / 1e9,
+                                                                Z * T * Y * X * 4 / 1e6),
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cb,
                 "clocks": clk}

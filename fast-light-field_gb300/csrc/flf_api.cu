@@ -73,7 +73,10 @@ struct flf_ctx {
   int planes_user_cap = 0;
   int *d_zero = nullptr;
   std::vector<int> rep_ch, rep_row, rep_kind;
-  Workspace wsS, wsO, wsImg;
+  Workspace wsS, wsO;             // channel spectra in / out of the multiply-accumulate
+  Workspace wsCvol;               // channel-major volume side (forward input, back projection output)
+  Workspace wsCimg;               // channel-major image side (back projection input, forward output)
+  Workspace wsCy;                 // channel-major measured image (standard RL numerator)
   int num_sms = 0;
   int req_f = 0, req_fp64 = 0;   // transform size / precision asked for by flf_prepare
   int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
@@ -562,14 +565,23 @@ int zgroup_for(const flf_ctx *ctx, int nz, int nkp) {
 }
 
 // Workspace needs of one projection over plane set ps (bytes of S and O).
-void ws_needs(const flf_ctx *ctx, const PlaneSet &ps, int nt, bool fwd, size_t &sS, size_t &sO) {
+// Floats of one channel-major image set (NN channel images of Ly x Lxp).
+size_t chan_set_floats(const flf_ctx *ctx) {
+  const Geometry &G = ctx->geo;
+  return (size_t)ctx->L.NN * G.Ly * channel_pitch(G.Lx);
+}
+
+// Workspace bytes of one projection of nt frames over the plane set ps.
+void ws_needs(const flf_ctx *ctx, const PlaneSet &ps, int nt, bool fwd, size_t &sS, size_t &sO, size_t &sCv) {
   const Geometry &G = ctx->geo;
   const int NN = ctx->L.NN;
-  sS = sO = 0;
+  const size_t cset = sizeof(float) * chan_set_floats(ctx);
+  sS = sO = sCv = 0;
   for (size_t g = 0; g < G.groups.size(); g++) {
     if (!ps.n[g]) continue;
     const size_t spec = sizeof(float2) * (size_t)NN * G.groups[g].f * G.groups[g].fh;
     const int n = ps.n[g];
+    sCv = std::max(sCv, cset * nt * n);
     if (fwd) {
       const int zg = zgroup_for(ctx, n, G.groups[g].nkp);
       sS = std::max(sS, spec * nt * n);
@@ -591,20 +603,69 @@ MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   return mp;
 }
 
-// Forward projection of frames [t0, t0+nt) of vol into out: each transform
-// group is projected and summed in Fourier space over its planes; the groups
-// are added in pixel space (the first stores, the others add).
+SplitParams split_params(const flf_ctx *ctx, const float *src, long long src_sz, long long src_st,
+                         const int *planes, int nz, int nt, float *dst) {
+  const Geometry &Gm = ctx->geo;
+  SplitParams sp{};
+  sp.src = src; sp.src_sz = src_sz; sp.src_st = src_st; sp.planes = planes;
+  sp.nz = nz; sp.nsets = nz * nt;
+  sp.N = ctx->N; sp.Y = Gm.Y; sp.X = Gm.X; sp.Ly = Gm.Ly; sp.Lx = Gm.Lx; sp.Lxp = channel_pitch(Gm.Lx);
+  sp.dst = dst;
+  return sp;
+}
+
+Rfft2Params rfft2_params(const flf_ctx *ctx, const Group &G, const float *chan, int nimg, void *dst) {
+  const Geometry &Gm = ctx->geo;
+  Rfft2Params rp{};
+  rp.plan = G.plan; rp.N = ctx->N; rp.Y = Gm.Y; rp.X = Gm.X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
+  rp.nimg = nimg; rp.mode = 0; rp.chan = chan; rp.Lxp = channel_pitch(Gm.Lx);
+  rp.dst = dst; rp.twiddle = G.tw;
+  return rp;
+}
+
+Irfft2Params irfft2_params(const flf_ctx *ctx, const Group &G, const float2 *src, int nimg, float *chan) {
+  const Geometry &Gm = ctx->geo;
+  Irfft2Params ip{};
+  ip.plan = G.plan; ip.N = ctx->N; ip.Y = Gm.Y; ip.X = Gm.X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
+  ip.nimg = nimg; ip.src = src; ip.sum_stride = 0; ip.nsum = 1;
+  ip.chan = chan; ip.Lxp = channel_pitch(Gm.Lx); ip.twiddle = G.tw;
+  return ip;
+}
+
+MergeParams merge_params(const flf_ctx *ctx, const float *src, const int *planes, int nzo, int nt, int epi,
+                         Strided out, Strided aux, Strided norm) {
+  const Geometry &Gm = ctx->geo;
+  MergeParams mg{};
+  mg.src = src; mg.nzo = nzo; mg.nsets = nzo * nt; mg.planes = planes;
+  mg.N = ctx->N; mg.Y = Gm.Y; mg.X = Gm.X; mg.Ly = Gm.Ly; mg.Lx = Gm.Lx; mg.Lxp = channel_pitch(Gm.Lx);
+  mg.epi = epi; mg.out = out; mg.aux = aux; mg.norm = norm;
+  return mg;
+}
+
+// Bytes of nsets channel-major image sets.
+double chan_bytes(const flf_ctx *ctx, int nsets) { return 4.0 * chan_set_floats(ctx) * nsets; }
+
+// Forward projection of frames [t0, t0+nt) of vol into the channel-major
+// image set `chan` ([nt][NN][Ly][Lxp]): each transform group is projected and
+// summed in Fourier space over its planes; the groups are added in the
+// channel-major domain.  The last group's pass zeroes the samples outside the
+// image and, with `num`, stores num / (H x) (the standard RL error image).
 int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneSet &ps, int t0, int nt,
-                  Strided out, cudaStream_t s) {
+                  float *chan, const float *num, cudaStream_t s) {
   Geometry &Gm = ctx->geo;
   const Layout &L = ctx->L;
   const int NN = L.NN, Y = Gm.Y, X = Gm.X;
-  size_t sS, sO;
-  ws_needs(ctx, ps, nt, true, sS, sO);
+  size_t sS, sO, sCv;
+  ws_needs(ctx, ps, nt, true, sS, sO, sCv);
   int rc = ensure_ws(ctx, ctx->wsS, sS);
   if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, sCv);
   if (rc != FLF_OK) return rc;
+  int last = -1;
+  for (size_t gi = 0; gi < Gm.groups.size(); gi++)
+    if (ps.n[gi]) last = (int)gi;
   bool first = true;
+  float *cvol = (float *)ctx->wsCvol.p;
   for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
     const int nplanes = ps.n[gi];
     if (!nplanes) continue;
@@ -613,13 +674,12 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneS
     const int zgroup = zgroup_for(ctx, nplanes, G.nkp);
     const int nzg = (nplanes + zgroup - 1) / zgroup;
 
-    Rfft2Params rp{};
-    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
-    rp.nimg = nt * nplanes * NN; rp.nz = nplanes; rp.mode = 0;
-    rp.src = vol + (long long)t0 * Y * X; rp.src_sz = vol_sz; rp.src_st = (long long)Y * X;
-    rp.planes = ps.ids[gi]; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
-    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
-    LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * Gm.Ly * Gm.Lx + 8.0 * ffh), s, launch_rfft2(rp, 0, s));
+    SplitParams sp = split_params(ctx, vol + (long long)t0 * Y * X, vol_sz, (long long)Y * X, ps.ids[gi],
+                                  nplanes, nt, cvol);
+    LAUNCH(ctx, "k_split", chan_bytes(ctx, nt * nplanes) + 4.0 * Y * X * nt * nplanes, s, launch_split(sp, s));
+
+    Rfft2Params rp = rfft2_params(ctx, G, cvol, nt * nplanes * NN, ctx->wsS.p);
+    LAUNCH(ctx, "k_rfft2", chan_bytes(ctx, nt * nplanes) + 8.0 * ffh * NN * nt * nplanes, s, launch_rfft2(rp, 0, s));
 
     const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
     MacParams mp = mac_params(ctx, G, FLF_DIR_FORWARD, nt);
@@ -628,47 +688,39 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneS
     mp.nzo_grid = nzg;
     LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
 
-    Irfft2Params ip{};
-    ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
-    ip.nimg = nt * NN; ip.nzo = 1; ip.src = (const float2 *)ctx->wsO.p;
-    ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg; ip.planes = nullptr;
-    ip.epi = first ? EPI_STORE : EPI_ADD; ip.out = out;
-    ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
-    ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
-    LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh * nzg + 4.0 * Gm.Ly * Gm.Lx * (first ? 1 : 2)), s,
-           launch_irfft2(ip, s));
+    Irfft2Params ip = irfft2_params(ctx, G, (const float2 *)ctx->wsO.p, nt * NN, chan);
+    ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg;
+    ip.add = !first; ip.final_pass = (int)gi == last; ip.num = ip.final_pass ? num : nullptr;
+    const double cb = chan_bytes(ctx, nt) * (1 + ip.add + (ip.num ? 1 : 0));
+    LAUNCH(ctx, "k_irfft2", 8.0 * ffh * NN * nt * nzg + cb, s, launch_irfft2(ip, s));
     first = false;
   }
   return FLF_OK;
 }
 
-// Back projection of frames [t0, t0+nt) of img (or of num / img when num is
-// given: the standard RL error image); out/aux/norm address volumes.
-int backward_chunk(flf_ctx *ctx, const float *img, const float *num, const PlaneSet &ps, int t0, int nt,
-                   Strided out, Strided aux, Strided norm, int epi, cudaStream_t s) {
+// Back projection of frames [t0, t0+nt) of the channel-major image set
+// `chan` into the volume `out` (planes of ps) with the epilogue `epi`
+// (aux / norm address volumes).
+int backward_chunk(flf_ctx *ctx, const float *chan, const PlaneSet &ps, int nt, Strided out, Strided aux,
+                   Strided norm, int epi, cudaStream_t s) {
   Geometry &Gm = ctx->geo;
   const Layout &L = ctx->L;
   const int NN = L.NN, Y = Gm.Y, X = Gm.X;
-  size_t sS, sO;
-  ws_needs(ctx, ps, nt, false, sS, sO);
+  size_t sS, sO, sCv;
+  ws_needs(ctx, ps, nt, false, sS, sO, sCv);
   int rc = ensure_ws(ctx, ctx->wsS, sS);
   if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, sCv);
   if (rc != FLF_OK) return rc;
+  float *cvol = (float *)ctx->wsCvol.p;
   for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
     const int nplanes = ps.n[gi];
     if (!nplanes) continue;
     const Group &G = Gm.groups[gi];
     const int ffh = G.f * G.fh;
 
-    Rfft2Params rp{};
-    rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
-    rp.nimg = nt * NN; rp.nz = 1; rp.mode = 0;
-    rp.src = img + (long long)t0 * Y * X; rp.src_sz = 0; rp.src_st = (long long)Y * X;
-    rp.num = num ? num + (long long)t0 * Y * X : nullptr;
-    rp.planes = ctx->d_zero; rp.dst = ctx->wsS.p; rp.twiddle = G.tw;
-    rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
-    LAUNCH(ctx, "k_rfft2", (double)rp.nimg * (4.0 * Gm.Ly * Gm.Lx * (num ? 2 : 1) + 8.0 * ffh), s,
-           launch_rfft2(rp, 0, s));
+    Rfft2Params rp = rfft2_params(ctx, G, chan, nt * NN, ctx->wsS.p);
+    LAUNCH(ctx, "k_rfft2", chan_bytes(ctx, nt) + 8.0 * ffh * NN * nt, s, launch_rfft2(rp, 0, s));
 
     const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
     const int zgb = zgroup_for(ctx, nplanes, G.nkp);
@@ -678,14 +730,14 @@ int backward_chunk(flf_ctx *ctx, const float *img, const float *num, const Plane
     mp.nzo_grid = (nplanes + zgb - 1) / zgb;
     LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
 
-    Irfft2Params ip{};
-    ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
-    ip.nimg = nt * nplanes * NN; ip.nzo = nplanes; ip.src = (const float2 *)ctx->wsO.p;
-    ip.sum_stride = 0; ip.nsum = 1; ip.planes = ps.ids[gi];
-    ip.epi = epi; ip.out = out; ip.aux = aux; ip.norm = norm;
-    ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
-    const double px = 4.0 * Gm.Ly * Gm.Lx * (epi == EPI_STORE ? 1 : (epi == EPI_RL_STANDARD && norm.p ? 4 : 3));
-    LAUNCH(ctx, "k_irfft2", (double)ip.nimg * (8.0 * ffh + px), s, launch_irfft2(ip, s));
+    Irfft2Params ip = irfft2_params(ctx, G, (const float2 *)ctx->wsO.p, nt * nplanes * NN, cvol);
+    ip.final_pass = 1;
+    LAUNCH(ctx, "k_irfft2", 8.0 * ffh * NN * nt * nplanes + chan_bytes(ctx, nt * nplanes), s, launch_irfft2(ip, s));
+
+    MergeParams mg = merge_params(ctx, cvol, ps.ids[gi], nplanes, nt, epi, out, aux, norm);
+    const int npix = epi == EPI_STORE ? 1 : (epi == EPI_RL_STANDARD && norm.p ? 4 : 3);
+    LAUNCH(ctx, "k_merge", chan_bytes(ctx, nt * nplanes) + 4.0 * npix * Y * X * nt * nplanes, s,
+           launch_merge(mg, s));
   }
   return FLF_OK;
 }
@@ -777,7 +829,7 @@ int flf_ctx_destroy(flf_ctx *ctx) {
   free_geometry(ctx->geo);
   void *ptrs[] = {ctx->d_rowS, ctx->d_slotcol, ctx->d_colslot, ctx->d_rep_ch, ctx->d_rep_row,
                   ctx->d_rep_kind, ctx->d_planes_all, ctx->d_planes_user, ctx->d_zero,
-                  ctx->wsS.p, ctx->wsO.p, ctx->wsImg.p};
+                  ctx->wsS.p, ctx->wsO.p, ctx->wsCvol.p, ctx->wsCimg.p, ctx->wsCy.p};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -847,10 +899,16 @@ int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
   const long long vol_sz = (long long)T * Y * X;
+  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, TF));
+  float *cimg = (float *)ctx->wsCimg.p;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
-    Strided out{img_dev + (long long)t0 * Y * X, 0, (long long)Y * X};
-    rc = forward_chunk(ctx, vol_dev, vol_sz, ps, t0, nt, out, s);
+    rc = forward_chunk(ctx, vol_dev, vol_sz, ps, t0, nt, cimg, nullptr, s);
+    if (rc != FLF_OK) break;
+    const Strided out{img_dev + (long long)t0 * Y * X, 0, (long long)Y * X};
+    MergeParams mg = merge_params(ctx, cimg, nullptr, 1, nt, EPI_STORE, out, Strided{nullptr, 0, 0},
+                                  Strided{nullptr, 0, 0});
+    LAUNCH(ctx, "k_merge", chan_bytes(ctx, nt) + 4.0 * Y * X * nt, s, launch_merge(mg, s));
   }
   return rc;
 }
@@ -869,11 +927,15 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
   if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
+  const long long YX = (long long)Y * X;
+  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, TF));
+  float *cimg = (float *)ctx->wsCimg.p;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
-    Strided out{vol_dev + (long long)t0 * Y * X, (long long)T * Y * X, (long long)Y * X};
-    rc = backward_chunk(ctx, img_dev, nullptr, ps, t0, nt, out, Strided{nullptr, 0, 0},
-                        Strided{nullptr, 0, 0}, EPI_STORE, s);
+    SplitParams sp = split_params(ctx, img_dev + t0 * YX, 0, YX, nullptr, 1, nt, cimg);
+    LAUNCH(ctx, "k_split", chan_bytes(ctx, nt) + 4.0 * YX * nt, s, launch_split(sp, s));
+    const Strided out{vol_dev + t0 * YX, (long long)T * YX, YX};
+    rc = backward_chunk(ctx, cimg, ps, nt, out, Strided{nullptr, 0, 0}, Strided{nullptr, 0, 0}, EPI_STORE, s);
   }
   return rc;
 }
@@ -892,8 +954,15 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
                 "with this image shape first", Y, X);
   const Layout &L = ctx->L;
   const int NN = L.NN;
+  // scratch: S (one frame's channel spectra) | C (its channel-major image) |
+  // blocks of zb planes of O (output spectra) and their channel-major images
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t cimg = up(sizeof(float) * chan_set_floats(ctx));
   size_t need = 0;
-  for (const Group &G : Gm.groups) need = std::max(need, 2 * sizeof(float2) * (size_t)NN * G.f * G.fh);
+  for (const Group &G : Gm.groups) {
+    const size_t spec = up(sizeof(float2) * (size_t)NN * G.f * G.fh);
+    need = std::max(need, spec + cimg + spec + cimg);
+  }
   if (need > FLF_NOALLOC_SCRATCH_BYTES)
     return fail(ctx, FLF_E_ARG,
                 "flf_backward_noalloc needs %zu bytes of scratch for this geometry (Nnum %d, transform %d), "
@@ -904,20 +973,21 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
   if (rc != FLF_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const long long YX = (long long)Y * X;
+  char *base = (char *)scratch;
+  float *C = (float *)base;
   for (int t = 0; t < T; t++) {
-    for (const Group &G : Gm.groups) {
-      const size_t spec = sizeof(float2) * (size_t)NN * G.f * G.fh;   // one frame or one plane
-      float2 *S = (float2 *)scratch;                        // channel spectra of the frame
-      float2 *O = (float2 *)((char *)scratch + spec);       // output spectra of a group of planes
+    cudaError_t e = launch_split(split_params(ctx, img_dev + t * YX, 0, YX, nullptr, 1, 1, C), s);
+    for (size_t gi = 0; gi < Gm.groups.size() && e == cudaSuccess; gi++) {
+      const Group &G = Gm.groups[gi];
+      const size_t spec = up(sizeof(float2) * (size_t)NN * G.f * G.fh);   // one frame or one plane
+      float2 *S = (float2 *)(base + cimg);
+      char *blocks = base + cimg + spec;
+      const size_t per_plane = spec + cimg;
       const int ng = (int)G.planes.size();
-      const int zb = std::max(1, std::min(ng, (int)((FLF_NOALLOC_SCRATCH_BYTES - spec) / spec)));
-      Rfft2Params rp{};
-      rp.plan = G.plan; rp.N = ctx->N; rp.Y = Y; rp.X = X; rp.Ly = Gm.Ly; rp.Lx = Gm.Lx;
-      rp.nimg = NN; rp.nz = 1; rp.mode = 0;
-      rp.src = img_dev + t * YX; rp.src_sz = 0; rp.src_st = YX;
-      rp.planes = ctx->d_zero; rp.dst = S; rp.twiddle = G.tw;
-      rp.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024); rp.nq_rows = (Gm.Ly + 1) / 2;
-      cudaError_t e = launch_rfft2(rp, 0, s);
+      const int zb = std::max(1, std::min(ng, (int)((FLF_NOALLOC_SCRATCH_BYTES - cimg - spec) / per_plane)));
+      float2 *O = (float2 *)blocks;
+      float *Co = (float *)(blocks + spec * zb);
+      e = launch_rfft2(rfft2_params(ctx, G, C, NN, S), 0, s);
       for (int z0 = 0; z0 < ng && e == cudaSuccess; z0 += zb) {
         const int nzl = std::min(zb, ng - z0);
         const int zg = zgroup_for(ctx, nzl, G.nkp);
@@ -926,17 +996,16 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
         mp.S = S; mp.nzS = 1; mp.O = O; mp.nzo = nzl; mp.nzo_grid = (nzl + zg - 1) / zg;
         e = launch_mac(mp, false, s);
         if (e != cudaSuccess) break;
-        Irfft2Params ip{};
-        ip.plan = G.plan; ip.N = ctx->N; ip.Y = Y; ip.X = X; ip.Ly = Gm.Ly; ip.Lx = Gm.Lx;
-        ip.nimg = nzl * NN; ip.nzo = nzl; ip.src = O; ip.sum_stride = 0; ip.nsum = 1;
-        ip.planes = G.d_ids + z0; ip.epi = EPI_STORE;
-        ip.out = Strided{vol_dev + t * YX, (long long)T * YX, YX};
-        ip.aux = Strided{nullptr, 0, 0}; ip.norm = Strided{nullptr, 0, 0};
-        ip.twiddle = G.tw; ip.imgs_per_cta = imgs_per_cta(G.f, 0, 110 * 1024);
+        Irfft2Params ip = irfft2_params(ctx, G, O, nzl * NN, Co);
+        ip.final_pass = 1;
         e = launch_irfft2(ip, s);
+        if (e != cudaSuccess) break;
+        const Strided out{vol_dev + t * YX, (long long)T * YX, YX};
+        e = launch_merge(merge_params(ctx, Co, G.d_ids + z0, nzl, 1, EPI_STORE, out, Strided{nullptr, 0, 0},
+                                      Strided{nullptr, 0, 0}), s);
       }
-      if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "flf_backward_noalloc launch failed: %s", cudaGetErrorString(e));
     }
+    if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "flf_backward_noalloc launch failed: %s", cudaGetErrorString(e));
   }
   return FLF_OK;
 }
@@ -958,25 +1027,33 @@ int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float
   if (rc != FLF_OK) return rc;
   const int TF = mac_max_frames();
   const long long YX = (long long)Y * X;
-  rc = ensure_ws(ctx, ctx->wsImg, sizeof(float) * (size_t)TF * YX);
+  const size_t cset = sizeof(float) * chan_set_floats(ctx) * std::min(T, TF);
+  rc = ensure_ws(ctx, ctx->wsCimg, cset);
+  if (rc == FLF_OK && variant == FLF_RL_STANDARD) rc = ensure_ws(ctx, ctx->wsCy, cset);
   PlaneSet ps;
   if (rc == FLF_OK) rc = make_plane_set(ctx, nullptr, ctx->nz, s, ps);
   if (rc != FLF_OK) return rc;
-  float *hx = (float *)ctx->wsImg.p;
+  float *cimg = (float *)ctx->wsCimg.p;
+  float *cy = (float *)ctx->wsCy.p;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
     const Strided xs{x_dev + t0 * YX, (long long)T * YX, YX};
+    if (variant == FLF_RL_STANDARD && iters > 0) {
+      SplitParams sp = split_params(ctx, ref_dev + t0 * YX, 0, YX, nullptr, 1, nt, cy);
+      LAUNCH(ctx, "k_split", chan_bytes(ctx, nt) + 4.0 * YX * nt, s, launch_split(sp, s));
+    }
     for (int it = 0; it < iters && rc == FLF_OK; it++) {
-      // H x, then Ht of (Htf update) or of y / H x (the division is fused into the gather)
-      rc = forward_chunk(ctx, x_dev, (long long)T * YX, ps, t0, nt, Strided{hx, 0, YX}, s);
+      // H x (Prevedel) or y / H x (standard) as channel-major images, then the
+      // back projection with the update fused into its pixel epilogue
+      rc = forward_chunk(ctx, x_dev, (long long)T * YX, ps, t0, nt, cimg,
+                         variant == FLF_RL_STANDARD ? cy : nullptr, s);
       if (rc != FLF_OK) break;
       if (variant == FLF_RL_PREVEDEL) {
         const Strided htf{const_cast<float *>(ref_dev) + t0 * YX, (long long)T * YX, YX};
-        rc = backward_chunk(ctx, hx, nullptr, ps, 0, nt, xs, htf, Strided{nullptr, 0, 0}, EPI_RL_PREVEDEL, s);
+        rc = backward_chunk(ctx, cimg, ps, nt, xs, htf, Strided{nullptr, 0, 0}, EPI_RL_PREVEDEL, s);
       } else {
         const Strided nrm{const_cast<float *>(norm_dev), YX, 0};
-        rc = backward_chunk(ctx, hx, ref_dev + t0 * YX, ps, 0, nt, xs, Strided{nullptr, 0, 0}, nrm,
-                            EPI_RL_STANDARD, s);
+        rc = backward_chunk(ctx, cimg, ps, nt, xs, Strided{nullptr, 0, 0}, nrm, EPI_RL_STANDARD, s);
       }
     }
   }
@@ -995,7 +1072,7 @@ int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {
     for (int d = 0; d < 2; d++)
       if (G.P[d]) b += pe;
   }
-  b += ctx->wsS.bytes + ctx->wsO.bytes + ctx->wsImg.bytes;
+  b += ctx->wsS.bytes + ctx->wsO.bytes + ctx->wsCvol.bytes + ctx->wsCimg.bytes + ctx->wsCy.bytes;
   *bytes = b;
   return FLF_OK;
 }
@@ -1005,7 +1082,7 @@ int flf_clear_cache(flf_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
   free_geometry(ctx->geo);
-  Workspace *ws[] = {&ctx->wsS, &ctx->wsO, &ctx->wsImg};
+  Workspace *ws[] = {&ctx->wsS, &ctx->wsO, &ctx->wsCvol, &ctx->wsCimg, &ctx->wsCy};
   for (Workspace *w : ws) {
     if (w->p) cudaFree(w->p);
     *w = Workspace();

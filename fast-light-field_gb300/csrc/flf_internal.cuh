@@ -63,7 +63,24 @@ inline Layout make_layout(int N) {
   return L;
 }
 
-// Epilogue modes of the inverse transform kernel.
+// ----------------------------------------------------------------------------
+// Runtime division by an invariant divisor d (1 <= d < 2^16) for n < 2^16:
+// n / d = (n * m) >> 32 with m = ceil(2^32 / d) (Granlund & Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994; exact
+// because n * (m * d - 2^32) < 2^32 for these ranges).  m is kept in 64 bits
+// (m = 2^32 for d = 1) and the product is one wide multiply.
+// ----------------------------------------------------------------------------
+struct Div16 {
+  unsigned long long m;
+  __host__ static Div16 make(unsigned d) {
+    Div16 r;
+    r.m = ((1ull << 32) + d - 1) / d;
+    return r;
+  }
+  __device__ __forceinline__ unsigned div(unsigned n) const { return (unsigned)(((unsigned long long)n * m) >> 32); }
+};
+
+// Epilogue modes of the pixel merge kernel.
 enum Epilogue : int {
   EPI_STORE = 0,         // out = value
   EPI_DIVIDE = 1,        // out = aux / value           (y / Hx)
@@ -81,38 +98,62 @@ struct Strided {         // base + plane*sz + frame*st + y*X + x
 // Kernel parameter blocks
 // ----------------------------------------------------------------------------
 
+// Channel-major images: image g is Ly rows of Lxp floats (Lxp = Lx rounded up
+// to a multiple of 4, so every row and image starts on a 16-byte boundary);
+// element (r, c) of channel ch = b*N + a is pixel (r*N + b, c*N + a).  The
+// columns c in [Lx, Lxp) are padding.
+inline int channel_pitch(int Lx) { return (Lx + 3) & ~3; }
+
 struct Rfft2Params {
   FftPlan plan;
   int N, Y, X, Ly, Lx;
   int nimg;                 // total images
-  int nz;                   // planes per frame in this launch
-  int mode;                 // 0: channel gather from [Z][T][Y][X]; 1: contiguous f*f images
-  const float *src;         // mode 0 (float input)
-  long long src_sz, src_st; // mode 0 strides (plane, frame)
-  const int *planes;        // mode 0: plane id per z index (device)
-  const float *num;         // mode 0, optional: gather num / src instead of src (same layout)
+  int mode;                 // 0: channel-major float images (chan); 1: contiguous f*f images
+  const float *chan;        // mode 0: [nimg][Ly][Lxp], image g = set * NN + ch
+  int Lxp;
   const void *src_img;      // mode 1: Real images [nimg][f][f]
   void *dst;                // Complex<Real> [nimg][f][fh]
   const void *twiddle;      // Complex<Real> [f]
-  int imgs_per_cta;
-  int nq_rows;              // row pairs carrying data (<= f/2)
+  int imgs_per_cta;         // mode 1
+  int nq_rows;              // mode 1: row pairs carrying data (<= f/2)
 };
 
 struct Irfft2Params {
   FftPlan plan;
   int N, Y, X, Ly, Lx;
-  int nimg;                 // images: (t*nzo + zo)*NN + j
-  int nzo;                  // output planes per frame
+  int nimg;                 // images g = set * NN + j
   const float2 *src;        // spectra [nsum][nimg][f][fh]
   long long sum_stride;     // elements between partial sums
   int nsum;
+  float *chan;              // output: channel-major [nimg][Ly][Lxp]
+  int Lxp;
+  int add;                  // add to chan instead of overwriting it
+  int final_pass;           // zero the positions outside the Y x X image (and the padding)
+  const float *num;         // final pass, optional: store num / value (channel-major, like chan)
+  const float2 *twiddle;
+};
+
+// Pixel images <-> channel-major images (the lenslet interleave).
+struct SplitParams {        // src + plane*src_sz + t*src_st: Y x X pixels
+  const float *src;
+  long long src_sz, src_st;
+  const int *planes;        // plane id per z index (device); NULL -> z index
+  int nz, nsets;            // set s = t * nz + zi
+  int N, Y, X, Ly, Lx, Lxp;
+  float *dst;               // [nsets][NN][Ly][Lxp]
+  Div16 dlxp;               // set by the launcher
+};
+
+struct MergeParams {
+  const float *src;         // [nsets][NN][Ly][Lxp], set s = t * nzo + zo
+  int nzo, nsets;
   const int *planes;        // plane id per zo (device); NULL -> zo
+  int N, Y, X, Ly, Lx, Lxp;
   int epi;
   Strided out;              // destination (or x for RL updates)
   Strided aux;              // y (EPI_DIVIDE) or Htf (EPI_RL_PREVEDEL)
   Strided norm;             // EPI_RL_STANDARD normaliser (p may be NULL)
-  const float2 *twiddle;
-  int imgs_per_cta;
+  Div16 dlx, dn;            // set by the launcher
 };
 
 struct MacParams {
@@ -162,11 +203,12 @@ struct PackParams {
 // Launchers (flf_kernels.cu)
 cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s);
 cudaError_t launch_irfft2(const Irfft2Params &p, cudaStream_t s);
+cudaError_t launch_split(const SplitParams &p, cudaStream_t s);
+cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);
 cudaError_t launch_pack(const PackParams &p, cudaStream_t s);
 size_t rfft2_smem_bytes(int f, int imgs, int fp64);
-size_t irfft2_smem_bytes(int f, int imgs);
 int mac_max_frames();
 size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int split, bool fwd);
 

@@ -3,6 +3,7 @@
 // crop / plane reduction / Richardson-Lucy epilogues, and the PSF transfer
 // matrix precompute.  Host code that sequences them is flf_api.cu.
 #include "flf_internal.cuh"
+#include "flf_fft.cuh"
 
 #include <cstdio>
 
@@ -132,11 +133,10 @@ __device__ C *fft_pass(C *A, C *B, int imgStride, int nimg, int ntrans, int es, 
 }
 
 // ----------------------------------------------------------------------------
-// Forward real 2-D transform f x f -> f x (f/2+1), with the lenslet-channel
-// gather of the input (the reference's strided sub-image FFT,
-// special_fftconvolve.py:85-105 / py_light_field.cpp:1001-1027, done for all
-// offsets at once).  Two real rows are packed into one complex row for the
-// row pass and split afterwards.
+// Forward real 2-D transform f x f -> f x (f/2+1) of contiguous images, in
+// float or double (the transfer-matrix precompute; the hot-path transforms are
+// the size-specialised kernels of flf_fft.cuh).  Two real rows are packed into
+// one complex row for the row pass and split afterwards.
 // ----------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_rfft2(Rfft2Params p) {
@@ -152,47 +152,13 @@ __global__ void __launch_bounds__(256) k_rfft2(Rfft2Params p) {
   const int g0 = blockIdx.x * p.imgs_per_cta;
   const int nb = min(p.imgs_per_cta, p.nimg - g0);
   const int nq = p.nq_rows;
-  const int N = p.N, NN = N * N;
 
   for (int idx = threadIdx.x; idx < nb * nq * f; idx += blockDim.x) {
     const int c = idx % f;
     const int q = (idx / f) % nq;
     const int img = idx / (f * nq);
-    const int g = g0 + img;
-    const int r0 = 2 * q, r1 = 2 * q + 1;
-    R v0 = 0, v1 = 0;
-    if (p.mode == 0) {
-      const int ch = g % NN;
-      const int tz = g / NN;
-      const int zi = tz % p.nz;
-      const int t = tz / p.nz;
-      const int b = ch / N, a = ch % N;
-      const int plane = p.planes ? p.planes[zi] : zi;
-      const float *base = p.src + plane * p.src_sz + t * p.src_st;
-      const int x = c * N + a;
-      if (c < p.Lx && x < p.X) {
-        const int y0 = r0 * N + b, y1 = r1 * N + b;
-        if (p.num) {   // the standard RL error image num / src (lfdeconv.py:192)
-          const float *nb = p.num + t * p.src_st;
-          if (r0 < p.Ly && y0 < p.Y) {
-            const long long o = (long long)y0 * p.X + x;
-            v0 = (R)__fdiv_rn(nb[o], base[o]);
-          }
-          if (r1 < p.Ly && y1 < p.Y) {
-            const long long o = (long long)y1 * p.X + x;
-            v1 = (R)__fdiv_rn(nb[o], base[o]);
-          }
-        } else {
-          if (r0 < p.Ly && y0 < p.Y) v0 = (R)base[(long long)y0 * p.X + x];
-          if (r1 < p.Ly && y1 < p.Y) v1 = (R)base[(long long)y1 * p.X + x];
-        }
-      }
-    } else {
-      const R *im = reinterpret_cast<const R *>(p.src_img) + (long long)g * f * f;
-      v0 = im[r0 * f + c];
-      v1 = im[r1 * f + c];
-    }
-    A[img * isz + q * f + c] = cmk<C>(v0, v1);
+    const R *im = reinterpret_cast<const R *>(p.src_img) + (long long)(g0 + img) * f * f;
+    A[img * isz + q * f + c] = cmk<C>(im[(2 * q) * f + c], im[(2 * q + 1) * f + c]);
   }
   __syncthreads();
 
@@ -220,105 +186,6 @@ __global__ void __launch_bounds__(256) k_rfft2(Rfft2Params p) {
   C *Out = fft_pass<C>(Yb, Rr, isz, nb, fh, fh, 1, p.plan, W, false);
   C *dst = reinterpret_cast<C *>(p.dst) + (long long)g0 * isz;
   for (int idx = threadIdx.x; idx < nb * isz; idx += blockDim.x) dst[idx] = Out[idx];
-}
-
-// ----------------------------------------------------------------------------
-// Inverse real 2-D transform f x (f/2+1) -> f x f (unscaled: 1/f^2 is folded
-// into the transfer matrices), summed over partial spectra, cropped to the
-// Ly x Lx lenslet grid and scattered back to pixels (p*N + beta, q*N + alpha).
-// This is the reference's InverseRFFTList + CropAfterFFT
-// (py_light_field.cpp:925-950, projector.py:792-796) with the RL update of
-// lfdeconv.py:112-183 fused into the store.
-// ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_irfft2(Irfft2Params p) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int f = p.plan.n, fh = f / 2 + 1, isz = f * fh;
-  float2 *W = reinterpret_cast<float2 *>(smraw);
-  float2 *A = W + f;
-  float2 *Bf = A + p.imgs_per_cta * isz;
-  for (int i = threadIdx.x; i < f; i += blockDim.x) W[i] = p.twiddle[i];
-
-  const int g0 = blockIdx.x * p.imgs_per_cta;
-  const int nb = min(p.imgs_per_cta, p.nimg - g0);
-  const float2 *src = p.src + (long long)g0 * isz;
-  for (int idx = threadIdx.x; idx < nb * isz; idx += blockDim.x) {
-    float2 v = src[idx];
-    for (int s = 1; s < p.nsum; s++) {
-      const float2 w = src[s * p.sum_stride + idx];
-      v.x += w.x;
-      v.y += w.y;
-    }
-    A[idx] = v;
-  }
-  __syncthreads();
-
-  float2 *Rr = fft_pass<float2>(A, Bf, isz, nb, fh, fh, 1, p.plan, W, true);
-  float2 *Zb = (Rr == A) ? Bf : A;
-
-  const int nq = (p.Ly + 1) / 2;
-  const int half = f / 2;
-  for (int idx = threadIdx.x; idx < nb * nq * f; idx += blockDim.x) {
-    const int c = idx % f;
-    const int q = (idx / f) % nq;
-    const int img = idx / (f * nq);
-    const float2 *r0 = Rr + img * isz + (2 * q) * fh;
-    const float2 *r1 = r0 + fh;
-    float2 a, b;
-    if (c <= half) {
-      a = r0[c];
-      b = r1[c];
-      if (c == 0 || c == half) { a.y = 0.f; b.y = 0.f; }
-    } else {
-      a = cconj(r0[f - c]);
-      b = cconj(r1[f - c]);
-    }
-    Zb[img * isz + q * f + c] = make_float2(a.x - b.y, a.y + b.x);
-  }
-  __syncthreads();
-
-  float2 *Out = fft_pass<float2>(Zb, Rr, isz, nb, nq, 1, f, p.plan, W, true);
-
-  const int N = p.N, NN = N * N;
-  for (int idx = threadIdx.x; idx < nb * p.Ly * p.Lx; idx += blockDim.x) {
-    const int c = idx % p.Lx;
-    const int r = (idx / p.Lx) % p.Ly;
-    const int img = idx / (p.Lx * p.Ly);
-    const int g = g0 + img;
-    const int j = g % NN;
-    const int tz = g / NN;
-    const int zo = tz % p.nzo;
-    const int t = tz / p.nzo;
-    const int y = r * N + j / N, x = c * N + j % N;
-    if (y >= p.Y || x >= p.X) continue;
-    const float2 zv = Out[img * isz + (r >> 1) * f + c];
-    const float val = (r & 1) ? zv.y : zv.x;
-    const int plane = p.planes ? p.planes[zo] : zo;
-    const long long pix = (long long)y * p.X + x;
-    float *o = p.out.p + plane * p.out.sz + t * p.out.st + pix;
-    switch (p.epi) {
-      case EPI_STORE: *o = val; break;
-      case EPI_ADD: *o += val; break;
-      case EPI_DIVIDE: {
-        const float yv = p.aux.p[plane * p.aux.sz + t * p.aux.st + pix];
-        *o = __fdiv_rn(yv, val);
-        break;
-      }
-      case EPI_RL_PREVEDEL: {
-        const float htf = p.aux.p[plane * p.aux.sz + t * p.aux.st + pix];
-        float r2 = __fmul_rn(*o, __fdiv_rn(htf, val));
-        if (r2 != r2) r2 = 0.f;
-        *o = r2;
-        break;
-      }
-      default: {
-        float r2 = __fmul_rn(*o, val);
-        if (p.norm.p) r2 = __fdiv_rn(r2, p.norm.p[plane * p.norm.sz + t * p.norm.st + pix]);
-        if (r2 != r2) r2 = 0.f;
-        *o = r2;
-        break;
-      }
-    }
-  }
 }
 
 // ----------------------------------------------------------------------------
@@ -881,16 +748,140 @@ size_t rfft2_smem_bytes(int f, int imgs, int fp64) {
   const size_t isz = (size_t)f * (f / 2 + 1);
   return cs * ((size_t)f + 2 * (size_t)imgs * isz);
 }
-size_t irfft2_smem_bytes(int f, int imgs) { return rfft2_smem_bytes(f, imgs, 0); }
-
 static cudaError_t set_smem(const void *fn, size_t bytes) {
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// ----------------------------------------------------------------------------
+// Lenslet interleave.  A pixel row y = r*N + b holds row r of the N channel
+// images (b, a), a = 0..N-1, interleaved with stride N.  Both kernels work
+// on one pixel row per CTA so that every global access is coalesced: the
+// pixel row is read or written contiguously and each channel row is a
+// contiguous run of Lxp floats.  This is the reference's strided sub-image
+// access (special_fftconvolve.py:85-105, py_light_field.cpp:1001-1027 on
+// input; projector.py:792-796 and the RL update of lfdeconv.py:112-183 on
+// output) moved out of the transforms.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_split(SplitParams p) {
+  extern __shared__ float row[];                 // X floats
+  const int y = blockIdx.x, s = blockIdx.y;
+  const int N = p.N, NN = N * N, X = p.X, Lx = p.Lx, Lxp = p.Lxp, Ly = p.Ly;
+  const int t = s / p.nz, zi = s - t * p.nz;
+  const int r = y / N, b = y - r * N;
+  const bool inside = y < p.Y;                   // rows of the last lenslet row beyond Y are zeros
+  if (inside) {
+    const int plane = p.planes ? p.planes[zi] : zi;
+    const float *src = p.src + plane * p.src_sz + t * p.src_st + (long long)y * X;
+    for (int x = threadIdx.x; x < X; x += blockDim.x) row[x] = __ldg(src + x);
+  }
+  __syncthreads();
+  float *dst = p.dst + ((long long)s * NN + b * N) * Ly * Lxp + (long long)r * Lxp;
+  const long long cstride = (long long)Ly * Lxp;
+  for (int i = threadIdx.x; i < N * Lxp; i += blockDim.x) {
+    const int a = (int)p.dlxp.div(i);
+    const int c = i - a * Lxp;
+    const int x = c * N + a;
+    dst[a * cstride + c] = (inside && c < Lx && x < X) ? row[x] : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_merge(MergeParams p) {
+  extern __shared__ float sm[];                  // N rows of pitch Lx | 1
+  const int y = blockIdx.x, s = blockIdx.y;
+  const int N = p.N, NN = N * N, X = p.X, Lx = p.Lx, Lxp = p.Lxp, Ly = p.Ly;
+  const int pitch = Lx | 1;
+  const int t = s / p.nzo, zo = s - t * p.nzo;
+  const int r = y / N, beta = y - r * N;
+  const float *src = p.src + ((long long)s * NN + beta * N) * Ly * Lxp + (long long)r * Lxp;
+  const long long cstride = (long long)Ly * Lxp;
+  for (int i = threadIdx.x; i < N * Lx; i += blockDim.x) {
+    const int a = (int)p.dlx.div(i);
+    const int c = i - a * Lx;
+    sm[a * pitch + c] = __ldg(src + a * cstride + c);
+  }
+  __syncthreads();
+  const int plane = p.planes ? p.planes[zo] : zo;
+  const long long row = (long long)y * X;
+  float *out = p.out.p + plane * p.out.sz + t * p.out.st + row;
+  const float *aux = p.aux.p ? p.aux.p + plane * p.aux.sz + t * p.aux.st + row : nullptr;
+  const float *nrm = p.norm.p ? p.norm.p + plane * p.norm.sz + t * p.norm.st + row : nullptr;
+  const int epi = p.epi;
+  const bool need_o = epi == EPI_ADD || epi == EPI_RL_PREVEDEL || epi == EPI_RL_STANDARD;
+  const bool need_a = epi == EPI_DIVIDE || epi == EPI_RL_PREVEDEL;
+  const bool need_n = epi == EPI_RL_STANDARD && nrm != nullptr;
+  constexpr int U = 4;                           // pixels per thread per round, loads first
+  for (int x0 = threadIdx.x; x0 < X; x0 += U * blockDim.x) {
+    float v[U], ov[U], av[U], nv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const int x = x0 + k * blockDim.x;
+      const bool ok = x < X;
+      const int c = ok ? (int)p.dn.div(x) : 0;
+      v[k] = ok ? sm[(x - c * N) * pitch + c] : 0.f;
+      ov[k] = (ok && need_o) ? out[x] : 0.f;
+      av[k] = (ok && need_a) ? __ldg(aux + x) : 0.f;
+      nv[k] = (ok && need_n) ? __ldg(nrm + x) : 1.f;
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const int x = x0 + k * blockDim.x;
+      if (x >= X) break;
+      float res;
+      switch (epi) {
+        case EPI_STORE: res = v[k]; break;
+        case EPI_ADD: res = ov[k] + v[k]; break;
+        case EPI_DIVIDE: res = __fdiv_rn(av[k], v[k]); break;
+        case EPI_RL_PREVEDEL:          // x * (Htf / Ht(H x)), lfdeconv.py:112-145
+          res = __fmul_rn(ov[k], __fdiv_rn(av[k], v[k]));
+          if (res != res) res = 0.f;
+          break;
+        default:                       // x * Ht(y / H x) [/ norm], lfdeconv.py:147-183
+          res = __fmul_rn(ov[k], v[k]);
+          if (need_n) res = __fdiv_rn(res, nv[k]);
+          if (res != res) res = 0.f;
+          break;
+      }
+      out[x] = res;
+    }
+  }
+}
+
+cudaError_t launch_split(const SplitParams &p0, cudaStream_t s) {
+  if (p0.nsets == 0) return cudaSuccess;
+  SplitParams p = p0;
+  p.dlxp = Div16::make((unsigned)p.Lxp);
+  const dim3 grid(p.Ly * p.N, p.nsets);
+  k_split<<<grid, 256, p.X * sizeof(float), s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_merge(const MergeParams &p0, cudaStream_t s) {
+  if (p0.nsets == 0) return cudaSuccess;
+  MergeParams p = p0;
+  p.dlx = Div16::make((unsigned)p.Lx);
+  p.dn = Div16::make((unsigned)p.N);
+  const dim3 grid(p.Y, p.nsets);
+  k_merge<<<grid, 256, p.N * (p.Lx | 1) * sizeof(float), s>>>(p);
+  return cudaGetLastError();
+}
+
+// Transforms: the hot path runs the size-specialised kernels (flf_fft.cuh),
+// one per even 7-smooth size up to kMaxF; the precompute (contiguous float or
+// double images) runs the runtime-plan kernel above.
 cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s) {
+  if (p.nimg == 0) return cudaSuccess;
+  if (p.mode == 0) {
+    if (fp64) return cudaErrorInvalidValue;
+    switch (p.plan.n) {
+#define FLF_CASE(F) \
+      case F: return sfft::rfft2_sized<F>(p, s);
+      FLF_SFFT_SIZES(FLF_CASE)
+#undef FLF_CASE
+      default: return cudaErrorInvalidValue;
+    }
+  }
   const size_t sm = rfft2_smem_bytes(p.plan.n, p.imgs_per_cta, fp64);
   const int grid = (p.nimg + p.imgs_per_cta - 1) / p.imgs_per_cta;
-  if (grid == 0) return cudaSuccess;
   cudaError_t e;
   if (fp64) {
     if ((e = set_smem((const void *)k_rfft2<double>, sm)) != cudaSuccess) return e;
@@ -903,13 +894,14 @@ cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s) {
 }
 
 cudaError_t launch_irfft2(const Irfft2Params &p, cudaStream_t s) {
-  const size_t sm = irfft2_smem_bytes(p.plan.n, p.imgs_per_cta);
-  const int grid = (p.nimg + p.imgs_per_cta - 1) / p.imgs_per_cta;
-  if (grid == 0) return cudaSuccess;
-  cudaError_t e = set_smem((const void *)k_irfft2, sm);
-  if (e != cudaSuccess) return e;
-  k_irfft2<<<grid, 256, sm, s>>>(p);
-  return cudaGetLastError();
+  if (p.nimg == 0) return cudaSuccess;
+  switch (p.plan.n) {
+#define FLF_CASE(F) \
+    case F: return sfft::irfft2_sized<F>(p, s);
+    FLF_SFFT_SIZES(FLF_CASE)
+#undef FLF_CASE
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 int mac_max_frames() { return 4; }

@@ -203,6 +203,48 @@ def test_transform_groups_match_uniform_transform(mods):
     assert rel(bk, bo) < PROJ_TOL
 
 
+SIZED_FFT_SIZES = [f for f in range(4, 161, 2)
+                   if all(f % p for p in (11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71, 73, 79))]
+
+
+@pytest.mark.parametrize("f", SIZED_FFT_SIZES)
+def test_every_transform_size(mods, f):
+    """Each size-specialised transform (every even 7-smooth f in [4, 160]) against
+    the oracle, forward and backward, on ragged lenslet grids (odd and even row
+    counts, images not a multiple of Nnum)."""
+    import torch
+    import synthetic
+    import _flf
+    N = 3
+    H, Ht = synthetic.random_psf(N, [3, 5], seed=f)          # kernel radius 1 lenslet
+    R = 2
+    Ly = max(1, f - R - (f % 3))
+    Lx = max(1, f - R - (f % 5) - 1)
+    Y, X = N * Ly - 1 if Ly > 1 else N, N * Lx - 2 if Lx > 1 else N
+    T = 2
+    rng = np.random.default_rng(f)
+    img = rng.random((T, Y, X)).astype(np.float32)
+    vol = rng.random((2, T, Y, X)).astype(np.float32)
+    dev = torch.device("cuda", 0)
+    ctx = _flf.Context(N, 2, 0)
+    for z in range(2):
+        ctx.upload_psf(z, _flf.FLF_DIR_FORWARD, H[z])
+        ctx.upload_psf(z, _flf.FLF_DIR_BACKWARD, Ht[z])
+    ctx.set_option("plane_transform_sizes", 0)
+    ctx.prepare(Y, X, fft_size=f)
+    assert ctx.geometry()["f"] == f
+    bk = torch.full((2, T, Y, X), float("nan"), device=dev)
+    fw = torch.full((T, Y, X), float("nan"), device=dev)
+    ctx.backward(torch.as_tensor(img, device=dev), bk, T, Y, X)
+    ctx.forward(torch.as_tensor(vol, device=dev), fw, T, Y, X)
+    ctx.synchronize()
+    ctx.close()
+    bo = O.backward_project(Ht, img, N, method="direct", dtype=np.float64)
+    fo = O.forward_project(H, vol, N, method="direct", dtype=np.float64)
+    assert rel(bk.cpu().numpy(), bo) < PROJ_TOL
+    assert rel(fw.cpu().numpy(), fo) < PROJ_TOL
+
+
 def test_planes_validation(mods):
     projector, lfdeconv, psfmatrix = mods
     c = case_inputs("planes_n7")
