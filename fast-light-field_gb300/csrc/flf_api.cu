@@ -228,16 +228,26 @@ int build_tables(flf_ctx *ctx) {
   auto My = [&](int i) { return (N - 1 - i / N) * N + i % N; };
   auto Mx = [&](int i) { return (i / N) * N + (N - 1 - i % N); };
   auto Mxy = [&](int i) { return NN - 1 - i; };
-  std::vector<short> slotcol;
+  // Slot order of a stored row: for the c^2 generic orbits o = be*c + al,
+  // four blocks of c^2 slots (q, My q, Mx q, Mxy q of every orbit), then the
+  // c orbits [q, My q] (alpha = c) as two blocks of c, the c orbits [q, Mx q]
+  // (beta = c) as two blocks of c, then the centre.  A warp's threads (one
+  // orbit each) read each block with consecutive addresses.
+  const int c2 = c * c;
+  std::vector<short> slotcol(NN, -1);
   for (int be = 0; be < c; be++)
     for (int al = 0; al < c; al++) {
-      int q = be * N + al;
-      slotcol.push_back(q); slotcol.push_back(My(q)); slotcol.push_back(Mx(q)); slotcol.push_back(Mxy(q));
+      const int o = be * c + al, q = be * N + al;
+      slotcol[o] = q; slotcol[c2 + o] = My(q); slotcol[2 * c2 + o] = Mx(q); slotcol[3 * c2 + o] = Mxy(q);
     }
-  for (int be = 0; be < c; be++) { int q = be * N + c; slotcol.push_back(q); slotcol.push_back(My(q)); }
-  for (int al = 0; al < c; al++) { int q = c * N + al; slotcol.push_back(q); slotcol.push_back(Mx(q)); }
-  slotcol.push_back(c * N + c);
-  if ((int)slotcol.size() != NN) return fail(ctx, FLF_E_STATE, "internal: slot table size");
+  for (int j = 0; j < c; j++) {
+    const int qa = j * N + c, qb = c * N + j;
+    slotcol[4 * c2 + j] = qa; slotcol[4 * c2 + c + j] = My(qa);
+    slotcol[4 * c2 + 2 * c + j] = qb; slotcol[4 * c2 + 3 * c + j] = Mx(qb);
+  }
+  slotcol[4 * c2 + 4 * c] = c * N + c;
+  for (int sl = 0; sl < NN; sl++)
+    if (slotcol[sl] < 0) return fail(ctx, FLF_E_STATE, "internal: slot table");
   std::vector<short> colslot(NN, -1);
   for (int s = 0; s < NN; s++) colslot[slotcol[s]] = s;
 
@@ -558,13 +568,14 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
 
 // Planes per CTA of the multiply-accumulate: enough CTAs for about 32 per SM
 // (a few waves at the kernel's occupancy), as few plane groups as that allows.
+// Planes per multiply-accumulate CTA: enough CTAs for 32 per SM, at most
+// kMacMaxZgroup planes each.
 int zgroup_for(const flf_ctx *ctx, int nz, int nkp) {
   const int target = 32 * std::max(1, ctx->num_sms);
   const int nzg_needed = std::min(nz, std::max(1, (target + nkp - 1) / nkp));
-  return std::max(1, (nz + nzg_needed - 1) / nzg_needed);
+  return std::min(kMacMaxZgroup, std::max(1, (nz + nzg_needed - 1) / nzg_needed));
 }
 
-// Workspace needs of one projection over plane set ps (bytes of S and O).
 // Floats of one channel-major image set (NN channel images of Ly x Lxp).
 size_t chan_set_floats(const flf_ctx *ctx) {
   const Geometry &G = ctx->geo;

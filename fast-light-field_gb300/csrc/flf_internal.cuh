@@ -28,6 +28,7 @@ namespace flf {
 constexpr int kMaxStages = 12;
 constexpr int kMaxF = 160;          // largest lenslet-grid FFT size (float)
 constexpr int kMaxF64 = 112;        // largest size for the fp64 precompute
+constexpr int kMacMaxZgroup = 64;   // planes per multiply-accumulate CTA
 
 struct FftPlan {
   int n;                 // transform length (f)
@@ -40,9 +41,10 @@ struct FftPlan {
 //   fq = f/2 + 1; rows = 2*n_h^2; slot stride RS = N*N rounded up to even.
 // Rows: 2c^2 "generic" input channels (b < c, a != c) stored at u, then for
 // each of the 2c+1 centre-cross channels (b < c, a = c), (b = c, a < c),
-// (c, c) a pair of rows holding u and u*.  Slots: output channels grouped by
-// mirror orbit: c^2 generic orbits [q, My q, Mx q, Mxy q], c orbits
-// [q, My q] (alpha = c), c orbits [q, Mx q] (beta = c), then the centre.
+// (c, c) a pair of rows holding u and u*.  Slots: output channels of the
+// mirror orbits, slot-major: the c^2 generic orbits [q, My q, Mx q, Mxy q]
+// as four blocks of c^2, the c orbits [q, My q] (alpha = c) and the c orbits
+// [q, Mx q] (beta = c) as two blocks of c each, then the centre.
 struct Layout {
   int N, NN, c, nh;
   int nrowG;      // 2c^2

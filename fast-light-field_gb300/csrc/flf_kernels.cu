@@ -258,27 +258,14 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned 
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // 1 s per wait
 
 // Loads the four virtual slots [q, My q, Mx q, Mxy q] of this thread's orbit
-// from one staged row.  Degenerate orbits repeat their stored entries:
-// alpha = c: [q, My q, q, My q]; beta = c: [q, q, Mx q, Mx q]; centre: [q]x4.
-// With that padding every thread runs the same 4-slot update (the padded
-// slots compute duplicates that are never written), so warps do not diverge.
-__device__ __forceinline__ void load_orbit(const float2 *ptr, int kind, float2 (&t)[4]) {
-  if (kind == 0) {
-    const float4 a = reinterpret_cast<const float4 *>(ptr)[0];
-    const float4 b = reinterpret_cast<const float4 *>(ptr)[1];
-    t[0] = make_float2(a.x, a.y); t[1] = make_float2(a.z, a.w);
-    t[2] = make_float2(b.x, b.y); t[3] = make_float2(b.z, b.w);
-  } else if (kind == 3) {
-    const float2 a = ptr[0];
-    t[0] = a; t[1] = a; t[2] = a; t[3] = a;
-  } else {
-    const float4 a = reinterpret_cast<const float4 *>(ptr)[0];
-    const float2 x = make_float2(a.x, a.y), y = make_float2(a.z, a.w);
-    t[0] = x;
-    t[1] = (kind == 1) ? y : x;
-    t[2] = (kind == 1) ? x : y;
-    t[3] = y;
-  }
+// from one staged row at the thread's slot offsets.  Degenerate orbits repeat
+// their stored entries (alpha = c: [q, My q, q, My q]; beta = c:
+// [q, q, Mx q, Mx q]; centre: [q] x 4), so every thread runs the same 4-slot
+// update with no branch (the padded slots compute duplicates that are never
+// written).
+__device__ __forceinline__ void load_slots(const float2 *row, const int (&off)[4], float2 (&t)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; k++) t[k] = row[off[k]];
 }
 
 // Slot permutations of the orbit [q, My q, Mx q, Mxy q].
@@ -286,29 +273,21 @@ __device__ __forceinline__ constexpr int sy(int k) { return k ^ 1; }
 __device__ __forceinline__ constexpr int sx(int k) { return k ^ 2; }
 __device__ __forceinline__ constexpr int sxy(int k) { return 3 - k; }
 
-// Packed two-lane FP32 arithmetic (sm_100+): one fma.rn.f32x2 performs two
-// independent IEEE fused multiply-adds, halving the issue slots of the
-// complex multiply-accumulate.
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x pk(float lo, float hi) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};\n" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ float2 unpk(f2x v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;\n" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ void ffma2(f2x &acc, f2x a, f2x b) {
-  asm("fma.rn.f32x2 %0, %1, %2, %0;\n" : "+l"(acc) : "l"(a), "l"(b));
-}
+// Packed two-lane FP32 arithmetic (sm_100+): __ffma2_rn performs two
+// independent IEEE fused multiply-adds in one instruction, halving the issue
+// slots of the complex multiply-accumulate.  f2x is the two-lane value.
+typedef float2 f2x;
+__device__ __forceinline__ f2x pk(float lo, float hi) { return make_float2(lo, hi); }
+__device__ __forceinline__ float2 unpk(f2x v) { return v; }
+__device__ __forceinline__ void ffma2(f2x &acc, f2x a, f2x b) { acc = __ffma2_rn(a, b, acc); }
 
 // Per stored row, the input spectra enter as four packed operand pairs
-// (A_j, B_j), j = 0..3, so that with Tn = (t.x, t.y), Ts = (t.y, t.x)
-//   acc += t * s        is  acc = fma2(Tn, (s.x, s.x)) ; fma2(Ts, (-s.y, s.y))
-//   acc += conj(t) * s  is  acc = fma2(Tn, (s.x,-s.x)) ; fma2(Ts, ( s.y, s.y))
-// sv[tf][row][j] = float4(A_j, B_j); built from comb once per plane.
+// (A_j, B_j), j = 0..3.  Each complex accumulator is kept as two lane pairs
+// P and Q with value (P.x - Q.y, P.y + Q.x), so that with t = (t.x, t.y)
+//   acc += t * s        is  P = fma2(t, (s.x, s.x)), Q = fma2(t, (s.y, s.y))
+//   acc += conj(t) * s  is  P = fma2(t, (s.x,-s.x)), Q = fma2(t, (s.y,-s.y))
+// and no lane swap of t is needed.  sv[tf][row][j] = float4(A_j, B_j); built
+// from comb once per plane.
 __device__ void build_sv(float4 *sv, const float2 *comb, const short4 *rowS, const Layout &L, int TF) {
   const int nrowT = L.nrowG + L.nrep, NN2 = 2 * L.NN;
   for (int idx = threadIdx.x; idx < TF * nrowT * 4; idx += blockDim.x) {
@@ -327,18 +306,31 @@ __device__ void build_sv(float4 *sv, const float2 *comb, const short4 *rowS, con
       if (rk == 3 && j >= 2) zero = true;
     }
     const float2 sc = zero ? make_float2(0.f, 0.f) : comb[tf * NN2 + ci];
-    sv[idx] = conj ? make_float4(sc.x, -sc.x, sc.y, sc.y) : make_float4(sc.x, sc.x, -sc.y, sc.y);
+    sv[idx] = conj ? make_float4(sc.x, -sc.x, sc.y, -sc.y) : make_float4(sc.x, sc.x, sc.y, sc.y);
   }
 }
+
+// Split accumulators of one thread: U (frequency u) and V (u*) for the four
+// virtual slots of its orbit and each frame, as P / Q lane pairs.
+template <int TF> struct MacAcc {
+  f2x UP[TF][4], UQ[TF][4], VP[TF][4], VQ[TF][4];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int tf = 0; tf < TF; tf++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        UP[tf][k] = make_float2(0.f, 0.f); UQ[tf][k] = make_float2(0.f, 0.f);
+        VP[tf][k] = make_float2(0.f, 0.f); VQ[tf][k] = make_float2(0.f, 0.f);
+      }
+  }
+};
+__device__ __forceinline__ float2 pq_value(f2x P, f2x Q) { return make_float2(P.x - Q.y, P.y + Q.x); }
 
 // One generic stored row t (input channel i at u): feeds channel i at u,
 // Mxy i at u, My i at u*, Mx i at u*.
 template <int TF>
 __device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const float4 *svr, int svstride,
-                                                f2x (&U)[TF][4], f2x (&V)[TF][4]) {
-  f2x Tn[4], Ts[4];
-#pragma unroll
-  for (int k = 0; k < 4; k++) { Tn[k] = pk(t[k].x, t[k].y); Ts[k] = pk(t[k].y, t[k].x); }
+                                                MacAcc<TF> &a) {
 #pragma unroll
   for (int tf = 0; tf < TF; tf++) {
     const float4 q0 = svr[tf * svstride + 0], q1 = svr[tf * svstride + 1];
@@ -347,14 +339,14 @@ __device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const floa
     const f2x A2 = pk(q2.x, q2.y), B2 = pk(q2.z, q2.w), A3 = pk(q3.x, q3.y), B3 = pk(q3.z, q3.w);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      ffma2(U[tf][k], Tn[k], A0);
-      ffma2(U[tf][k], Ts[k], B0);
-      ffma2(U[tf][k], Tn[sxy(k)], A1);
-      ffma2(U[tf][k], Ts[sxy(k)], B1);
-      ffma2(V[tf][sy(k)], Tn[k], A2);
-      ffma2(V[tf][sy(k)], Ts[k], B2);
-      ffma2(V[tf][sx(k)], Tn[k], A3);
-      ffma2(V[tf][sx(k)], Ts[k], B3);
+      ffma2(a.UP[tf][k], t[k], A0);
+      ffma2(a.UQ[tf][k], t[k], B0);
+      ffma2(a.UP[tf][k], t[sxy(k)], A1);
+      ffma2(a.UQ[tf][k], t[sxy(k)], B1);
+      ffma2(a.VP[tf][sy(k)], t[k], A2);
+      ffma2(a.VQ[tf][sy(k)], t[k], B2);
+      ffma2(a.VP[tf][sx(k)], t[k], A3);
+      ffma2(a.VQ[tf][sx(k)], t[k], B3);
     }
   }
 }
@@ -362,24 +354,17 @@ __device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const floa
 // A centre-cross row pair (t at u, s at u*) of representative kind rk.
 template <int TF>
 __device__ __forceinline__ void mac_pair_rows(const float2 (&t)[4], const float2 (&s)[4], int rk,
-                                              const float4 *svr, int svstride, f2x (&U)[TF][4],
-                                              f2x (&V)[TF][4]) {
-  f2x Tn[4], Ts[4], Sn[4], Ss[4];
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    Tn[k] = pk(t[k].x, t[k].y); Ts[k] = pk(t[k].y, t[k].x);
-    Sn[k] = pk(s[k].x, s[k].y); Ss[k] = pk(s[k].y, s[k].x);
-  }
+                                              const float4 *svr, int svstride, MacAcc<TF> &a) {
 #pragma unroll
   for (int tf = 0; tf < TF; tf++) {
     const float4 q0 = svr[tf * svstride + 0], q1 = svr[tf * svstride + 1];
     const f2x A0 = pk(q0.x, q0.y), B0 = pk(q0.z, q0.w), A1 = pk(q1.x, q1.y), B1 = pk(q1.z, q1.w);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      ffma2(U[tf][k], Tn[k], A0);
-      ffma2(U[tf][k], Ts[k], B0);
-      ffma2(V[tf][k], Sn[k], A1);
-      ffma2(V[tf][k], Ss[k], B1);
+      ffma2(a.UP[tf][k], t[k], A0);
+      ffma2(a.UQ[tf][k], t[k], B0);
+      ffma2(a.VP[tf][k], s[k], A1);
+      ffma2(a.VQ[tf][k], s[k], B1);
     }
     if (rk != 3) {
       const float4 q2 = svr[tf * svstride + 2], q3 = svr[tf * svstride + 3];
@@ -387,18 +372,18 @@ __device__ __forceinline__ void mac_pair_rows(const float2 (&t)[4], const float2
       if (rk == 1) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          ffma2(V[tf][sy(k)], Tn[k], A2);
-          ffma2(V[tf][sy(k)], Ts[k], B2);
-          ffma2(U[tf][sy(k)], Sn[k], A3);
-          ffma2(U[tf][sy(k)], Ss[k], B3);
+          ffma2(a.VP[tf][sy(k)], t[k], A2);
+          ffma2(a.VQ[tf][sy(k)], t[k], B2);
+          ffma2(a.UP[tf][sy(k)], s[k], A3);
+          ffma2(a.UQ[tf][sy(k)], s[k], B3);
         }
       } else {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          ffma2(V[tf][sx(k)], Tn[k], A2);
-          ffma2(V[tf][sx(k)], Ts[k], B2);
-          ffma2(U[tf][sx(k)], Sn[k], A3);
-          ffma2(U[tf][sx(k)], Ss[k], B3);
+          ffma2(a.VP[tf][sx(k)], t[k], A2);
+          ffma2(a.VQ[tf][sx(k)], t[k], B2);
+          ffma2(a.UP[tf][sx(k)], s[k], A3);
+          ffma2(a.UQ[tf][sx(k)], s[k], B3);
         }
       }
     }
@@ -445,8 +430,13 @@ size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int s
          2 * sizeof(unsigned long long) * stages + 16;
 }
 
-template <int TF> struct MacOcc { static constexpr int v = 2; };
-template <> struct MacOcc<4> { static constexpr int v = 1; };
+// Launch bounds: blocks of at most 128 threads (orbit groups of Nnum <= 15
+// with a row split of 2) or of at most 256, and the CTAs per SM the register
+// budget is sized for.
+template <int TF, bool WIDE> struct MacOcc {
+  static constexpr int threads = WIDE ? 256 : 128;
+  static constexpr int v = WIDE ? (TF == 1 ? 2 : 1) : (TF == 1 ? 5 : (TF == 2 ? 3 : 2));
+};
 
 // One CTA = one frequency pair and a group of planes.  Thread (h, o) owns the
 // mirror orbit o of output channels for the rows of its share h (rows are
@@ -460,10 +450,11 @@ template <> struct MacOcc<4> { static constexpr int v = 1; };
 // added by the inverse transform); back projection writes each plane's
 // spectra when the plane is done.  The spectra of the next plane are staged
 // with cp.async while the current plane streams.
-template <int TF, bool FWD>
-__global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
+template <int TF, bool FWD, bool WIDE>
+__global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v) k_mac(MacParams p) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_abort;
+  __shared__ int s_plane[kMacMaxZgroup];        // plane slots of this CTA's z range
   volatile int *abortf = &s_abort;
   const Layout &L = p.L;
   const int NN = L.NN, NT = L.nthr, c = L.c, c2 = c * c, RS = L.RS, NN2 = 2 * L.NN;
@@ -489,6 +480,10 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
     fence_mbar_init();
   }
   for (int i = tid; i < nrowT; i += blockDim.x) rowS[i] = p.rowS[i];
+  {
+    const int zb = blockIdx.y * p.zgroup, nzl = min(p.zgroup, p.nz - zb);
+    for (int i = tid; i < nzl; i += blockDim.x) s_plane[i] = p.planes[zb + i];
+  }
 
   const int kp = blockIdx.x;
   const int uy = kp / p.fq, ux = kp % p.fq;
@@ -498,11 +493,21 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
   const int h = tid / NTP, o = tid - h * NTP;
   const bool active = o < NT;
   const int kind = (o < c2) ? 0 : ((o < c2 + c) ? 1 : ((o < c2 + 2 * c) ? 2 : 3));
-  const int slotbase = !active ? 0
-                      : (kind == 0) ? 4 * o
-                      : (kind == 1) ? 4 * c2 + 2 * (o - c2)
-                      : (kind == 2) ? 4 * c2 + 2 * c + 2 * (o - c2 - c)
-                                    : NN - 1;
+  // slot offsets of the orbit's virtual slots in a stored row (slot-major layout)
+  int off[4];
+  if (!active) {
+    off[0] = off[1] = off[2] = off[3] = 0;
+  } else if (kind == 0) {
+    off[0] = o; off[1] = c2 + o; off[2] = 2 * c2 + o; off[3] = 3 * c2 + o;
+  } else if (kind == 1) {
+    const int j = o - c2;
+    off[0] = off[2] = 4 * c2 + j; off[1] = off[3] = 4 * c2 + c + j;
+  } else if (kind == 2) {
+    const int j = o - c2 - c;
+    off[0] = off[1] = 4 * c2 + 2 * c + j; off[2] = off[3] = 4 * c2 + 3 * c + j;
+  } else {
+    off[0] = off[1] = off[2] = off[3] = NN - 1;
+  }
   const int ns = (kind == 0) ? 4 : ((kind == 3) ? 1 : 2);
   const int z0 = blockIdx.y * p.zgroup;
   const int z1 = min(z0 + p.zgroup, p.nz);
@@ -510,11 +515,8 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
   const int total = (z1 - z0) * cpb;
   const size_t blockElems = (size_t)L.nrow * RS;
 
-  f2x U[TF][4], V[TF][4];
-#pragma unroll
-  for (int tf = 0; tf < TF; tf++)
-#pragma unroll
-    for (int k = 0; k < 4; k++) { U[tf][k] = 0ull; V[tf][k] = 0ull; }
+  MacAcc<TF> acc;
+  acc.zero();
 
   stage_comb(scratch, p, TF, FWD ? z0 : 0, uy, us, ux);
   cp_async_wait_all();
@@ -522,28 +524,30 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
   build_sv(sv, scratch, rowS, L, TF);
   __syncthreads();   // (back projection: the staging area is free for the reduction)
 
-  // producer: chunk g -> ring slot g % NST
-  int issued = 0;
-  auto issue = [&](int g) {
-    const int zl = g / cpb, ch = g - zl * cpb;
-    const int plane = p.planes[z0 + zl];
-    const int r0 = ch * CH;
+  // producer (thread 0): chunks in order, chunk g -> ring slot g % NST; the
+  // counters advance instead of dividing
+  int issued = 0, p_zl = 0, p_ch = 0, p_slot = 0;
+  unsigned p_round = 0;
+  auto issue = [&]() {
+    const int r0 = p_ch * CH;
     const int nr = min(CH, L.nrow - r0);
-    const float2 *src = p.P + ((long long)plane * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
-    const int slot = g % NST;
+    const float2 *src = p.P + ((long long)s_plane[p_zl] * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
     const unsigned bytes = (unsigned)(nr * RS * sizeof(float2));
-    mbar_arrive_expect_tx(full + slot, bytes);
-    bulk_g2s(ring + (size_t)slot * CH * RS, src, bytes, full + slot);
+    mbar_arrive_expect_tx(full + p_slot, bytes);
+    bulk_g2s(ring + (size_t)p_slot * CH * RS, src, bytes, full + p_slot);
+    issued++;
+    if (++p_ch == cpb) { p_ch = 0; p_zl++; }
+    if (++p_slot == NST) { p_slot = 0; p_round++; }
   };
   if (tid == 0) {
     const int pre = min(NST - 1, total);
-    for (int g = 0; g < pre; g++) issue(g);
-    issued = pre;
+    for (int g = 0; g < pre; g++) issue();
   }
 
   bool dead = false;
+  int zl = 0, ch = 0, slot = 0;
+  unsigned round = 0;
   for (int g = 0; g < total; g++) {
-    const int zl = g / cpb, ch = g - zl * cpb;
     const int zi = z0 + zl;
     if (FWD && ch == 0) {
       if (zl > 0) {
@@ -557,19 +561,14 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
     if (*abortf) dead = true;
     // producer step: refill the slot freed by chunk g-1 with chunk g+NST-1
     if (tid == 0 && !dead && issued < total) {
-      const int gn = issued;
-      if (gn >= NST) {
-        const int slot = gn % NST;
-        if (!mbar_wait(empty + slot, ((gn / NST) - 1) & 1, kWaitLimitNs)) {
-          dead = true;
-          *abortf = 1;
-          atomicExch(p.err, 1);
-        }
+      if (issued >= NST && !mbar_wait(empty + p_slot, (p_round - 1) & 1, kWaitLimitNs)) {
+        dead = true;
+        *abortf = 1;
+        atomicExch(p.err, 1);
       }
-      if (!dead) { issue(gn); issued = gn + 1; }
+      if (!dead) issue();
     }
-    const int slot = g % NST;
-    if (!dead && !mbar_wait(full + slot, (g / NST) & 1, kWaitLimitNs)) {
+    if (!dead && !mbar_wait(full + slot, round & 1, kWaitLimitNs)) {
       dead = true;
       *abortf = 1;
       atomicExch(p.err, 2);
@@ -577,24 +576,24 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
     if (!dead && active) {
       const int r0 = ch * CH;
       const int r1 = min(L.nrow, r0 + CH);
-      const float2 *stage = ring + (size_t)slot * CH * RS + slotbase;
+      const float2 *stage = ring + (size_t)slot * CH * RS;
       const int rg = min(r1, L.nrowG);
       const int svs = nrowT * 4;
 #pragma unroll 2
       for (int r = r0 + h; r < rg; r += H) {
         float2 t[4];
-        load_orbit(stage + (size_t)(r - r0) * RS, kind, t);
-        mac_generic_row<TF>(t, sv + r * 4, svs, U, V);
+        load_slots(stage + (size_t)(r - r0) * RS, off, t);
+        mac_generic_row<TF>(t, sv + r * 4, svs, acc);
       }
       // centre-cross row pairs of this chunk, dealt round-robin over the split
       const int pr0 = max(r0, L.nrowG);
       for (int r = pr0 + 2 * h; r < r1; r += 2 * H) {
         const int k2 = (r - L.nrowG) >> 1;
         float2 t[4], s2[4];
-        load_orbit(stage + (size_t)(r - r0) * RS, kind, t);
-        load_orbit(stage + (size_t)(r + 1 - r0) * RS, kind, s2);
+        load_slots(stage + (size_t)(r - r0) * RS, off, t);
+        load_slots(stage + (size_t)(r + 1 - r0) * RS, off, s2);
         const int rk = (k2 < c) ? 1 : ((k2 < 2 * c) ? 2 : 3);
-        mac_pair_rows<TF>(t, s2, rk, sv + (L.nrowG + k2) * 4, svs, U, V);
+        mac_pair_rows<TF>(t, s2, rk, sv + (L.nrowG + k2) * 4, svs, acc);
       }
     }
     __syncwarp();
@@ -602,6 +601,14 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
 
     const bool out_due = (ch == cpb - 1) && (!FWD || zi + 1 == z1);
     if (out_due) {
+      f2x U[TF][4], V[TF][4];
+#pragma unroll
+      for (int tf = 0; tf < TF; tf++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          U[tf][k] = pq_value(acc.UP[tf][k], acc.UQ[tf][k]);
+          V[tf][k] = pq_value(acc.VP[tf][k], acc.VQ[tf][k]);
+        }
       if (H > 1) {
         // add the partial sums of the other row shares into share 0
         if (FWD) cp_async_wait_all();   // the staging area doubles as reduction buffer
@@ -639,7 +646,11 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
           for (int k = 0; k < 4; k++) {
             const int vk = (kind == 2) ? ((k & 1) ? 2 : 0) : k;   // stored slot k -> virtual slot
             if (k < ns) {
-              const int q = p.slotcol[slotbase + k];
+              int sl = off[0];
+#pragma unroll
+              for (int m = 1; m < 4; m++)
+                if (m == vk) sl = off[m];
+              const int q = p.slotcol[sl];
               float2 *op = p.O + obase + (long long)q * ffh;
               float2 u = unpk(U[tf][0]), v = unpk(V[tf][0]);
 #pragma unroll
@@ -655,12 +666,11 @@ __global__ void __launch_bounds__(256, MacOcc<TF>::v) k_mac(MacParams p) {
           }
         }
       }
-#pragma unroll
-      for (int tf = 0; tf < TF; tf++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) { U[tf][k] = 0ull; V[tf][k] = 0ull; }
+      acc.zero();
       if (H > 1) __syncthreads();   // the reduction buffer is free again
     }
+    if (++ch == cpb) { ch = 0; zl++; }
+    if (++slot == NST) { slot = 0; round++; }
   }
   // Never leave a bulk copy in flight into this CTA's shared memory.
   if (tid == 0 && dead) {
@@ -911,13 +921,16 @@ static cudaError_t launch_mac_tf(const MacParams &p, bool fwd, cudaStream_t s) {
   const size_t sm = mac_smem_bytes(p.L, TF, p.stages, p.chunk_rows, p.split, fwd);
   dim3 grid(p.nkp, p.nzo_grid);
   const int block = p.split * (((p.L.nthr + 31) / 32) * 32);
-  cudaError_t e;
-  if (fwd) {
-    if ((e = set_smem((const void *)k_mac<TF, true>, sm)) != cudaSuccess) return e;
-    k_mac<TF, true><<<grid, block, sm, s>>>(p);
+  const void *fn = block <= 128 ? (fwd ? (const void *)k_mac<TF, true, false> : (const void *)k_mac<TF, false, false>)
+                                : (fwd ? (const void *)k_mac<TF, true, true> : (const void *)k_mac<TF, false, true>);
+  cudaError_t e = set_smem(fn, sm);
+  if (e != cudaSuccess) return e;
+  if (block <= 128) {
+    if (fwd) k_mac<TF, true, false><<<grid, block, sm, s>>>(p);
+    else k_mac<TF, false, false><<<grid, block, sm, s>>>(p);
   } else {
-    if ((e = set_smem((const void *)k_mac<TF, false>, sm)) != cudaSuccess) return e;
-    k_mac<TF, false><<<grid, block, sm, s>>>(p);
+    if (fwd) k_mac<TF, true, true><<<grid, block, sm, s>>>(p);
+    else k_mac<TF, false, true><<<grid, block, sm, s>>>(p);
   }
   return cudaGetLastError();
 }
