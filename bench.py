@@ -30,6 +30,12 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "volumes/s to plain-RL(8 it) accuracy: learned warm-start vs plain RL, 1 GB300"
+
+# DRAM bytes (read + write) per k_mac launch over its algorithmic bytes, from one
+# ncu --set full capture of the full-field f = 96 launches (4 planes, 2401
+# frequency pairs: 1.001 forward, 1.005 back projection).  The matrices dominate
+# both, so the traffic of a launch scales with the bytes it streams.
+MAC_TRAFFIC_RATIO = 1.003
 UNIT = "volumes/s"
 
 WORKLOADS = {
@@ -336,7 +342,11 @@ def run_gb300(args, rank, world, local):
     n_mac = sum(v["launches"] for v in mac.values())
     achieved = tot_bytes / (tot_ms / 1000.0) / 1e9 if tot_ms > 0 else 0.0
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_mac_fwd+k_mac_bwd",
+            "frac": round(achieved / peak, 4), "traffic": round(tot_bytes / max(n_mac, 1) * MAC_TRAFFIC_RATIO),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, as a ratio to the "
+                              "algorithmic bytes (%.3f), times this run's algorithmic bytes per launch"
+                              % MAC_TRAFFIC_RATIO,
+            "kernel": "k_mac_fwd+k_mac_bwd",
             "peak_source": peak_kind, "launches": n_mac,
             "bytes_per_launch": tot_bytes / max(n_mac, 1), "avg_launch_ms": tot_ms / max(n_mac, 1),
             "kernel_share": {k: round(v["ms"] / sum(w["ms"] for w in prof.values()), 4) for k, v in prof.items()}}

@@ -1178,7 +1178,7 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
 
 int flf_version(char *buf, size_t len) {
   if (!buf || len == 0) return FLF_E_ARG;
-  snprintf(buf, len, "libflf 0.1 sm_103a kernels: k_rfft2 k_mac k_irfft2 k_build_k k_pack");
+  snprintf(buf, len, "libflf 0.2 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack");
   return FLF_OK;
 }
 

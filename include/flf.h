@@ -104,12 +104,14 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
  *  - The caller passes the image and the output volume; the transfer matrices
  *    must already exist for this Y x X (call flf_prepare earlier), otherwise
  *    FLF_E_STATE is returned instead of building them.
- *  - The intermediate spectra live in one fixed device array of
- *    FLF_NOALLOC_SCRATCH_BYTES (16 MiB) inside the library: one frame of
- *    channel spectra plus the output spectra of as many planes as fit.  Every
- *    GPU that loads the library holds this array until the process exits.
- *    Geometries that need more (2 * Nnum^2 * f * (f/2+1) * 8 bytes, e.g. the
- *    1005 x 1005 full field) are rejected with FLF_E_ARG; use flf_backward.
+ *  - The intermediate spectra and channel images live in one fixed device
+ *    array of FLF_NOALLOC_SCRATCH_BYTES (16 MiB) inside the library: one
+ *    frame's channel images and spectra plus the output spectra and channel
+ *    images of as many planes as fit.  Every GPU that loads the library holds
+ *    this array until the process exits.  Geometries that need more
+ *    (2 * (Nnum^2 * f * (f/2+1) * 8 + Nnum^2 * Ly * Lxp * 4) bytes, Lxp =
+ *    ceil(X/Nnum) rounded up to 4; e.g. the 1005 x 1005 full field) are
+ *    rejected with FLF_E_ARG; use flf_backward.
  *  - The first call on each device looks up the array's device address (a
  *    one-time set-up with that device current); make that first call before
  *    any stream capture.
