@@ -255,6 +255,12 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned 
       : "memory");
 }
 
+// Orders this thread's earlier generic-proxy shared-memory accesses (as seen
+// through a CTA fence) before its later async-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // 1 s per wait
 
 // Loads the four virtual slots [q, My q, Mx q, Mxy q] of this thread's orbit
@@ -454,6 +460,7 @@ template <int TF, bool FWD, bool WIDE>
 __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v) k_mac(MacParams p) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_abort;
+  __shared__ int s_issued;                      // chunks handed to the bulk-copy engine
   __shared__ int s_plane[kMacMaxZgroup];        // plane slots of this CTA's z range
   volatile int *abortf = &s_abort;
   const Layout &L = p.L;
@@ -467,16 +474,17 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   f2x *red = reinterpret_cast<f2x *>(scratch);                              // [H-1][NTP][TF][8]
   short4 *rowS = reinterpret_cast<short4 *>(scratch + mac_scratch_elems(L, TF, H, FWD));
   unsigned long long *full = reinterpret_cast<unsigned long long *>(rowS + nrowT);
-  unsigned long long *empty = full + NST;
+  int *released = reinterpret_cast<int *>(full + NST);   // [NST] warps done with each slot, ever
 
   const int tid = threadIdx.x;
   const int nwarps = (blockDim.x + 31) >> 5;
   if (tid == 0) {
     for (int i = 0; i < NST; i++) {
       mbar_init(full + i, 1);
-      mbar_init(empty + i, nwarps);
+      released[i] = 0;
     }
     *abortf = 0;
+    s_issued = 0;
     fence_mbar_init();
   }
   for (int i = tid; i < nrowT; i += blockDim.x) rowS[i] = p.rowS[i];
@@ -524,29 +532,28 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   build_sv(sv, scratch, rowS, L, TF);
   __syncthreads();   // (back projection: the staging area is free for the reduction)
 
-  // producer (thread 0): chunks in order, chunk g -> ring slot g % NST; the
-  // counters advance instead of dividing
-  int issued = 0, p_zl = 0, p_ch = 0, p_slot = 0;
-  unsigned p_round = 0;
-  auto issue = [&]() {
-    const int r0 = p_ch * CH;
+  // Chunk g goes to ring slot g % NST.  Thread 0 fills the whole ring; after
+  // that, the warp that releases a slot last (each warp counts itself out
+  // once it has finished its rows of the chunk) refills it at once with chunk
+  // g + NST, so no thread ever waits for a slot to drain.
+  auto issue = [&](int gn) {
+    const int zl_n = gn / cpb, ch_n = gn - zl_n * cpb, sl = gn % NST;
+    const int r0 = ch_n * CH;
     const int nr = min(CH, L.nrow - r0);
-    const float2 *src = p.P + ((long long)s_plane[p_zl] * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
+    const float2 *src = p.P + ((long long)s_plane[zl_n] * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
     const unsigned bytes = (unsigned)(nr * RS * sizeof(float2));
-    mbar_arrive_expect_tx(full + p_slot, bytes);
-    bulk_g2s(ring + (size_t)p_slot * CH * RS, src, bytes, full + p_slot);
-    issued++;
-    if (++p_ch == cpb) { p_ch = 0; p_zl++; }
-    if (++p_slot == NST) { p_slot = 0; p_round++; }
+    mbar_arrive_expect_tx(full + sl, bytes);
+    bulk_g2s(ring + (size_t)sl * CH * RS, src, bytes, full + sl);
   };
   if (tid == 0) {
-    const int pre = min(NST - 1, total);
-    for (int g = 0; g < pre; g++) issue();
+    const int pre = min(NST, total);
+    for (int g = 0; g < pre; g++) issue(g);
+    s_issued = pre;
   }
 
   bool dead = false;
   int zl = 0, ch = 0, slot = 0;
-  unsigned round = 0;
+  int round = 0;
   for (int g = 0; g < total; g++) {
     const int zi = z0 + zl;
     if (FWD && ch == 0) {
@@ -559,15 +566,6 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
       if (zi + 1 < z1) stage_comb(scratch + ((zl + 1) & 1) * TF * NN2, p, TF, zi + 1, uy, us, ux);
     }
     if (*abortf) dead = true;
-    // producer step: refill the slot freed by chunk g-1 with chunk g+NST-1
-    if (tid == 0 && !dead && issued < total) {
-      if (issued >= NST && !mbar_wait(empty + p_slot, (p_round - 1) & 1, kWaitLimitNs)) {
-        dead = true;
-        *abortf = 1;
-        atomicExch(p.err, 1);
-      }
-      if (!dead) issue();
-    }
     if (!dead && !mbar_wait(full + slot, round & 1, kWaitLimitNs)) {
       dead = true;
       *abortf = 1;
@@ -597,7 +595,16 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
       }
     }
     __syncwarp();
-    if ((tid & 31) == 0 && !dead) mbar_arrive(empty + slot);
+    if ((tid & 31) == 0 && !dead) {
+      __threadfence_block();                       // this warp's reads of the slot come first
+      const int before = atomicAdd(released + slot, 1);
+      if (before == round * nwarps + nwarps - 1 && g + NST < total && !*abortf) {
+        __threadfence_block();
+        fence_proxy_async_smem();                  // ... before the bulk copy that overwrites it
+        issue(g + NST);
+        atomicAdd(&s_issued, 1);
+      }
+    }
 
     const bool out_due = (ch == cpb - 1) && (!FWD || zi + 1 == z1);
     if (out_due) {
@@ -673,7 +680,9 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
     if (++slot == NST) { slot = 0; round++; }
   }
   // Never leave a bulk copy in flight into this CTA's shared memory.
-  if (tid == 0 && dead) {
+  __syncthreads();
+  if (tid == 0 && *abortf) {
+    const int issued = s_issued;
     for (int g = max(0, issued - NST); g < issued; g++) mbar_wait(full + (g % NST), (g / NST) & 1, kWaitLimitNs / 10);
   }
   cp_async_wait_all();
