@@ -80,7 +80,7 @@ struct flf_ctx {
   int num_sms = 0;
   int req_f = 0, req_fp64 = 0;   // transform size / precision asked for by flf_prepare
   int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
-  int opt_chunk_rows = 8;        // tunable: stored rows per pipeline stage
+  int opt_chunk_rows[2] = {16, 12};   // tunable: stored rows per pipeline stage (forward, backward)
   int opt_split = 2;             // tunable: threads sharing one orbit's rows
   int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
@@ -609,7 +609,7 @@ MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
   mp.P = G.P[dir];
   mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
-  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows; mp.split = ctx->opt_split;
+  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows[dir]; mp.split = ctx->opt_split;
   mp.err = ctx->d_err;
   return mp;
 }
@@ -1157,19 +1157,25 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     }
     return FLF_OK;
   }
-  if (!strcmp(name, "mac_stages") || !strcmp(name, "mac_chunk_rows") || !strcmp(name, "mac_split")) {
+  const bool cr_all = !strcmp(name, "mac_chunk_rows");
+  const bool cr_fwd = !strcmp(name, "mac_chunk_rows_forward"), cr_bwd = !strcmp(name, "mac_chunk_rows_backward");
+  if (!strcmp(name, "mac_stages") || cr_all || cr_fwd || cr_bwd || !strcmp(name, "mac_split")) {
     const int st = !strcmp(name, "mac_stages") ? (int)value : ctx->opt_stages;
-    const int cr = !strcmp(name, "mac_chunk_rows") ? (int)value : ctx->opt_chunk_rows;
+    const int crf = (cr_all || cr_fwd) ? (int)value : ctx->opt_chunk_rows[FLF_DIR_FORWARD];
+    const int crb = (cr_all || cr_bwd) ? (int)value : ctx->opt_chunk_rows[FLF_DIR_BACKWARD];
     const int sp = !strcmp(name, "mac_split") ? (int)value : ctx->opt_split;
     if (st < 2 || st > 16) return fail(ctx, FLF_E_ARG, "mac_stages must be in [2, 16]");
-    if (cr < 2 || cr > 64 || (cr & 1)) return fail(ctx, FLF_E_ARG, "mac_chunk_rows must be even, in [2, 64]");
+    for (int cr : {crf, crb})
+      if (cr < 2 || cr > 64 || (cr & 1)) return fail(ctx, FLF_E_ARG, "mac_chunk_rows must be even, in [2, 64]");
     const int ntp = (ctx->L.nthr + 31) / 32 * 32;
     if (sp < 1 || sp > 4 || sp * ntp > 256)
       return fail(ctx, FLF_E_ARG, "mac_split must be in [1, 4] with at most 256 threads per block");
-    if (mac_smem_bytes(ctx->L, mac_max_frames(), st, cr, sp, true) > 227 * 1024)
-      return fail(ctx, FLF_E_ARG, "pipeline of %d stages x %d rows exceeds shared memory", st, cr);
+    for (int cr : {crf, crb})
+      if (mac_smem_bytes(ctx->L, mac_max_frames(), st, cr, sp, true) > 227 * 1024)
+        return fail(ctx, FLF_E_ARG, "pipeline of %d stages x %d rows exceeds shared memory", st, cr);
     ctx->opt_stages = st;
-    ctx->opt_chunk_rows = cr;
+    ctx->opt_chunk_rows[FLF_DIR_FORWARD] = crf;
+    ctx->opt_chunk_rows[FLF_DIR_BACKWARD] = crb;
     ctx->opt_split = sp;
     return FLF_OK;
   }

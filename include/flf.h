@@ -158,7 +158,8 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
  * block-shape knobs gBlockSelection / gCalculateRowsBlocks,
  * projector.py:26-36).  Options: "mac_stages" (shared-memory pipeline
  * stages of the multiply-accumulate, 2..16), "mac_chunk_rows" (stored rows
- * per stage, even, 2..64), "mac_split" (threads sharing an orbit's rows,
+ * per stage, even, 2..64, both directions; "mac_chunk_rows_forward" and
+ * "mac_chunk_rows_backward" set one), "mac_split" (threads sharing an orbit's rows,
  * 1..4) and "plane_transform_sizes" (1: each plane uses the smallest
  * transform its PSF allows, planes grouped by size - the default; 0: one
  * size for all planes).  Results agree to rounding whatever the values. */
