@@ -352,6 +352,23 @@ def run_gb300(args, rank, world, local):
             "kernel_share": {k: round(v["ms"] / sum(w["ms"] for w in prof.values()), 4) for k, v in prof.items()}}
     launches = sum(v["launches"] for v in prof.values()) // args.steps
 
+    # accuracy of the volume the timed step produced (outside the timed region):
+    # relative data-fit residual ||y - Hx|| / ||y|| and error against the
+    # ground-truth volume, reduced in FP64
+    hx = torch.empty((T, Y, X), dtype=torch.float32, device=dev)
+    ctx.forward(x, hx, T, Y, X, None, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    y64 = img_d.double()
+    resid = float(torch.linalg.vector_norm(y64 - hx.double()) / torch.linalg.vector_norm(y64))
+    x64 = x.double()
+    g64 = gt_d.double()
+    scale = float((x64 * g64).sum() / (x64 * x64).sum())     # RL recovers the volume up to the PSF's scale
+    accuracy = {"rl_iterations": args.iters, "residual_rel_l2": resid,
+                "truth_rel_l2": float(torch.linalg.vector_norm(x64 - g64) / torch.linalg.vector_norm(g64)),
+                "truth_rel_l2_scaled": float(torch.linalg.vector_norm(scale * x64 - g64) / torch.linalg.vector_norm(g64)),
+                "reductions": "f64"}
+    del hx, y64, x64, g64
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(hm, H, Ht, z, Y, X, N, args.iters, args.cpu_sample_planes, os.cpu_count() or 1)
@@ -372,6 +389,7 @@ def run_gb300(args, rank, world, local):
                                  "projection, %.0f MB volume" % (tot_bytes / args.steps / (1 + 2 * args.iters) / 1e9,
                                                                 Z * T * Y * X * 4 / 1e6),
                            "parallelism": "replicas" if world > 1 else "single"},
+                "rl_iterations_per_s": value * args.iters, "accuracy": accuracy,
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cb,
                 "clocks": clk}
         print(json.dumps(line), flush=True)
