@@ -44,6 +44,10 @@ WORKLOADS = {
                       label="full-field 1005x1005 px, Nnum 15, 41 planes -100..100 um, plain RL"),
     "small": dict(Nnum=15, lenslets=30, z=(-25, 25, 5), img_size_ref=7, beads=200, filaments=0,
                   label="450x450 px, Nnum 15, 11 planes -25..25 um, plain RL"),
+    # a time series of frames of three sizes (--frames per size), 500 drifting beads each
+    "timeseries": dict(Nnum=15, sizes=(30, 45, 67), z=(-75, 75, 5), img_size_ref=21, beads=500,
+                       label="time series, Nnum 15, 31 planes -75..75 um, frames at 30x30, 45x45 and 67x67 "
+                             "lenslets, RL from x0 = Htf"),
 }
 
 
@@ -236,6 +240,10 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    if args.workload == "timeseries":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the single-size "
+                          "workloads; the time series is a GB300-only measurement"}), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     N = wl["Nnum"]
     hm, H, Ht, z, gt, Y, X = build_problem(wl)
@@ -397,11 +405,91 @@ def run_gb300(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def run_timeseries(args):
+    """Mixed-size time series on one device: per size, T frames back projected and
+    deconvolved together (x0 = Htf, as the time-series driver does); one step =
+    every frame of every size.  The geometries of all sizes stay resident."""
+    import torch
+    import projector
+    import psfmatrix
+    import synthetic
+    import _flf
+    import build_lib
+    build_lib.build()
+    dev = torch.device("cuda", 0)
+    wl = WORKLOADS["timeseries"]
+    N = wl["Nnum"]
+    T = max(args.frames, 1)
+    z0, z1, dz = wl["z"]
+    z = np.arange(z0, z1 + dz / 2, dz)
+    Z = len(z)
+    H, Ht = synthetic.synthetic_psf(N, z, wl["img_size_ref"])
+    hm = psfmatrix.HMatrixArrays(H, Ht, name="bench-timeseries")
+    p = projector.Projector_gb300(device=0)
+    p.storeVolumesOnGPU = True
+    ctx = p.context(hm)
+    ctx.set_option("geometry_cache", len(wl["sizes"]))
+    rng = np.random.default_rng(4321)
+    data = []
+    t_setup = time.time()
+    for L in wl["sizes"]:
+        Y = X = L * N
+        vol0, pos = synthetic.bead_volume((Z, Y, X), wl["beads"], seed=int(rng.integers(1 << 30)), sigma=1.0,
+                                          amp_range=(500.0, 1000.0))
+        frames = [vol0]
+        for _ in range(T - 1):       # drift N(0, 0.5 voxel) per frame
+            pos = pos + rng.normal(0.0, 0.5, pos.shape)
+            frames.append(synthetic.bead_volume((Z, Y, X), 0, positions=pos, sigma=1.0, amp_range=(500.0, 1000.0))[0])
+        gt = torch.as_tensor(np.stack(frames, axis=1), device=dev)
+        clean = p.ForwardProjectACC(hm, gt, None)
+        img = torch.poisson((clean.double() + 100.0).clamp_min(0)).float()
+        data.append((Y, X, img))
+        del gt, clean
+    setup_s = time.time() - t_setup
+    s = torch.cuda.current_stream(dev)
+    bufs = [(torch.empty((Z, T, Y, X), device=dev), torch.empty((Z, T, Y, X), device=dev)) for Y, X, _ in data]
+
+    def step():
+        for (Y, X, img), (htf, x) in zip(data, bufs):
+            p._prepare(ctx, Y, X, hm)
+            ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
+            x.copy_(htf)
+            ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=s.cuda_stream)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    nvol = T * len(data)
+    line = {"metric": "volumes/s, mixed-size time series (8 plain-RL iterations from x0 = Htf), 1 GB300",
+            "value": nvol / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl["label"], "frames_per_size": T, "sizes_px": [Y for Y, _, _ in data],
+                       "planes": Z, "nnum": N, "rl_iterations": args.iters, "volumes_per_step": nvol,
+                       "device_gb": round(ctx.memory_usage() / 1e9, 2), "setup_s": round(setup_s, 1),
+                       "l2": "inputs larger than L2 (transfer matrices of three geometries)"},
+            "rl_iterations_per_s": nvol * args.iters / (ms / 1000.0), "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "timeseries":
+        run_timeseries(args)
     else:
         run_gb300(args, rank, world, local)
 

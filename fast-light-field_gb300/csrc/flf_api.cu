@@ -83,6 +83,8 @@ struct flf_ctx {
   int opt_chunk_rows[2] = {16, 12};   // tunable: stored rows per pipeline stage (forward, backward)
   int opt_split = 2;             // tunable: threads sharing one orbit's rows
   int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
+  int opt_geometry_cache = 2;    // geometries of other image shapes kept resident (most recent first)
+  std::vector<Geometry> parked;  // those geometries
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
   int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
@@ -219,6 +221,28 @@ void free_geometry(Geometry &G) {
       if (p) cudaFree(p);
   }
   G = Geometry();
+}
+
+// Keep a geometry of another image shape resident (most recent first), within
+// opt_geometry_cache entries; the oldest beyond that is freed.
+void park_geometry(flf_ctx *ctx, Geometry &&G) {
+  if (!G.valid || ctx->opt_geometry_cache <= 0) {
+    free_geometry(G);
+    return;
+  }
+  ctx->parked.insert(ctx->parked.begin(), std::move(G));
+  G = Geometry();
+  while ((int)ctx->parked.size() > ctx->opt_geometry_cache) {
+    free_geometry(ctx->parked.back());
+    ctx->parked.pop_back();
+  }
+}
+
+// Free the active geometry and every parked one (the PSFs or the size rule changed).
+void free_all_geometries(flf_ctx *ctx) {
+  free_geometry(ctx->geo);
+  for (Geometry &g : ctx->parked) free_geometry(g);
+  ctx->parked.clear();
 }
 
 // Host-side index tables of the packed layout (see flf_internal.cuh).
@@ -427,15 +451,27 @@ int prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
                 "(image %d x %d, Nnum %d, kernel radius %d lenslets)", fmax, kMaxF, Y, X, N, Rmax);
   if (fp64 && fmax > kMaxF64) fp64 = 0;   // double buffers do not fit shared memory
   Geometry &G = ctx->geo;
-  if (G.valid && G.Ly == Ly && G.Lx == Lx && G.fp64 == fp64 && (int)G.plane_group.size() == nz) {
-    bool same = true;
-    for (int z = 0; z < nz && same; z++) same = (G.groups[G.plane_group[z]].f == fz[z]);
-    if (same) {
+  auto matches = [&](const Geometry &g) {
+    if (!g.valid || g.Ly != Ly || g.Lx != Lx || g.fp64 != fp64 || (int)g.plane_group.size() != nz) return false;
+    for (int z = 0; z < nz; z++)
+      if (g.groups[g.plane_group[z]].f != fz[z]) return false;
+    return true;
+  };
+  if (matches(G)) {
+    G.Y = Y; G.X = X;
+    return FLF_OK;
+  }
+  // another image shape: park the active geometry; reuse a parked one that fits
+  for (size_t i = 0; i < ctx->parked.size(); i++)
+    if (matches(ctx->parked[i])) {
+      Geometry found = std::move(ctx->parked[i]);
+      ctx->parked.erase(ctx->parked.begin() + i);
+      park_geometry(ctx, std::move(G));
+      G = std::move(found);
       G.Y = Y; G.X = X;
       return FLF_OK;
     }
-  }
-  free_geometry(G);
+  park_geometry(ctx, std::move(G));
   G.Y = Y; G.X = X; G.Ly = Ly; G.Lx = Lx; G.fp64 = fp64; G.uniform_f = fft_size;
   G.plane_group.assign(nz, -1);
   G.plane_slot.assign(nz, -1);
@@ -837,7 +873,7 @@ int flf_ctx_destroy(flf_ctx *ctx) {
       if (p) cudaFree(p);
   resolve_pending(ctx);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
-  free_geometry(ctx->geo);
+  free_all_geometries(ctx);
   void *ptrs[] = {ctx->d_rowS, ctx->d_slotcol, ctx->d_colslot, ctx->d_rep_ch, ctx->d_rep_row,
                   ctx->d_rep_kind, ctx->d_planes_all, ctx->d_planes_user, ctx->d_zero,
                   ctx->wsS.p, ctx->wsO.p, ctx->wsCvol.p, ctx->wsCimg.p, ctx->wsCy.p};
@@ -876,7 +912,7 @@ int flf_psf_upload(flf_ctx *ctx, int plane, int direction, const float *H_host, 
   CUDA_TRY(ctx, cudaMemcpy(dst, H_host, bytes, cudaMemcpyHostToDevice));
   ctx->h[direction][plane] = h;
   // transfer matrices depend on the PSF and on the kernel radius
-  free_geometry(ctx->geo);
+  free_all_geometries(ctx);
   return FLF_OK;
 }
 
@@ -1077,12 +1113,14 @@ int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {
   for (int d = 0; d < 2; d++)
     for (int z = 0; z < ctx->nz; z++)
       if (ctx->dH[d][z]) b += sizeof(float) * (size_t)ctx->L.nh * ctx->L.nh * ctx->h[d][z] * ctx->h[d][z];
-  const Geometry &Gm = ctx->geo;
-  for (const Group &G : Gm.groups) {
-    const size_t pe = (size_t)G.nkp * ctx->L.nrow * ctx->L.RS * G.planes.size() * sizeof(float2);
-    for (int d = 0; d < 2; d++)
-      if (G.P[d]) b += pe;
-  }
+  std::vector<const Geometry *> geos{&ctx->geo};
+  for (const Geometry &g : ctx->parked) geos.push_back(&g);
+  for (const Geometry *Gm : geos)
+    for (const Group &G : Gm->groups) {
+      const size_t pe = (size_t)G.nkp * ctx->L.nrow * ctx->L.RS * G.planes.size() * sizeof(float2);
+      for (int d = 0; d < 2; d++)
+        if (G.P[d]) b += pe;
+    }
   b += ctx->wsS.bytes + ctx->wsO.bytes + ctx->wsCvol.bytes + ctx->wsCimg.bytes + ctx->wsCy.bytes;
   *bytes = b;
   return FLF_OK;
@@ -1092,7 +1130,7 @@ int flf_clear_cache(flf_ctx *ctx) {
   if (!ctx) return FLF_E_ARG;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
-  free_geometry(ctx->geo);
+  free_all_geometries(ctx);
   Workspace *ws[] = {&ctx->wsS, &ctx->wsO, &ctx->wsCvol, &ctx->wsCimg, &ctx->wsCy};
   for (Workspace *w : ws) {
     if (w->p) cudaFree(w->p);
@@ -1153,7 +1191,17 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     if (ctx->opt_plane_sizes != (int)value) {
       ctx->opt_plane_sizes = (int)value;
       cudaDeviceSynchronize();
-      free_geometry(ctx->geo);   // rebuilt on the next call
+      free_all_geometries(ctx);   // rebuilt on the next call
+    }
+    return FLF_OK;
+  }
+  if (!strcmp(name, "geometry_cache")) {
+    if (value < 0 || value > 16) return fail(ctx, FLF_E_ARG, "geometry_cache must be in [0, 16]");
+    ctx->opt_geometry_cache = (int)value;
+    while ((int)ctx->parked.size() > ctx->opt_geometry_cache) {
+      cudaDeviceSynchronize();
+      free_geometry(ctx->parked.back());
+      ctx->parked.pop_back();
     }
     return FLF_OK;
   }

@@ -268,3 +268,30 @@ def test_context_errors(mods):
     with pytest.raises(_flf.FlfError):
         ctx.prepare(30, 30)          # PSFs not uploaded
     ctx.close()
+
+
+def test_geometry_cache_across_image_shapes(mods):
+    """Alternating image shapes in one context: results equal fresh contexts', and a
+    shape seen before reuses its parked transfer matrices (no new device memory)."""
+    projector, lfdeconv, psfmatrix = mods
+    import synthetic
+    N = 5
+    H, Ht = synthetic.random_psf(N, [21, 11, 31], seed=7)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(3)
+    imgs = {s: rng.random((1,) + s).astype(np.float32) for s in [(40, 35), (30, 30), (55, 50)]}
+    fresh = {s: projector.Projector_gb300().BackwardProjectACC(hm, im, None) for s, im in imgs.items()}
+    p = projector.Projector_gb300()
+    mem = []
+    for s in [(40, 35), (30, 30), (40, 35), (55, 50), (30, 30)]:
+        out = p.BackwardProjectACC(hm, imgs[s], None)
+        assert np.array_equal(out, fresh[s]), s
+        mem.append(p.context(hm).memory_usage())
+    assert mem[2] == mem[1]            # (40, 35) came back from the cache
+    assert mem[3] > mem[2]             # a third shape: two parked + one active
+    assert mem[4] == mem[3]            # (30, 30) still parked (cache of 2)
+    ctx = p.context(hm)
+    ctx.set_option("geometry_cache", 0)
+    out = p.BackwardProjectACC(hm, imgs[(40, 35)], None)
+    assert np.array_equal(out, fresh[(40, 35)])
+    assert ctx.memory_usage() < mem[4]
