@@ -43,6 +43,7 @@ _SIGS = {
     "flf_set_option": (_I, [_P, ctypes.c_char_p, ctypes.c_longlong]),
     "flf_synchronize": (_I, [_P, _P]),
     "flf_backward_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "flf_resample_bilinear": (_I, [_P, _I, _I, _P, _I, _P, _I, _P, _P]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 
@@ -96,6 +97,19 @@ def _ptr(x):
     if isinstance(x, np.ndarray):
         return x.ctypes.data
     raise TypeError("cannot take a pointer of %r" % type(x))
+
+
+def resample_bilinear(img, yq, xq, out, stream=None):
+    """flf_resample_bilinear on device tensors: img float32 [H, W], yq / xq float64,
+    out float64 [len(yq), len(xq)]."""
+    lib = load_library()
+    H, W = int(img.shape[0]), int(img.shape[1])
+    rc = lib.flf_resample_bilinear(_ptr(img), H, W, _ptr(yq), int(yq.shape[0]), _ptr(xq), int(xq.shape[0]),
+                                   _ptr(out), _ptr(stream))
+    if rc != FLF_OK:
+        buf = ctypes.create_string_buffer(1024)
+        lib.flf_last_error(None, buf, 1024)
+        raise FlfError(rc, buf.value.decode(errors="replace"))
 
 
 class Context:

@@ -1230,9 +1230,20 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
   return fail(ctx, FLF_E_ARG, "unknown option '%s'", name);
 }
 
+int flf_resample_bilinear(const float *img_dev, int H, int W, const double *yq_dev, int ny, const double *xq_dev,
+                          int nx, double *out_dev, void *stream) {
+  if (!img_dev || !yq_dev || !xq_dev || !out_dev) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (H <= 0 || W <= 0 || ny < 0 || nx < 0)
+    return fail(nullptr, FLF_E_ARG, "invalid sizes (image %d x %d, queries %d x %d)", H, W, ny, nx);
+  ResampleParams rp{img_dev, H, W, yq_dev, xq_dev, ny, nx, out_dev};
+  const cudaError_t e = launch_resample_bilinear(rp, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "resample launch failed: %s", cudaGetErrorString(e));
+  return FLF_OK;
+}
+
 int flf_version(char *buf, size_t len) {
   if (!buf || len == 0) return FLF_E_ARG;
-  snprintf(buf, len, "libflf 0.2 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack");
+  snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear");
   return FLF_OK;
 }
 

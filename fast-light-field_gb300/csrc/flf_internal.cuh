@@ -158,6 +158,14 @@ struct MergeParams {
   Div16 dlx, dn;            // set by the launcher
 };
 
+struct ResampleParams {     // bilinear resample of img [H][W] at yq [ny] x xq [nx] -> out [ny][nx]
+  const float *img;
+  int H, W;
+  const double *yq, *xq;
+  int ny, nx;
+  double *out;
+};
+
 struct MacParams {
   Layout L;
   int f, fh, fq, nkp;       // transform size, f/2+1, f/2+1, fq*fq
@@ -206,6 +214,7 @@ struct PackParams {
 cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s);
 cudaError_t launch_irfft2(const Irfft2Params &p, cudaStream_t s);
 cudaError_t launch_split(const SplitParams &p, cudaStream_t s);
+cudaError_t launch_resample_bilinear(const ResampleParams &p, cudaStream_t s);
 cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);

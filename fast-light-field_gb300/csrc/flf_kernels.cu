@@ -884,6 +884,42 @@ cudaError_t launch_merge(const MergeParams &p0, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ----------------------------------------------------------------------------
+// Rectification resample: bilinear interpolation of a float image at a
+// separable grid of query coordinates, in double precision.  This is the
+// reference's RectBivariateSpline(kx = ky = 1) evaluation (rectify.py:8-81):
+// a degree-1 B-spline through the pixel values is the bilinear interpolant.
+// Queries outside [0, H-1] x [0, W-1] are clamped to the edge.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void bilinear_cell(double q, int n, int &i0, double &t) {
+  if (n < 2) { i0 = 0; t = 0.0; return; }
+  const double qc = fmin(fmax(q, 0.0), (double)(n - 1));
+  i0 = min((int)floor(qc), n - 2);
+  t = qc - (double)i0;
+}
+
+__global__ void __launch_bounds__(256) k_resample_bilinear(ResampleParams p) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)p.ny * p.nx) return;
+  const int r = (int)(idx / p.nx), c = (int)(idx - (long long)r * p.nx);
+  int y0, x0;
+  double fy, fx;
+  bilinear_cell(p.yq[r], p.H, y0, fy);
+  bilinear_cell(p.xq[c], p.W, x0, fx);
+  const int y1 = min(y0 + 1, p.H - 1), x1 = min(x0 + 1, p.W - 1);
+  const float *row0 = p.img + (long long)y0 * p.W, *row1 = p.img + (long long)y1 * p.W;
+  const double top = (1.0 - fx) * (double)row0[x0] + fx * (double)row0[x1];
+  const double bot = (1.0 - fx) * (double)row1[x0] + fx * (double)row1[x1];
+  p.out[idx] = (1.0 - fy) * top + fy * bot;
+}
+
+cudaError_t launch_resample_bilinear(const ResampleParams &p, cudaStream_t s) {
+  const long long n = (long long)p.ny * p.nx;
+  if (n == 0) return cudaSuccess;
+  k_resample_bilinear<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
 // Transforms: the hot path runs the size-specialised kernels (flf_fft.cuh),
 // one per even 7-smooth size up to kMaxF; the precompute (contiguous float or
 // double images) runs the runtime-plan kernel above.

@@ -177,6 +177,17 @@ int flf_synchronize(flf_ctx *ctx, void *stream);
  * arch, kernel list) into buf. */
 int flf_version(char *buf, size_t len);
 
+/* Rectification resample (replaces the interpolation of the reference's
+ * rectify.RectifyImage, rectify.py:56-57, a RectBivariateSpline with
+ * kx = ky = 1, i.e. bilinear): out[r][c] = bilinear value of the image
+ * img [H][W] (float, row-major) at (yq[r], xq[c]), 0-based pixel
+ * coordinates, in double precision; coordinates outside the image are
+ * clamped to its edge.  The query grids are built by the caller exactly as
+ * the reference builds them.  Device pointers; no context; allocates
+ * nothing.  Errors are read with flf_last_error(NULL, ...). */
+int flf_resample_bilinear(const float *img_dev, int H, int W, const double *yq_dev, int ny,
+                          const double *xq_dev, int nx, double *out_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
