@@ -44,6 +44,8 @@ WORKLOADS = {
                       label="full-field 1005x1005 px, Nnum 15, 41 planes -100..100 um, plain RL"),
     "small": dict(Nnum=15, lenslets=30, z=(-25, 25, 5), img_size_ref=7, beads=200, filaments=0,
                   label="450x450 px, Nnum 15, 11 planes -25..25 um, plain RL"),
+    # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
+    "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
     # a time series of frames of three sizes (--frames per size), 500 drifting beads each
     "timeseries": dict(Nnum=15, sizes=(30, 45, 67), z=(-75, 75, 5), img_size_ref=21, beads=500,
                        label="time series, Nnum 15, 31 planes -75..75 um, frames at 30x30, 45x45 and 67x67 "
@@ -240,9 +242,9 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload == "timeseries":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the single-size "
-                          "workloads; the time series is a GB300-only measurement"}), flush=True)
+    if args.workload in ("timeseries", "rectify"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
+                          "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
     wl = WORKLOADS[args.workload]
     N = wl["Nnum"]
@@ -483,6 +485,69 @@ def run_timeseries(args):
     print(json.dumps(line), flush=True)
 
 
+def run_rectify(args):
+    """Rectification throughput (images/s): the device resample alone (value) and the
+    public RectifyImage call with host image in and host result out (e2e), beside the
+    CPU oracle of the reference's RectifyImage on one image."""
+    import torch
+    import build_lib
+    import rectify
+    import _flf
+    from oracle import rectify_oracle as R
+    build_lib.build()
+    wl = WORKLOADS["rectify"]
+    T = max(args.frames, 8)
+    H, W = wl["raw"]
+    rng = np.random.default_rng(5)
+    imgs = (rng.random((T, H, W)) * 60000).astype(np.uint16)
+    kw = dict(xCenter_m=W / 2 + 0.37, yCenter_m=H / 2 - 0.21, dx=wl["dx"], Nnum=wl["Nnum"], Crop=False,
+              XcutLeft=0, XcutRight=0, YcutUp=0, YcutDown=0)
+    yq, xq, ny, nx = rectify.rectify_grid((H, W), kw["xCenter_m"], kw["yCenter_m"], kw["dx"], kw["Nnum"])
+    dev = torch.device("cuda", 0)
+    s = torch.cuda.current_stream(dev)
+    img_d = torch.as_tensor(imgs.astype(np.float32), device=dev)
+    yq_d = torch.as_tensor(np.ascontiguousarray(yq[:ny]), device=dev)
+    xq_d = torch.as_tensor(np.ascontiguousarray(xq[:nx]), device=dev)
+    out = torch.empty((T, ny, nx), dtype=torch.float64, device=dev)
+
+    def step():
+        for t in range(T):
+            _flf.resample_bilinear(img_d[t], yq_d, xq_d, out[t], s.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    rectify.RectifyImage(imgs[0], **kw)
+    t0 = time.perf_counter()
+    for t in range(T):
+        rectify.RectifyImage(imgs[t], **kw)
+    e2e_s = (time.perf_counter() - t0) / T
+    t0 = time.perf_counter()
+    R.rectify_image(imgs[0], **kw)
+    cpu_s = time.perf_counter() - t0
+    bytes_per_image = 4.0 * H * W + 8.0 * ny * nx
+    line = {"metric": "raw light-field images/s rectified (bilinear resample), 1 GB300", "value": T / (ms / 1000.0),
+            "unit": "images/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["label"], "images_per_step": T, "out_px": [int(ny), int(nx)],
+                       "l2": "inputs 16 MB per image, %d images per step" % T},
+            "e2e": {"value": 1.0 / e2e_s, "unit": "images/s", "h2d_bytes_per_step": int(imgs[0].size * 4),
+                    "d2h_bytes_per_step": int(8 * ny * nx)},
+            "roofline": {"bound": "hbm", "achieved": round(bytes_per_image * T / (ms / 1000.0) / 1e9, 1),
+                         "peak": measured_peaks()[0], "unit": "GB/s",
+                         "frac": round(bytes_per_image * T / (ms / 1000.0) / 1e9 / measured_peaks()[0], 4)},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "images/s", "cores": 1, "kind": "port",
+                             "sample": "one image through the oracle restatement of RectifyImage (numpy)"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -490,6 +555,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "timeseries":
         run_timeseries(args)
+    elif args.workload == "rectify":
+        run_rectify(args)
     else:
         run_gb300(args, rank, world, local)
 

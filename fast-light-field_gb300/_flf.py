@@ -44,8 +44,11 @@ _SIGS = {
     "flf_synchronize": (_I, [_P, _P]),
     "flf_backward_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "flf_resample_bilinear": (_I, [_P, _I, _I, _P, _I, _P, _I, _P, _P]),
+    "flf_autotune": (_I, [_P, _I, _I, _I, ctypes.POINTER(ctypes.c_int), _P]),
+    "flf_set_tuned": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_int)]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
+TUNED_KEYS = ("stages", "chunk_rows_forward", "chunk_rows_backward", "split")
 
 _lib = None
 
@@ -209,6 +212,17 @@ class Context:
             name, n, ms, b = line.split()
             out[name] = {"launches": int(n), "ms": float(ms), "bytes": float(b)}
         return out
+
+    def autotune(self, T, Y, X, stream=None):
+        """Launch shape of the multiply-accumulate for T frames of Y x X images:
+        {"stages", "chunk_rows_forward", "chunk_rows_backward", "split"}."""
+        out = (ctypes.c_int * 4)()
+        self._check(self._lib.flf_autotune(self._h, int(T), int(Y), int(X), out, _ptr(stream)))
+        return dict(zip(TUNED_KEYS, list(out)))
+
+    def set_tuned(self, Y, X, tuned):
+        arr = (ctypes.c_int * 4)(*[int(tuned[k]) for k in TUNED_KEYS])
+        self._check(self._lib.flf_set_tuned(self._h, int(Y), int(X), arr))
 
     def geometry(self):
         out = (ctypes.c_int * 4)()

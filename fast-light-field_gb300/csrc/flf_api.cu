@@ -42,6 +42,8 @@ struct Group {
 struct Geometry {
   bool valid = false;
   int Y = 0, X = 0, Ly = 0, Lx = 0, fp64 = 0, uniform_f = 0;
+  int tuned[4] = {0, 0, 0, 0};   // multiply-accumulate launch shape chosen by flf_autotune
+                                 // (stages, chunk rows forward, backward, split); 0: context options
   std::vector<Group> groups;
   std::vector<int> plane_group, plane_slot;
   bool built(int dir) const {
@@ -645,9 +647,31 @@ MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
   mp.P = G.P[dir];
   mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
-  mp.stages = ctx->opt_stages; mp.chunk_rows = ctx->opt_chunk_rows[dir]; mp.split = ctx->opt_split;
+  const int *tn = ctx->geo.tuned;
+  mp.stages = tn[0] ? tn[0] : ctx->opt_stages;
+  mp.chunk_rows = tn[1 + dir] ? tn[1 + dir] : ctx->opt_chunk_rows[dir];
+  mp.split = tn[3] ? tn[3] : ctx->opt_split;
   mp.err = ctx->d_err;
   return mp;
+}
+
+// One multiply-accumulate launch of group gi over all its planes for nt
+// frames, on the workspaces (flf_autotune's timing unit).
+cudaError_t mac_group_launch(flf_ctx *ctx, size_t gi, int dir, int nt, const PlaneSet &ps, int stages, int chunk,
+                             int split, cudaStream_t s) {
+  const Group &G = ctx->geo.groups[gi];
+  const int nplanes = ps.n[gi];
+  const int zg = zgroup_for(ctx, nplanes, G.nkp);
+  MacParams mp = mac_params(ctx, G, dir, nt);
+  mp.stages = stages; mp.chunk_rows = chunk; mp.split = split;
+  mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zg;
+  mp.S = (const float2 *)ctx->wsS.p; mp.O = (float2 *)ctx->wsO.p;
+  if (dir == FLF_DIR_FORWARD) {
+    mp.nzS = nplanes; mp.nzo = (nplanes + zg - 1) / zg; mp.nzo_grid = mp.nzo;
+  } else {
+    mp.nzS = 1; mp.nzo = nplanes; mp.nzo_grid = (nplanes + zg - 1) / zg;
+  }
+  return launch_mac(mp, dir == FLF_DIR_FORWARD, s);
 }
 
 SplitParams split_params(const flf_ctx *ctx, const float *src, long long src_sz, long long src_st,
@@ -1228,6 +1252,102 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     return FLF_OK;
   }
   return fail(ctx, FLF_E_ARG, "unknown option '%s'", name);
+}
+
+int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream) {
+  if (!ctx || !out4) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int d = 0; d < 2; d++)
+    for (int z = 0; z < ctx->nz; z++)
+      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+  int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
+  if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
+  PlaneSet ps;
+  if (rc == FLF_OK) rc = make_plane_set(ctx, nullptr, ctx->nz, s, ps);
+  if (rc != FLF_OK) return rc;
+  Geometry &Gm = ctx->geo;
+  const int nt = std::min(T, mac_max_frames());
+  size_t sSf, sOf, sCf, sSb, sOb, sCb;
+  ws_needs(ctx, ps, nt, true, sSf, sOf, sCf);
+  ws_needs(ctx, ps, nt, false, sSb, sOb, sCb);
+  rc = ensure_ws(ctx, ctx->wsS, std::max(sSf, sSb));
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, std::max(sOf, sOb));
+  if (rc != FLF_OK) return rc;
+  CUDA_TRY(ctx, cudaMemsetAsync(ctx->wsS.p, 0, ctx->wsS.bytes, s));
+  // time the group that streams the most matrix bytes
+  size_t gi = 0;
+  double most = -1;
+  for (size_t g = 0; g < Gm.groups.size(); g++) {
+    const double b = (double)Gm.groups[g].nkp * ps.n[g];
+    if (b > most) { most = b; gi = g; }
+  }
+  const int ntp = (ctx->L.nthr + 31) / 32 * 32;
+  const int stages_c[] = {2, 3};
+  const int chunk_c[] = {8, 10, 12, 16, 20};
+  const int split_c[] = {1, 2};
+  cudaEvent_t e0, e1;
+  CUDA_TRY(ctx, cudaEventCreate(&e0));
+  CUDA_TRY(ctx, cudaEventCreate(&e1));
+  // best[dir][stages][split] = (time, chunk)
+  double bt[2][2][2];
+  int bc[2][2][2];
+  for (int d = 0; d < 2; d++)
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) { bt[d][a][b] = 1e30; bc[d][a][b] = 0; }
+  cudaError_t e = cudaSuccess;
+  for (int d = 0; d < 2 && e == cudaSuccess; d++)
+    for (int a = 0; a < 2 && e == cudaSuccess; a++)
+      for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        if (split_c[b] * ntp > 256) continue;
+        for (int ch : chunk_c) {
+          if (mac_smem_bytes(ctx->L, mac_max_frames(), stages_c[a], ch, split_c[b], true) > 227 * 1024) continue;
+          e = mac_group_launch(ctx, gi, d, nt, ps, stages_c[a], ch, split_c[b], s);   // warm-up
+          if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+          for (int k = 0; k < 3 && e == cudaSuccess; k++) e = mac_group_launch(ctx, gi, d, nt, ps, stages_c[a], ch, split_c[b], s);
+          if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          float ms = 0;
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          if (e != cudaSuccess) break;
+          if (ms < bt[d][a][b]) { bt[d][a][b] = ms; bc[d][a][b] = ch; }
+        }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(ctx, FLF_E_CUDA, "autotune launch failed: %s", cudaGetErrorString(e));
+  if ((rc = check_device_flag(ctx)) != FLF_OK) return rc;
+  int ba = 0, bb = 0;
+  double best = 1e30;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      if (bc[0][a][b] && bc[1][a][b] && bt[0][a][b] + bt[1][a][b] < best) {
+        best = bt[0][a][b] + bt[1][a][b];
+        ba = a; bb = b;
+      }
+  if (best >= 1e30) return fail(ctx, FLF_E_STATE, "autotune found no launch shape that fits this geometry");
+  Gm.tuned[0] = stages_c[ba];
+  Gm.tuned[1] = bc[FLF_DIR_FORWARD][ba][bb];
+  Gm.tuned[2] = bc[FLF_DIR_BACKWARD][ba][bb];
+  Gm.tuned[3] = split_c[bb];
+  for (int i = 0; i < 4; i++) out4[i] = Gm.tuned[i];
+  return FLF_OK;
+}
+
+int flf_set_tuned(flf_ctx *ctx, int Y, int X, const int *in4) {
+  if (!ctx || !in4) return FLF_E_ARG;
+  Geometry &Gm = ctx->geo;
+  if (!Gm.valid || Gm.Y != Y || Gm.X != X)
+    return fail(ctx, FLF_E_STATE, "no prepared geometry for %d x %d: call flf_prepare first", Y, X);
+  const int ntp = (ctx->L.nthr + 31) / 32 * 32;
+  if (in4[0] < 2 || in4[0] > 16 || in4[3] < 1 || in4[3] > 4 || in4[3] * ntp > 256)
+    return fail(ctx, FLF_E_ARG, "invalid launch shape");
+  for (int d = 1; d <= 2; d++)
+    if (in4[d] < 2 || in4[d] > 64 || (in4[d] & 1) ||
+        mac_smem_bytes(ctx->L, mac_max_frames(), in4[0], in4[d], in4[3], true) > 227 * 1024)
+      return fail(ctx, FLF_E_ARG, "invalid rows per chunk %d", in4[d]);
+  for (int i = 0; i < 4; i++) Gm.tuned[i] = in4[i];
+  return FLF_OK;
 }
 
 int flf_resample_bilinear(const float *img_dev, int H, int W, const double *yq_dev, int ny, const double *xq_dev,

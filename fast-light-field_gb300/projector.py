@@ -13,6 +13,8 @@ There is no CPU fallback: a projector raises ``_flf.FlfError`` when the CUDA
 library or a GPU is missing.
 """
 
+import os
+
 import numpy as np
 
 import _flf
@@ -154,6 +156,41 @@ class Projector_gb300(Projector_base):
             fp64 = self._auto_fp64(hMatrix, Y, X) if hMatrix is not None else False
         ctx.prepare(Y, X, self.fft_size, fp64)
         self._shape_key = key
+
+    def autotune(self, hMatrix, T, Y, X, cache_path=None):
+        """Pick the multiply-accumulate launch shape for T frames of Y x X images
+        (flf_autotune) and keep it with this image shape's transfer matrices.
+
+        With ``cache_path`` the choice is stored in, and on later calls read back
+        from, a JSON file keyed by device, Nnum, plane count, PSF sizes, image
+        shape, frames per launch and transform size, so tuning runs once per
+        configuration."""
+        ctx = self.context(hMatrix)
+        self._prepare(ctx, Y, X, hMatrix)
+        key = cache = None
+        if cache_path:
+            import json
+            key = "|".join(str(v) for v in (
+                torch.cuda.get_device_name(self._dev()), hMatrix.Nnum, hMatrix.numZ,
+                tuple(tuple(hMatrix.PSFShape(cc)) for cc in range(hMatrix.numZ)), Y, X,
+                min(int(T), 4), self.fft_size, self._shape_key[3]))
+            try:
+                with open(cache_path) as f:
+                    cache = json.load(f)
+            except (OSError, ValueError):
+                cache = {}
+            if key in cache:
+                ctx.set_tuned(Y, X, cache[key])
+                return dict(cache[key])
+        tuned = ctx.autotune(T, Y, X, self._stream())
+        if cache_path:
+            import json
+            cache[key] = tuned
+            tmp = cache_path + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(cache, f, indent=1)
+            os.replace(tmp, cache_path)
+        return tuned
 
     def ClearCache(self):
         if self._ctx is not None:

@@ -177,6 +177,22 @@ int flf_synchronize(flf_ctx *ctx, void *stream);
  * arch, kernel list) into buf. */
 int flf_version(char *buf, size_t len);
 
+/* Autotuner (the GB300 counterpart of the reference's FFTW planning mode,
+ * SetPlanningMode, and of its block-shape knobs, projector.py:26-36): for
+ * T frames of Y x X images, builds the transfer matrices if needed, then
+ * times the multiply-accumulate of both directions on the transform group
+ * that streams the most bytes, over ring stages {2, 3} x rows per chunk
+ * {8, 10, 12, 16, 20} x row split {1, 2} (shapes that fit shared memory).
+ * The fastest shape is kept with this image shape's transfer matrices and
+ * used by every later call on it; out4 = {stages, rows per chunk forward,
+ * rows per chunk backward, split}.  Runs work on `stream` and waits for it.
+ * Results do not depend on the launch shape beyond rounding. */
+int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream);
+
+/* Apply a launch shape found earlier by flf_autotune (for example read back
+ * from a cache file) to the prepared geometry of Y x X images. */
+int flf_set_tuned(flf_ctx *ctx, int Y, int X, const int *in4);
+
 /* Rectification resample (replaces the interpolation of the reference's
  * rectify.RectifyImage, rectify.py:56-57, a RectBivariateSpline with
  * kx = ky = 1, i.e. bilinear): out[r][c] = bilinear value of the image

@@ -295,3 +295,39 @@ def test_geometry_cache_across_image_shapes(mods):
     out = p.BackwardProjectACC(hm, imgs[(40, 35)], None)
     assert np.array_equal(out, fresh[(40, 35)])
     assert ctx.memory_usage() < mem[4]
+
+
+def test_autotune_keeps_results_and_caches(mods, tmp_path):
+    """flf_autotune picks a launch shape per image shape; results do not change
+    beyond rounding, and a cache file brings the choice back without timing."""
+    projector, lfdeconv, psfmatrix = mods
+    import json
+    import synthetic
+    N = 7
+    H, Ht = synthetic.random_psf(N, [43, 15, 29], seed=5)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(8)
+    img = rng.random((2, 56, 63)).astype(np.float32)
+    vol = rng.random((3, 2, 56, 63)).astype(np.float32)
+    p = projector.Projector_gb300()
+    bk0, fw0 = p.BackwardProjectACC(hm, img, None), p.ForwardProjectACC(hm, vol, None)
+    cache = str(tmp_path / "tune.json")
+    tuned = p.autotune(hm, 2, 56, 63, cache_path=cache)
+    assert tuned["stages"] in (2, 3) and tuned["split"] in (1, 2)
+    assert tuned["chunk_rows_forward"] in (8, 10, 12, 16, 20) and tuned["chunk_rows_backward"] in (8, 10, 12, 16, 20)
+    bk1, fw1 = p.BackwardProjectACC(hm, img, None), p.ForwardProjectACC(hm, vol, None)
+    assert rel(bk1, bk0) < PROJ_TOL and rel(fw1, fw0) < PROJ_TOL
+    # the choice stays with its image shape across a shape switch
+    p.BackwardProjectACC(hm, img[:, :40, :40], None)
+    bk2 = p.BackwardProjectACC(hm, img, None)
+    assert np.array_equal(bk2, bk1)
+    # a fresh projector reads the cache (a planted shape proves no timing ran)
+    with open(cache) as f:
+        d = json.load(f)
+    (k,) = d.keys()
+    d[k] = {"stages": 3, "chunk_rows_forward": 10, "chunk_rows_backward": 8, "split": 1}
+    with open(cache, "w") as f:
+        json.dump(d, f)
+    q = projector.Projector_gb300()
+    assert q.autotune(hm, 2, 56, 63, cache_path=cache) == d[k]
+    assert rel(q.BackwardProjectACC(hm, img, None), bk0) < PROJ_TOL
