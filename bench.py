@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--iters", type=int, default=8)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-planes", type=int, default=5)
     ap.add_argument("--planes", default=None,
@@ -296,10 +297,27 @@ def run_gb300(args, rank, world, local):
     htf = torch.empty((Z, T, Y, X), dtype=torch.float32, device=dev)
     x = torch.empty((Z, T, Y, X), dtype=torch.float32, device=dev)
 
-    def step():
+    # the RL iterations of a step replay one CUDA graph (flf_rl_graph_create)
+    graph = None if args.no_graph else ctx.rl_graph(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X)
+
+    def step(direct=False):
         ctx.backward(img_d, htf, T, Y, X, None, stream=stream.cuda_stream)
         x.fill_(1.0)
-        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=stream.cuda_stream)
+        if graph is None or direct:
+            ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=stream.cuda_stream)
+        else:
+            graph.launch(stream.cuda_stream)
+
+    def timed(direct):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(direct)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
 
     for _ in range(args.warmup):
         step()
@@ -309,19 +327,15 @@ def run_gb300(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
+    ms = timed(direct=False)
+    clk = clocks.stop()
+    # per-kernel durations: the same steps again, launched directly with CUDA
+    # events around every kernel on the launching stream (a graph replay has
+    # no per-kernel events)
     ctx.profile(True)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms_direct = timed(direct=True)
     prof = ctx.profile_read()
     ctx.profile(False)
-    clk = clocks.stop()
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -398,7 +412,10 @@ def run_gb300(args, rank, world, local):
                            "l2": "inputs larger than L2: %.1f GB of transfer matrices streamed per "
                                  "projection, %.0f MB volume" % (tot_bytes / args.steps / (1 + 2 * args.iters) / 1e9,
                                                                 Z * T * Y * X * 4 / 1e6),
-                           "parallelism": "replicas" if world > 1 else "single"},
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "rl_launch": "direct" if graph is None else
+                           "CUDA graph replay of the RL iterations (%d kernels)" % graph.kernels},
+                "ms_per_step_direct_profiled": ms_direct,
                 "rl_iterations_per_s": value * args.iters, "accuracy": accuracy,
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cb,
                 "clocks": clk}

@@ -45,6 +45,10 @@ _SIGS = {
     "flf_backward_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "flf_resample_bilinear": (_I, [_P, _I, _I, _P, _I, _P, _I, _P, _P]),
     "flf_autotune": (_I, [_P, _I, _I, _I, ctypes.POINTER(ctypes.c_int), _P]),
+    "flf_rl_graph_create": (_I, [_P, ctypes.POINTER(_P), _P, _P, _P, _I, _I, _I, _I, _I]),
+    "flf_graph_launch": (_I, [_P, _P]),
+    "flf_graph_kernels": (_I, [_P]),
+    "flf_graph_destroy": (_I, [_P]),
     "flf_set_tuned": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_int)]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
@@ -113,6 +117,30 @@ def resample_bilinear(img, yq, xq, out, stream=None):
         buf = ctypes.create_string_buffer(1024)
         lib.flf_last_error(None, buf, 1024)
         raise FlfError(rc, buf.value.decode(errors="replace"))
+
+
+class RLGraph:
+    """A captured RL run; launch() replays it on a stream.  Keeps its tensors alive."""
+
+    def __init__(self, ctx, handle, keep):
+        self._ctx, self._h, self._keep = ctx, handle, keep
+        self.kernels = ctx._lib.flf_graph_kernels(handle)
+
+    def launch(self, stream=None):
+        if not (self._h and self._h.value and self._ctx._h and self._ctx._h.value):
+            raise FlfError(-4, "the RL graph or its context was closed")
+        self._ctx._check(self._ctx._lib.flf_graph_launch(self._h, _ptr(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._ctx._lib.flf_graph_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Context:
@@ -212,6 +240,13 @@ class Context:
             name, n, ms, b = line.split()
             out[name] = {"launches": int(n), "ms": float(ms), "bytes": float(b)}
         return out
+
+    def rl_graph(self, x, ref, norm, variant, iters, T, Y, X):
+        """RLGraph replaying `iters` RL iterations on these tensors (flf_rl_graph_create)."""
+        h = _P()
+        self._check(self._lib.flf_rl_graph_create(self._h, ctypes.byref(h), _ptr(x), _ptr(ref), _ptr(norm),
+                                                  int(variant), int(iters), int(T), int(Y), int(X)))
+        return RLGraph(self, h, (x, ref, norm))
 
     def autotune(self, T, Y, X, stream=None):
         """Launch shape of the multiply-accumulate for T frames of Y x X images:

@@ -87,6 +87,7 @@ struct flf_ctx {
   int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
   int opt_geometry_cache = 2;    // geometries of other image shapes kept resident (most recent first)
   std::vector<Geometry> parked;  // those geometries
+  unsigned long long mem_epoch = 0;   // bumped whenever a workspace or geometry buffer is freed
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
   int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
@@ -203,7 +204,10 @@ FftPlan make_plan(int n) {
 
 int ensure_ws(flf_ctx *ctx, Workspace &w, size_t bytes) {
   if (w.bytes >= bytes) return FLF_OK;
-  if (w.p) cudaFree(w.p);
+  if (w.p) {
+    cudaFree(w.p);
+    ctx->mem_epoch++;
+  }
   w.p = nullptr;
   w.bytes = 0;
   cudaError_t e = cudaMalloc(&w.p, bytes);
@@ -230,11 +234,13 @@ void free_geometry(Geometry &G) {
 void park_geometry(flf_ctx *ctx, Geometry &&G) {
   if (!G.valid || ctx->opt_geometry_cache <= 0) {
     free_geometry(G);
+    ctx->mem_epoch++;
     return;
   }
   ctx->parked.insert(ctx->parked.begin(), std::move(G));
   G = Geometry();
   while ((int)ctx->parked.size() > ctx->opt_geometry_cache) {
+    ctx->mem_epoch++;
     free_geometry(ctx->parked.back());
     ctx->parked.pop_back();
   }
@@ -242,6 +248,7 @@ void park_geometry(flf_ctx *ctx, Geometry &&G) {
 
 // Free the active geometry and every parked one (the PSFs or the size rule changed).
 void free_all_geometries(flf_ctx *ctx) {
+  ctx->mem_epoch++;
   free_geometry(ctx->geo);
   for (Geometry &g : ctx->parked) free_geometry(g);
   ctx->parked.clear();
@@ -1081,31 +1088,47 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
   return FLF_OK;
 }
 
-int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev,
-                   int variant, int iters, int T, int Y, int X, void *stream) {
-  if (!ctx) return FLF_E_ARG;
+}  // extern "C"
+
+namespace {
+
+// Argument checks, transfer matrices and every workspace of an RL run of T
+// frames of Y x X images, so that the loop itself allocates nothing.
+int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int iters, int T, int Y, int X,
+             cudaStream_t s, PlaneSet &ps) {
   if (!x_dev || !ref_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
   if (variant != FLF_RL_PREVEDEL && variant != FLF_RL_STANDARD)
     return fail(ctx, FLF_E_ARG, "unknown RL variant %d", variant);
   if (iters < 0) return fail(ctx, FLF_E_ARG, "iters must be >= 0");
-  cudaSetDevice(ctx->device);
-  cudaStream_t s = (cudaStream_t)stream;
   for (int d = 0; d < 2; d++)
     for (int z = 0; z < ctx->nz; z++)
       if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
   int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   if (rc != FLF_OK) return rc;
-  const int TF = mac_max_frames();
-  const long long YX = (long long)Y * X;
-  const size_t cset = sizeof(float) * chan_set_floats(ctx) * std::min(T, TF);
+  const int nt = std::min(T, mac_max_frames());
+  const size_t cset = sizeof(float) * chan_set_floats(ctx) * nt;
   rc = ensure_ws(ctx, ctx->wsCimg, cset);
   if (rc == FLF_OK && variant == FLF_RL_STANDARD) rc = ensure_ws(ctx, ctx->wsCy, cset);
-  PlaneSet ps;
   if (rc == FLF_OK) rc = make_plane_set(ctx, nullptr, ctx->nz, s, ps);
   if (rc != FLF_OK) return rc;
+  size_t a, b, c, a2, b2, c2;
+  ws_needs(ctx, ps, nt, true, a, b, c);
+  ws_needs(ctx, ps, nt, false, a2, b2, c2);
+  rc = ensure_ws(ctx, ctx->wsS, std::max(a, a2));
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, std::max(b, b2));
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, std::max(c, c2));
+  return rc;
+}
+
+// The RL loop on stream s (after rl_setup).
+int rl_run(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev, int variant, int iters, int T,
+           int Y, int X, const PlaneSet &ps, cudaStream_t s) {
+  const int TF = mac_max_frames();
+  const long long YX = (long long)Y * X;
   float *cimg = (float *)ctx->wsCimg.p;
   float *cy = (float *)ctx->wsCy.p;
+  int rc = FLF_OK;
   for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
     const int nt = std::min(TF, T - t0);
     const Strided xs{x_dev + t0 * YX, (long long)T * YX, YX};
@@ -1129,6 +1152,96 @@ int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float
     }
   }
   return rc;
+}
+
+}  // namespace
+
+struct flf_graph {
+  flf_ctx *ctx = nullptr;
+  int device = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+  unsigned long long epoch = 0;   // ctx->mem_epoch at capture: the buffers baked into the graph
+};
+
+extern "C" {
+
+int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev,
+                   int variant, int iters, int T, int Y, int X, void *stream) {
+  if (!ctx) return FLF_E_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  PlaneSet ps;
+  int rc = rl_setup(ctx, x_dev, ref_dev, variant, iters, T, Y, X, s, ps);
+  if (rc != FLF_OK) return rc;
+  return rl_run(ctx, x_dev, ref_dev, norm_dev, variant, iters, T, Y, X, ps, s);
+}
+
+int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float *ref_dev, const float *norm_dev,
+                        int variant, int iters, int T, int Y, int X) {
+  if (!ctx || !out) return FLF_E_ARG;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  PlaneSet ps;
+  int rc = rl_setup(ctx, x_dev, ref_dev, variant, iters, T, Y, X, nullptr, ps);
+  if (rc != FLF_OK) return rc;
+  CUDA_TRY(ctx, cudaDeviceSynchronize());
+  cudaStream_t cs = nullptr;
+  CUDA_TRY(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  const bool prof = ctx->profiling;
+  ctx->profiling = false;           // no per-launch events inside the graph
+  long long before = 0;
+  for (auto &kv : ctx->kstats) before += kv.second.launches;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) rc = rl_run(ctx, x_dev, ref_dev, norm_dev, variant, iters, T, Y, X, ps, cs);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(cs, &g) : e;
+  ctx->profiling = prof;
+  long long after = 0;
+  for (auto &kv : ctx->kstats) after += kv.second.launches;
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess || e2 != cudaSuccess || rc != FLF_OK) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc != FLF_OK) return rc;
+    return fail(ctx, FLF_E_CUDA, "capture of the RL loop failed: %s",
+                cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ctx, FLF_E_CUDA, "instantiating the RL graph failed: %s", cudaGetErrorString(e));
+  }
+  flf_graph *gr = new flf_graph;
+  gr->ctx = ctx; gr->graph = g; gr->exec = ex; gr->launches = (int)(after - before);
+  gr->epoch = ctx->mem_epoch;
+  gr->device = ctx->device;
+  *out = gr;
+  return FLF_OK;
+}
+
+int flf_graph_launch(flf_graph *g, void *stream) {
+  if (!g || !g->exec) return FLF_E_ARG;
+  cudaSetDevice(g->ctx->device);
+  if (g->epoch != g->ctx->mem_epoch)
+    return fail(g->ctx, FLF_E_STATE, "the RL graph refers to workspaces or transfer matrices that were freed "
+                                     "since its capture (clear_cache, new PSFs or larger images): create it again");
+  if (int rc = check_device_flag(g->ctx)) return rc;
+  CUDA_TRY(g->ctx, cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_graph_kernels(const flf_graph *g) { return g ? g->launches : -1; }
+
+int flf_graph_destroy(flf_graph *g) {
+  if (!g) return FLF_OK;
+  cudaSetDevice(g->device);   // the context may already be gone
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return FLF_OK;
 }
 
 int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {

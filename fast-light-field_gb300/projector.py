@@ -90,6 +90,11 @@ class Projector_gb300(Projector_base):
         self._ctx = None
         self._ctx_key = None
         self._shape_key = None
+        # RichardsonLucy replays a CUDA graph of the whole loop; the graph runs on
+        # staging tensors of its own (one entry per volume shape / iteration count)
+        self.useGraphs = True
+        self.maxGraphs = 3
+        self._graphs = {}
 
     # -- native array helpers (torch CUDA tensors play cupy's role) ---------
     def _dev(self):
@@ -193,6 +198,7 @@ class Projector_gb300(Projector_base):
         return tuned
 
     def ClearCache(self):
+        self._drop_graphs()
         if self._ctx is not None:
             self._ctx.close()
         self._ctx = None
@@ -258,8 +264,61 @@ class Projector_gb300(Projector_base):
         Z, T, Y, X = x.shape
         self._prepare(ctx, Y, X, hMatrix)
         variant = _flf.FLF_RL_PREVEDEL if prevedel else _flf.FLF_RL_STANDARD
-        ctx.rl_iterate(x, ref, norm, variant, iters, T, Y, X, stream=self._stream())
+        if not self.useGraphs or iters <= 0:
+            ctx.rl_iterate(x, ref, norm, variant, iters, T, Y, X, stream=self._stream())
+            return x
+        key = (Z, T, Y, X, int(iters), variant, norm is not None)
+        for attempt in (0, 1):
+            ent = self._graphs.pop(key, None)
+            if ent is None:
+                ent = self._make_rl_graph(ctx, key, ref, norm)
+            self._graphs[key] = ent            # most recent last
+            gx, gref, gnorm = ent["x"], ent["ref"], ent["norm"]
+            if gx.data_ptr() != x.data_ptr():
+                gx.copy_(x)
+            if gref.data_ptr() != ref.data_ptr():
+                gref.copy_(ref)
+            if gnorm is not None and gnorm.data_ptr() != norm.data_ptr():
+                gnorm.copy_(norm)
+            try:
+                ent["graph"].launch(self._stream())
+                break
+            except _flf.FlfError as e:
+                # the context freed buffers the graph refers to (new PSFs, larger
+                # images, clear_cache): capture it again once
+                self._graphs.pop(key)["graph"].close()
+                if e.code != -4 or attempt:
+                    raise
+        if gx.data_ptr() != x.data_ptr():
+            x.copy_(gx)
         return x
+
+    def _make_rl_graph(self, ctx, key, ref, norm):
+        Z, T, Y, X, iters, variant, _ = key
+        while len(self._graphs) >= max(1, self.maxGraphs):
+            self._graphs.pop(next(iter(self._graphs)))["graph"].close()
+        gx = torch.empty((Z, T, Y, X), dtype=torch.float32, device=self._dev())
+        gref = torch.empty(tuple(ref.shape), dtype=torch.float32, device=self._dev())
+        gnorm = None if norm is None else torch.empty(tuple(norm.shape), dtype=torch.float32, device=self._dev())
+        torch.cuda.current_stream(self._dev()).synchronize()
+        g = ctx.rl_graph(gx, gref, gnorm, variant, iters, T, Y, X)
+        return {"graph": g, "x": gx, "ref": gref, "norm": gnorm}
+
+    def _drop_graphs(self):
+        for ent in self._graphs.values():
+            ent["graph"].close()
+        self._graphs = {}
+
+    def RichardsonLucyGraph(self, hMatrix, x, ref, iters, prevedel=True, norm=None):
+        """RichardsonLucy captured as a CUDA graph on these tensors;
+        ``g.launch(stream)`` runs the ``iters`` iterations with one call.  Refill
+        ``x`` / ``ref`` in place between launches: the graph keeps their addresses."""
+        ctx = self.context(hMatrix)
+        Z, T, Y, X = x.shape
+        self._prepare(ctx, Y, X, hMatrix)
+        variant = _flf.FLF_RL_PREVEDEL if prevedel else _flf.FLF_RL_STANDARD
+        torch.cuda.current_stream(self._dev()).synchronize()
+        return ctx.rl_graph(x, ref, norm, variant, iters, T, Y, X)
 
 
 # Reference class names resolve to the GB300 backend (drop-in).

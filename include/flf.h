@@ -177,6 +177,21 @@ int flf_synchronize(flf_ctx *ctx, void *stream);
  * arch, kernel list) into buf. */
 int flf_version(char *buf, size_t len);
 
+/* CUDA graph of a whole RL run (the replay form of flf_rl_iterate): the
+ * launches of `iters` iterations over T frames of Y x X images are captured
+ * once, with these pointers baked in, and each flf_graph_launch replays them
+ * with one call, as one unit of stream work.  Create builds the transfer
+ * matrices and sizes every workspace first; the context must outlive the
+ * graph, and its workspaces must not shrink meanwhile (flf_clear_cache
+ * invalidates graphs).  Replays on one context must not overlap.  Replaces the
+ * per-iteration calls of the DeconvRL loop (lfdeconv.py:185-196). */
+typedef struct flf_graph flf_graph;
+int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float *ref_dev,
+                        const float *norm_dev, int variant, int iters, int T, int Y, int X);
+int flf_graph_launch(flf_graph *graph, void *stream);
+int flf_graph_kernels(const flf_graph *graph);   /* kernels per replay */
+int flf_graph_destroy(flf_graph *graph);
+
 /* Autotuner (the GB300 counterpart of the reference's FFTW planning mode,
  * SetPlanningMode, and of its block-shape knobs, projector.py:26-36): for
  * T frames of Y x X images, builds the transfer matrices if needed, then
