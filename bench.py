@@ -44,6 +44,11 @@ WORKLOADS = {
                       label="full-field 1005x1005 px, Nnum 15, 41 planes -100..100 um, plain RL"),
     "small": dict(Nnum=15, lenslets=30, z=(-25, 25, 5), img_size_ref=7, beads=200, filaments=0,
                   label="450x450 px, Nnum 15, 11 planes -25..25 um, plain RL"),
+    # GPU PSF generation for the optics of the 450 x 450 workload (M40 / NA 0.95 water, 150 um
+    # lenslets, f_ml 3000 um, 520 nm, OSR 3)
+    "psf": dict(Nnum=15, z=(-25, 25, 5), optics=dict(M=40, NA=0.95, MLPitch=150e-6, OSR=3, n=1.33, fml=3000e-6,
+                                                     lam=520e-9),
+                label="PSF generation, Nnum 15, M40 NA 0.95, OSR 3, 11 planes -25..25 um"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
     # a time series of frames of three sizes (--frames per size), 500 drifting beads each
@@ -243,7 +248,7 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload in ("timeseries", "rectify"):
+    if args.workload in ("timeseries", "rectify", "psf"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
                           "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
@@ -565,6 +570,68 @@ def run_rectify(args):
     print(json.dumps(line), flush=True)
 
 
+def run_psf(args):
+    """PSF generation (planes/s): GeneratePSFArrays on the device (value) and GeneratePSF
+    writing the memmap files (e2e), beside the CPU oracle of the reference's generator on
+    a 3-plane sample of the same optics."""
+    import tempfile
+    import warnings
+    import torch
+    import build_lib
+    import generate_psf
+    from oracle import psf_oracle as P
+    build_lib.build()
+    warnings.simplefilter("ignore")
+    wl = WORKLOADS["psf"]
+    z0, z1, dz = wl["z"]
+    kw = dict(Nnum=wl["Nnum"], zmin=z0 * 1e-6, zmax=z1 * 1e-6, zspacing=dz * 1e-6, **wl["optics"])
+    Z = len(np.arange(z0, z1 + dz / 2, dz))
+    for _ in range(max(args.warmup, 3)):
+        r = generate_psf.GeneratePSFArrays(**kw)
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    tim = []
+    for _ in range(steps):
+        r = generate_psf.GeneratePSFArrays(**kw)
+        tim.append(r["timings"])
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / steps
+    clk = clocks.stop()
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        generate_psf.GeneratePSF(matrixSaveDir=d, **kw)
+        e2e_s = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(os.path.join(dp, f)) for dp, _, fs in os.walk(d) for f in fs)
+    sample = dict(kw, zspacing=(z1 - z0) / 2 * 1e-6)
+    t0 = time.perf_counter()
+    P.generate_psf(sample)
+    cpu_s = time.perf_counter() - t0
+    mean = {k: float(np.mean([t[k] for t in tim])) for k in tim[0]}
+    line = {"metric": "PSF planes/s generated (Debye integral, microlens Fresnel propagation, binning, Ht), 1 GB300",
+            "value": Z / sec, "unit": "planes/s", "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": sec * 1000.0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["label"], "planes": Z, "image_grid": r["image_size"],
+                       "psf_sizes": [int(h.shape[-1]) for h in r["H"]], "quadrature_nodes": mean["quadrature_nodes"],
+                       "l2": "per plane 64 fields of %d x %d complex128 (%.0f MB)" % (
+                           r["image_size"], r["image_size"], 64 * 16 * r["image_size"] ** 2 / 1e6)},
+            "phases_s": {k: round(v, 4) for k, v in mean.items() if k.endswith("_s")},
+            "e2e": {"value": Z / e2e_s, "unit": "planes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(nbytes)},
+            "roofline": {"bound": "fp64", "kernel": "k_psf_debye + cuFFT Z2Z (FP64 arithmetic)",
+                         "achieved": None, "peak": None, "unit": None, "frac": None,
+                         "note": "FP64-arithmetic bound; MEASURED_PEAKS has no FP64 figure"},
+            "cpu_baseline": {"value": 3 / cpu_s, "unit": "planes/s", "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": "oracle restatement of the reference's GeneratePSF (scipy quad_vec, numpy "
+                                       "FFTs) on 3 of the 11 planes (z = %g, %g, %g um: the two largest and the "
+                                       "smallest), %.1f s" % (z0, (z0 + z1) / 2, z1, cpu_s)},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -574,6 +641,8 @@ def main():
         run_timeseries(args)
     elif args.workload == "rectify":
         run_rectify(args)
+    elif args.workload == "psf":
+        run_psf(args)
     else:
         run_gb300(args, rank, world, local)
 

@@ -25,6 +25,7 @@ _ERRNAMES = {-1: "FLF_E_ARG", -2: "FLF_E_CUDA", -3: "FLF_E_NOMEM", -4: "FLF_E_ST
 # name -> (restype, argtypes); mirrors include/flf.h
 _P = ctypes.c_void_p
 _I = ctypes.c_int
+_D = ctypes.c_double
 _SIGS = {
     "flf_ctx_create": (_I, [ctypes.POINTER(_P), _I, _I, _I]),
     "flf_ctx_destroy": (_I, [_P]),
@@ -50,6 +51,10 @@ _SIGS = {
     "flf_graph_kernels": (_I, [_P]),
     "flf_graph_destroy": (_I, [_P]),
     "flf_set_tuned": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_int)]),
+    "flf_psf_debye": (_I, [_P, _I, ctypes.c_longlong, _D, _D, _D, _D, _P, _P, _I, _D, _D, _P]),
+    "flf_psf_lf_input": (_I, [_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_psf_lf_bin": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 TUNED_KEYS = ("stages", "chunk_rows_forward", "chunk_rows_backward", "split")
@@ -117,6 +122,38 @@ def resample_bilinear(img, yq, xq, out, stream=None):
         buf = ctypes.create_string_buffer(1024)
         lib.flf_last_error(None, buf, 1024)
         raise FlfError(rc, buf.value.decode(errors="replace"))
+
+
+def _check_global(rc):
+    if rc != FLF_OK:
+        buf = ctypes.create_string_buffer(1024)
+        _lib.flf_last_error(None, buf, 1024)
+        raise FlfError(rc, buf.value.decode(errors="replace"))
+
+
+def psf_debye(out, mode, npoints, dx, M, k, sin_alpha, s, cw, koi, stream=None):
+    """flf_psf_debye on device tensors (out / cw complex128, s float64)."""
+    lib = load_library()
+    _check_global(lib.flf_psf_debye(_ptr(out), int(mode), int(npoints), float(dx), float(M), float(k),
+                                    float(sin_alpha), _ptr(s), _ptr(cw), int(s.shape[0]), float(koi.real),
+                                    float(koi.imag), _ptr(stream)))
+
+
+def psf_lf_input(out, wave, support, max_bug, lens, lens_h, L, nh, osr, q0, nq, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_psf_lf_input(_ptr(out), _ptr(wave), int(support), int(bool(max_bug)), _ptr(lens),
+                                       int(lens_h), int(L), int(nh), int(osr), int(q0), int(nq), _ptr(stream)))
+
+
+def psf_lf_bin(out, field, L, S, nh, osr, q0, nq, lo, hi, first, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_psf_lf_bin(_ptr(out), _ptr(field), int(L), int(S), int(nh), int(osr), int(q0), int(nq),
+                                     int(lo), int(hi), int(first), _ptr(stream)))
+
+
+def psf_ht(Ht, H, Z, nh, S, N, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_psf_ht(_ptr(Ht), _ptr(H), int(Z), int(nh), int(S), int(N), _ptr(stream)))
 
 
 class RLGraph:

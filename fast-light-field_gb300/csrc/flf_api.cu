@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -1474,9 +1475,67 @@ int flf_resample_bilinear(const float *img_dev, int H, int W, const double *yq_d
   return FLF_OK;
 }
 
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+int flf_psf_debye(double *out_dev, int mode, long long npoints, double dx, double M, double k, double sin_alpha,
+                  const double *s_dev, const double *cw_dev, int nodes, double koi_re, double koi_im,
+                  void *stream) {
+  if (!out_dev || !s_dev || !cw_dev) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if ((mode != 0 && mode != 1) || npoints < 0 || nodes <= 0 || !(M > 0) || !(sin_alpha > 0))
+    return fail(nullptr, FLF_E_ARG, "invalid Debye arguments (mode %d, points %lld, nodes %d)", mode, npoints,
+                nodes);
+  if (!aligned16(out_dev) || !aligned16(cw_dev))
+    return fail(nullptr, FLF_E_ARG, "complex arrays must be 16-byte aligned");
+  PsfDebyeParams p{(double2 *)out_dev, mode, npoints, dx, M, k, sin_alpha, s_dev, (const double2 *)cw_dev,
+                   nodes, koi_re, koi_im};
+  const cudaError_t e = launch_psf_debye(p, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "Debye launch failed: %s", cudaGetErrorString(e));
+  return FLF_OK;
+}
+
+int flf_psf_lf_input(double *out_dev, const double *wave_dev, int support, int max_bug, const double *lens_dev,
+                     int lens_h, int L, int nh, int osr, int q0, int nq, void *stream) {
+  if (!out_dev || !wave_dev || !lens_dev) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (L <= 0 || (L % 2) == 0 || support < 0 || support > (L - 1) / 2 || lens_h < 0 || nh <= 0 || osr <= 0 ||
+      q0 < 0 || nq < 0 || q0 + nq > nh * nh || nq > 65535)
+    return fail(nullptr, FLF_E_ARG, "invalid light-field input arguments (L %d, support %d, offsets %d+%d)", L,
+                support, q0, nq);
+  if (!aligned16(out_dev) || !aligned16(wave_dev) || !aligned16(lens_dev))
+    return fail(nullptr, FLF_E_ARG, "complex arrays must be 16-byte aligned");
+  PsfInputParams p{(double2 *)out_dev, (const double2 *)wave_dev, support, max_bug ? 1 : 0,
+                   (const double2 *)lens_dev, lens_h, L, nh, osr, q0, nq};
+  const cudaError_t e = launch_psf_lf_input(p, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "light-field input launch failed: %s", cudaGetErrorString(e));
+  return FLF_OK;
+}
+
+int flf_psf_lf_bin(float *out_dev, const double *field_dev, int L, int S, int nh, int osr, int q0, int nq, int lo,
+                   int hi, int first, void *stream) {
+  if (!out_dev || !field_dev) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (L <= 0 || S <= 0 || nh <= 0 || osr <= 0 || q0 < 0 || nq < 0 || q0 + nq > nh * nh || nq > 65535 ||
+      first < 0 || first + S * osr > L)
+    return fail(nullptr, FLF_E_ARG, "invalid binning arguments (L %d, S %d, OSR %d, first %d)", L, S, osr, first);
+  if (!aligned16(field_dev)) return fail(nullptr, FLF_E_ARG, "complex arrays must be 16-byte aligned");
+  PsfBinParams p{out_dev, (const double2 *)field_dev, L, S, nh, osr, q0, nq, lo, hi, first};
+  const cudaError_t e = launch_psf_lf_bin(p, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "binning launch failed: %s", cudaGetErrorString(e));
+  return FLF_OK;
+}
+
+int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, void *stream) {
+  if (!Ht_dev || !H_dev) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (Z <= 0 || N <= 0 || (N % 2) == 0 || nh != (N + 1) / 2 || S <= 0 || (S % 2) == 0 || ((S / 2) % N) != 0 ||
+      (long long)Z * nh * nh > 65535)
+    return fail(nullptr, FLF_E_ARG, "invalid Ht arguments (Z %d, N %d, S %d)", Z, N, S);
+  PsfHtParams p{Ht_dev, H_dev, Z, nh, S, N};
+  const cudaError_t e = launch_psf_ht(p, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "Ht launch failed: %s", cudaGetErrorString(e));
+  return FLF_OK;
+}
+
 int flf_version(char *buf, size_t len) {
   if (!buf || len == 0) return FLF_E_ARG;
-  snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear");
+  snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear k_psf_debye k_psf_lf_input k_psf_lf_bin k_psf_ht");
   return FLF_OK;
 }
 

@@ -215,6 +215,39 @@ cudaError_t launch_rfft2(const Rfft2Params &p, int fp64, cudaStream_t s);
 cudaError_t launch_irfft2(const Irfft2Params &p, cudaStream_t s);
 cudaError_t launch_split(const SplitParams &p, cudaStream_t s);
 cudaError_t launch_resample_bilinear(const ResampleParams &p, cudaStream_t s);
+
+// PSF generation (flf_psf.cu)
+struct PsfDebyeParams {      // Koi * sum_q cw[q] J0(s[q] vFactor) per point
+  double2 *out;
+  int mode;                  // 0: octant points m2 <= m1 (npoints = (n+1)(n+2)/2); 1: line m1 = t, m2 = 0
+  long long npoints;
+  double dx, M, k, sin_alpha;
+  const double *s;           // sin(theta) at the nodes
+  const double2 *cw;         // node weight x smooth integrand x depth phase
+  int nodes;
+  double koi_re, koi_im;
+};
+struct PsfInputParams {      // shifted field x microlens array for nq lenslet offsets
+  double2 *out;              // [nq][L][L]
+  const double2 *wave;       // octant values, (support+1)(support+2)/2
+  int support, max_bug;
+  const double2 *lens;       // [2h+1][2h+1]
+  int lens_h, L, nh, osr, q0, nq;
+};
+struct PsfBinParams {        // |f|^2 binned onto the lenslet-grid crop
+  float *out;                // [nq][S][S]
+  const double2 *field;      // [nq][L][L]
+  int L, S, nh, osr, q0, nq, lo, hi, first;
+};
+struct PsfHtParams {         // Ht gathered from H, both [Z][nh][nh][S][S]
+  float *Ht;
+  const float *H;
+  int Z, nh, S, N;
+};
+cudaError_t launch_psf_debye(const PsfDebyeParams &p, cudaStream_t s);
+cudaError_t launch_psf_lf_input(const PsfInputParams &p, cudaStream_t s);
+cudaError_t launch_psf_lf_bin(const PsfBinParams &p, cudaStream_t s);
+cudaError_t launch_psf_ht(const PsfHtParams &p, cudaStream_t s);
 cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);

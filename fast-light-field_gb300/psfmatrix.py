@@ -129,7 +129,7 @@ def LoadRawMatrixData(matPath, expectedNnum=None, createPSF=True):
     except ImportError as e:
         raise ImportError("reading PSF .mat files needs h5py, which is not installed") from e
     if not os.path.exists(matPath):
-        raise FileNotFoundError("%s does not exist; PSF generation is not part of this package" % matPath)
+        raise FileNotFoundError("%s does not exist (LoadMatrix(..., createPSF=True) generates it)" % matPath)
     mmapPath, hPathFormat, htPathFormat = GetPathFormats(matPath)
     os.makedirs(mmapPath, exist_ok=True)
     with h5py.File(matPath, "r") as f:
@@ -156,8 +156,14 @@ def LoadRawMatrixData(matPath, expectedNnum=None, createPSF=True):
 
 
 def LoadMatrix(matPath, numZ=None, zStart=0, forceRegeneration=False, cacheH=False, createPSF=False):
-    """HMatrix for a .mat file, using its memmap folder when present (psfmatrix.py:169-188)."""
+    """HMatrix for a .mat file, using its memmap folder when present (psfmatrix.py:169-188).
+
+    With ``createPSF`` a matrix that exists neither as .mat nor as memmap folder is
+    generated on the GPU from the parameters in its file name (generate_psf.py)."""
     mmapPath, hPathFormat, htPathFormat = GetPathFormats(matPath)
+    if createPSF:
+        import generate_psf
+        generate_psf.EnsureMatrixFileExists(matPath)
     try:
         if forceRegeneration:
             raise FileNotFoundError("forced regeneration")

@@ -177,6 +177,39 @@ int flf_synchronize(flf_ctx *ctx, void *stream);
  * arch, kernel list) into buf. */
 int flf_version(char *buf, size_t len);
 
+/* PSF generation (the reference's generate_psf.py GeneratePSF, :63-737), as
+ * four kernels a host driver chains with FFTs.  All arrays are device
+ * pointers; complex arrays are interleaved (re, im) doubles, 16-byte aligned.
+ *
+ * flf_psf_debye: Debye integral of the objective's field (generate_psf.py:
+ *   96-144, 263-315) at image-side points, out[t] = Koi * sum_q cw[q] *
+ *   J0(s[q] * vFactor(t)), vFactor = k r sin(alpha) / sin(alpha), r =
+ *   sqrt(x1^2 + x2^2) / M, x = dx * offset.  mode 0: the octant of offsets
+ *   (m1, m2), 0 <= m2 <= m1, t = m1 (m1 + 1) / 2 + m2 (npoints = (n+1)(n+2)/2
+ *   for offsets up to n); mode 1: the line (t, 0).  s / cw: nodes of a
+ *   quadrature over theta in [0, alpha] (sin theta; weight x smooth
+ *   integrand x depth phase).  out: npoints complex.
+ * flf_psf_lf_input: for lenslet offsets q = q0 .. q0+nq-1 (a = q / nh,
+ *   b = q % nh), out[q-q0][i][j] = wave(i - sx, j - sy) * lens(nearest lens
+ *   centre), sx = osr (a + 1 - nh); wave from the octant array of flf_psf_debye
+ *   (mode 0, up to `support`), zero outside; max_bug applies the reference's
+ *   z = 0 maximum over rotations (generate_psf.py:338-341).  lens: the
+ *   (2 lens_h + 1)^2 phase of one microlens.  out: nq L L complex (L odd).
+ * flf_psf_lf_bin: after the Fresnel propagation of those fields, out[q-q0][I][J]
+ *   = sum over an osr x osr block at (first + I osr, first + J osr) of
+ *   |field[i + sx][j + sy]|^2 inside the aperture window [lo, hi]^2
+ *   (generate_psf.py:529-546, pixelBinning :479-513).  out: nq S S floats.
+ * flf_psf_ht: Ht from H (generate_psf.py:624-690), both [Z][nh][nh][S][S]
+ *   floats, nh = (N+1)/2, S odd with (S/2) % N == 0. */
+int flf_psf_debye(double *out_dev, int mode, long long npoints, double dx, double M, double k, double sin_alpha,
+                  const double *s_dev, const double *cw_dev, int nodes, double koi_re, double koi_im,
+                  void *stream);
+int flf_psf_lf_input(double *out_dev, const double *wave_dev, int support, int max_bug, const double *lens_dev,
+                     int lens_h, int L, int nh, int osr, int q0, int nq, void *stream);
+int flf_psf_lf_bin(float *out_dev, const double *field_dev, int L, int S, int nh, int osr, int q0, int nq, int lo,
+                   int hi, int first, void *stream);
+int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, void *stream);
+
 /* CUDA graph of a whole RL run (the replay form of flf_rl_iterate): the
  * launches of `iters` iterations over T frames of Y x X images are captured
  * once, with these pointers baked in, and each flf_graph_launch replays them
