@@ -49,6 +49,11 @@ WORKLOADS = {
     "psf": dict(Nnum=15, z=(-25, 25, 5), optics=dict(M=40, NA=0.95, MLPitch=150e-6, OSR=3, n=1.33, fml=3000e-6,
                                                      lam=520e-9),
                 label="PSF generation, Nnum 15, M40 NA 0.95, OSR 3, 11 planes -25..25 um"),
+    # learned warm start (450 x 450 px, Nnum 15, 21 planes at -50..50 um, PSF generated on the GPU for
+    # the M40 / NA 0.95 optics); 200 beads per volume, background 100, Poisson noise
+    "warmstart": dict(Nnum=15, lenslets=30, z=(-50, 50, 5), beads=200,
+                      optics=dict(M=40, NA=0.95, MLPitch=150e-6, OSR=3, n=1.33, fml=3000e-6, lam=520e-9),
+                      label="learned warm start + RL vs plain RL(8 it), 450x450 px, Nnum 15, 21 planes -50..50 um"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
     # a time series of frames of three sizes (--frames per size), 500 drifting beads each
@@ -68,6 +73,7 @@ def parse():
     ap.add_argument("--iters", type=int, default=8)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--train-steps", type=int, default=800, help="warm-start network training steps")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-planes", type=int, default=5)
@@ -248,7 +254,7 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload in ("timeseries", "rectify", "psf"):
+    if args.workload in ("timeseries", "rectify", "psf", "warmstart"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
                           "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
@@ -632,6 +638,122 @@ def run_psf(args):
     print(json.dumps(line), flush=True)
 
 
+def run_warmstart(args):
+    """Volumes/s to the data-fit residual of 8 plain-RL iterations: plain RL from a
+    uniform volume against the learned warm start plus as many RL iterations as the
+    held-out volumes need (the largest over them)."""
+    import warnings
+    import torch
+    import build_lib
+    import generate_psf
+    import psfmatrix
+    import projector
+    import warmstart
+    build_lib.build()
+    warnings.simplefilter("ignore")
+    wl = WORKLOADS["warmstart"]
+    z0, z1, dz = wl["z"]
+    t0 = time.time()
+    r = generate_psf.GeneratePSFArrays(Nnum=wl["Nnum"], zmin=z0 * 1e-6, zmax=z1 * 1e-6, zspacing=dz * 1e-6,
+                                       **wl["optics"])
+    hm = psfmatrix.HMatrixArrays(r["H"], r["Ht"], name="bench-warmstart")
+    psf_s = time.time() - t0
+    Y = X = wl["lenslets"] * wl["Nnum"]
+    Z = hm.numZ
+    p = projector.Projector_gb300()
+    ws = warmstart.WarmStart(p, hm, Y, X, beads=wl["beads"])
+    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=32, log_every=100)
+    dev = ws.dev
+    s = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(2024)
+    nseed = 16
+    _, imgs, htfs = ws.make_batch(nseed, rng)
+    ctx = ws.ctx
+
+    def resid(x, img):
+        T = img.shape[0]
+        hx = torch.empty_like(img)
+        ctx.forward(x, hx, T, Y, X, None, stream=s.cuda_stream)
+        d = (img.double() - hx.double()).reshape(T, -1)
+        return (d.norm(dim=1) / img.double().reshape(T, -1).norm(dim=1)).cpu().numpy()
+
+    xu = torch.ones_like(htfs)
+    p.RichardsonLucy(hm, xu, htfs, 8)
+    r_plain = resid(xu, imgs)
+    x = ws.initial_volume(htfs)
+    need = np.full(nseed, -1)
+    curve = []
+    for k in range(0, 9):
+        if k > 0:
+            p.RichardsonLucy(hm, x, htfs, 1)
+        rk = resid(x, imgs)
+        curve.append(float(rk.mean()))
+        need[(need < 0) & (rk <= r_plain)] = k
+    if (need < 0).any():
+        k_warm = None
+    else:
+        k_warm = int(need.max())
+    img1 = imgs[:1].contiguous()
+    htf1 = torch.empty((Z, 1, Y, X), device=dev)
+    xp = torch.empty((Z, 1, Y, X), device=dev)
+
+    def plain_step():
+        ctx.backward(img1, htf1, 1, Y, X, None, stream=s.cuda_stream)
+        xp.fill_(1.0)
+        p.RichardsonLucy(hm, xp, htf1, 8)
+
+    def warm_step():
+        ctx.backward(img1, htf1, 1, Y, X, None, stream=s.cuda_stream)
+        xw = ws.initial_volume(htf1)
+        if k_warm:
+            p.RichardsonLucy(hm, xw, htf1, k_warm)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms_plain = timed(plain_step)
+    ms_warm = timed(warm_step) if k_warm is not None else None
+    clk = clocks.stop()
+    net_ms = timed(lambda: ws.initial_volume(htf1))
+    img_h = img1.cpu().numpy()
+    warmstart.DeconvRLWarm(ws, img_h, k_warm or 0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ne = 5
+    for _ in range(ne):
+        out = warmstart.DeconvRLWarm(ws, img_h, k_warm or 0).cpu().numpy()
+    e2e_s = (time.perf_counter() - t0) / ne
+    line = {"metric": "volumes/s to plain-RL(8 it) accuracy: learned warm-start vs plain RL, 1 GB300",
+            "value": 1000.0 / ms_warm if ms_warm else None, "unit": "volumes/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_warm, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 network (fp32 accumulation), f32 projections", "data": "synthetic",
+            "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": wl["Nnum"], "frames": 1,
+                       "psf": "generated on the GPU (generate_psf.py), sizes %s" % [int(h.shape[-1]) for h in r["H"]],
+                       "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
+                       "network_parameters": ws.net.num_parameters(), "held_out_volumes": nseed,
+                       "l2": "transfer matrices and volumes larger than L2"},
+            "plain_rl": {"volumes_per_s": 1000.0 / ms_plain, "ms_per_volume": ms_plain, "iterations": 8,
+                         "residual_rel_l2_mean": float(r_plain.mean())},
+            "warm_start": {"rl_iterations_needed": k_warm, "network_ms": net_ms,
+                           "residual_after_k_mean": [round(v, 5) for v in curve],
+                           "speedup_vs_plain": (ms_plain / ms_warm) if ms_warm else None},
+            "e2e": {"value": 1.0 / e2e_s, "unit": "volumes/s", "h2d_bytes_per_step": int(img_h.nbytes),
+                    "d2h_bytes_per_step": int(out.nbytes)},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -643,6 +765,8 @@ def main():
         run_rectify(args)
     elif args.workload == "psf":
         run_psf(args)
+    elif args.workload == "warmstart":
+        run_warmstart(args)
     else:
         run_gb300(args, rank, world, local)
 

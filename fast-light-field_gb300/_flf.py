@@ -26,6 +26,7 @@ _ERRNAMES = {-1: "FLF_E_ARG", -2: "FLF_E_CUDA", -3: "FLF_E_NOMEM", -4: "FLF_E_ST
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
+_F = ctypes.c_float
 _SIGS = {
     "flf_ctx_create": (_I, [ctypes.POINTER(_P), _I, _I, _I]),
     "flf_ctx_destroy": (_I, [_P]),
@@ -55,6 +56,17 @@ _SIGS = {
     "flf_psf_lf_input": (_I, [_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_lf_bin": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
+    "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
+    "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P]),
+    "flf_pool2": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_pool2_bwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_up2_add": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_up2_bwd": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_mse_grad": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _I, _P]),
+    "flf_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, _F, _F, _F, _F, _F, _F, _F, _P]),
+    "flf_render_blobs": (_I, [_P, _I, _I, _I, _P, _I, _F, _P]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 TUNED_KEYS = ("stages", "chunk_rows_forward", "chunk_rows_backward", "split")
@@ -156,6 +168,81 @@ def psf_ht(Ht, H, Z, nh, S, N, stream=None):
     _check_global(lib.flf_psf_ht(_ptr(Ht), _ptr(H), int(Z), int(nh), int(S), int(N), _ptr(stream)))
 
 
+def _vshape(t):
+    """(B, Z, Y, X, C) of a channels-last volume tensor."""
+    B, Z, Y, X, C = (int(v) for v in t.shape)
+    return B, Z, Y, X, C
+
+
+def conv3d(x, w, bias, y, relu=False, mask=None, stream=None):
+    """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16."""
+    lib = load_library()
+    B, Z, Y, X, Ci = _vshape(x)
+    Co = int(y.shape[-1])
+    _check_global(lib.flf_conv3d(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X, Ci, Co,
+                                 int(bool(relu)), _ptr(stream)))
+
+
+def conv3d_wgrad(x, dy, dw, stream=None):
+    """dw [27,Ci,Co] float32 += weight gradient of conv3d(x, .) for output gradient dy."""
+    lib = load_library()
+    B, Z, Y, X, Ci = _vshape(x)
+    _check_global(lib.flf_conv3d_wgrad(_ptr(x), _ptr(dy), _ptr(dw), B, Z, Y, X, Ci, int(dy.shape[-1]),
+                                       _ptr(stream)))
+
+
+def conv3d_flip(w, w2, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_conv3d_flip(_ptr(w), _ptr(w2), int(w.shape[1]), int(w.shape[2]), _ptr(stream)))
+
+
+def bias_grad(g, db, stream=None):
+    lib = load_library()
+    C = int(g.shape[-1])
+    _check_global(lib.flf_bias_grad(_ptr(g), _ptr(db), int(g.numel() // C), C, _ptr(stream)))
+
+
+def pool2(x, out, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_pool2(_ptr(x), _ptr(out), *_vshape(x), _ptr(stream)))
+
+
+def pool2_bwd(gpool, gskip, act, gin, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_pool2_bwd(_ptr(gpool), _ptr(gskip), _ptr(act), _ptr(gin), *_vshape(gin), _ptr(stream)))
+
+
+def up2_add(low, skip, out, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_up2_add(_ptr(low), _ptr(skip), _ptr(out), *_vshape(out), _ptr(stream)))
+
+
+def up2_bwd(g, act, glow, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_up2_bwd(_ptr(g), _ptr(act), _ptr(glow), *_vshape(g), _ptr(stream)))
+
+
+def mse_grad(y, target, g, loss, stream=None):
+    lib = load_library()
+    C = int(y.shape[-1])
+    _check_global(lib.flf_mse_grad(_ptr(y), _ptr(target), _ptr(g), _ptr(loss), int(y.numel() // C), C,
+                                   _ptr(stream)))
+
+
+def adam(w, g, m, v, wb, lr, b1, b2, eps, c1, c2, wd, stream=None):
+    lib = load_library()
+    _check_global(lib.flf_adam(_ptr(w), _ptr(g), _ptr(m), _ptr(v), _ptr(wb), int(w.numel()), lr, b1, b2, eps, c1,
+                               c2, wd, _ptr(stream)))
+
+
+def render_blobs(vol, pts, sigma, stream=None):
+    """vol [Z,Y,X] float32 += Gaussian blobs at pts [n,4] = (z, y, x, amplitude)."""
+    lib = load_library()
+    Z, Y, X = (int(v) for v in vol.shape)
+    _check_global(lib.flf_render_blobs(_ptr(vol), Z, Y, X, _ptr(pts), int(pts.shape[0]), float(sigma),
+                                       _ptr(stream)))
+
+
 class RLGraph:
     """A captured RL run; launch() replays it on a stream.  Keeps its tensors alive."""
 
@@ -200,6 +287,8 @@ class Context:
 
     def _check(self, rc):
         if rc != FLF_OK:
+            if not (self._h and self._h.value):
+                raise FlfError(rc, "the context was closed")
             raise FlfError(rc, self._msg(self._h))
 
     def close(self):

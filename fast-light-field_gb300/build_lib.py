@@ -17,7 +17,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libflf.so")
 OBJDIR = os.path.join(HERE, "_build")
 SOURCES = ["flf_kernels.cu", "flf_api.cu", "flf_fft_part0.cu", "flf_fft_part1.cu", "flf_fft_part2.cu",
-           "flf_fft_part3.cu", "flf_psf.cu"]
+           "flf_fft_part3.cu", "flf_psf.cu", "flf_net.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

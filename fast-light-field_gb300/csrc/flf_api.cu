@@ -1533,9 +1533,124 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
   return FLF_OK;
 }
 
+static int net_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 132;
+  }
+  return sms;
+}
+
+static int net_shape(int B, int Z, int Y, int X, int C) {
+  if (B <= 0 || Z <= 0 || Y <= 0 || X <= 0 || C <= 0 || (C % 16) != 0)
+    return fail(nullptr, FLF_E_ARG, "invalid volume shape %d x %d x %d x %d x %d (channels a multiple of 16)", B, Z,
+                Y, X, C);
+  return FLF_OK;
+}
+
+#define NET_CHECK(call)                                                                          \
+  do {                                                                                           \
+    const cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(nullptr, FLF_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
+               int Ci, int Co, int relu, void *stream) {
+  if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
+  if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
+  if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
+    return fail(nullptr, FLF_E_ARG, "volumes and weights must be 16-byte aligned");
+  ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
+               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0};
+  NET_CHECK(launch_conv3d(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
+                     void *stream) {
+  if (!x || !dy || !dw) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
+  if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
+  if (!aligned16(x) || !aligned16(dy)) return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
+  WgradParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)dy, dw, B, Z, Y, X, Ci, Co, 0};
+  NET_CHECK(launch_conv3d_wgrad(p, (cudaStream_t)stream, net_sms()));
+  return FLF_OK;
+}
+
+int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream) {
+  if (!w || !w2 || Ci <= 0 || Co <= 0) return fail(nullptr, FLF_E_ARG, "invalid weight flip arguments");
+  NET_CHECK(launch_conv3d_flip(w, w2, Ci, Co, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream) {
+  if (!g || !db || M < 0 || C <= 0 || C > 128) return fail(nullptr, FLF_E_ARG, "invalid bias gradient arguments");
+  if (M > 0) NET_CHECK(launch_bias_grad(g, db, M, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+static int even_shape(int B, int Z, int Y, int X, int C) {
+  if (B <= 0 || Z <= 0 || Y <= 0 || X <= 0 || C <= 0 || (Z | Y | X) & 1)
+    return fail(nullptr, FLF_E_ARG, "pooling needs positive, even Z / Y / X (got %d x %d x %d)", Z, Y, X);
+  return FLF_OK;
+}
+
+int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream) {
+  if (!in || !out) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = even_shape(B, Z, Y, X, C)) return rc;
+  NET_CHECK(launch_pool2(in, out, B, Z, Y, X, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y, int X, int C,
+                  void *stream) {
+  if (!gpool || !gin) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = even_shape(B, Z, Y, X, C)) return rc;
+  NET_CHECK(launch_pool2_bwd(gpool, gskip, act, gin, B, Z, Y, X, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C, void *stream) {
+  if (!low || !out) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = even_shape(B, Z, Y, X, C)) return rc;
+  NET_CHECK(launch_up2_add(low, skip, out, B, Z, Y, X, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C, void *stream) {
+  if (!g || !glow) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = even_shape(B, Z, Y, X, C)) return rc;
+  NET_CHECK(launch_up2_bwd(g, act, glow, B, Z, Y, X, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C, void *stream) {
+  if (!y || !target || !g || !loss || M <= 0 || C <= 0) return fail(nullptr, FLF_E_ARG, "invalid loss arguments");
+  NET_CHECK(launch_mse_grad(y, target, g, loss, M, C, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1, float b2,
+             float eps, float c1, float c2, float wd, void *stream) {
+  if (!w || !g || !m || !v || n < 0) return fail(nullptr, FLF_E_ARG, "invalid Adam arguments");
+  if (n > 0) NET_CHECK(launch_adam(w, g, m, v, wb, n, lr, b1, b2, eps, c1, c2, wd, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *stream) {
+  if (!vol || (!pts && npts > 0) || Z <= 0 || Y <= 0 || X <= 0 || npts < 0 || !(sigma > 0) || sigma > 8)
+    return fail(nullptr, FLF_E_ARG, "invalid blob rendering arguments");
+  if (!aligned16(pts)) return fail(nullptr, FLF_E_ARG, "blob array must be 16-byte aligned");
+  NET_CHECK(launch_render_blobs(vol, Z, Y, X, pts, npts, sigma, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
 int flf_version(char *buf, size_t len) {
   if (!buf || len == 0) return FLF_E_ARG;
-  snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear k_psf_debye k_psf_lf_input k_psf_lf_bin k_psf_ht");
+  snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear k_psf_debye k_psf_lf_input k_psf_lf_bin k_psf_ht k_conv3d k_conv3d_wgrad");
   return FLF_OK;
 }
 

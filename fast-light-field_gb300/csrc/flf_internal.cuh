@@ -20,6 +20,7 @@
 //    half of the rows; see the packed layout below.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -248,6 +249,40 @@ cudaError_t launch_psf_debye(const PsfDebyeParams &p, cudaStream_t s);
 cudaError_t launch_psf_lf_input(const PsfInputParams &p, cudaStream_t s);
 cudaError_t launch_psf_lf_bin(const PsfBinParams &p, cudaStream_t s);
 cudaError_t launch_psf_ht(const PsfHtParams &p, cudaStream_t s);
+
+// Learned warm start (flf_net.cu): channels-last BF16 volumes [B][Z][Y][X][C]
+struct ConvParams {          // y = act(conv3x3x3(x, w) + bias) (* (mask > 0))
+  const __nv_bfloat16 *x;    // [M][Ci]
+  const __nv_bfloat16 *w;    // [27][Ci][Co], tap = (dz+1)*9 + (dy+1)*3 + (dx+1)
+  const float *bias;         // [Co] or null
+  const __nv_bfloat16 *mask; // [M][Co] or null
+  __nv_bfloat16 *y;          // [M][Co]
+  int B, Z, Y, X, Ci, Co, relu;
+};
+struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co]
+  const __nv_bfloat16 *x;
+  const __nv_bfloat16 *dy;
+  float *dw;
+  int B, Z, Y, X, Ci, Co;
+  long long chunk;           // voxels per CTA (set by the launcher)
+};
+cudaError_t launch_conv3d(const ConvParams &p, cudaStream_t s);
+cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms);
+cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s);
+cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s);
+cudaError_t launch_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, cudaStream_t s);
+cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y,
+                             int X, int C, cudaStream_t s);
+cudaError_t launch_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C,
+                           cudaStream_t s);
+cudaError_t launch_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C,
+                           cudaStream_t s);
+cudaError_t launch_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C,
+                            cudaStream_t s);
+cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
+                        float b2, float eps, float c1, float c2, float wd, cudaStream_t s);
+cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,
+                                cudaStream_t s);
 cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);

@@ -1,0 +1,516 @@
+// Kernels of the learned warm start: a 3-D U-Net on channels-last BF16
+// volumes [B][Z][Y][X][C] with FP32 accumulation.
+//
+//   k_conv3d<BN>      3x3x3 'same' convolution as an implicit GEMM
+//                     (M = voxels, N = output channels, K = 27 taps x input
+//                     channels) on the BF16 tensor cores (mma.sync m16n8k16),
+//                     4-stage cp.async ring, swizzled shared tiles read with
+//                     ldmatrix; epilogue: bias, ReLU, gradient mask, BF16.
+//                     The data gradient is the same kernel on the flipped,
+//                     transposed weights (k_conv3d_flip_weights).
+//   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
+//                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
+//                     split-K over its 4 warps, FP32 atomics into dW.
+//   small kernels     bias gradient, 2x2x2 average pooling and its adjoint,
+//                     nearest 2x2x2 upsampling + skip and its adjoint with the
+//                     ReLU mask, MSE loss gradient, Adam, bead rendering.
+#include "flf_internal.cuh"
+
+#include <cuda_bf16.h>
+
+namespace flf {
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void *src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void ldsm4(uint32_t a, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a));
+}
+__device__ __forceinline__ void ldsm4t(uint32_t a, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// XOR swizzle of 16-byte chunks in rows of R chunks: the 8 consecutive rows an
+// ldmatrix reads at one logical chunk land in 8 distinct 4-bank groups.
+template <int R>
+__device__ __forceinline__ int swz(int row) {
+  return R == 8 ? (row & 7) : R == 4 ? ((row >> 1) & 3) : ((row >> 2) & 1);
+}
+
+struct Vox {
+  int b, z, y, x;
+};
+__device__ __forceinline__ Vox decode(long long m, int Z, int Y, int X) {
+  Vox v;
+  v.x = (int)(m % X);
+  m /= X;
+  v.y = (int)(m % Y);
+  m /= Y;
+  v.z = (int)(m % Z);
+  v.b = (int)(m / Z);
+  return v;
+}
+
+}  // namespace
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
+  constexpr int BM = 128, NS = 4, RB = BN / 8;
+  __shared__ __align__(128) bf16 As[NS][BM * 16];
+  __shared__ __align__(128) bf16 Bs[NS][16 * BN];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  const long long m0 = (long long)blockIdx.x * BM;
+  const int n0 = blockIdx.y * BN;
+  const long long mrow = m0 + tid;
+  const bool rowok = mrow < M;
+  const Vox v = decode(rowok ? mrow : 0, p.Z, p.Y, p.X);
+  const int cch = p.Ci / 16;
+  const int KS = 27 * cch;
+
+  auto load = [&](int ks, int st) {
+    const int tap = ks / cch, c0 = (ks - tap * cch) * 16;
+    const int z = v.z + tap / 9 - 1, y = v.y + (tap / 3) % 3 - 1, x = v.x + tap % 3 - 1;
+    const bool ok = rowok && z >= 0 && z < p.Z && y >= 0 && y < p.Y && x >= 0 && x < p.X;
+    const bf16 *src = ok ? p.x + ((((long long)v.b * p.Z + z) * p.Y + y) * p.X + x) * p.Ci + c0 : p.x;
+    const uint32_t base = su32(&As[st][tid * 16]);
+    const int s = swz<2>(tid);
+    cp16(base + ((0 ^ s) << 4), src, ok);
+    cp16(base + ((1 ^ s) << 4), ok ? src + 8 : p.x, ok);
+    if (tid < 16 * RB) {
+      const int k = tid / RB, c = tid - k * RB;
+      const bf16 *wsrc = p.w + ((long long)tap * p.Ci + c0 + k) * p.Co + n0 + c * 8;
+      cp16(su32(&Bs[st][k * BN]) + ((c ^ swz<RB>(k)) << 4), wsrc, true);
+    }
+  };
+
+  float acc[2][BN / 8][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < BN / 8; j++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+
+#pragma unroll
+  for (int s = 0; s < NS - 1; s++) {
+    if (s < KS) load(s, s);
+    cp_commit();
+  }
+  const int mat = lane >> 3, r8 = lane & 7;
+  for (int ks = 0; ks < KS; ks++) {
+    cp_wait<NS - 2>();
+    __syncthreads();
+    const int st = ks % NS;
+    uint32_t a[2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++) {
+      const int row = warp * 32 + mt * 16 + r8 + 8 * (mat & 1);
+      const int chunk = mat >> 1;
+      ldsm4(su32(&As[st][row * 16]) + ((chunk ^ swz<2>(row)) << 4), a[mt][0], a[mt][1], a[mt][2], a[mt][3]);
+    }
+#pragma unroll
+    for (int n2 = 0; n2 < BN / 16; n2++) {
+      const int k = r8 + 8 * (mat & 1);
+      const int c = n2 * 2 + (mat >> 1);
+      uint32_t b0, b1, b2, b3;
+      ldsm4t(su32(&Bs[st][k * BN]) + ((c ^ swz<RB>(k)) << 4), b0, b1, b2, b3);
+#pragma unroll
+      for (int mt = 0; mt < 2; mt++) {
+        mma_bf16(acc[mt][2 * n2], a[mt], b0, b1);
+        mma_bf16(acc[mt][2 * n2 + 1], a[mt], b2, b3);
+      }
+    }
+    const int nk = ks + NS - 1;
+    if (nk < KS) load(nk, nk % NS);
+    cp_commit();
+  }
+  cp_wait<0>();
+
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int nt = 0; nt < BN / 8; nt++) {
+      const int col = n0 + nt * 8 + 2 * (lane & 3);
+      const float b0 = p.bias ? p.bias[col] : 0.f, b1 = p.bias ? p.bias[col + 1] : 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const long long row = m0 + warp * 32 + mt * 16 + (lane >> 2) + 8 * h;
+        if (row >= M) continue;
+        float v0 = acc[mt][nt][2 * h] + b0, v1 = acc[mt][nt][2 * h + 1] + b1;
+        if (p.relu) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        const long long o = row * p.Co + col;
+        if (p.mask) {
+          const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(p.mask + o);
+          if (!(__bfloat162float(mk.x) > 0.f)) v0 = 0.f;
+          if (!(__bfloat162float(mk.y) > 0.f)) v1 = 0.f;
+        }
+        *reinterpret_cast<__nv_bfloat162 *>(p.y + o) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+}
+
+// Weight gradient.  CTA = (voxel chunk, tap) x (ci tile CM, co tile CN); the 4
+// warps take alternate k16 steps of its voxels (split-K) and are summed in
+// shared memory at the end, then added to dW with FP32 atomics.
+template <int CM, int CN>
+__global__ void __launch_bounds__(128) k_conv3d_wgrad(WgradParams p) {
+  constexpr int BK = 64, NS = 3, RA = CM / 8, RBc = CN / 8;
+  __shared__ __align__(128) bf16 Xs[NS][BK * CM];
+  __shared__ __align__(128) bf16 Ds[NS][BK * CN];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  const int tap = blockIdx.x % 27;
+  const long long chunk = blockIdx.x / 27;
+  const int ctiles = p.Co / CN;
+  const int ci0 = (blockIdx.y / ctiles) * CM, co0 = (blockIdx.y % ctiles) * CN;
+  const long long v0 = chunk * p.chunk;
+  const long long v1 = v0 + p.chunk < M ? v0 + p.chunk : M;
+  const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  const int KS = (int)((v1 - v0 + BK - 1) / BK);
+
+  auto load = [&](int ks, int st) {
+    for (int i = tid; i < BK * (RA + RBc); i += 128) {
+      const int row = i / (RA + RBc), c = i - row * (RA + RBc);
+      const long long vv = v0 + (long long)ks * BK + row;
+      const bool in = vv < v1;
+      if (c < RA) {
+        bool ok = false;
+        const bf16 *src = p.x;
+        if (in) {
+          const Vox q = decode(vv, p.Z, p.Y, p.X);
+          const int z = q.z + dz, y = q.y + dy, x = q.x + dx;
+          ok = z >= 0 && z < p.Z && y >= 0 && y < p.Y && x >= 0 && x < p.X;
+          if (ok) src = p.x + ((((long long)q.b * p.Z + z) * p.Y + y) * p.X + x) * p.Ci + ci0 + c * 8;
+        }
+        cp16(su32(&Xs[st][row * CM]) + ((c ^ swz<RA>(row)) << 4), src, ok);
+      } else {
+        const int cc = c - RA;
+        const bf16 *src = in ? p.dy + vv * p.Co + co0 + cc * 8 : p.dy;
+        cp16(su32(&Ds[st][row * CN]) + ((cc ^ swz<RBc>(row)) << 4), src, in);
+      }
+    }
+  };
+
+  float acc[CM / 16][CN / 8][4];
+#pragma unroll
+  for (int i = 0; i < CM / 16; i++)
+#pragma unroll
+    for (int j = 0; j < CN / 8; j++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+
+#pragma unroll
+  for (int s = 0; s < NS - 1; s++) {
+    if (s < KS) load(s, s);
+    cp_commit();
+  }
+  const int mat = lane >> 3, r8 = lane & 7;
+  for (int ks = 0; ks < KS; ks++) {
+    cp_wait<NS - 2>();
+    __syncthreads();
+    const int st = ks % NS;
+    const int kr = warp * 16;   // this warp's 16 voxels of the stage
+    uint32_t a[CM / 16][4];
+#pragma unroll
+    for (int mt = 0; mt < CM / 16; mt++) {
+      // A[ci][k] from Xs[k][ci]: transposed 8x8 blocks (k rows, ci chunk)
+      const int row = kr + r8 + 8 * (mat >> 1);
+      const int c = mt * 2 + (mat & 1);
+      ldsm4t(su32(&Xs[st][row * CM]) + ((c ^ swz<RA>(row)) << 4), a[mt][0], a[mt][1], a[mt][2], a[mt][3]);
+    }
+#pragma unroll
+    for (int n2 = 0; n2 < CN / 16; n2++) {
+      const int row = kr + r8 + 8 * (mat & 1);
+      const int c = n2 * 2 + (mat >> 1);
+      uint32_t b0, b1, b2, b3;
+      ldsm4t(su32(&Ds[st][row * CN]) + ((c ^ swz<RBc>(row)) << 4), b0, b1, b2, b3);
+#pragma unroll
+      for (int mt = 0; mt < CM / 16; mt++) {
+        mma_bf16(acc[mt][2 * n2], a[mt], b0, b1);
+        mma_bf16(acc[mt][2 * n2 + 1], a[mt], b2, b3);
+      }
+    }
+    const int nk = ks + NS - 1;
+    if (nk < KS) load(nk, nk % NS);
+    cp_commit();
+  }
+  cp_wait<0>();
+  __syncthreads();
+  // sum the 4 warps' partial tiles in shared memory (reuses the ring)
+  float *red = reinterpret_cast<float *>(&Xs[0][0]);
+  static_assert(sizeof(Xs) >= sizeof(float) * CM * CN, "reduction buffer");
+  for (int i = tid; i < CM * CN; i += 128) red[i] = 0.f;
+  __syncthreads();
+  for (int w = 0; w < 4; w++) {
+    if (warp == w) {
+#pragma unroll
+      for (int mt = 0; mt < CM / 16; mt++)
+#pragma unroll
+        for (int nt = 0; nt < CN / 8; nt++)
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int ci = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+            const int co = nt * 8 + 2 * (lane & 3) + (e & 1);
+            red[ci * CN + co] += acc[mt][nt][e];
+          }
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < CM * CN; i += 128) {
+    const int ci = i / CN, co = i - ci * CN;
+    atomicAdd(p.dw + ((long long)tap * p.Ci + ci0 + ci) * p.Co + co0 + co, red[i]);
+  }
+}
+
+// w2[26 - tap][co][ci] = w[tap][ci][co]: the data-gradient convolution's weights.
+__global__ void k_conv3d_flip_weights(const bf16 *w, bf16 *w2, int Ci, int Co) {
+  const long long n = 27LL * Ci * Co;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int co = (int)(i % Co);
+    const long long t = i / Co;
+    const int ci = (int)(t % Ci), tap = (int)(t / Ci);
+    w2[((long long)(26 - tap) * Co + co) * Ci + ci] = w[i];
+  }
+}
+
+// db[c] += sum over rows of g[M][C]
+__global__ void k_bias_grad(const bf16 *g, float *db, long long M, int C, long long rows_per_block) {
+  const int c = threadIdx.x;
+  if (c >= C) return;
+  const long long r0 = (long long)blockIdx.x * rows_per_block;
+  const long long r1 = r0 + rows_per_block < M ? r0 + rows_per_block : M;
+  float s = 0.f;
+  for (long long r = r0; r < r1; r++) s += __bfloat162float(g[r * C + c]);
+  atomicAdd(db + c, s);
+}
+
+// out[b][z][y][x][c] = mean of the 2x2x2 block of in (Z, Y, X even)
+__global__ void k_pool2(const bf16 *in, bf16 *out, int B, int Z, int Y, int X, int C) {
+  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2;
+  const long long n = (long long)B * Zo * Yo * Xo * C;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const Vox o = decode(i / C, Zo, Yo, Xo);
+    float s = 0.f;
+    for (int d = 0; d < 8; d++) {
+      const long long src = ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X +
+                             2 * o.x + (d & 1)) * C + c;
+      s += __bfloat162float(in[src]);
+    }
+    out[i] = __float2bfloat16_rn(0.125f * s);
+  }
+}
+
+// Adjoint of k_pool2 plus a second gradient, under a ReLU mask:
+// gin[v] = (gpool[v/2] / 8 + gskip[v]) * (act[v] > 0)   (gskip may be null)
+__global__ void k_pool2_bwd(const bf16 *gpool, const bf16 *gskip, const bf16 *act, bf16 *gin, int B, int Z, int Y,
+                            int X, int C) {
+  const long long n = (long long)B * Z * Y * X * C;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const Vox v = decode(i / C, Z, Y, X);
+    const long long o = ((((long long)v.b * (Z / 2) + v.z / 2) * (Y / 2) + v.y / 2) * (X / 2) + v.x / 2) * C + c;
+    float g = 0.125f * __bfloat162float(gpool[o]);
+    if (gskip) g += __bfloat162float(gskip[i]);
+    if (act && !(__bfloat162float(act[i]) > 0.f)) g = 0.f;
+    gin[i] = __float2bfloat16_rn(g);
+  }
+}
+
+// out[v] = low[v/2] + skip[v]  (nearest 2x2x2 upsampling; low has C channels)
+__global__ void k_up2_add(const bf16 *low, const bf16 *skip, bf16 *out, int B, int Z, int Y, int X, int C) {
+  const long long n = (long long)B * Z * Y * X * C;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const Vox v = decode(i / C, Z, Y, X);
+    const long long o = ((((long long)v.b * (Z / 2) + v.z / 2) * (Y / 2) + v.y / 2) * (X / 2) + v.x / 2) * C + c;
+    out[i] = __float2bfloat16_rn(__bfloat162float(low[o]) + (skip ? __bfloat162float(skip[i]) : 0.f));
+  }
+}
+
+// Adjoint of the upsampling: glow[u] = sum of g over its 2x2x2 block, times (act[u] > 0)
+__global__ void k_up2_bwd(const bf16 *g, const bf16 *act, bf16 *glow, int B, int Z, int Y, int X, int C) {
+  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2;
+  const long long n = (long long)B * Zo * Yo * Xo * C;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const Vox o = decode(i / C, Zo, Yo, Xo);
+    float s = 0.f;
+    for (int d = 0; d < 8; d++) {
+      const long long src = ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X +
+                             2 * o.x + (d & 1)) * C + c;
+      s += __bfloat162float(g[src]);
+    }
+    if (act && !(__bfloat162float(act[i]) > 0.f)) s = 0.f;
+    glow[i] = __float2bfloat16_rn(s);
+  }
+}
+
+// Prediction = channel 0 of y (C channels); loss terms and the gradient of
+// mean((pred - target)^2) into channel 0 of g (other channels 0).
+__global__ void k_mse_grad(const bf16 *y, const float *target, bf16 *g, float *loss, long long M, int C) {
+  float s = 0.f;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const float d = __bfloat162float(y[i * C]) - target[i];
+    s += d * d;
+    g[i * C] = __float2bfloat16_rn(2.f * d / (float)M);
+    for (int c = 1; c < C; c++) g[i * C + c] = __float2bfloat16_rn(0.f);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s / (float)M);
+}
+
+// Adam on FP32 master weights; writes the BF16 copy the kernels read.
+__global__ void k_adam(float *w, const float *g, float *m, float *v, bf16 *wb, long long n, float lr, float b1,
+                       float b2, float eps, float c1, float c2, float wd) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i] + wd * w[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+// Gaussian blobs: vol[z][y][x] += amp exp(-|p - c|^2 / (2 sigma^2)) within 3 sigma;
+// pts[k] = (z, y, x, amp), one warp per blob.
+__global__ void k_render_blobs(float *vol, int Z, int Y, int X, const float4 *pts, int npts, float sigma) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (k >= npts) return;
+  const float4 q = pts[k];
+  const int r = (int)ceilf(3.f * sigma);
+  const int w = 2 * r + 1;
+  const float inv = 1.f / (2.f * sigma * sigma);
+  for (int t = lane; t < w * w * w; t += 32) {
+    const int dz = t / (w * w) - r, dy = (t / w) % w - r, dx = t % w - r;
+    const int z = (int)floorf(q.x + 0.5f) + dz, y = (int)floorf(q.y + 0.5f) + dy, x = (int)floorf(q.z + 0.5f) + dx;
+    if (z < 0 || z >= Z || y < 0 || y >= Y || x < 0 || x >= X) continue;
+    const float d2 = (z - q.x) * (z - q.x) + (y - q.y) * (y - q.y) + (x - q.z) * (x - q.z);
+    atomicAdd(vol + ((long long)z * Y + y) * X + x, q.w * __expf(-d2 * inv));
+  }
+}
+
+static unsigned grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  return (unsigned)(g < 152LL * 32 ? (g < 1 ? 1 : g) : 152LL * 32);
+}
+
+cudaError_t launch_conv3d(const ConvParams &p, cudaStream_t s) {
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  if (M == 0) return cudaSuccess;
+  const int BN = p.Co >= 64 ? 64 : p.Co;
+  dim3 grid((unsigned)((M + 127) / 128), (unsigned)(p.Co / BN));
+  if (BN == 64) k_conv3d<64><<<grid, 128, 0, s>>>(p);
+  else if (BN == 32) k_conv3d<32><<<grid, 128, 0, s>>>(p);
+  else k_conv3d<16><<<grid, 128, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms) {
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  if (M == 0) return cudaSuccess;
+  const int CM = p.Ci >= 32 ? 32 : 16, CN = p.Co >= 64 ? 64 : p.Co;
+  const int tiles = (p.Ci / CM) * (p.Co / CN);
+  long long chunks = (4LL * num_sms + 27 * tiles - 1) / (27 * tiles);
+  if (chunks < 1) chunks = 1;
+  long long per = (M + chunks - 1) / chunks;
+  per = (per + 63) / 64 * 64;
+  chunks = (M + per - 1) / per;
+  p.chunk = per;
+  dim3 grid((unsigned)(chunks * 27), (unsigned)tiles);
+#define FLF_WG(a, b) else if (CM == a && CN == b) k_conv3d_wgrad<a, b><<<grid, 128, 0, s>>>(p);
+  if (false) {
+  }
+  FLF_WG(16, 16) FLF_WG(16, 32) FLF_WG(16, 64) FLF_WG(32, 16) FLF_WG(32, 32) FLF_WG(32, 64)
+#undef FLF_WG
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s) {
+  k_conv3d_flip_weights<<<grid_for(27LL * Ci * Co, 256), 256, 0, s>>>((const bf16 *)w, (bf16 *)w2, Ci, Co);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s) {
+  const long long rows = 2048;
+  k_bias_grad<<<(unsigned)((M + rows - 1) / rows), 128, 0, s>>>((const bf16 *)g, db, M, C, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, cudaStream_t s) {
+  k_pool2<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)in, (bf16 *)out, B, Z, Y, X, C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y,
+                             int X, int C, cudaStream_t s) {
+  k_pool2_bwd<<<grid_for((long long)B * Z * Y * X * C, 256), 256, 0, s>>>(
+      (const bf16 *)gpool, (const bf16 *)gskip, (const bf16 *)act, (bf16 *)gin, B, Z, Y, X, C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C,
+                           cudaStream_t s) {
+  k_up2_add<<<grid_for((long long)B * Z * Y * X * C, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
+                                                                          (bf16 *)out, B, Z, Y, X, C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C,
+                           cudaStream_t s) {
+  k_up2_bwd<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)g, (const bf16 *)act,
+                                                                              (bf16 *)glow, B, Z, Y, X, C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C,
+                            cudaStream_t s) {
+  k_mse_grad<<<grid_for(M, 256), 256, 0, s>>>((const bf16 *)y, target, (bf16 *)g, loss, M, C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
+                        float b2, float eps, float c1, float c2, float wd, cudaStream_t s) {
+  k_adam<<<grid_for(n, 256), 256, 0, s>>>(w, g, m, v, (bf16 *)wb, n, lr, b1, b2, eps, c1, c2, wd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,
+                                cudaStream_t s) {
+  if (npts <= 0) return cudaSuccess;
+  k_render_blobs<<<(unsigned)((npts * 32 + 255) / 256), 256, 0, s>>>(vol, Z, Y, X, (const float4 *)pts, npts, sigma);
+  return cudaGetLastError();
+}
+
+}  // namespace flf

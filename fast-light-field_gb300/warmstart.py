@@ -1,0 +1,370 @@
+"""Learned warm start for Richardson-Lucy: a 3-D U-Net on the normalised back projection.
+
+The network maps ``Htf / Ht1`` (the back projection of the camera image over
+the back projection of ones) to an estimate of the volume; RL then runs from
+that estimate instead of from a uniform volume.  Everything runs on the
+GPU with this package's own kernels (include/flf.h, csrc/flf_net.cu):
+BF16 activations and weights, FP32 accumulation, FP32 master weights and Adam;
+torch provides the tensors only.
+
+Architecture (channels-last [B][Z][Y][X][C], 3x3x3 convolutions, ReLU):
+four levels of 16-32-64-128 channels with two convolutions each on the way
+down (2x2x2 average pooling between levels), and on the way up a
+convolution that halves the channels at the coarse level, nearest 2x
+upsampling plus the encoder feature of that level (additive skip), and one
+convolution; a 16-channel head whose channel 0 is the prediction.  Volumes
+are zero-padded to multiples of 8 in Z, Y and X.
+
+Training data come from the method itself: random bead and filament volumes
+(``k_render_blobs``) are forward projected with the GPU projector, a
+background is added and Poisson noise drawn, and the noisy image is back
+projected.  The target is the volume that plain RL reaches from a uniform
+start after ``target_iters`` iterations (32 by default).  The Prevedel update
+x <- x Htf / (Ht H x) sees the image only through Htf, so that volume is a
+function of the network's input; RL's data-fit residual falls slowly with the
+iterations (microscope images carry background the volume cannot explain
+where the lenslets are dark), so a good prediction of the 32-iteration volume
+sits below the 8-iteration residual without further iterations.  Input and
+target are divided by the mean of the input (the Prevedel update is invariant
+to the start volume's scale after its first iteration); the loss is their mean
+squared error.
+"""
+
+import time
+
+import numpy as np
+
+import _flf
+
+try:
+    import torch
+except ImportError:  # torch is needed for device arrays
+    torch = None
+
+__all__ = ["UNet3D", "WarmStart", "synthetic_volume_points", "DeconvRLWarm"]
+
+CIN = 16
+# (name, input channels, output channels, ReLU)
+LAYERS = [("e0a", CIN, 16, True), ("e0b", 16, 16, True), ("e1a", 16, 32, True), ("e1b", 32, 32, True),
+          ("e2a", 32, 64, True), ("e2b", 64, 64, True), ("e3a", 64, 128, True), ("e3b", 128, 128, True),
+          ("u2", 128, 64, True), ("d2", 64, 64, True), ("u1", 64, 32, True), ("d1", 32, 32, True),
+          ("u0", 32, 16, True), ("d0", 16, 16, True), ("head", 16, 16, False)]
+
+
+def _bf(shape, dev):
+    return torch.empty(shape, dtype=torch.bfloat16, device=dev)
+
+
+class UNet3D:
+    """The warm-start network: parameters, forward, backward and Adam on the device."""
+
+    def __init__(self, device=0, seed=0):
+        if torch is None:
+            raise _flf.FlfError(-4, "PyTorch is required for device arrays")
+        _flf.load_library()
+        self.dev = torch.device("cuda", device)
+        g = torch.Generator().manual_seed(seed)
+        self.p = {}
+        for name, ci, co, relu in LAYERS:
+            std = np.sqrt((2.0 if relu else 1.0) / (27 * ci))
+            w = torch.randn((27, ci, co), generator=g) * std
+            if name == "head":
+                w[:, :, 1:] = 0
+            b = torch.zeros(co)
+            self.p[name] = {"w": w.to(self.dev), "b": b.to(self.dev), "ci": ci, "co": co, "relu": relu}
+        self.adam_t = 0
+        for q in self.p.values():
+            q["wb"] = _bf(q["w"].shape, self.dev)
+            q["wf"] = _bf((27, q["co"], q["ci"]), self.dev)
+            for k in ("gw", "mw", "vw"):
+                q[k] = torch.zeros_like(q["w"])
+            for k in ("gb", "mb", "vb"):
+                q[k] = torch.zeros_like(q["b"])
+        self._sync_weights()
+
+    def _sync_weights(self):
+        s = torch.cuda.current_stream(self.dev).cuda_stream
+        for q in self.p.values():
+            q["wb"].copy_(q["w"])
+            _flf.conv3d_flip(q["wb"], q["wf"], s)
+
+    def num_parameters(self):
+        return int(sum(q["w"].numel() + q["b"].numel() for q in self.p.values()))
+
+    def _conv(self, name, x, relu=None, mask=None, flip=False, out=None):
+        q = self.p[name]
+        co = q["ci"] if flip else q["co"]
+        y = out if out is not None else _bf(tuple(x.shape[:4]) + (co,), self.dev)
+        if relu is None:
+            relu = q["relu"] and not flip       # a data gradient is linear
+        _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,
+                    stream=torch.cuda.current_stream(self.dev).cuda_stream)
+        return y
+
+    def _pool(self, x):
+        B, Z, Y, X, C = x.shape
+        y = _bf((B, Z // 2, Y // 2, X // 2, C), self.dev)
+        _flf.pool2(x, y, torch.cuda.current_stream(self.dev).cuda_stream)
+        return y
+
+    def _up_add(self, low, skip):
+        y = _bf(tuple(skip.shape[:4]) + (low.shape[4],), self.dev)
+        _flf.up2_add(low, skip, y, torch.cuda.current_stream(self.dev).cuda_stream)
+        return y
+
+    def forward(self, x):
+        """x [B, Z, Y, X, 16] bf16 (Z, Y, X multiples of 8) -> (out [B, Z, Y, X, 16], cache)."""
+        a = {"x": x}
+        a["e0a"] = self._conv("e0a", x)
+        a["e0b"] = self._conv("e0b", a["e0a"])
+        a["p1"] = self._pool(a["e0b"])
+        a["e1a"] = self._conv("e1a", a["p1"])
+        a["e1b"] = self._conv("e1b", a["e1a"])
+        a["p2"] = self._pool(a["e1b"])
+        a["e2a"] = self._conv("e2a", a["p2"])
+        a["e2b"] = self._conv("e2b", a["e2a"])
+        a["p3"] = self._pool(a["e2b"])
+        a["e3a"] = self._conv("e3a", a["p3"])
+        a["e3b"] = self._conv("e3b", a["e3a"])
+        a["u2"] = self._conv("u2", a["e3b"])
+        a["s2"] = self._up_add(a["u2"], a["e2b"])
+        a["d2"] = self._conv("d2", a["s2"])
+        a["u1"] = self._conv("u1", a["d2"])
+        a["s1"] = self._up_add(a["u1"], a["e1b"])
+        a["d1"] = self._conv("d1", a["s1"])
+        a["u0"] = self._conv("u0", a["d1"])
+        a["s0"] = self._up_add(a["u0"], a["e0b"])
+        a["d0"] = self._conv("d0", a["s0"])
+        a["out"] = self._conv("head", a["d0"])
+        return a["out"], a
+
+    def _wgrad(self, name, x, g):
+        q = self.p[name]
+        s = torch.cuda.current_stream(self.dev).cuda_stream
+        _flf.conv3d_wgrad(x, g, q["gw"], s)
+        _flf.bias_grad(g, q["gb"], s)
+
+    def backward(self, a, dout):
+        """Gradients of all parameters (accumulated into gw / gb) for dL/d(out) = dout."""
+        s = torch.cuda.current_stream(self.dev).cuda_stream
+        for q in self.p.values():
+            q["gw"].zero_()
+            q["gb"].zero_()
+        # head (linear) and d0
+        self._wgrad("head", a["d0"], dout)
+        g = self._conv("head", dout, flip=True, mask=a["d0"])            # d(pre d0)
+        self._wgrad("d0", a["s0"], g)
+        gs0 = self._conv("d0", g, flip=True)                             # d s0
+        gu0 = _bf(a["u0"].shape, self.dev)
+        _flf.up2_bwd(gs0, a["u0"], gu0, s)                               # d(pre u0)
+        self._wgrad("u0", a["d1"], gu0)
+        g = self._conv("u0", gu0, flip=True, mask=a["d1"])               # d(pre d1)
+        self._wgrad("d1", a["s1"], g)
+        gs1 = self._conv("d1", g, flip=True)
+        gu1 = _bf(a["u1"].shape, self.dev)
+        _flf.up2_bwd(gs1, a["u1"], gu1, s)
+        self._wgrad("u1", a["d2"], gu1)
+        g = self._conv("u1", gu1, flip=True, mask=a["d2"])
+        self._wgrad("d2", a["s2"], g)
+        gs2 = self._conv("d2", g, flip=True)
+        gu2 = _bf(a["u2"].shape, self.dev)
+        _flf.up2_bwd(gs2, a["u2"], gu2, s)
+        self._wgrad("u2", a["e3b"], gu2)
+        g = self._conv("u2", gu2, flip=True, mask=a["e3b"])              # d(pre e3b)
+        self._wgrad("e3b", a["e3a"], g)
+        g = self._conv("e3b", g, flip=True, mask=a["e3a"])
+        self._wgrad("e3a", a["p3"], g)
+        gp3 = self._conv("e3a", g, flip=True)                            # d p3
+        g = _bf(a["e2b"].shape, self.dev)
+        _flf.pool2_bwd(gp3, gs2, a["e2b"], g, s)                         # d(pre e2b): pool path + skip
+        self._wgrad("e2b", a["e2a"], g)
+        g = self._conv("e2b", g, flip=True, mask=a["e2a"])
+        self._wgrad("e2a", a["p2"], g)
+        gp2 = self._conv("e2a", g, flip=True)
+        g = _bf(a["e1b"].shape, self.dev)
+        _flf.pool2_bwd(gp2, gs1, a["e1b"], g, s)
+        self._wgrad("e1b", a["e1a"], g)
+        g = self._conv("e1b", g, flip=True, mask=a["e1a"])
+        self._wgrad("e1a", a["p1"], g)
+        gp1 = self._conv("e1a", g, flip=True)
+        g = _bf(a["e0b"].shape, self.dev)
+        _flf.pool2_bwd(gp1, gs0, a["e0b"], g, s)
+        self._wgrad("e0b", a["e0a"], g)
+        g = self._conv("e0b", g, flip=True, mask=a["e0a"])
+        self._wgrad("e0a", a["x"], g)
+
+    def adam_step(self, lr, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        self.adam_t += 1
+        c1, c2 = 1 - b1 ** self.adam_t, 1 - b2 ** self.adam_t
+        s = torch.cuda.current_stream(self.dev).cuda_stream
+        for name, q in self.p.items():
+            if name == "head":
+                q["gw"][:, :, 1:] = 0
+            _flf.adam(q["w"], q["gw"], q["mw"], q["vw"], q["wb"], lr, b1, b2, eps, c1, c2, wd, s)
+            _flf.adam(q["b"], q["gb"], q["mb"], q["vb"], None, lr, b1, b2, eps, c1, c2, 0.0, s)
+            _flf.conv3d_flip(q["wb"], q["wf"], s)
+
+    def state_dict(self):
+        return {"%s.%s" % (n, k): q[k].cpu().numpy() for n, q in self.p.items() for k in ("w", "b")}
+
+    def load_state_dict(self, d):
+        for n, q in self.p.items():
+            q["w"].copy_(torch.as_tensor(d["%s.w" % n]))
+            q["b"].copy_(torch.as_tensor(d["%s.b" % n]))
+        self._sync_weights()
+
+    def save(self, path):
+        np.savez(path, **self.state_dict())
+
+    def load(self, path):
+        with np.load(path) as d:
+            self.load_state_dict(dict(d))
+
+
+def synthetic_volume_points(shape, beads, filaments, rng, bead_amp=(500.0, 1000.0), fil_intensity=500.0,
+                            fil_steps=60):
+    """Blob list (z, y, x, amplitude) of a bead + filament volume: uniform bead positions
+    and amplitudes, random-walk filaments drawn as a chain of unit-spaced blobs."""
+    Z, Y, X = shape
+    pts = [np.stack([rng.uniform(0, Z - 1, beads), rng.uniform(0, Y - 1, beads), rng.uniform(0, X - 1, beads),
+                     rng.uniform(*bead_amp, beads)], axis=1)]
+    for _ in range(filaments):
+        p = np.array([rng.uniform(0, Z - 1), rng.uniform(0, Y - 1), rng.uniform(0, X - 1)])
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        path = []
+        for _ in range(fil_steps):
+            d = d + 0.3 * rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            p = p + d
+            if not (0 <= p[0] <= Z - 1 and 0 <= p[1] <= Y - 1 and 0 <= p[2] <= X - 1):
+                break
+            path.append(p.copy())
+        if path:
+            q = np.array(path)
+            pts.append(np.concatenate([q, np.full((len(q), 1), fil_intensity * 0.4)], axis=1))
+    return np.ascontiguousarray(np.concatenate(pts).astype(np.float32))
+
+
+class WarmStart:
+    """A trained (or training) warm-start network for one PSF matrix and image size.
+
+    ``projector`` is a ``Projector_gb300``; ``hMatrix`` its PSF matrix.  Call
+    ``train`` once (or ``load`` saved weights), then ``initial_volume`` gives
+    the RL start for camera images of the same size.
+    """
+
+    def __init__(self, projector, hMatrix, Y, X, device=0, seed=0, background=100.0, beads=200, filaments=0,
+                 sigma=1.0):
+        self.proj, self.hm = projector, hMatrix
+        self.Y, self.X, self.Z = int(Y), int(X), int(hMatrix.numZ)
+        self.dev = torch.device("cuda", device)
+        self.net = UNet3D(device, seed)
+        self.background, self.beads, self.filaments, self.sigma = background, beads, filaments, sigma
+        projector._prepare(self.ctx, self.Y, self.X, hMatrix)
+        self.pad = tuple(-(-v // 8) * 8 for v in (self.Z, self.Y, self.X))
+        ones = torch.ones((1, self.Y, self.X), device=self.dev)
+        self.ht1 = torch.empty((self.Z, 1, self.Y, self.X), device=self.dev)
+        self.ctx.backward(ones, self.ht1, 1, self.Y, self.X, None, stream=self._s())
+        self.ht1.clamp_(min=1e-12)
+        self.losses = []
+
+    @property
+    def ctx(self):
+        """The projector's context for this PSF matrix (prepared for Y x X)."""
+        c = self.proj.context(self.hm)
+        self.proj._prepare(c, self.Y, self.X, self.hm)
+        return c
+
+    def _s(self):
+        return torch.cuda.current_stream(self.dev).cuda_stream
+
+    def _inputs(self, htf):
+        """Network input (channels-last bf16, padded) and the per-frame scale from
+        Htf [Z, T, Y, X]."""
+        nrm = htf / self.ht1
+        T = htf.shape[1]
+        scale = nrm.reshape(self.Z, T, -1).mean(dim=(0, 2)).clamp_min(1e-12)    # [T]
+        Zp, Yp, Xp = self.pad
+        x = torch.zeros((T, Zp, Yp, Xp, CIN), dtype=torch.bfloat16, device=self.dev)
+        x[:, :self.Z, :self.Y, :self.X, 0] = (nrm / scale[None, :, None, None]).permute(1, 0, 2, 3)
+        return x, scale
+
+    def make_batch(self, T, rng):
+        """T synthetic (truth [Z, T, Y, X], noisy image [T, Y, X], Htf [Z, T, Y, X])."""
+        truth = torch.zeros((T, self.Z, self.Y, self.X), device=self.dev)
+        for t in range(T):
+            pts = torch.as_tensor(synthetic_volume_points((self.Z, self.Y, self.X), self.beads, self.filaments, rng),
+                                  device=self.dev)
+            _flf.render_blobs(truth[t], pts, self.sigma, self._s())
+        truth = truth.permute(1, 0, 2, 3).contiguous()
+        clean = torch.empty((T, self.Y, self.X), device=self.dev)
+        self.ctx.forward(truth, clean, T, self.Y, self.X, None, stream=self._s())
+        gen = torch.Generator(device=self.dev).manual_seed(int(rng.integers(1 << 62)))
+        img = torch.poisson((clean + self.background).clamp_min(0), generator=gen)
+        htf = torch.empty((self.Z, T, self.Y, self.X), device=self.dev)
+        self.ctx.backward(img, htf, T, self.Y, self.X, None, stream=self._s())
+        return truth, img, htf
+
+    def rl_target(self, htf, iters):
+        """Plain RL from a uniform volume (the method the network stands in for)."""
+        x = torch.ones_like(htf)
+        self.proj.RichardsonLucy(self.hm, x, htf, iters)
+        return x
+
+    def train(self, steps=1500, batch=4, crop=128, volumes_per_refresh=8, refresh_every=8, lr=1e-3, seed=1,
+              target_iters=32, log_every=0):
+        """Train on crops of freshly generated synthetic volumes; returns seconds taken."""
+        rng = np.random.default_rng(seed)
+        t0 = time.time()
+        cy, cx = min(crop, self.pad[1]), min(crop, self.pad[2])
+        pool = None
+        for step in range(steps):
+            if step % refresh_every == 0:
+                _, _, htf = self.make_batch(volumes_per_refresh, rng)
+                xin, scale = self._inputs(htf)
+                ref = self.rl_target(htf, target_iters)
+                Zp, Yp, Xp = self.pad
+                tgt = torch.zeros((volumes_per_refresh, Zp, Yp, Xp), device=self.dev)
+                tgt[:, :self.Z, :self.Y, :self.X] = (ref / scale[None, :, None, None]).permute(1, 0, 2, 3)
+                pool = (xin, tgt)
+            idx = rng.integers(0, pool[0].shape[0], batch)
+            ys = rng.integers(0, self.pad[1] - cy + 1, batch) // 8 * 8
+            xs = rng.integers(0, self.pad[2] - cx + 1, batch) // 8 * 8
+            xb = torch.stack([pool[0][i, :, y:y + cy, x:x + cx] for i, y, x in zip(idx, ys, xs)]).contiguous()
+            tb = torch.stack([pool[1][i, :, y:y + cy, x:x + cx] for i, y, x in zip(idx, ys, xs)]).contiguous()
+            out, cache = self.net.forward(xb)
+            dout = torch.empty_like(out)
+            loss = torch.zeros(1, device=self.dev)
+            _flf.mse_grad(out, tb, dout, loss, self._s())
+            self.net.backward(cache, dout)
+            frac = step / max(steps - 1, 1)
+            self.net.adam_step(lr * 0.5 * (1 + np.cos(np.pi * frac)))
+            if log_every and (step % log_every == 0 or step == steps - 1):
+                self.losses.append((step, float(loss)))
+        torch.cuda.synchronize(self.dev)
+        return time.time() - t0
+
+    def initial_volume(self, htf, floor=1e-3):
+        """RL start volume [Z, T, Y, X] from Htf [Z, T, Y, X] (device): the network's
+        prediction, clamped below at floor x the input mean (RL keeps zeros at zero)."""
+        xin, scale = self._inputs(htf)
+        out, _ = self.net.forward(xin)
+        pred = out[:, :self.Z, :self.Y, :self.X, 0].float().permute(1, 0, 2, 3)
+        x0 = pred.clamp_min(floor) * scale[None, :, None, None]
+        return x0.contiguous()
+
+
+def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):
+    """RL from the network's start volume: back projection, warm start, ``maxIter``
+    Prevedel iterations (the reference's default update), on the device; returns the
+    volume [Z, T, Y, X] as a device tensor."""
+    p = projector or warm.proj
+    img = p.asnative(im)
+    T, Y, X = img.shape
+    htf = torch.empty((warm.Z, T, Y, X), device=warm.dev)
+    warm.ctx.backward(img, htf, T, Y, X, None, stream=warm._s())
+    x = warm.initial_volume(htf)
+    if maxIter > 0:
+        p.RichardsonLucy(warm.hm, x, htf if prevedel else img, maxIter, prevedel=prevedel)
+    return x

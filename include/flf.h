@@ -210,6 +210,48 @@ int flf_psf_lf_bin(float *out_dev, const double *field_dev, int L, int S, int nh
                    int hi, int first, void *stream);
 int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, void *stream);
 
+/* Learned warm start: kernels of a 3-D U-Net on channels-last BF16 volumes
+ * [B][Z][Y][X][C] (C a multiple of 16), FP32 accumulation.  All pointers are
+ * device pointers; volumes and weights 16-byte aligned.  These are the
+ * network's own forward and backward kernels (the reference has no learned
+ * part; its DeconvRL starts from Htf or a given guess, lfdeconv.py:72-202).
+ *
+ * flf_conv3d: y = act(conv3x3x3(x, w) + bias), zero padding, w [27][Ci][Co]
+ *   (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), bias [Co] float or NULL, act = ReLU
+ *   when relu != 0; with mask != NULL ([..][Co] bf16) entries whose mask is
+ *   not > 0 are zeroed (the ReLU derivative in a backward pass).
+ * flf_conv3d_wgrad: dw [27][Ci][Co] float += sum_v x[v + tap][ci] dy[v][co].
+ * flf_conv3d_flip: w2[26 - tap][co][ci] = w[tap][ci][co]; conv3d with w2 is
+ *   the data gradient.
+ * flf_bias_grad: db[c] += sum over the M rows of g[M][C] (C <= 128).
+ * flf_pool2 / flf_pool2_bwd: 2x2x2 average pooling (Z, Y, X even) and its
+ *   adjoint plus an optional second gradient gskip, times (act > 0) if act.
+ * flf_up2_add / flf_up2_bwd: out = nearest 2x upsampling of low (+ skip);
+ *   adjoint: 2x2x2 block sums times (act > 0) if act.  Shapes are those of
+ *   the full-resolution tensor.
+ * flf_mse_grad: loss += mean((y[:, 0] - target)^2), g = its gradient in
+ *   channel 0 (other channels 0); M voxels, y / g [M][C] bf16.
+ * flf_adam: Adam step on FP32 weights w with gradient g and moments m, v
+ *   (bias corrections c1, c2, decoupled weight decay wd); writes the BF16
+ *   copy wb when not NULL.
+ * flf_render_blobs: vol [Z][Y][X] float += amp exp(-d^2 / 2 sigma^2) within
+ *   3 sigma of each pts[k] = (z, y, x, amp) (float4 array). */
+int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
+               int Ci, int Co, int relu, void *stream);
+int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
+                     void *stream);
+int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
+int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream);
+int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);
+int flf_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y, int X, int C,
+                  void *stream);
+int flf_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C, void *stream);
+int flf_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C, void *stream);
+int flf_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C, void *stream);
+int flf_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1, float b2,
+             float eps, float c1, float c2, float wd, void *stream);
+int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *stream);
+
 /* CUDA graph of a whole RL run (the replay form of flf_rl_iterate): the
  * launches of `iters` iterations over T frames of Y x X images are captured
  * once, with these pointers baked in, and each flf_graph_launch replays them

@@ -1,0 +1,152 @@
+"""The warm-start network's kernels against torch CPU float64 references.
+
+Inputs and weights are BF16 (exactly representable, so the reference sees the
+same numbers); the kernels accumulate in FP32.  Tolerances: BF16 outputs
+carry one rounding (2^-8 relative) -> 1e-2 of the reference's magnitude plus
+1e-3 of its maximum; FP32 weight gradients -> 1e-4 of their maximum.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env(built_lib):
+    import torch
+    import _flf
+    _flf.load_library()
+    return torch, _flf
+
+
+def _ref_conv(torch, x, w, bias=None):
+    """x [B,Z,Y,X,Ci], w [27,Ci,Co] (float64 CPU) -> [B,Z,Y,X,Co]."""
+    Ci, Co = w.shape[1], w.shape[2]
+    wt = w.reshape(3, 3, 3, Ci, Co).permute(4, 3, 0, 1, 2)
+    y = torch.nn.functional.conv3d(x.permute(0, 4, 1, 2, 3), wt, bias=bias, padding=1)
+    return y.permute(0, 2, 3, 4, 1)
+
+
+def _close(torch, got, ref, rel=1e-2, absf=1e-3):
+    got = got.double().cpu()
+    err = (got - ref).abs()
+    lim = rel * ref.abs() + absf * ref.abs().max()
+    assert bool((err <= lim).all()), float((err - lim).max())
+
+
+@pytest.mark.parametrize("shape,Ci,Co,relu", [
+    ((2, 4, 6, 10), 16, 16, False), ((1, 3, 7, 9), 32, 64, True), ((1, 5, 5, 13), 64, 128, True),
+    ((3, 2, 4, 4), 128, 32, False), ((1, 8, 16, 16), 16, 64, True),
+])
+def test_conv3d_forward(env, shape, Ci, Co, relu):
+    torch, _flf = env
+    g = torch.Generator().manual_seed(Ci * Co + shape[1])
+    x = torch.randn(shape + (Ci,), generator=g).bfloat16()
+    w = (torch.randn((27, Ci, Co), generator=g) / np.sqrt(27 * Ci)).bfloat16()
+    b = torch.randn(Co, generator=g).float()
+    y = torch.empty(shape + (Co,), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu)
+    ref = _ref_conv(torch, x.double(), w.double(), b.double())
+    if relu:
+        ref = ref.clamp_min(0)
+    _close(torch, y, ref)
+
+
+def test_conv3d_mask_and_data_gradient(env):
+    torch, _flf = env
+    g = torch.Generator().manual_seed(3)
+    shape, Ci, Co = (2, 4, 6, 10), 32, 16
+    x = torch.randn(shape + (Ci,), generator=g).bfloat16().double().requires_grad_()
+    w = (torch.randn((27, Ci, Co), generator=g) / 15).bfloat16()
+    dy = torch.randn(shape + (Co,), generator=g).bfloat16()
+    act = torch.randn(shape + (Ci,), generator=g).bfloat16()     # ReLU output of the layer before
+    y = _ref_conv(torch, x, w.double())
+    y.backward(dy.double())
+    ref = x.grad * (act.double() > 0)
+    w2 = torch.empty((27, Co, Ci), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d_flip(w.cuda(), w2)
+    dx = torch.empty(shape + (Ci,), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda())
+    _close(torch, dx, ref)
+
+
+@pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 16, 16), ((1, 6, 9, 11), 32, 64), ((2, 3, 8, 8), 128, 128),
+                                         ((1, 4, 4, 4), 64, 32)])
+def test_conv3d_weight_and_bias_gradient(env, shape, Ci, Co):
+    torch, _flf = env
+    g = torch.Generator().manual_seed(Ci + Co)
+    x = torch.randn(shape + (Ci,), generator=g).bfloat16()
+    w = torch.zeros((27, Ci, Co), dtype=torch.float64, requires_grad=True)
+    b = torch.zeros(Co, dtype=torch.float64, requires_grad=True)
+    dy = torch.randn(shape + (Co,), generator=g).bfloat16()
+    _ref_conv(torch, x.double(), w, b).backward(dy.double())
+    dw = torch.zeros((27, Ci, Co), dtype=torch.float32, device="cuda")
+    db = torch.zeros(Co, dtype=torch.float32, device="cuda")
+    _flf.conv3d_wgrad(x.cuda(), dy.cuda(), dw)
+    _flf.bias_grad(dy.cuda(), db)
+    assert float((dw.double().cpu() - w.grad).abs().max()) <= 1e-4 * float(w.grad.abs().max())
+    assert float((db.double().cpu() - b.grad).abs().max()) <= 1e-4 * float(b.grad.abs().max())
+
+
+def test_pool_upsample_and_their_adjoints(env):
+    torch, _flf = env
+    g = torch.Generator().manual_seed(5)
+    B, Z, Y, X, C = 2, 4, 6, 8, 16
+    x = torch.randn((B, Z, Y, X, C), generator=g).bfloat16()
+    p = torch.empty((B, Z // 2, Y // 2, X // 2, C), dtype=torch.bfloat16, device="cuda")
+    _flf.pool2(x.cuda(), p)
+    ref = x.double().reshape(B, Z // 2, 2, Y // 2, 2, X // 2, 2, C).mean(dim=(2, 4, 6))
+    _close(torch, p, ref)
+    low = torch.randn((B, Z // 2, Y // 2, X // 2, C), generator=g).bfloat16()
+    skip = torch.randn((B, Z, Y, X, C), generator=g).bfloat16()
+    up = torch.empty((B, Z, Y, X, C), dtype=torch.bfloat16, device="cuda")
+    _flf.up2_add(low.cuda(), skip.cuda(), up)
+    upr = low.double().repeat_interleave(2, 1).repeat_interleave(2, 2).repeat_interleave(2, 3) + skip.double()
+    _close(torch, up, upr)
+    # adjoints: <pool(x), q> = <x, pool^T(q)>, <up(l), u> = <l, up^T(u)>, with masks
+    gp = torch.empty((B, Z, Y, X, C), dtype=torch.bfloat16, device="cuda")
+    act = torch.randn((B, Z, Y, X, C), generator=g).bfloat16()
+    _flf.pool2_bwd(low.cuda(), skip.cuda(), act.cuda(), gp)
+    refp = (low.double().repeat_interleave(2, 1).repeat_interleave(2, 2).repeat_interleave(2, 3) / 8 +
+            skip.double()) * (act.double() > 0)
+    _close(torch, gp, refp)
+    gl = torch.empty((B, Z // 2, Y // 2, X // 2, C), dtype=torch.bfloat16, device="cuda")
+    actl = torch.randn((B, Z // 2, Y // 2, X // 2, C), generator=g).bfloat16()
+    _flf.up2_bwd(skip.cuda(), actl.cuda(), gl)
+    refl = skip.double().reshape(B, Z // 2, 2, Y // 2, 2, X // 2, 2, C).sum(dim=(2, 4, 6)) * (actl.double() > 0)
+    _close(torch, gl, refl)
+
+
+def test_mse_adam_and_blobs(env):
+    torch, _flf = env
+    g = torch.Generator().manual_seed(7)
+    M, C = 1000, 16
+    y = torch.randn((M, C), generator=g).bfloat16()
+    t = torch.randn(M, generator=g)
+    gr = torch.empty((M, C), dtype=torch.bfloat16, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    _flf.mse_grad(y.cuda(), t.cuda(), gr, loss)
+    d = y[:, 0].double() - t.double()
+    assert abs(float(loss) - float((d ** 2).mean())) <= 1e-5 * float((d ** 2).mean())
+    _close(torch, gr[:, 0], 2 * d / M)
+    assert float(gr[:, 1:].abs().max()) == 0
+    w = torch.randn(500, generator=g)
+    gw = torch.randn(500, generator=g)
+    wd, m, v = w.clone().cuda(), torch.zeros(500, device="cuda"), torch.zeros(500, device="cuda")
+    wb = torch.empty(500, dtype=torch.bfloat16, device="cuda")
+    _flf.adam(wd, gw.cuda(), m, v, wb, 1e-2, 0.9, 0.999, 1e-8, 0.1, 0.001, 0.0)
+    mr, vr = 0.1 * gw, 0.001 * gw * gw
+    wr = w - 1e-2 * (mr / 0.1) / ((vr / 0.001).sqrt() + 1e-8)
+    assert float((wd.cpu() - wr).abs().max()) < 1e-6
+    assert float((wb.float().cpu() - wr).abs().max()) < 1e-2
+    vol = torch.zeros((6, 20, 30), device="cuda")
+    pts = torch.tensor([[2.0, 10.0, 12.5, 3.0], [0.2, 0.0, 29.0, 1.0]], device="cuda")
+    _flf.render_blobs(vol, pts, 1.0)
+    zz, yy, xx = np.meshgrid(np.arange(6), np.arange(20), np.arange(30), indexing="ij")
+    ref = np.zeros((6, 20, 30))
+    for z0, y0, x0, a in pts.cpu().numpy():
+        cz, cy, cx = np.floor(np.array([z0, y0, x0]) + 0.5)
+        near = (np.abs(zz - cz) <= 3) & (np.abs(yy - cy) <= 3) & (np.abs(xx - cx) <= 3)
+        ref += near * a * np.exp(-((zz - z0) ** 2 + (yy - y0) ** 2 + (xx - x0) ** 2) / 2)
+    assert np.max(np.abs(vol.cpu().numpy() - ref)) < 1e-5

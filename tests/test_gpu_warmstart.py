@@ -1,0 +1,111 @@
+"""The learned warm start: the whole network's gradients against a torch CPU
+float64 restatement, training, and RL from the warm start.
+
+Gradient check: the device network keeps activations in BF16, so each
+parameter gradient must agree with the float64 restatement (same BF16 weights
+and input, FP64 activations) in direction (cosine >= 0.99) and to 10 % in
+norm.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env(built_lib):
+    import torch
+    import warmstart
+    return torch, warmstart
+
+
+def _reference_forward(torch, ws_mod, net, x):
+    """The network in float64 on the CPU with the device network's BF16 weights."""
+    F = torch.nn.functional
+    P = {n: (q["wb"].double().cpu().requires_grad_(), q["b"].double().cpu().requires_grad_())
+         for n, q in net.p.items()}
+
+    def conv(name, t, relu):
+        w, b = P[name]
+        ci, co = w.shape[1], w.shape[2]
+        y = F.conv3d(t, w.reshape(3, 3, 3, ci, co).permute(4, 3, 0, 1, 2), b, padding=1)
+        return F.relu(y) if relu else y
+
+    def up(t):
+        return t.repeat_interleave(2, 2).repeat_interleave(2, 3).repeat_interleave(2, 4)
+
+    t = x.double().cpu().permute(0, 4, 1, 2, 3)
+    e0 = conv("e0b", conv("e0a", t, True), True)
+    e1 = conv("e1b", conv("e1a", F.avg_pool3d(e0, 2), True), True)
+    e2 = conv("e2b", conv("e2a", F.avg_pool3d(e1, 2), True), True)
+    e3 = conv("e3b", conv("e3a", F.avg_pool3d(e2, 2), True), True)
+    d2 = conv("d2", up(conv("u2", e3, True)) + e2, True)
+    d1 = conv("d1", up(conv("u1", d2, True)) + e1, True)
+    d0 = conv("d0", up(conv("u0", d1, True)) + e0, True)
+    out = conv("head", d0, False)
+    return out.permute(0, 2, 3, 4, 1), P
+
+
+def test_network_gradients_match_float64(env):
+    torch, ws_mod = env
+    net = ws_mod.UNet3D(seed=3)
+    g = torch.Generator().manual_seed(0)
+    x = torch.zeros((2, 8, 16, 24, ws_mod.CIN))
+    x[..., :3] = torch.rand((2, 8, 16, 24, 3), generator=g)
+    x = x.bfloat16()
+    target = torch.rand((2, 8, 16, 24), generator=g)
+    out, cache = net.forward(x.cuda())
+    ref, P = _reference_forward(torch, ws_mod, net, x)
+    assert float((out.double().cpu() - ref.detach()).abs().max()) <= 0.05 * float(ref.detach().abs().max())
+    dout = torch.empty_like(out)
+    loss = torch.zeros(1, device="cuda")
+    import _flf
+    _flf.mse_grad(out, target.cuda(), dout, loss)
+    ((ref[..., 0] - target.double()) ** 2).mean().backward()
+    net.backward(cache, dout)
+    for name, q in net.p.items():
+        for key, gref in (("gw", P[name][0].grad), ("gb", P[name][1].grad)):
+            gd = q[key].double().cpu()
+            if name == "head" and key == "gw":
+                gd, gref = gd[:, :, 0], gref[:, :, 0]
+            if name == "head" and key == "gb":
+                gd, gref = gd[:1], gref[:1]
+            nr = float(gref.norm())
+            if nr == 0:
+                continue
+            cos = float((gd * gref).sum() / (gd.norm() * gref.norm() + 1e-300))
+            assert cos >= 0.99, (name, key, cos)
+            assert abs(float(gd.norm()) - nr) <= 0.1 * nr, (name, key, float(gd.norm()), nr)
+
+
+def test_training_and_warm_started_rl(env):
+    torch, ws_mod = env
+    import projector
+    import psfmatrix
+    import synthetic
+    N = 5
+    H, Ht = synthetic.synthetic_psf(N, np.arange(-4, 5, 2), 3)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    p = projector.Projector_gb300()
+    Y = X = 60
+    ws = ws_mod.WarmStart(p, hm, Y, X, beads=30)
+    ws.train(steps=150, batch=2, crop=32, volumes_per_refresh=4, refresh_every=10, target_iters=16, log_every=10)
+    first = np.mean([l for _, l in ws.losses[:2]])
+    last = np.mean([l for _, l in ws.losses[-3:]])
+    assert last < first
+    rng = np.random.default_rng(99)
+    truth, img, htf = ws.make_batch(2, rng)
+    x0 = ws.initial_volume(htf)
+    assert x0.shape == htf.shape and bool(torch.isfinite(x0).all()) and float(x0.min()) > 0
+    s = torch.cuda.current_stream().cuda_stream
+
+    def resid(x):
+        hx = torch.empty_like(img)
+        ws.ctx.forward(x, hx, 2, Y, X, None, stream=s)
+        return float(torch.linalg.vector_norm(img.double() - hx.double()) / torch.linalg.vector_norm(img.double()))
+
+    xu = torch.ones_like(htf)
+    p.RichardsonLucy(hm, xu, htf, 8)
+    xw = ws_mod.DeconvRLWarm(ws, img, 8)
+    assert resid(xw) <= 1.01 * resid(xu)
