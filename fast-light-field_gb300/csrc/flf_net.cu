@@ -8,6 +8,9 @@
 //                     ldmatrix; epilogue: bias, ReLU, gradient mask, BF16.
 //                     The data gradient is the same kernel on the flipped,
 //                     transposed weights (k_conv3d_flip_weights).
+//   k_conv3d_tiled    the same for 16 / 32 channels in and out: persistent
+//                     CTAs with the weights resident in shared memory and
+//                     one staged input patch per output tile for all taps.
 //   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
 //                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
 //                     split-K over its 4 warps, FP32 atomics into dW.
@@ -175,6 +178,128 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
         *reinterpret_cast<__nv_bfloat162 *>(p.y + o) = __floats2bfloat162_rn(v0, v1);
       }
     }
+}
+
+// Persistent variant for the wide, shallow layers (Ci, Co in {16, 32}): all
+// 27 x Ci x Co weights stay in shared memory; each CTA walks output tiles of
+// one z slice, 8 rows x 16 columns, staging the 3 x 10 x 18 input patch of a
+// tile (double-buffered with cp.async) and reading every tap's A fragments
+// straight from the patch with shifted ldmatrix row addresses.  Each input
+// voxel is fetched about 4 times instead of 27.
+template <int CI, int CO>
+__global__ void __launch_bounds__(128) k_conv3d_tiled(ConvParams p, int tiles_x, int tiles_y, long long ntiles) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int PY = 10, PX = 18, PR = 3 * PY * PX;
+  constexpr int RA = CI / 8, RB = CO / 8;
+  bf16 *Ws = reinterpret_cast<bf16 *>(smem);     // [27 * CI][CO]
+  bf16 *Ps = Ws + 27 * CI * CO;                   // [2][PR][CI]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  for (int i = tid; i < 27 * CI * RB; i += 128) {
+    const int row = i / RB, c = i - row * RB;
+    cp16(su32(Ws + row * CO) + ((c ^ swz<RB>(row)) << 4), p.w + (long long)row * CO + c * 8, true);
+  }
+  auto tile_pos = [&](long long t, int &b, int &z, int &y0, int &x0) {
+    const int tx = (int)(t % tiles_x);
+    t /= tiles_x;
+    const int ty = (int)(t % tiles_y);
+    t /= tiles_y;
+    z = (int)(t % p.Z);
+    b = (int)(t / p.Z);
+    y0 = ty * 8;
+    x0 = tx * 16;
+  };
+  auto load_patch = [&](long long t, int buf) {
+    int b, z, y0, x0;
+    tile_pos(t, b, z, y0, x0);
+    bf16 *P = Ps + buf * PR * CI;
+    for (int i = tid; i < PR * RA; i += 128) {
+      const int r = i / RA, c = i - r * RA;
+      const int pz = r / (PY * PX), py = (r / PX) % PY, px = r % PX;
+      const int gz = z + pz - 1, gy = y0 + py - 1, gx = x0 + px - 1;
+      const bool ok = gz >= 0 && gz < p.Z && gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X;
+      const bf16 *src = ok ? p.x + ((((long long)b * p.Z + gz) * p.Y + gy) * p.X + gx) * CI + c * 8 : p.x;
+      cp16(su32(P + r * CI) + ((c ^ swz<RA>(r)) << 4), src, ok);
+    }
+  };
+
+  const int mat = lane >> 3, r8 = lane & 7;
+  long long t = blockIdx.x;
+  int buf = 0;
+  if (t < ntiles) load_patch(t, 0);
+  cp_commit();
+  for (; t < ntiles; t += gridDim.x) {
+    const long long nt_ = t + gridDim.x;
+    if (nt_ < ntiles) load_patch(nt_, buf ^ 1);
+    cp_commit();
+    cp_wait<1>();
+    __syncthreads();
+    const bf16 *P = Ps + buf * PR * CI;
+    float acc[2][CO / 8][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int j = 0; j < CO / 8; j++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+#pragma unroll 1
+    for (int tap = 0; tap < 27; tap++) {
+      const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+      for (int kc = 0; kc < CI / 16; kc++) {
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+          const int yy = 2 * warp + mt, xx = r8 + 8 * (mat & 1);
+          const int pr = (dz * PY + yy + dy) * PX + xx + dx;
+          const int chunk = 2 * kc + (mat >> 1);
+          ldsm4(su32(P + pr * CI) + ((chunk ^ swz<RA>(pr)) << 4), a[mt][0], a[mt][1], a[mt][2], a[mt][3]);
+        }
+#pragma unroll
+        for (int n2 = 0; n2 < CO / 16; n2++) {
+          const int row = tap * CI + kc * 16 + r8 + 8 * (mat & 1);
+          const int c = n2 * 2 + (mat >> 1);
+          uint32_t b0, b1, b2, b3;
+          ldsm4t(su32(Ws + row * CO) + ((c ^ swz<RB>(row)) << 4), b0, b1, b2, b3);
+#pragma unroll
+          for (int mt = 0; mt < 2; mt++) {
+            mma_bf16(acc[mt][2 * n2], a[mt], b0, b1);
+            mma_bf16(acc[mt][2 * n2 + 1], a[mt], b2, b3);
+          }
+        }
+      }
+    }
+    int b, z, y0, x0;
+    tile_pos(t, b, z, y0, x0);
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+      for (int nt = 0; nt < CO / 8; nt++) {
+        const int col = nt * 8 + 2 * (lane & 3);
+        const float b0 = p.bias ? p.bias[col] : 0.f, b1 = p.bias ? p.bias[col + 1] : 0.f;
+        const int y = y0 + 2 * warp + mt;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int x = x0 + (lane >> 2) + 8 * h;
+          if (y >= p.Y || x >= p.X) continue;
+          float v0 = acc[mt][nt][2 * h] + b0, v1 = acc[mt][nt][2 * h + 1] + b1;
+          if (p.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          const long long o = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO + col;
+          if (p.mask) {
+            const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(p.mask + o);
+            if (!(__bfloat162float(mk.x) > 0.f)) v0 = 0.f;
+            if (!(__bfloat162float(mk.y) > 0.f)) v1 = 0.f;
+          }
+          *reinterpret_cast<__nv_bfloat162 *>(p.y + o) = __floats2bfloat162_rn(v0, v1);
+        }
+      }
+    __syncthreads();   // the next iteration refills this buffer
+    buf ^= 1;
+  }
+  cp_wait<0>();
 }
 
 // Weight gradient.  CTA = (voxel chunk, tap) x (ci tile CM, co tile CN); the 4
@@ -426,9 +551,35 @@ static unsigned grid_for(long long n, int block) {
   return (unsigned)(g < 152LL * 32 ? (g < 1 ? 1 : g) : 152LL * 32);
 }
 
+template <int CI, int CO>
+static cudaError_t launch_tiled(const ConvParams &p, cudaStream_t s) {
+  static int grid_cap = 0;
+  const size_t smem = sizeof(bf16) * (27 * CI * CO + 2 * 540 * CI);
+  if (!grid_cap) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tiled<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, dev = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tiled<CI, CO>, 128, smem);
+    if (e != cudaSuccess) return e;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid_cap = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  }
+  const int tiles_x = (p.X + 15) / 16, tiles_y = (p.Y + 7) / 8;
+  const long long ntiles = (long long)p.B * p.Z * tiles_y * tiles_x;
+  const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
+  k_conv3d_tiled<CI, CO><<<grid, 128, smem, s>>>(p, tiles_x, tiles_y, ntiles);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_conv3d(const ConvParams &p, cudaStream_t s) {
   const long long M = (long long)p.B * p.Z * p.Y * p.X;
   if (M == 0) return cudaSuccess;
+  if (p.Ci == 16 && p.Co == 16) return launch_tiled<16, 16>(p, s);
+  if (p.Ci == 16 && p.Co == 32) return launch_tiled<16, 32>(p, s);
+  if (p.Ci == 32 && p.Co == 16) return launch_tiled<32, 16>(p, s);
+  if (p.Ci == 32 && p.Co == 32) return launch_tiled<32, 32>(p, s);
   const int BN = p.Co >= 64 ? 64 : p.Co;
   dim3 grid((unsigned)((M + 127) / 128), (unsigned)(p.Co / BN));
   if (BN == 64) k_conv3d<64><<<grid, 128, 0, s>>>(p);

@@ -38,6 +38,9 @@ def _close(torch, got, ref, rel=1e-2, absf=1e-3):
 @pytest.mark.parametrize("shape,Ci,Co,relu", [
     ((2, 4, 6, 10), 16, 16, False), ((1, 3, 7, 9), 32, 64, True), ((1, 5, 5, 13), 64, 128, True),
     ((3, 2, 4, 4), 128, 32, False), ((1, 8, 16, 16), 16, 64, True),
+    # the persistent patch-tiled kernel (16 / 32 channels in and out), ragged tiles
+    ((2, 3, 9, 20), 16, 32, True), ((1, 5, 17, 33), 32, 16, False), ((1, 4, 8, 16), 32, 32, True),
+    ((1, 2, 3, 5), 16, 16, True), ((2, 6, 24, 40), 16, 16, False),
 ])
 def test_conv3d_forward(env, shape, Ci, Co, relu):
     torch, _flf = env
