@@ -67,6 +67,8 @@ _SIGS = {
     "flf_mse_grad": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _I, _P]),
     "flf_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, _F, _F, _F, _F, _F, _F, _F, _P]),
     "flf_render_blobs": (_I, [_P, _I, _I, _I, _P, _I, _F, _P]),
+    "flf_ws_input": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _F, _F, _P]),
+    "flf_ws_head": (_I, [_P, _P, _F, _F, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
 }
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 TUNED_KEYS = ("stages", "chunk_rows_forward", "chunk_rows_backward", "split")
@@ -241,6 +243,24 @@ def render_blobs(vol, pts, sigma, stream=None):
     Z, Y, X = (int(v) for v in vol.shape)
     _check_global(lib.flf_render_blobs(_ptr(vol), Z, Y, X, _ptr(pts), int(pts.shape[0]), float(sigma),
                                        _ptr(stream)))
+
+
+def ws_input(htf, hth1, ht1, sum_x1, out, c2, c3, stream=None):
+    """Warm-start network input [T, Zp, Yp, Xp, 16] from Htf [Z, T, Y, X] (flf_ws_input)."""
+    lib = load_library()
+    Z, T, Y, X = (int(v) for v in htf.shape)
+    Zp, Yp, Xp = (int(v) for v in out.shape[1:4])
+    _check_global(lib.flf_ws_input(_ptr(htf), _ptr(hth1), _ptr(ht1), _ptr(sum_x1), _ptr(out), T, Z, Y, X, Zp, Yp,
+                                   Xp, float(c2), float(c3), _ptr(stream)))
+
+
+def ws_head(d, w, bias, floor, sum_x1, x0, stream=None):
+    """Start volume x0 [Z, T, Y, X] from the last features d (flf_ws_head)."""
+    lib = load_library()
+    T, Zp, Yp, Xp = (int(v) for v in d.shape[:4])
+    Z, _, Y, X = (int(v) for v in x0.shape)
+    _check_global(lib.flf_ws_head(_ptr(d), _ptr(w), float(bias), float(floor), _ptr(sum_x1), _ptr(x0), T, Z, Y, X,
+                                  Zp, Yp, Xp, _ptr(stream)))
 
 
 class RLGraph:

@@ -1648,6 +1648,28 @@ int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts
   return FLF_OK;
 }
 
+int flf_ws_input(const float *htf, const float *hth1, const float *ht1, float *sum_x1, void *out, int T, int Z,
+                 int Y, int X, int Zp, int Yp, int Xp, float c2, float c3, void *stream) {
+  if (!htf || !hth1 || !ht1 || !sum_x1 || !out) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (T <= 0 || Z <= 0 || Y <= 0 || X <= 0 || Zp < Z || Yp < Y || Xp < X || T > 65535)
+    return fail(nullptr, FLF_E_ARG, "invalid warm-start input shape");
+  if (!aligned16(out)) return fail(nullptr, FLF_E_ARG, "network input must be 16-byte aligned");
+  WsInputParams p{htf, hth1, ht1, sum_x1, (__nv_bfloat16 *)out, T, Z, Y, X, Zp, Yp, Xp, (float)Z * Y * X, c2, c3};
+  NET_CHECK(launch_ws_input(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_ws_head(const void *d, const float *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
+                int Y, int X, int Zp, int Yp, int Xp, void *stream) {
+  if (!d || !w || !sum_x1 || !x0) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (T <= 0 || Z <= 0 || Y <= 0 || X <= 0 || Zp < Z || Yp < Y || Xp < X)
+    return fail(nullptr, FLF_E_ARG, "invalid warm-start head shape");
+  if (!aligned16(d)) return fail(nullptr, FLF_E_ARG, "network features must be 16-byte aligned");
+  WsHeadParams p{(const __nv_bfloat16 *)d, w, bias, floor_, sum_x1, (float)Z * Y * X, x0, T, Z, Y, X, Zp, Yp, Xp};
+  NET_CHECK(launch_ws_head(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
 int flf_version(char *buf, size_t len) {
   if (!buf || len == 0) return FLF_E_ARG;
   snprintf(buf, len, "libflf 0.3 sm_103a kernels: k_split k_rfft2_sized k_mac k_irfft2_sized k_merge k_build_k k_rfft2 k_pack k_resample_bilinear k_psf_debye k_psf_lf_input k_psf_lf_bin k_psf_ht k_conv3d k_conv3d_wgrad");

@@ -283,6 +283,26 @@ cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, 
                         float b2, float eps, float c1, float c2, float wd, cudaStream_t s);
 cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,
                                 cudaStream_t s);
+struct WsInputParams {        // warm-start network input from Htf
+  const float *htf;           // [Z][T][Y][X]
+  const float *hth1, *ht1;    // [Z][Y][X]
+  float *sum_x1;              // [T] scratch: frame sums of Htf / HtH1
+  __nv_bfloat16 *out;         // [T][Zp][Yp][Xp][16]
+  int T, Z, Y, X, Zp, Yp, Xp;
+  float count;                // Z * Y * X (frame sums -> means)
+  float c2, c3;               // 1 / mean(HtH1), 1 / mean(Ht1)
+};
+struct WsHeadParams {         // warm-start head: channel 0 of a 3x3x3 conv, clamped and scaled
+  const __nv_bfloat16 *d;     // [T][Zp][Yp][Xp][16]
+  const float *w;             // [27][16]
+  float bias, floor;
+  const float *sum_x1;        // [T] frame sums of Htf / HtH1 (from the input pass)
+  float count;                // Z * Y * X
+  float *x0;                  // [Z][T][Y][X]
+  int T, Z, Y, X, Zp, Yp, Xp;
+};
+cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s);
+cudaError_t launch_ws_head(const WsHeadParams &p, cudaStream_t s);
 cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);

@@ -546,6 +546,100 @@ __global__ void k_render_blobs(float *vol, int Z, int Y, int X, const float4 *pt
   }
 }
 
+// Frame sums of the first RL iterate Htf / HtH1 (Htf [Z][T][Y][X], HtH1 [Z][Y][X]).
+__global__ void __launch_bounds__(256) k_ws_sum(const float *htf, const float *hth1, float *sum, int T, long long V,
+                                                long long YX) {
+  __shared__ float red[8];
+  const int t = blockIdx.y;
+  float part = 0.f;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const long long z = v / YX, yx = v - z * YX;
+    part += htf[(z * T + t) * YX + yx] / hth1[v];
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int w = 0; w < 8; w++) b += red[w];
+    atomicAdd(sum + t, b);
+  }
+}
+
+// Network input, channels-last [T][Zp][Yp][Xp][16] from Htf [Z][T][Y][X]:
+// channel 0 = Htf / HtH1 / m[t] (the first RL iterate over its frame mean m),
+// 1 = Htf / Ht1 / m[t], 2 = HtH1 * c2, 3 = Ht1 * c3, 4..15 = 0; zero in the padding.
+__global__ void __launch_bounds__(256) k_ws_input(WsInputParams p) {
+  const long long n = (long long)p.T * p.Zp * p.Yp * p.Xp;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % p.Xp);
+    long long r = i / p.Xp;
+    const int y = (int)(r % p.Yp);
+    r /= p.Yp;
+    const int z = (int)(r % p.Zp);
+    const int t = (int)(r / p.Zp);
+    __nv_bfloat162 c[8];
+    for (int k = 0; k < 8; k++) c[k] = __floats2bfloat162_rn(0.f, 0.f);
+    if (z < p.Z && y < p.Y && x < p.X) {
+      const long long v = ((long long)z * p.Y + y) * p.X + x;
+      const float h = p.htf[(((long long)z * p.T + t) * p.Y + y) * p.X + x];
+      const float a = p.hth1[v], b = p.ht1[v];
+      const float inv = p.count / fmaxf(p.sum_x1[t], 1e-30f);
+      c[0] = __floats2bfloat162_rn(h / a * inv, h / b * inv);
+      c[1] = __floats2bfloat162_rn(a * p.c2, b * p.c3);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(p.out + i * 16);
+    dst[0] = *reinterpret_cast<uint4 *>(&c[0]);
+    dst[1] = *reinterpret_cast<uint4 *>(&c[4]);
+  }
+}
+
+// Head: x0[z][t][y][x] = max(conv3x3x3(d, w)[channel 0] + bias, floor) * scale[t]
+// for the unpadded voxels; d [T][Zp][Yp][Xp][16] bf16, w [27][16] float.  One
+// thread per output voxel of an 8 x 16 tile, the 3 x 10 x 18 input patch staged
+// in shared memory.
+__global__ void __launch_bounds__(128) k_ws_head(WsHeadParams p, int tiles_x, int tiles_y) {
+  constexpr int PY = 10, PX = 18, PR = 3 * PY * PX;
+  __shared__ __align__(16) bf16 P[PR * 16];
+  __shared__ float W[27 * 16];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 27 * 16; i += 128) W[i] = p.w[i];
+  long long t = blockIdx.x;
+  const int tx = (int)(t % tiles_x);
+  t /= tiles_x;
+  const int ty = (int)(t % tiles_y);
+  t /= tiles_y;
+  const int z = (int)(t % p.Zp), f = (int)(t / p.Zp);
+  const int y0 = ty * 8, x0 = tx * 16;
+  for (int i = tid; i < PR * 2; i += 128) {
+    const int r = i >> 1, c = i & 1;
+    const int pz = r / (PY * PX), py = (r / PX) % PY, px = r % PX;
+    const int gz = z + pz - 1, gy = y0 + py - 1, gx = x0 + px - 1;
+    const bool ok = gz >= 0 && gz < p.Zp && gy >= 0 && gy < p.Yp && gx >= 0 && gx < p.Xp;
+    const bf16 *src = ok ? p.d + ((((long long)f * p.Zp + gz) * p.Yp + gy) * p.Xp + gx) * 16 + c * 8 : p.d;
+    cp16(su32(P + r * 16 + c * 8), src, ok);
+  }
+  cp_commit();
+  cp_wait<0>();
+  __syncthreads();
+  const int yy = tid >> 4, xx = tid & 15;
+  const int y = y0 + yy, x = x0 + xx;
+  if (z >= p.Z || y >= p.Y || x >= p.X) return;
+  float acc = p.bias;
+  for (int tap = 0; tap < 27; tap++) {
+    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+    const __nv_bfloat162 *v = reinterpret_cast<const __nv_bfloat162 *>(P + ((dz * PY + yy + dy) * PX + xx + dx) * 16);
+    const float *w = W + tap * 16;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const float2 q = __bfloat1622float2(v[c]);
+      acc = fmaf(q.x, w[2 * c], acc);
+      acc = fmaf(q.y, w[2 * c + 1], acc);
+    }
+  }
+  p.x0[(((long long)z * p.T + f) * p.Y + y) * p.X + x] = fmaxf(acc, p.floor) * p.sum_x1[f] / p.count;
+}
+
 static unsigned grid_for(long long n, int block) {
   long long g = (n + block - 1) / block;
   return (unsigned)(g < 152LL * 32 ? (g < 1 ? 1 : g) : 152LL * 32);
@@ -654,6 +748,28 @@ cudaError_t launch_mse_grad(const void *y, const float *target, void *g, float *
 cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
                         float b2, float eps, float c1, float c2, float wd, cudaStream_t s) {
   k_adam<<<grid_for(n, 256), 256, 0, s>>>(w, g, m, v, (bf16 *)wb, n, lr, b1, b2, eps, c1, c2, wd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s) {
+  const long long n = (long long)p.T * p.Zp * p.Yp * p.Xp;
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(p.sum_x1, 0, sizeof(float) * p.T, s);
+  if (e != cudaSuccess) return e;
+  const long long V = (long long)p.Z * p.Y * p.X;
+  long long blocks = (V + 2047) / 2048;
+  if (blocks > 1024) blocks = 1024;
+  k_ws_sum<<<dim3((unsigned)blocks, (unsigned)p.T), 256, 0, s>>>(p.htf, p.hth1, p.sum_x1, p.T, V,
+                                                                  (long long)p.Y * p.X);
+  k_ws_input<<<grid_for(n, 256), 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ws_head(const WsHeadParams &p, cudaStream_t s) {
+  const int tiles_x = (p.Xp + 15) / 16, tiles_y = (p.Yp + 7) / 8;
+  const long long n = (long long)p.T * p.Zp * tiles_y * tiles_x;
+  if (n == 0) return cudaSuccess;
+  k_ws_head<<<(unsigned)n, 128, 0, s>>>(p, tiles_x, tiles_y);
   return cudaGetLastError();
 }
 

@@ -1,7 +1,8 @@
 """Learned warm start for Richardson-Lucy: a 3-D U-Net on the normalised back projection.
 
-The network maps ``Htf / Ht1`` (the back projection of the camera image over
-the back projection of ones) to an estimate of the volume; RL then runs from
+The network maps the first RL iterate ``Htf / HtH1`` (with ``Htf / Ht1`` and
+the two sensitivity maps as further input channels) to an estimate of the
+volume; RL then runs from
 that estimate instead of from a uniform volume.  Everything runs on the
 GPU with this package's own kernels (include/flf.h, csrc/flf_net.cu):
 BF16 activations and weights, FP32 accumulation, FP32 master weights and Adam;
@@ -73,6 +74,7 @@ class UNet3D:
             b = torch.zeros(co)
             self.p[name] = {"w": w.to(self.dev), "b": b.to(self.dev), "ci": ci, "co": co, "relu": relu}
         self.adam_t = 0
+        self.loads = 0
         for q in self.p.values():
             q["wb"] = _bf(q["w"].shape, self.dev)
             q["wf"] = _bf((27, q["co"], q["ci"]), self.dev)
@@ -112,8 +114,9 @@ class UNet3D:
         _flf.up2_add(low, skip, y, torch.cuda.current_stream(self.dev).cuda_stream)
         return y
 
-    def forward(self, x):
-        """x [B, Z, Y, X, 16] bf16 (Z, Y, X multiples of 8) -> (out [B, Z, Y, X, 16], cache)."""
+    def forward(self, x, head=True):
+        """x [B, Z, Y, X, 16] bf16 (Z, Y, X multiples of 8) -> (out [B, Z, Y, X, 16], cache);
+        with head=False the last features d0 come back in place of out."""
         a = {"x": x}
         a["e0a"] = self._conv("e0a", x)
         a["e0b"] = self._conv("e0b", a["e0a"])
@@ -135,6 +138,8 @@ class UNet3D:
         a["u0"] = self._conv("u0", a["d1"])
         a["s0"] = self._up_add(a["u0"], a["e0b"])
         a["d0"] = self._conv("d0", a["s0"])
+        if not head:
+            return a["d0"], a
         a["out"] = self._conv("head", a["d0"])
         return a["out"], a
 
@@ -211,6 +216,7 @@ class UNet3D:
         for n, q in self.p.items():
             q["w"].copy_(torch.as_tensor(d["%s.w" % n]))
             q["b"].copy_(torch.as_tensor(d["%s.b" % n]))
+        self.loads += 1
         self._sync_weights()
 
     def save(self, path):
@@ -267,6 +273,15 @@ class WarmStart:
         self.ht1 = torch.empty((self.Z, 1, self.Y, self.X), device=self.dev)
         self.ctx.backward(ones, self.ht1, 1, self.Y, self.X, None, stream=self._s())
         self.ht1.clamp_(min=1e-12)
+        # HtH1 = Ht H 1: the first Prevedel iteration from a uniform volume is Htf / HtH1
+        h1 = torch.empty((1, self.Y, self.X), device=self.dev)
+        self.ctx.forward(torch.ones((self.Z, 1, self.Y, self.X), device=self.dev), h1, 1, self.Y, self.X, None,
+                         stream=self._s())
+        self.hth1 = torch.empty((self.Z, 1, self.Y, self.X), device=self.dev)
+        self.ctx.backward(h1, self.hth1, 1, self.Y, self.X, None, stream=self._s())
+        self.hth1.clamp_(min=1e-12)
+        self.c2 = float(1.0 / self.hth1.mean())
+        self.c3 = float(1.0 / self.ht1.mean())
         self.losses = []
 
     @property
@@ -280,15 +295,16 @@ class WarmStart:
         return torch.cuda.current_stream(self.dev).cuda_stream
 
     def _inputs(self, htf):
-        """Network input (channels-last bf16, padded) and the per-frame scale from
-        Htf [Z, T, Y, X]."""
-        nrm = htf / self.ht1
-        T = htf.shape[1]
-        scale = nrm.reshape(self.Z, T, -1).mean(dim=(0, 2)).clamp_min(1e-12)    # [T]
+        """Network input (channels-last bf16, padded) and the frame sums of the first RL
+        iterate, from Htf [Z, T, Y, X] (flf_ws_input).  Channels: the first RL iterate
+        Htf / HtH1 and Htf / Ht1, both over the frame's mean of the first, and the
+        sensitivity maps HtH1 and Ht1 over their means."""
+        T = int(htf.shape[1])
         Zp, Yp, Xp = self.pad
-        x = torch.zeros((T, Zp, Yp, Xp, CIN), dtype=torch.bfloat16, device=self.dev)
-        x[:, :self.Z, :self.Y, :self.X, 0] = (nrm / scale[None, :, None, None]).permute(1, 0, 2, 3)
-        return x, scale
+        x = torch.empty((T, Zp, Yp, Xp, CIN), dtype=torch.bfloat16, device=self.dev)
+        sums = torch.empty(T, dtype=torch.float32, device=self.dev)
+        _flf.ws_input(htf.contiguous(), self.hth1, self.ht1, sums, x, self.c2, self.c3, self._s())
+        return x, sums / float(self.Z * self.Y * self.X)
 
     def make_batch(self, T, rng):
         """T synthetic (truth [Z, T, Y, X], noisy image [T, Y, X], Htf [Z, T, Y, X])."""
@@ -347,12 +363,23 @@ class WarmStart:
 
     def initial_volume(self, htf, floor=1e-3):
         """RL start volume [Z, T, Y, X] from Htf [Z, T, Y, X] (device): the network's
-        prediction, clamped below at floor x the input mean (RL keeps zeros at zero)."""
-        xin, scale = self._inputs(htf)
-        out, _ = self.net.forward(xin)
-        pred = out[:, :self.Z, :self.Y, :self.X, 0].float().permute(1, 0, 2, 3)
-        x0 = pred.clamp_min(floor) * scale[None, :, None, None]
-        return x0.contiguous()
+        prediction, clamped below at floor x the frame mean of the first RL iterate (RL
+        keeps zeros at zero), written by the head kernel (flf_ws_head)."""
+        htf = htf.contiguous()
+        T = int(htf.shape[1])
+        Zp, Yp, Xp = self.pad
+        xin = torch.empty((T, Zp, Yp, Xp, CIN), dtype=torch.bfloat16, device=self.dev)
+        sums = torch.empty(T, dtype=torch.float32, device=self.dev)
+        _flf.ws_input(htf, self.hth1, self.ht1, sums, xin, self.c2, self.c3, self._s())
+        feats, _ = self.net.forward(xin, head=False)
+        key = (self.net.adam_t, self.net.loads)
+        if getattr(self, "_head_key", None) != key:
+            q = self.net.p["head"]
+            self._head = (q["wb"][:, :, 0].float().contiguous(), float(q["b"][0]))
+            self._head_key = key
+        x0 = torch.empty_like(htf)
+        _flf.ws_head(feats, self._head[0], self._head[1], floor, sums, x0, self._s())
+        return x0
 
 
 def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):

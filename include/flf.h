@@ -251,6 +251,17 @@ int flf_mse_grad(const void *y, const float *target, void *g, float *loss, long 
 int flf_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1, float b2,
              float eps, float c1, float c2, float wd, void *stream);
 int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *stream);
+/* Warm-start inference glue.  flf_ws_input: network input [T][Zp][Yp][Xp][16]
+ * bf16 from Htf [Z][T][Y][X] float and the sensitivity maps HtH1, Ht1
+ * [Z][Y][X]: channel 0 = Htf / HtH1 / m_t (m_t = frame mean of Htf / HtH1,
+ * whose sums are left in sum_x1 [T]), 1 = Htf / Ht1 / m_t, 2 = HtH1 * c2,
+ * 3 = Ht1 * c3, others and the padding 0.  flf_ws_head: the start volume
+ * x0 [Z][T][Y][X] = max(conv3x3x3(d, w)[0] + bias, floor) * m_t from the last
+ * features d [T][Zp][Yp][Xp][16] and the head's channel-0 weights w [27][16]. */
+int flf_ws_input(const float *htf, const float *hth1, const float *ht1, float *sum_x1, void *out, int T, int Z,
+                 int Y, int X, int Zp, int Yp, int Xp, float c2, float c3, void *stream);
+int flf_ws_head(const void *d, const float *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
+                int Y, int X, int Zp, int Yp, int Xp, void *stream);
 
 /* CUDA graph of a whole RL run (the replay form of flf_rl_iterate): the
  * launches of `iters` iterations over T frames of Y x X images are captured

@@ -109,3 +109,37 @@ def test_training_and_warm_started_rl(env):
     p.RichardsonLucy(hm, xu, htf, 8)
     xw = ws_mod.DeconvRLWarm(ws, img, 8)
     assert resid(xw) <= 1.01 * resid(xu)
+
+
+def test_fused_input_and_head_kernels(env):
+    """flf_ws_input / flf_ws_head against their torch formulas."""
+    torch, ws_mod = env
+    import _flf
+    g = torch.Generator().manual_seed(11)
+    Z, T, Y, X = 5, 2, 13, 21
+    Zp, Yp, Xp = 8, 16, 24
+    htf = (torch.rand((Z, T, Y, X), generator=g) + 0.5).cuda()
+    hth1 = (torch.rand((Z, 1, Y, X), generator=g) + 0.2).cuda()
+    ht1 = (torch.rand((Z, 1, Y, X), generator=g) + 0.2).cuda()
+    c2, c3 = 1.0 / float(hth1.mean()), 1.0 / float(ht1.mean())
+    out = torch.empty((T, Zp, Yp, Xp, 16), dtype=torch.bfloat16, device="cuda")
+    sums = torch.empty(T, device="cuda")
+    _flf.ws_input(htf, hth1, ht1, sums, out, c2, c3)
+    x1 = htf / hth1
+    m = x1.reshape(Z, T, -1).mean(dim=(0, 2))
+    assert float((sums / (Z * Y * X) - m).abs().max()) <= 1e-5 * float(m.abs().max())
+    ref = torch.zeros((T, Zp, Yp, Xp, 16), device="cuda")
+    ref[:, :Z, :Y, :X, 0] = (x1 / m[None, :, None, None]).permute(1, 0, 2, 3)
+    ref[:, :Z, :Y, :X, 1] = (htf / ht1 / m[None, :, None, None]).permute(1, 0, 2, 3)
+    ref[:, :Z, :Y, :X, 2] = (hth1 * c2).permute(1, 0, 2, 3)
+    ref[:, :Z, :Y, :X, 3] = (ht1 * c3).permute(1, 0, 2, 3)
+    assert float((out.float() - ref).abs().max()) <= 1e-2 * float(ref.abs().max())
+    d = torch.rand((T, Zp, Yp, Xp, 16), generator=g).bfloat16().cuda()
+    w = torch.randn((27, 16), generator=g).cuda() / 20
+    x0 = torch.empty((Z, T, Y, X), device="cuda")
+    _flf.ws_head(d, w, 0.1, 1e-3, sums, x0)
+    W = w.double().cpu().reshape(3, 3, 3, 16).permute(3, 0, 1, 2)[None]
+    conv = torch.nn.functional.conv3d(d.double().cpu().permute(0, 4, 1, 2, 3), W, padding=1)[:, 0] + 0.1
+    want = conv.clamp_min(1e-3)[:, :Z, :Y, :X].permute(1, 0, 2, 3) * (sums.double().cpu() / (Z * Y * X))[None, :,
+                                                                                                         None, None]
+    assert float((x0.double().cpu() - want).abs().max()) <= 1e-4 * float(want.abs().max())
