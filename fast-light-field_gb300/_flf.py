@@ -56,7 +56,7 @@ _SIGS = {
     "flf_psf_lf_input": (_I, [_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_lf_bin": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
-    "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
     "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
     "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P]),
@@ -176,13 +176,15 @@ def _vshape(t):
     return B, Z, Y, X, C
 
 
-def conv3d(x, w, bias, y, relu=False, mask=None, stream=None):
-    """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16."""
+def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
+    """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16;
+    ws: optional float32 workspace (at least B*Z*Y*X*Co elements) for split-K layers."""
     lib = load_library()
     B, Z, Y, X, Ci = _vshape(x)
     Co = int(y.shape[-1])
     _check_global(lib.flf_conv3d(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X, Ci, Co,
-                                 int(bool(relu)), _ptr(stream)))
+                                 int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0,
+                                 _ptr(stream)))
 
 
 def conv3d_wgrad(x, dy, dw, stream=None):

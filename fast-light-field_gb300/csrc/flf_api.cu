@@ -1557,15 +1557,16 @@ static int net_shape(int B, int Z, int Y, int X, int C) {
   } while (0)
 
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, void *stream) {
+               int Ci, int Co, int relu, float *ws, long long ws_elems, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
   if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
   if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
     return fail(nullptr, FLF_E_ARG, "volumes and weights must be 16-byte aligned");
+  if (ws && !aligned16(ws)) return fail(nullptr, FLF_E_ARG, "workspace must be 16-byte aligned");
   ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
-               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0};
-  NET_CHECK(launch_conv3d(p, (cudaStream_t)stream));
+               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0, ws, 1};
+  NET_CHECK(launch_conv3d(p, ws ? ws_elems : 0, (cudaStream_t)stream));
   return FLF_OK;
 }
 
@@ -1659,14 +1660,13 @@ int flf_ws_input(const float *htf, const float *hth1, const float *ht1, float *s
   return FLF_OK;
 }
 
-int flf_ws_head(const void *d, const float *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
+int flf_ws_head(const void *d, const void *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
                 int Y, int X, int Zp, int Yp, int Xp, void *stream) {
   if (!d || !w || !sum_x1 || !x0) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (T <= 0 || Z <= 0 || Y <= 0 || X <= 0 || Zp < Z || Yp < Y || Xp < X)
     return fail(nullptr, FLF_E_ARG, "invalid warm-start head shape");
-  if (!aligned16(d)) return fail(nullptr, FLF_E_ARG, "network features must be 16-byte aligned");
-  WsHeadParams p{(const __nv_bfloat16 *)d, w, bias, floor_, sum_x1, (float)Z * Y * X, x0, T, Z, Y, X, Zp, Yp, Xp};
-  NET_CHECK(launch_ws_head(p, (cudaStream_t)stream));
+  if (!aligned16(d) || !aligned16(w)) return fail(nullptr, FLF_E_ARG, "features and weights must be 16-byte aligned");
+  NET_CHECK(launch_ws_head(d, w, bias, floor_, sum_x1, x0, T, Z, Y, X, Zp, Yp, Xp, (cudaStream_t)stream));
   return FLF_OK;
 }
 

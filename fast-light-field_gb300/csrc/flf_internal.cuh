@@ -258,6 +258,8 @@ struct ConvParams {          // y = act(conv3x3x3(x, w) + bias) (* (mask > 0))
   const __nv_bfloat16 *mask; // [M][Co] or null
   __nv_bfloat16 *y;          // [M][Co]
   int B, Z, Y, X, Ci, Co, relu;
+  float *ws;                 // [M][Co] FP32 partial sums when the K loop is split (splits > 1)
+  int splits;
 };
 struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co]
   const __nv_bfloat16 *x;
@@ -266,7 +268,7 @@ struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co
   int B, Z, Y, X, Ci, Co;
   long long chunk;           // voxels per CTA (set by the launcher)
 };
-cudaError_t launch_conv3d(const ConvParams &p, cudaStream_t s);
+cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
 cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms);
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s);
 cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s);
@@ -292,17 +294,16 @@ struct WsInputParams {        // warm-start network input from Htf
   float count;                // Z * Y * X (frame sums -> means)
   float c2, c3;               // 1 / mean(HtH1), 1 / mean(Ht1)
 };
-struct WsHeadParams {         // warm-start head: channel 0 of a 3x3x3 conv, clamped and scaled
-  const __nv_bfloat16 *d;     // [T][Zp][Yp][Xp][16]
-  const float *w;             // [27][16]
+struct HeadOut {              // warm-start head output (k_conv3d_t16<true>)
+  float *x0;                  // [Zr][T][Yr][Xr] start volume
+  const float *sum_x1;        // [T] frame sums of Htf / HtH1
+  float count;                // Zr * Yr * Xr
   float bias, floor;
-  const float *sum_x1;        // [T] frame sums of Htf / HtH1 (from the input pass)
-  float count;                // Z * Y * X
-  float *x0;                  // [Z][T][Y][X]
-  int T, Z, Y, X, Zp, Yp, Xp;
+  int T, Zr, Yr, Xr;
 };
 cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s);
-cudaError_t launch_ws_head(const WsHeadParams &p, cudaStream_t s);
+cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor_, const float *sum_x1, float *x0,
+                           int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s);
 cudaError_t launch_merge(const MergeParams &p, cudaStream_t s);
 cudaError_t launch_mac(const MacParams &p, bool forward, cudaStream_t s);
 cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);

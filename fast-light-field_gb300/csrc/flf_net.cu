@@ -11,6 +11,9 @@
 //   k_conv3d_tiled    the same for 16 / 32 channels in and out: persistent
 //                     CTAs with the weights resident in shared memory and
 //                     one staged input patch per output tile for all taps.
+//   k_conv3d_t16      16 -> 16 channels: 16 x 16-voxel tiles, 4 rows per warp,
+//                     one z slice of weight fragments in registers at a time;
+//                     with HEAD, the warm-start head writing the start volume.
 //   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
 //                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
 //                     split-K over its 4 warps, FP32 atomics into dW.
@@ -93,9 +96,12 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
   const bool rowok = mrow < M;
   const Vox v = decode(rowok ? mrow : 0, p.Z, p.Y, p.X);
   const int cch = p.Ci / 16;
-  const int KS = 27 * cch;
+  const int KT = 27 * cch;
+  const int kb = (int)((long long)blockIdx.z * KT / p.splits), ke = (int)((long long)(blockIdx.z + 1) * KT / p.splits);
+  const int KS = ke - kb;
 
-  auto load = [&](int ks, int st) {
+  auto load = [&](int kr, int st) {
+    const int ks = kb + kr;
     const int tap = ks / cch, c0 = (ks - tap * cch) * 16;
     const int z = v.z + tap / 9 - 1, y = v.y + (tap / 3) % 3 - 1, x = v.x + tap % 3 - 1;
     const bool ok = rowok && z >= 0 && z < p.Z && y >= 0 && y < p.Y && x >= 0 && x < p.X;
@@ -154,6 +160,21 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
   }
   cp_wait<0>();
 
+  if (p.splits > 1) {   // partial sums of this CTA's K range
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+      for (int nt = 0; nt < BN / 8; nt++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const long long row = m0 + warp * 32 + mt * 16 + (lane >> 2) + 8 * h;
+          if (row >= M) continue;
+          const int col = n0 + nt * 8 + 2 * (lane & 3);
+          atomicAdd(reinterpret_cast<float2 *>(p.ws + row * p.Co + col),
+                    make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
+        }
+    return;
+  }
 #pragma unroll
   for (int mt = 0; mt < 2; mt++)
 #pragma unroll
@@ -183,16 +204,16 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
 // Persistent variant for the wide, shallow layers (Ci, Co in {16, 32}): all
 // 27 x Ci x Co weights stay in shared memory; each CTA walks output tiles of
 // one z slice, 8 rows x 16 columns, staging the 3 x 10 x 18 input patch of a
-// tile (double-buffered with cp.async) and reading every tap's A fragments
+// tile (one buffer; two CTAs per SM overlap loads and math) and reading every tap's A fragments
 // straight from the patch with shifted ldmatrix row addresses.  Each input
 // voxel is fetched about 4 times instead of 27.
 template <int CI, int CO>
-__global__ void __launch_bounds__(128) k_conv3d_tiled(ConvParams p, int tiles_x, int tiles_y, long long ntiles) {
+__global__ void __launch_bounds__(128, 2) k_conv3d_tiled(ConvParams p, int tiles_x, int tiles_y, long long ntiles) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PY = 10, PX = 18, PR = 3 * PY * PX;
   constexpr int RA = CI / 8, RB = CO / 8;
   bf16 *Ws = reinterpret_cast<bf16 *>(smem);     // [27 * CI][CO]
-  bf16 *Ps = Ws + 27 * CI * CO;                   // [2][PR][CI]
+  bf16 *Ps = Ws + 27 * CI * CO;                   // [PR][CI] (one buffer: several CTAs per SM overlap)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int i = tid; i < 27 * CI * RB; i += 128) {
@@ -224,17 +245,12 @@ __global__ void __launch_bounds__(128) k_conv3d_tiled(ConvParams p, int tiles_x,
   };
 
   const int mat = lane >> 3, r8 = lane & 7;
-  long long t = blockIdx.x;
-  int buf = 0;
-  if (t < ntiles) load_patch(t, 0);
-  cp_commit();
-  for (; t < ntiles; t += gridDim.x) {
-    const long long nt_ = t + gridDim.x;
-    if (nt_ < ntiles) load_patch(nt_, buf ^ 1);
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    load_patch(t, 0);
     cp_commit();
-    cp_wait<1>();
+    cp_wait<0>();
     __syncthreads();
-    const bf16 *P = Ps + buf * PR * CI;
+    const bf16 *P = Ps;
     float acc[2][CO / 8][4];
 #pragma unroll
     for (int i = 0; i < 2; i++)
@@ -269,6 +285,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tiled(ConvParams p, int tiles_x,
         }
       }
     }
+    __syncthreads();   // the patch is refilled for the next tile
     int b, z, y0, x0;
     tile_pos(t, b, z, y0, x0);
 #pragma unroll
@@ -296,8 +313,124 @@ __global__ void __launch_bounds__(128) k_conv3d_tiled(ConvParams p, int tiles_x,
           *reinterpret_cast<__nv_bfloat162 *>(p.y + o) = __floats2bfloat162_rn(v0, v1);
         }
       }
-    __syncthreads();   // the next iteration refills this buffer
-    buf ^= 1;
+  }
+  cp_wait<0>();
+}
+
+// 16 -> 16 channels (the full-resolution layers).  A tile is 16 rows x 16
+// columns of one z slice, 4 rows per warp (8 independent accumulator chains),
+// staged as a 3 x 18 x 18 input patch; the weights stay in shared memory and
+// the B fragments of one z slice of taps (9 taps) are held in registers while
+// they are used.  Single-buffered patches keep shared memory and registers low
+// enough for several CTAs per SM, whose loads overlap one another's math.
+// HEAD: the warm-start head -- only output channel 0 is kept, written as the
+// start volume max(v + bias, floor) * mean_t into x0 [Zr][T][Yr][Xr].
+template <bool HEAD>
+__global__ void __launch_bounds__(128, 4) k_conv3d_t16(ConvParams p, HeadOut h, int tiles_x, int tiles_y,
+                                                       long long ntiles) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int PY = 18, PX = 18, PR = 3 * PY * PX;
+  bf16 *Ws = reinterpret_cast<bf16 *>(smem);     // [27 * 16][16]
+  bf16 *P = Ws + 27 * 16 * 16;                    // [PR][16]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < 27 * 16 * 2; i += 128) {
+    const int row = i >> 1, c = i & 1;
+    cp16(su32(Ws + row * 16) + ((c ^ swz<2>(row)) << 4), p.w + (long long)row * 16 + c * 8, true);
+  }
+  cp_commit();
+  const int mat = lane >> 3, r8 = lane & 7;
+  const int xx = r8 + 8 * (mat & 1), chunk = mat >> 1;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    long long q = t;
+    const int tx = (int)(q % tiles_x);
+    q /= tiles_x;
+    const int ty = (int)(q % tiles_y);
+    q /= tiles_y;
+    const int z = (int)(q % p.Z), b = (int)(q / p.Z);
+    const int y0 = ty * 16, x0 = tx * 16;
+    for (int i = tid; i < PR * 2; i += 128) {
+      const int r = i >> 1, c = i & 1;
+      const int pz = r / (PY * PX), py = (r / PX) % PY, px = r % PX;
+      const int gz = z + pz - 1, gy = y0 + py - 1, gx = x0 + px - 1;
+      const bool ok = gz >= 0 && gz < p.Z && gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X;
+      const bf16 *src = ok ? p.x + ((((long long)b * p.Z + gz) * p.Y + gy) * p.X + gx) * 16 + c * 8 : p.x;
+      cp16(su32(P + r * 16) + ((c ^ swz<2>(r)) << 4), src, ok);
+    }
+    cp_commit();
+    cp_wait<0>();
+    __syncthreads();
+    float acc[4][2][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+#pragma unroll 1
+    for (int dz = 0; dz < 3; dz++) {
+      uint32_t bw[9][4];
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const int row = (dz * 9 + k) * 16 + r8 + 8 * (mat & 1);
+        ldsm4t(su32(Ws + row * 16) + (((mat >> 1) ^ swz<2>(row)) << 4), bw[k][0], bw[k][1], bw[k][2], bw[k][3]);
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const int dy = k / 3, dx = k % 3;
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) {
+          const int pr = (dz * PY + 4 * warp + mt + dy) * PX + xx + dx;
+          uint32_t a[4];
+          ldsm4(su32(P + pr * 16) + ((chunk ^ swz<2>(pr)) << 4), a[0], a[1], a[2], a[3]);
+          mma_bf16(acc[mt][0], a, bw[k][0], bw[k][1]);
+          if (!HEAD) mma_bf16(acc[mt][1], a, bw[k][2], bw[k][3]);
+        }
+      }
+    }
+    __syncthreads();   // the patch is refilled for the next tile
+    if (HEAD) {
+      // channel 0 sits in lanes with (lane & 3) == 0: rows lane/4 and lane/4 + 8
+      if ((lane & 3) == 0 && b < h.T && z < h.Zr) {
+        const float sc = h.sum_x1[b] / h.count;
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) {
+          const int y = y0 + 4 * warp + mt;
+#pragma unroll
+          for (int hh = 0; hh < 2; hh++) {
+            const int x = x0 + (lane >> 2) + 8 * hh;
+            if (y >= h.Yr || x >= h.Xr) continue;
+            const float v = acc[mt][0][2 * hh] + h.bias;
+            h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(v, h.floor) * sc;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+      for (int nt = 0; nt < 2; nt++) {
+        const int col = nt * 8 + 2 * (lane & 3);
+        const float b0 = p.bias ? p.bias[col] : 0.f, b1 = p.bias ? p.bias[col + 1] : 0.f;
+        const int y = y0 + 4 * warp + mt;
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          const int x = x0 + (lane >> 2) + 8 * hh;
+          if (y >= p.Y || x >= p.X) continue;
+          float v0 = acc[mt][nt][2 * hh] + b0, v1 = acc[mt][nt][2 * hh + 1] + b1;
+          if (p.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          const long long o = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16 + col;
+          if (p.mask) {
+            const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(p.mask + o);
+            if (!(__bfloat162float(mk.x) > 0.f)) v0 = 0.f;
+            if (!(__bfloat162float(mk.y) > 0.f)) v1 = 0.f;
+          }
+          *reinterpret_cast<__nv_bfloat162 *>(p.y + o) = __floats2bfloat162_rn(v0, v1);
+        }
+      }
+    }
   }
   cp_wait<0>();
 }
@@ -437,65 +570,161 @@ __global__ void k_bias_grad(const bf16 *g, float *db, long long M, int C, long l
   atomicAdd(db + c, s);
 }
 
-// out[b][z][y][x][c] = mean of the 2x2x2 block of in (Z, Y, X even)
-__global__ void k_pool2(const bf16 *in, bf16 *out, int B, int Z, int Y, int X, int C) {
-  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2;
-  const long long n = (long long)B * Zo * Yo * Xo * C;
+// Epilogue of a split convolution: y = act(ws + bias) (* (mask > 0)), 8 channels per thread.
+__global__ void k_conv3d_finish(ConvParams p, long long M) {
+  const int G = p.Co / 8;
+  const long long n = M * G;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const Vox o = decode(i / C, Zo, Yo, Xo);
-    float s = 0.f;
-    for (int d = 0; d < 8; d++) {
-      const long long src = ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X +
-                             2 * o.x + (d & 1)) * C + c;
-      s += __bfloat162float(in[src]);
+    const int c0 = (int)(i % G) * 8;
+    const long long o = (i / G) * p.Co + c0;
+    const float4 a = *reinterpret_cast<const float4 *>(p.ws + o);
+    const float4 b = *reinterpret_cast<const float4 *>(p.ws + o + 4);
+    float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    uint4 mk;
+    if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + o);
+    const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
+    uint4 u;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      float v0 = v[2 * k] + (p.bias ? p.bias[c0 + 2 * k] : 0.f);
+      float v1 = v[2 * k + 1] + (p.bias ? p.bias[c0 + 2 * k + 1] : 0.f);
+      if (p.relu) {
+        v0 = fmaxf(v0, 0.f);
+        v1 = fmaxf(v1, 0.f);
+      }
+      if (p.mask) {
+        const float2 mf = __bfloat1622float2(m2[k]);
+        if (!(mf.x > 0.f)) v0 = 0.f;
+        if (!(mf.y > 0.f)) v1 = 0.f;
+      }
+      h[k] = __floats2bfloat162_rn(v0, v1);
     }
-    out[i] = __float2bfloat16_rn(0.125f * s);
+    *reinterpret_cast<uint4 *>(p.y + o) = u;
+  }
+}
+
+// 8 BF16 channels as one 16-byte vector.
+struct V8 {
+  float v[8];
+  __device__ __forceinline__ void load(const bf16 *p) {
+    const uint4 u = *reinterpret_cast<const uint4 *>(p);
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float2 f = __bfloat1622float2(h[k]);
+      v[2 * k] = f.x;
+      v[2 * k + 1] = f.y;
+    }
+  }
+  __device__ __forceinline__ void store(bf16 *p) const {
+    uint4 u;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; k++) h[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    *reinterpret_cast<uint4 *>(p) = u;
+  }
+};
+
+__device__ __forceinline__ long long half_index(const Vox &v, int Z, int Y, int X, int C) {
+  return ((((long long)v.b * (Z / 2) + v.z / 2) * (Y / 2) + v.y / 2) * (X / 2) + v.x / 2) * C;
+}
+
+// out[b][z][y][x][c] = mean of the 2x2x2 block of in (Z, Y, X even); one thread
+// per output voxel and 8 channels.
+__global__ void k_pool2(const bf16 *in, bf16 *out, int B, int Z, int Y, int X, int C) {
+  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2, G = C / 8;
+  const long long n = (long long)B * Zo * Yo * Xo * G;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(i % G);
+    const Vox o = decode(i / G, Zo, Yo, Xo);
+    V8 acc;
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc.v[k] = 0.f;
+    for (int d = 0; d < 8; d++) {
+      V8 q;
+      q.load(in + ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X + 2 * o.x + (d & 1)) *
+                      C + g * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc.v[k] += q.v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc.v[k] *= 0.125f;
+    acc.store(out + (i / G) * C + g * 8);
   }
 }
 
 // Adjoint of k_pool2 plus a second gradient, under a ReLU mask:
-// gin[v] = (gpool[v/2] / 8 + gskip[v]) * (act[v] > 0)   (gskip may be null)
+// gin[v] = (gpool[v/2] / 8 + gskip[v]) * (act[v] > 0)   (gskip, act may be null)
 __global__ void k_pool2_bwd(const bf16 *gpool, const bf16 *gskip, const bf16 *act, bf16 *gin, int B, int Z, int Y,
                             int X, int C) {
-  const long long n = (long long)B * Z * Y * X * C;
+  const int G = C / 8;
+  const long long n = (long long)B * Z * Y * X * G;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const Vox v = decode(i / C, Z, Y, X);
-    const long long o = ((((long long)v.b * (Z / 2) + v.z / 2) * (Y / 2) + v.y / 2) * (X / 2) + v.x / 2) * C + c;
-    float g = 0.125f * __bfloat162float(gpool[o]);
-    if (gskip) g += __bfloat162float(gskip[i]);
-    if (act && !(__bfloat162float(act[i]) > 0.f)) g = 0.f;
-    gin[i] = __float2bfloat16_rn(g);
+    const int g = (int)(i % G);
+    const long long vox = i / G;
+    const Vox v = decode(vox, Z, Y, X);
+    V8 r, q;
+    r.load(gpool + half_index(v, Z, Y, X, C) + g * 8);
+#pragma unroll
+    for (int k = 0; k < 8; k++) r.v[k] *= 0.125f;
+    if (gskip) {
+      q.load(gskip + vox * C + g * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++) r.v[k] += q.v[k];
+    }
+    if (act) {
+      q.load(act + vox * C + g * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if (!(q.v[k] > 0.f)) r.v[k] = 0.f;
+    }
+    r.store(gin + vox * C + g * 8);
   }
 }
 
 // out[v] = low[v/2] + skip[v]  (nearest 2x2x2 upsampling; low has C channels)
 __global__ void k_up2_add(const bf16 *low, const bf16 *skip, bf16 *out, int B, int Z, int Y, int X, int C) {
-  const long long n = (long long)B * Z * Y * X * C;
+  const int G = C / 8;
+  const long long n = (long long)B * Z * Y * X * G;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const Vox v = decode(i / C, Z, Y, X);
-    const long long o = ((((long long)v.b * (Z / 2) + v.z / 2) * (Y / 2) + v.y / 2) * (X / 2) + v.x / 2) * C + c;
-    out[i] = __float2bfloat16_rn(__bfloat162float(low[o]) + (skip ? __bfloat162float(skip[i]) : 0.f));
+    const int g = (int)(i % G);
+    const long long vox = i / G;
+    const Vox v = decode(vox, Z, Y, X);
+    V8 r, q;
+    r.load(low + half_index(v, Z, Y, X, C) + g * 8);
+    if (skip) {
+      q.load(skip + vox * C + g * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++) r.v[k] += q.v[k];
+    }
+    r.store(out + vox * C + g * 8);
   }
 }
 
 // Adjoint of the upsampling: glow[u] = sum of g over its 2x2x2 block, times (act[u] > 0)
 __global__ void k_up2_bwd(const bf16 *g, const bf16 *act, bf16 *glow, int B, int Z, int Y, int X, int C) {
-  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2;
-  const long long n = (long long)B * Zo * Yo * Xo * C;
+  const int Zo = Z / 2, Yo = Y / 2, Xo = X / 2, G = C / 8;
+  const long long n = (long long)B * Zo * Yo * Xo * G;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const Vox o = decode(i / C, Zo, Yo, Xo);
-    float s = 0.f;
+    const int gi = (int)(i % G);
+    const Vox o = decode(i / G, Zo, Yo, Xo);
+    V8 acc, q;
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc.v[k] = 0.f;
     for (int d = 0; d < 8; d++) {
-      const long long src = ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X +
-                             2 * o.x + (d & 1)) * C + c;
-      s += __bfloat162float(g[src]);
+      q.load(g + ((((long long)o.b * Z + 2 * o.z + (d >> 2)) * Y + 2 * o.y + ((d >> 1) & 1)) * X + 2 * o.x + (d & 1)) *
+                     C + gi * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc.v[k] += q.v[k];
     }
-    if (act && !(__bfloat162float(act[i]) > 0.f)) s = 0.f;
-    glow[i] = __float2bfloat16_rn(s);
+    if (act) {
+      q.load(act + (i / G) * C + gi * 8);
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if (!(q.v[k] > 0.f)) acc.v[k] = 0.f;
+    }
+    acc.store(glow + (i / G) * C + gi * 8);
   }
 }
 
@@ -594,52 +823,6 @@ __global__ void __launch_bounds__(256) k_ws_input(WsInputParams p) {
   }
 }
 
-// Head: x0[z][t][y][x] = max(conv3x3x3(d, w)[channel 0] + bias, floor) * scale[t]
-// for the unpadded voxels; d [T][Zp][Yp][Xp][16] bf16, w [27][16] float.  One
-// thread per output voxel of an 8 x 16 tile, the 3 x 10 x 18 input patch staged
-// in shared memory.
-__global__ void __launch_bounds__(128) k_ws_head(WsHeadParams p, int tiles_x, int tiles_y) {
-  constexpr int PY = 10, PX = 18, PR = 3 * PY * PX;
-  __shared__ __align__(16) bf16 P[PR * 16];
-  __shared__ float W[27 * 16];
-  const int tid = threadIdx.x;
-  for (int i = tid; i < 27 * 16; i += 128) W[i] = p.w[i];
-  long long t = blockIdx.x;
-  const int tx = (int)(t % tiles_x);
-  t /= tiles_x;
-  const int ty = (int)(t % tiles_y);
-  t /= tiles_y;
-  const int z = (int)(t % p.Zp), f = (int)(t / p.Zp);
-  const int y0 = ty * 8, x0 = tx * 16;
-  for (int i = tid; i < PR * 2; i += 128) {
-    const int r = i >> 1, c = i & 1;
-    const int pz = r / (PY * PX), py = (r / PX) % PY, px = r % PX;
-    const int gz = z + pz - 1, gy = y0 + py - 1, gx = x0 + px - 1;
-    const bool ok = gz >= 0 && gz < p.Zp && gy >= 0 && gy < p.Yp && gx >= 0 && gx < p.Xp;
-    const bf16 *src = ok ? p.d + ((((long long)f * p.Zp + gz) * p.Yp + gy) * p.Xp + gx) * 16 + c * 8 : p.d;
-    cp16(su32(P + r * 16 + c * 8), src, ok);
-  }
-  cp_commit();
-  cp_wait<0>();
-  __syncthreads();
-  const int yy = tid >> 4, xx = tid & 15;
-  const int y = y0 + yy, x = x0 + xx;
-  if (z >= p.Z || y >= p.Y || x >= p.X) return;
-  float acc = p.bias;
-  for (int tap = 0; tap < 27; tap++) {
-    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-    const __nv_bfloat162 *v = reinterpret_cast<const __nv_bfloat162 *>(P + ((dz * PY + yy + dy) * PX + xx + dx) * 16);
-    const float *w = W + tap * 16;
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const float2 q = __bfloat1622float2(v[c]);
-      acc = fmaf(q.x, w[2 * c], acc);
-      acc = fmaf(q.y, w[2 * c + 1], acc);
-    }
-  }
-  p.x0[(((long long)z * p.T + f) * p.Y + y) * p.X + x] = fmaxf(acc, p.floor) * p.sum_x1[f] / p.count;
-}
-
 static unsigned grid_for(long long n, int block) {
   long long g = (n + block - 1) / block;
   return (unsigned)(g < 152LL * 32 ? (g < 1 ? 1 : g) : 152LL * 32);
@@ -648,7 +831,7 @@ static unsigned grid_for(long long n, int block) {
 template <int CI, int CO>
 static cudaError_t launch_tiled(const ConvParams &p, cudaStream_t s) {
   static int grid_cap = 0;
-  const size_t smem = sizeof(bf16) * (27 * CI * CO + 2 * 540 * CI);
+  const size_t smem = sizeof(bf16) * (27 * CI * CO + 540 * CI);
   if (!grid_cap) {
     cudaError_t e = cudaFuncSetAttribute(k_conv3d_tiled<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -667,18 +850,60 @@ static cudaError_t launch_tiled(const ConvParams &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_conv3d(const ConvParams &p, cudaStream_t s) {
+template <bool HEAD>
+static cudaError_t launch_t16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
+  static int grid_cap = 0;
+  const size_t smem = sizeof(bf16) * (27 * 16 * 16 + 972 * 16);
+  if (!grid_cap) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_t16<HEAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, dev = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_t16<HEAD>, 128, smem);
+    if (e != cudaSuccess) return e;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid_cap = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  }
+  const int tiles_x = (p.X + 15) / 16, tiles_y = (p.Y + 15) / 16;
+  const long long ntiles = (long long)p.B * p.Z * tiles_y * tiles_x;
+  const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
+  k_conv3d_t16<HEAD><<<grid, 128, smem, s>>>(p, h, tiles_x, tiles_y, ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
   const long long M = (long long)p.B * p.Z * p.Y * p.X;
   if (M == 0) return cudaSuccess;
-  if (p.Ci == 16 && p.Co == 16) return launch_tiled<16, 16>(p, s);
+  p.splits = 1;
+  if (p.Ci == 16 && p.Co == 16) return launch_t16<false>(p, HeadOut{}, s);
   if (p.Ci == 16 && p.Co == 32) return launch_tiled<16, 32>(p, s);
   if (p.Ci == 32 && p.Co == 16) return launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32) return launch_tiled<32, 32>(p, s);
   const int BN = p.Co >= 64 ? 64 : p.Co;
-  dim3 grid((unsigned)((M + 127) / 128), (unsigned)(p.Co / BN));
+  const long long ctas = (M + 127) / 128 * (p.Co / BN);
+  const int KT = 27 * (p.Ci / 16);
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  // few CTAs with long K loops (the coarse levels): split K over up to 3 waves
+  if (p.ws && ws_elems >= M * p.Co && ctas < 2LL * sms) {
+    long long sp = (3LL * sms + ctas - 1) / ctas;
+    if (sp > KT / 8) sp = KT / 8;
+    if (sp > 1) p.splits = (int)sp;
+  }
+  if (p.splits > 1) {
+    cudaError_t e = cudaMemsetAsync(p.ws, 0, sizeof(float) * M * p.Co, s);
+    if (e != cudaSuccess) return e;
+  }
+  dim3 grid((unsigned)((M + 127) / 128), (unsigned)(p.Co / BN), (unsigned)p.splits);
   if (BN == 64) k_conv3d<64><<<grid, 128, 0, s>>>(p);
   else if (BN == 32) k_conv3d<32><<<grid, 128, 0, s>>>(p);
   else k_conv3d<16><<<grid, 128, 0, s>>>(p);
+  if (p.splits > 1) k_conv3d_finish<<<grid_for(M * p.Co / 8, 256), 256, 0, s>>>(p, M);
   return cudaGetLastError();
 }
 
@@ -714,27 +939,27 @@ cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaS
 }
 
 cudaError_t launch_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, cudaStream_t s) {
-  k_pool2<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)in, (bf16 *)out, B, Z, Y, X, C);
+  k_pool2<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)in, (bf16 *)out, B, Z, Y, X, C);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y,
                              int X, int C, cudaStream_t s) {
-  k_pool2_bwd<<<grid_for((long long)B * Z * Y * X * C, 256), 256, 0, s>>>(
+  k_pool2_bwd<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>(
       (const bf16 *)gpool, (const bf16 *)gskip, (const bf16 *)act, (bf16 *)gin, B, Z, Y, X, C);
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C,
                            cudaStream_t s) {
-  k_up2_add<<<grid_for((long long)B * Z * Y * X * C, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
+  k_up2_add<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
                                                                           (bf16 *)out, B, Z, Y, X, C);
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C,
                            cudaStream_t s) {
-  k_up2_bwd<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)g, (const bf16 *)act,
+  k_up2_bwd<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)g, (const bf16 *)act,
                                                                               (bf16 *)glow, B, Z, Y, X, C);
   return cudaGetLastError();
 }
@@ -765,12 +990,11 @@ cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ws_head(const WsHeadParams &p, cudaStream_t s) {
-  const int tiles_x = (p.Xp + 15) / 16, tiles_y = (p.Yp + 7) / 8;
-  const long long n = (long long)p.T * p.Zp * tiles_y * tiles_x;
-  if (n == 0) return cudaSuccess;
-  k_ws_head<<<(unsigned)n, 128, 0, s>>>(p, tiles_x, tiles_y);
-  return cudaGetLastError();
+cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor_, const float *sum_x1, float *x0,
+                           int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s) {
+  ConvParams p{(const bf16 *)d, (const bf16 *)w, nullptr, nullptr, nullptr, T, Zp, Yp, Xp, 16, 16, 0, nullptr, 1};
+  HeadOut h{x0, sum_x1, (float)Z * Y * X, bias, floor_, T, Z, Y, X};
+  return launch_t16<true>(p, h, s);
 }
 
 cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,

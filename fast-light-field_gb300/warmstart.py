@@ -75,6 +75,7 @@ class UNet3D:
             self.p[name] = {"w": w.to(self.dev), "b": b.to(self.dev), "ci": ci, "co": co, "relu": relu}
         self.adam_t = 0
         self.loads = 0
+        self._ws = None             # split-K workspace of the convolutions
         for q in self.p.values():
             q["wb"] = _bf(q["w"].shape, self.dev)
             q["wf"] = _bf((27, q["co"], q["ci"]), self.dev)
@@ -99,8 +100,11 @@ class UNet3D:
         y = out if out is not None else _bf(tuple(x.shape[:4]) + (co,), self.dev)
         if relu is None:
             relu = q["relu"] and not flip       # a data gradient is linear
+        need = y.numel()
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
         _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,
-                    stream=torch.cuda.current_stream(self.dev).cuda_stream)
+                    stream=torch.cuda.current_stream(self.dev).cuda_stream, ws=self._ws)
         return y
 
     def _pool(self, x):
@@ -375,7 +379,7 @@ class WarmStart:
         key = (self.net.adam_t, self.net.loads)
         if getattr(self, "_head_key", None) != key:
             q = self.net.p["head"]
-            self._head = (q["wb"][:, :, 0].float().contiguous(), float(q["b"][0]))
+            self._head = (q["wb"], float(q["b"][0]))
             self._head_key = key
         x0 = torch.empty_like(htf)
         _flf.ws_head(feats, self._head[0], self._head[1], floor, sums, x0, self._s())

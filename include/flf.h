@@ -219,7 +219,9 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  * flf_conv3d: y = act(conv3x3x3(x, w) + bias), zero padding, w [27][Ci][Co]
  *   (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), bias [Co] float or NULL, act = ReLU
  *   when relu != 0; with mask != NULL ([..][Co] bf16) entries whose mask is
- *   not > 0 are zeroed (the ReLU derivative in a backward pass).
+ *   not > 0 are zeroed (the ReLU derivative in a backward pass).  ws (float,
+ *   ws_elems >= B Z Y X Co, or NULL) lets layers with few output tiles split
+ *   their K loop across CTAs; it must not be shared by concurrent calls.
  * flf_conv3d_wgrad: dw [27][Ci][Co] float += sum_v x[v + tap][ci] dy[v][co].
  * flf_conv3d_flip: w2[26 - tap][co][ci] = w[tap][ci][co]; conv3d with w2 is
  *   the data gradient.
@@ -237,7 +239,7 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  * flf_render_blobs: vol [Z][Y][X] float += amp exp(-d^2 / 2 sigma^2) within
  *   3 sigma of each pts[k] = (z, y, x, amp) (float4 array). */
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, void *stream);
+               int Ci, int Co, int relu, float *ws, long long ws_elems, void *stream);
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      void *stream);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
@@ -257,10 +259,11 @@ int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts
  * whose sums are left in sum_x1 [T]), 1 = Htf / Ht1 / m_t, 2 = HtH1 * c2,
  * 3 = Ht1 * c3, others and the padding 0.  flf_ws_head: the start volume
  * x0 [Z][T][Y][X] = max(conv3x3x3(d, w)[0] + bias, floor) * m_t from the last
- * features d [T][Zp][Yp][Xp][16] and the head's channel-0 weights w [27][16]. */
+ * features d [T][Zp][Yp][Xp][16] and the head's BF16 weights w [27][16][16]
+ * (output channel 0 is used). */
 int flf_ws_input(const float *htf, const float *hth1, const float *ht1, float *sum_x1, void *out, int T, int Z,
                  int Y, int X, int Zp, int Yp, int Xp, float c2, float c3, void *stream);
-int flf_ws_head(const void *d, const float *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
+int flf_ws_head(const void *d, const void *w, float bias, float floor_, const float *sum_x1, float *x0, int T, int Z,
                 int Y, int X, int Zp, int Yp, int Xp, void *stream);
 
 /* CUDA graph of a whole RL run (the replay form of flf_rl_iterate): the

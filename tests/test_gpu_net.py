@@ -41,6 +41,8 @@ def _close(torch, got, ref, rel=1e-2, absf=1e-3):
     # the persistent patch-tiled kernel (16 / 32 channels in and out), ragged tiles
     ((2, 3, 9, 20), 16, 32, True), ((1, 5, 17, 33), 32, 16, False), ((1, 4, 8, 16), 32, 32, True),
     ((1, 2, 3, 5), 16, 16, True), ((2, 6, 24, 40), 16, 16, False),
+    # few output tiles and a long K loop: split across CTAs through the workspace
+    ((1, 3, 6, 6), 128, 64, True), ((1, 2, 5, 7), 64, 128, False), ((2, 3, 9, 9), 64, 32, True),
 ])
 def test_conv3d_forward(env, shape, Ci, Co, relu):
     torch, _flf = env
@@ -49,17 +51,18 @@ def test_conv3d_forward(env, shape, Ci, Co, relu):
     w = (torch.randn((27, Ci, Co), generator=g) / np.sqrt(27 * Ci)).bfloat16()
     b = torch.randn(Co, generator=g).float()
     y = torch.empty(shape + (Co,), dtype=torch.bfloat16, device="cuda")
-    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu)
+    ws = torch.empty(int(np.prod(shape)) * Co, device="cuda")
+    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws)
     ref = _ref_conv(torch, x.double(), w.double(), b.double())
     if relu:
         ref = ref.clamp_min(0)
     _close(torch, y, ref)
 
 
-def test_conv3d_mask_and_data_gradient(env):
+@pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 32, 16), ((1, 3, 6, 6), 64, 128)])
+def test_conv3d_mask_and_data_gradient(env, shape, Ci, Co):
     torch, _flf = env
     g = torch.Generator().manual_seed(3)
-    shape, Ci, Co = (2, 4, 6, 10), 32, 16
     x = torch.randn(shape + (Ci,), generator=g).bfloat16().double().requires_grad_()
     w = (torch.randn((27, Ci, Co), generator=g) / 15).bfloat16()
     dy = torch.randn(shape + (Co,), generator=g).bfloat16()
@@ -70,7 +73,8 @@ def test_conv3d_mask_and_data_gradient(env):
     w2 = torch.empty((27, Co, Ci), dtype=torch.bfloat16, device="cuda")
     _flf.conv3d_flip(w.cuda(), w2)
     dx = torch.empty(shape + (Ci,), dtype=torch.bfloat16, device="cuda")
-    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda())
+    ws = torch.empty(int(np.prod(shape)) * Ci, device="cuda")
+    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws)
     _close(torch, dx, ref)
 
 

@@ -135,10 +135,12 @@ def test_fused_input_and_head_kernels(env):
     ref[:, :Z, :Y, :X, 3] = (ht1 * c3).permute(1, 0, 2, 3)
     assert float((out.float() - ref).abs().max()) <= 1e-2 * float(ref.abs().max())
     d = torch.rand((T, Zp, Yp, Xp, 16), generator=g).bfloat16().cuda()
-    w = torch.randn((27, 16), generator=g).cuda() / 20
+    wfull = torch.zeros((27, 16, 16))
+    wfull[:, :, 0] = torch.randn((27, 16), generator=g) / 20
+    wfull = wfull.bfloat16()
     x0 = torch.empty((Z, T, Y, X), device="cuda")
-    _flf.ws_head(d, w, 0.1, 1e-3, sums, x0)
-    W = w.double().cpu().reshape(3, 3, 3, 16).permute(3, 0, 1, 2)[None]
+    _flf.ws_head(d, wfull.cuda(), 0.1, 1e-3, sums, x0)
+    W = wfull[:, :, 0].double().reshape(3, 3, 3, 16).permute(3, 0, 1, 2)[None]
     conv = torch.nn.functional.conv3d(d.double().cpu().permute(0, 4, 1, 2, 3), W, padding=1)[:, 0] + 0.1
     want = conv.clamp_min(1e-3)[:, :Z, :Y, :X].permute(1, 0, 2, 3) * (sums.double().cpu() / (Z * Y * X))[None, :,
                                                                                                          None, None]
