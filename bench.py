@@ -54,6 +54,11 @@ WORKLOADS = {
     "warmstart": dict(Nnum=15, lenslets=30, z=(-50, 50, 5), beads=200,
                       optics=dict(M=40, NA=0.95, MLPitch=150e-6, OSR=3, n=1.33, fml=3000e-6, lam=520e-9),
                       label="learned warm start + RL vs plain RL(8 it), 450x450 px, Nnum 15, 21 planes -50..50 um"),
+    # the learned warm start on the full-field workload (synthetic PSF of the default workload)
+    "warmstart_fullfield": dict(Nnum=15, lenslets=67, z=(-100, 100, 5), img_size_ref=28, beads=2000, filaments=50,
+                                psf="synthetic",
+                                label="learned warm start + RL vs plain RL(8 it), full field 1005x1005 px, Nnum 15, "
+                                      "41 planes -100..100 um"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
     # a time series of frames of three sizes (--frames per size), 500 drifting beads each
@@ -73,7 +78,9 @@ def parse():
     ap.add_argument("--iters", type=int, default=8)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--train-steps", type=int, default=800, help="warm-start network training steps")
+    ap.add_argument("--train-steps", type=int, default=1600, help="warm-start network training steps")
+    ap.add_argument("--tune-steps", type=int, default=0,
+                    help="warm-start fine-tuning steps on the data-fit residual (whole volumes)")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-planes", type=int, default=5)
@@ -254,7 +261,7 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload in ("timeseries", "rectify", "psf", "warmstart"):
+    if args.workload in ("timeseries", "rectify", "psf", "warmstart", "warmstart_fullfield"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
                           "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
@@ -651,23 +658,30 @@ def run_warmstart(args):
     import warmstart
     build_lib.build()
     warnings.simplefilter("ignore")
-    wl = WORKLOADS["warmstart"]
+    wl = WORKLOADS[args.workload]
     z0, z1, dz = wl["z"]
     t0 = time.time()
-    r = generate_psf.GeneratePSFArrays(Nnum=wl["Nnum"], zmin=z0 * 1e-6, zmax=z1 * 1e-6, zspacing=dz * 1e-6,
-                                       **wl["optics"])
-    hm = psfmatrix.HMatrixArrays(r["H"], r["Ht"], name="bench-warmstart")
+    if wl.get("psf") == "synthetic":
+        hm = build_problem(wl)[0]
+        psf_desc = "synthetic (the default workload's), sizes %s" % [int(hm.PSFShape(c)[-1]) for c in range(hm.numZ)]
+    else:
+        r = generate_psf.GeneratePSFArrays(Nnum=wl["Nnum"], zmin=z0 * 1e-6, zmax=z1 * 1e-6, zspacing=dz * 1e-6,
+                                           **wl["optics"])
+        hm = psfmatrix.HMatrixArrays(r["H"], r["Ht"], name="bench-warmstart")
+        psf_desc = "generated on the GPU (generate_psf.py), sizes %s" % [int(h.shape[-1]) for h in r["H"]]
     psf_s = time.time() - t0
     Y = X = wl["lenslets"] * wl["Nnum"]
     Z = hm.numZ
     p = projector.Projector_gb300()
-    ws = warmstart.WarmStart(p, hm, Y, X, beads=wl["beads"])
-    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=32, log_every=100)
+    ws = warmstart.WarmStart(p, hm, Y, X, beads=wl["beads"], filaments=wl.get("filaments", 0))
+    refresh = 8 if Y * X * Z < 10_000_000 else 16
+    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=32, log_every=100,
+                       refresh_every=refresh)
+    tune_s = ws.finetune_residual(steps=args.tune_steps, log_every=50) if args.tune_steps > 0 else 0.0
     dev = ws.dev
     s = torch.cuda.current_stream(dev)
     rng = np.random.default_rng(2024)
     nseed = 16
-    _, imgs, htfs = ws.make_batch(nseed, rng)
     ctx = ws.ctx
 
     def resid(x, img):
@@ -677,22 +691,31 @@ def run_warmstart(args):
         d = (img.double() - hx.double()).reshape(T, -1)
         return (d.norm(dim=1) / img.double().reshape(T, -1).norm(dim=1)).cpu().numpy()
 
-    xu = torch.ones_like(htfs)
-    p.RichardsonLucy(hm, xu, htfs, 8)
-    r_plain = resid(xu, imgs)
-    x = ws.initial_volume(htfs)
-    need = np.full(nseed, -1)
-    curve = []
-    for k in range(0, 9):
-        if k > 0:
-            p.RichardsonLucy(hm, x, htfs, 1)
-        rk = resid(x, imgs)
-        curve.append(float(rk.mean()))
-        need[(need < 0) & (rk <= r_plain)] = k
-    if (need < 0).any():
-        k_warm = None
-    else:
-        k_warm = int(need.max())
+    # held-out volumes in chunks that keep the network's activations small
+    chunk = max(1, min(nseed, 40_000_000 // (Z * Y * X)))
+    r_plain, curves, need = [], [], []
+    for c0 in range(0, nseed, chunk):
+        _, imgs, htfs = ws.make_batch(min(chunk, nseed - c0), rng)
+        xu = torch.ones_like(htfs)
+        p.RichardsonLucy(hm, xu, htfs, 8)
+        rp = resid(xu, imgs)
+        x = ws.initial_volume(htfs)
+        nd = np.full(len(rp), -1)
+        cv = []
+        for k in range(0, 9):
+            if k > 0:
+                p.RichardsonLucy(hm, x, htfs, 1)
+            rk = resid(x, imgs)
+            cv.append(rk)
+            nd[(nd < 0) & (rk <= rp)] = k
+        r_plain.append(rp)
+        curves.append(np.stack(cv))
+        need.append(nd)
+        del xu, x
+    r_plain = np.concatenate(r_plain)
+    curve = [float(v) for v in np.concatenate(curves, axis=1).mean(axis=1)]
+    need = np.concatenate(need)
+    k_warm = None if (need < 0).any() else int(need.max())
     img1 = imgs[:1].contiguous()
     htf1 = torch.empty((Z, 1, Y, X), device=dev)
     xp = torch.empty((Z, 1, Y, X), device=dev)
@@ -739,8 +762,11 @@ def run_warmstart(args):
             "warmup": max(args.warmup, 3), "ms_per_step": ms_warm, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 network (fp32 accumulation), f32 projections", "data": "synthetic",
             "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": wl["Nnum"], "frames": 1,
-                       "psf": "generated on the GPU (generate_psf.py), sizes %s" % [int(h.shape[-1]) for h in r["H"]],
+                       "psf": psf_desc,
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
+                       "residual_finetune_steps": args.tune_steps, "finetune_s": round(tune_s, 1),
+                       "losses": [[round(float(v), 6) if isinstance(v, float) else v for v in l]
+                                  for l in ws.losses[-8:]],
                        "network_parameters": ws.net.num_parameters(), "held_out_volumes": nseed,
                        "l2": "transfer matrices and volumes larger than L2"},
             "plain_rl": {"volumes_per_s": 1000.0 / ms_plain, "ms_per_volume": ms_plain, "iterations": 8,
@@ -765,7 +791,7 @@ def main():
         run_rectify(args)
     elif args.workload == "psf":
         run_psf(args)
-    elif args.workload == "warmstart":
+    elif args.workload in ("warmstart", "warmstart_fullfield"):
         run_warmstart(args)
     else:
         run_gb300(args, rank, world, local)

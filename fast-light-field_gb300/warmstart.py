@@ -365,6 +365,39 @@ class WarmStart:
         torch.cuda.synchronize(self.dev)
         return time.time() - t0
 
+    def finetune_residual(self, steps=200, lr=1e-4, frames=1, seed=7, floor=1e-3, log_every=0):
+        """Fine-tune on the data-fit residual itself, on whole volumes: loss =
+        ||y - H x0||^2 / ||y||^2 for the start volume x0 the network gives, with the
+        gradient 2 Ht(H x0 - y) / ||y||^2 from the GPU projector."""
+        rng = np.random.default_rng(seed)
+        t0 = time.time()
+        Z, Y, X = self.Z, self.Y, self.X
+        s = self._s()
+        for step in range(steps):
+            _, img, htf = self.make_batch(frames, rng)
+            xin, scale = self._inputs(htf)
+            out, cache = self.net.forward(xin)
+            pred = out[:, :Z, :Y, :X, 0].float()                            # [T, Z, Y, X]
+            sc = scale[:, None, None, None]
+            x0 = (pred.clamp_min(floor) * sc).permute(1, 0, 2, 3).contiguous()
+            hx = torch.empty_like(img)
+            self.ctx.forward(x0, hx, frames, Y, X, None, stream=s)
+            r = hx - img
+            ny = (img.double() ** 2).sum()
+            loss = float((r.double() ** 2).sum() / ny)
+            gx = torch.empty_like(htf)
+            self.ctx.backward((r * float(2.0 / ny)).contiguous(), gx, frames, Y, X, None, stream=s)
+            gp = gx.permute(1, 0, 2, 3) * sc * (pred > floor)
+            dout = torch.zeros_like(out)
+            dout[:, :Z, :Y, :X, 0] = gp.to(torch.bfloat16)
+            self.net.backward(cache, dout)
+            self.net.adam_step(lr)
+            if log_every and (step % log_every == 0 or step == steps - 1):
+                self.losses.append(("residual", step, loss))
+            del cache, out
+        torch.cuda.synchronize(self.dev)
+        return time.time() - t0
+
     def initial_volume(self, htf, floor=1e-3):
         """RL start volume [Z, T, Y, X] from Htf [Z, T, Y, X] (device): the network's
         prediction, clamped below at floor x the frame mean of the first RL iterate (RL
