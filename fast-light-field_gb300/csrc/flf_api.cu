@@ -1570,6 +1570,25 @@ int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask
   return FLF_OK;
 }
 
+int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
+                  int X, int relu, void *stream) {
+  if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = net_shape(B, Z, Y, X, 16)) return rc;
+  if (!aligned16(x) || !aligned16(y) || (mask && !aligned16(mask)))
+    return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
+  ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
+               (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16, relu ? 1 : 0, nullptr, 1};
+  NET_CHECK(launch_conv3d_tc16(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_net_status(void) {
+  const int v = net_status_read_and_clear();
+  if (v < 0) return fail(nullptr, FLF_E_CUDA, "reading the network status flag failed");
+  if (v) return fail(nullptr, FLF_E_TIMEOUT, "a bounded wait in a tensor-core convolution gave up (code %d)", v);
+  return FLF_OK;
+}
+
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      void *stream) {
   if (!x || !dy || !dw) return fail(nullptr, FLF_E_ARG, "NULL array pointer");

@@ -435,6 +435,215 @@ __global__ void __launch_bounds__(128, 4) k_conv3d_t16(ConvParams p, HeadOut h, 
   cp_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// 16 -> 16 channels on the 5th-generation tensor cores (tcgen05).  A tile is
+// 128 consecutive voxels of one x row (M = 128); each of the 27 taps is one
+// tcgen05.mma (M 128, N 16, K 16, BF16 in, FP32 accumulate in TMEM) issued by
+// one thread with both operands read from shared memory through matrix
+// descriptors in the canonical K-major, no-swizzle layout (8-row x 16-byte
+// core matrices).  The 3 x 3 x 130-voxel input patch is stored as two planes
+// of 8 channels, so the A tile of every tap is a uniformly strided window of
+// it (start + (dz*3+dy)*130 + dx voxels; core matrices 128 B apart along M,
+// one plane apart along K).  The accumulator is read back with tcgen05.ld
+// (warp w holds rows 32w..32w+31).  Every wait is bounded; a wait that gives
+// up sets g_net_err (flf_net_status) and the kernel stops cleanly.
+// ---------------------------------------------------------------------------
+__device__ int g_net_err;
+
+namespace {
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;                          // descriptor version (bits 46-48 = 0b001); no swizzle
+  return d;
+}
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void net_mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ bool net_mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+  unsigned long long t0 = 0;
+  for (int it = 0;; it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    if (it == 0) t0 = t;
+    else if (t - t0 > limit_ns) return false;
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, long long ntiles) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  constexpr int PXW = 130, PV = 9 * PXW;          // patch voxels: 3 (z) x 3 (y) x 130 (x)
+  constexpr uint32_t PLANE = PV * 16;             // bytes of one 8-channel plane
+  // layout: [B: 27 taps x 512 B][patch buffers 2 x 2 planes][mbarrier 8 B][tmem address 4 B]
+  unsigned char *Wb = smem;
+  unsigned char *Pb = smem + 27 * 512;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Pb + 4 * PLANE);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t wb_s = su32(Wb), pb_s = su32(Pb), bar_s = su32(bar);
+
+  // B operands: per tap, co-major rows of 16 ci: core matrix (co/8, ci/8) at
+  // (ci/8)*128 + (co/8)*256, row co%8 at 16 B, element ci%8 at 2 B.
+  for (int i = tid; i < 27 * 16; i += 128) {
+    const int tap = i >> 4, co = i & 15;
+    uint32_t pk[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const unsigned short lo = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c) * 16 + co]);
+      const unsigned short hi = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c + 1) * 16 + co]);
+      pk[c] = (uint32_t)lo | ((uint32_t)hi << 16);
+    }
+    unsigned char *row = Wb + tap * 512 + (co >> 3) * 256 + (co & 7) * 16;
+    *reinterpret_cast<uint4 *>(row) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    *reinterpret_cast<uint4 *>(row + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(su32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) net_mbar_init(bar_s, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 16, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+  bool ok = true;
+  uint32_t phase = 0;
+  auto tile_of = [&](long long t, int &b, int &z, int &y, int &x0) {
+    long long q = t;
+    const int tx = (int)(q % tiles_x);
+    q /= tiles_x;
+    y = (int)(q % p.Y);
+    q /= p.Y;
+    z = (int)(q % p.Z);
+    b = (int)(q / p.Z);
+    x0 = tx * 128;
+  };
+  auto load_patch = [&](long long t, int buf) {
+    int b, z, y, x0;
+    tile_of(t, b, z, y, x0);
+    const uint32_t base = pb_s + buf * 2 * PLANE;
+    for (int i = tid; i < PV * 2; i += 128) {
+      const int v = i >> 1, pl = i & 1;
+      const int pz = v / (3 * PXW), py = (v / PXW) % 3, px = v % PXW;
+      const int gz = z + pz - 1, gy = y + py - 1, gx = x0 + px - 1;
+      const bool in = gz >= 0 && gz < p.Z && gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X;
+      const bf16 *src = in ? p.x + ((((long long)b * p.Z + gz) * p.Y + gy) * p.X + gx) * 16 + pl * 8 : p.x;
+      cp16(base + pl * PLANE + v * 16, src, in);
+    }
+  };
+  int buf = 0;
+  if ((long long)blockIdx.x < ntiles) load_patch(blockIdx.x, 0);
+  cp_commit();
+  for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    int b, z, y, x0;
+    tile_of(t, b, z, y, x0);
+    // the next tile's patch streams in while this tile multiplies
+    if (t + gridDim.x < ntiles) load_patch(t + gridDim.x, buf ^ 1);
+    cp_commit();
+    cp_wait<1>();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    const uint32_t pbuf = pb_s + buf * 2 * PLANE;
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll 1
+      for (int tap = 0; tap < 27; tap++) {
+        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+        const uint64_t ad = umma_desc(pbuf + ((dz * 3 + dy) * PXW + dx) * 16, PLANE, 128);
+        const uint64_t bd = umma_desc(wb_s + tap * 512, 128, 256);
+        umma_f16(tmem, ad, bd, idesc, tap > 0 ? 1u : 0u);
+      }
+      umma_commit(bar_s);
+    }
+    const int late = net_mbar_wait(bar_s, phase, 1000000000ULL) ? 0 : 1;
+    if (__syncthreads_or(late)) {     // one decision for the whole CTA
+      if (tid == 0) atomicExch(&g_net_err, 2);
+      ok = false;
+      break;
+    }
+    phase ^= 1;
+    tc_fence_after();
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(tmem + ((uint32_t)(warp * 32) << 16)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    tc_fence_before();
+    const int x = x0 + warp * 32 + lane;
+    if (x < p.X) {
+      const long long o = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16;
+      uint4 mk[2];
+      if (p.mask) {
+        mk[0] = *reinterpret_cast<const uint4 *>(p.mask + o);
+        mk[1] = *reinterpret_cast<const uint4 *>(p.mask + o + 8);
+      }
+      uint4 outv[2];
+      __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(outv);
+      const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        float v0 = __uint_as_float(r[2 * k]) + (p.bias ? p.bias[2 * k] : 0.f);
+        float v1 = __uint_as_float(r[2 * k + 1]) + (p.bias ? p.bias[2 * k + 1] : 0.f);
+        if (p.relu) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        if (p.mask) {
+          const float2 mf = __bfloat1622float2(m2[k]);
+          if (!(mf.x > 0.f)) v0 = 0.f;
+          if (!(mf.y > 0.f)) v1 = 0.f;
+        }
+        h[k] = __floats2bfloat162_rn(v0, v1);
+      }
+      *reinterpret_cast<uint4 *>(p.y + o) = outv[0];
+      *reinterpret_cast<uint4 *>(p.y + o + 8) = outv[1];
+    }
+    __syncthreads();   // TMEM and this patch buffer are reused two tiles on
+    buf ^= 1;
+  }
+  cp_wait<0>();
+  if (!ok) {
+    // let any MMA still in flight finish before the accumulator is released
+    if (!net_mbar_wait(bar_s, phase, 1000000000ULL)) atomicExch(&g_net_err, 3);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem) : "memory");
+  }
+}
+
 // Weight gradient.  CTA = (voxel chunk, tap) x (ci tile CM, co tile CN); the 4
 // warps take alternate k16 steps of its voxels (split-K) and are summed in
 // shared memory at the end, then added to dW with FP32 atomics.
@@ -925,6 +1134,43 @@ cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms) {
   FLF_WG(16, 16) FLF_WG(16, 32) FLF_WG(16, 64) FLF_WG(32, 16) FLF_WG(32, 32) FLF_WG(32, 64)
 #undef FLF_WG
   return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s) {
+  static int grid_cap = 0;
+  const size_t smem = 27 * 512 + 4 * 9 * 130 * 16 + 16;
+  if (!grid_cap) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tc16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_conv3d_tc16, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, dev = 0, sms = 0, smem_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc16, 128, smem);
+    if (e != cudaSuccess) return e;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int by_smem = smem_sm > 0 ? (int)(smem_sm / (smem + 1024)) : 1;
+    if (per_sm < by_smem) per_sm = by_smem;
+    // TMEM: 32 columns per CTA, 512 per SM
+    if (per_sm > 16) per_sm = 16;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid_cap = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  }
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  if (M == 0) return cudaSuccess;
+  const int tiles_x = (p.X + 127) / 128;
+  const long long ntiles = (long long)p.B * p.Z * p.Y * tiles_x;
+  const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
+  k_conv3d_tc16<<<grid, 128, smem, s>>>(p, tiles_x, ntiles);
+  return cudaGetLastError();
+}
+
+int net_status_read_and_clear() {
+  int v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_net_err, sizeof(int)) != cudaSuccess) return -1;
+  if (v) cudaMemcpyToSymbol(g_net_err, &z, sizeof(int));
+  return v;
 }
 
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s) {

@@ -157,3 +157,25 @@ def test_mse_adam_and_blobs(env):
         near = (np.abs(zz - cz) <= 3) & (np.abs(yy - cy) <= 3) & (np.abs(xx - cx) <= 3)
         ref += near * a * np.exp(-((zz - z0) ** 2 + (yy - y0) ** 2 + (xx - x0) ** 2) / 2)
     assert np.max(np.abs(vol.cpu().numpy() - ref)) < 1e-5
+
+
+@pytest.mark.parametrize("shape,relu,masked", [((1, 2, 3, 5), True, False), ((2, 3, 4, 130), False, False),
+                                               ((1, 4, 9, 300), True, True), ((2, 5, 6, 128), True, False)])
+def test_conv3d_tcgen05(env, shape, relu, masked):
+    """The 16 -> 16 convolution on the tcgen05 tensor cores (TMEM accumulator)."""
+    torch, _flf = env
+    g = torch.Generator().manual_seed(sum(shape))
+    x = torch.randn(shape + (16,), generator=g).bfloat16()
+    w = (torch.randn((27, 16, 16), generator=g) / np.sqrt(27 * 16)).bfloat16()
+    b = torch.randn(16, generator=g).float()
+    m = torch.randn(shape + (16,), generator=g).bfloat16() if masked else None
+    y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d_tc(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, mask=m.cuda() if masked else None)
+    torch.cuda.synchronize()
+    _flf.net_status()
+    ref = _ref_conv(torch, x.double(), w.double(), b.double())
+    if relu:
+        ref = ref.clamp_min(0)
+    if masked:
+        ref = ref * (m.double() > 0)
+    _close(torch, y, ref)
