@@ -58,7 +58,7 @@ _SIGS = {
     "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
     "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
-    "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
     "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P]),
@@ -189,14 +189,14 @@ def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
                                  _ptr(stream)))
 
 
-def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None):
-    """conv3d for 16 -> 16 channels on the tcgen05 tensor cores."""
+def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):
+    """conv3d for 16 -> 16 channels on the tcgen05 tensor cores (tiles of rows x 128 voxels)."""
     lib = load_library()
     B, Z, Y, X, C = _vshape(x)
     if C != 16 or int(y.shape[-1]) != 16:
         raise ValueError("conv3d_tc takes 16 channels in and out")
     _check_global(lib.flf_conv3d_tc(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X,
-                                    int(bool(relu)), _ptr(stream)))
+                                    int(bool(relu)), int(rows), _ptr(stream)))
 
 
 def net_status():

@@ -1571,13 +1571,15 @@ int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask
 }
 
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
-                  int X, int relu, void *stream) {
+                  int X, int relu, int rows, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = net_shape(B, Z, Y, X, 16)) return rc;
   if (!aligned16(x) || !aligned16(y) || (mask && !aligned16(mask)))
     return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
   ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
-               (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16, relu ? 1 : 0, nullptr, 1};
+               (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16, relu ? 1 : 0, nullptr, rows};
+  if (rows != 1 && rows != 4 && rows != 5)
+    return fail(nullptr, FLF_E_ARG, "tile choice must be 1, 4 or 5 (4 rows, double-buffered)");
   NET_CHECK(launch_conv3d_tc16(p, (cudaStream_t)stream));
   return FLF_OK;
 }

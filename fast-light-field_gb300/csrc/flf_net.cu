@@ -495,17 +495,19 @@ __device__ __forceinline__ bool net_mbar_wait(uint32_t bar, uint32_t parity, uns
 
 }  // namespace
 
+template <int ROWS, int NBUF>
 __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, long long ntiles) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  constexpr int PXW = 130, PV = 9 * PXW;          // patch voxels: 3 (z) x 3 (y) x 130 (x)
-  constexpr uint32_t PLANE = PV * 16;             // bytes of one 8-channel plane
-  // layout: [B: 27 taps x 512 B][patch buffers 2 x 2 planes][mbarrier 8 B][tmem address 4 B]
+  constexpr int PXW = 130, PYH = ROWS + 2, PV = 3 * PYH * PXW;   // patch voxels: 3 (z) x (ROWS+2) (y) x 130 (x)
+  constexpr uint32_t PLANE = PV * 16;                            // bytes of one 8-channel plane
+  // layout: [B: 27 taps x 512 B][patch buffers x 2 planes][mbarrier 8 B][tmem address 4 B]
   unsigned char *Wb = smem;
   unsigned char *Pb = smem + 27 * 512;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Pb + 4 * PLANE);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Pb + NBUF * 2 * PLANE);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t wb_s = su32(Wb), pb_s = su32(Pb), bar_s = su32(bar);
+  constexpr uint32_t TCOLS = ROWS * 16 <= 32 ? 32 : (ROWS * 16 <= 64 ? 64 : 128);
 
   // B operands: per tap, co-major rows of 16 ci: core matrix (co/8, ci/8) at
   // (ci/8)*128 + (co/8)*256, row co%8 at 16 B, element ci%8 at 2 B.
@@ -523,7 +525,8 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
     *reinterpret_cast<uint4 *>(row + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(su32(tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
+                 "r"(TCOLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
@@ -536,39 +539,46 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
   bool ok = true;
   uint32_t phase = 0;
-  auto tile_of = [&](long long t, int &b, int &z, int &y, int &x0) {
+  const int tiles_y = (p.Y + ROWS - 1) / ROWS;
+  auto tile_of = [&](long long t, int &b, int &z, int &y0, int &x0) {
     long long q = t;
     const int tx = (int)(q % tiles_x);
     q /= tiles_x;
-    y = (int)(q % p.Y);
-    q /= p.Y;
+    y0 = (int)(q % tiles_y) * ROWS;
+    q /= tiles_y;
     z = (int)(q % p.Z);
     b = (int)(q / p.Z);
     x0 = tx * 128;
   };
   auto load_patch = [&](long long t, int buf) {
-    int b, z, y, x0;
-    tile_of(t, b, z, y, x0);
+    int b, z, y0, x0;
+    tile_of(t, b, z, y0, x0);
     const uint32_t base = pb_s + buf * 2 * PLANE;
     for (int i = tid; i < PV * 2; i += 128) {
       const int v = i >> 1, pl = i & 1;
-      const int pz = v / (3 * PXW), py = (v / PXW) % 3, px = v % PXW;
-      const int gz = z + pz - 1, gy = y + py - 1, gx = x0 + px - 1;
+      const int pz = v / (PYH * PXW), py = (v / PXW) % PYH, px = v % PXW;
+      const int gz = z + pz - 1, gy = y0 + py - 1, gx = x0 + px - 1;
       const bool in = gz >= 0 && gz < p.Z && gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X;
       const bf16 *src = in ? p.x + ((((long long)b * p.Z + gz) * p.Y + gy) * p.X + gx) * 16 + pl * 8 : p.x;
       cp16(base + pl * PLANE + v * 16, src, in);
     }
   };
   int buf = 0;
-  if ((long long)blockIdx.x < ntiles) load_patch(blockIdx.x, 0);
+  if (NBUF == 2 && (long long)blockIdx.x < ntiles) load_patch(blockIdx.x, 0);
   cp_commit();
   for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    int b, z, y, x0;
-    tile_of(t, b, z, y, x0);
-    // the next tile's patch streams in while this tile multiplies
-    if (t + gridDim.x < ntiles) load_patch(t + gridDim.x, buf ^ 1);
-    cp_commit();
-    cp_wait<1>();
+    int b, z, y0, x0;
+    tile_of(t, b, z, y0, x0);
+    if (NBUF == 2) {
+      // the next tile's patch streams in while this tile multiplies
+      if (t + gridDim.x < ntiles) load_patch(t + gridDim.x, buf ^ 1);
+      cp_commit();
+      cp_wait<1>();
+    } else {
+      load_patch(t, 0);
+      cp_commit();
+      cp_wait<0>();
+    }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
     const uint32_t pbuf = pb_s + buf * 2 * PLANE;
@@ -577,9 +587,12 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 #pragma unroll 1
       for (int tap = 0; tap < 27; tap++) {
         const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-        const uint64_t ad = umma_desc(pbuf + ((dz * 3 + dy) * PXW + dx) * 16, PLANE, 128);
         const uint64_t bd = umma_desc(wb_s + tap * 512, 128, 256);
-        umma_f16(tmem, ad, bd, idesc, tap > 0 ? 1u : 0u);
+#pragma unroll
+        for (int r = 0; r < ROWS; r++) {   // independent accumulators, one per output row
+          const uint64_t ad = umma_desc(pbuf + ((dz * PYH + r + dy) * PXW + dx) * 16, PLANE, 128);
+          umma_f16(tmem + r * 16, ad, bd, idesc, tap > 0 ? 1u : 0u);
+        }
       }
       umma_commit(bar_s);
     }
@@ -591,45 +604,48 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
     }
     phase ^= 1;
     tc_fence_after();
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(tmem + ((uint32_t)(warp * 32) << 16)));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    tc_fence_before();
-    const int x = x0 + warp * 32 + lane;
-    if (x < p.X) {
-      const long long o = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16;
-      uint4 mk[2];
-      if (p.mask) {
-        mk[0] = *reinterpret_cast<const uint4 *>(p.mask + o);
-        mk[1] = *reinterpret_cast<const uint4 *>(p.mask + o + 8);
-      }
-      uint4 outv[2];
-      __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(outv);
-      const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        float v0 = __uint_as_float(r[2 * k]) + (p.bias ? p.bias[2 * k] : 0.f);
-        float v1 = __uint_as_float(r[2 * k + 1]) + (p.bias ? p.bias[2 * k + 1] : 0.f);
-        if (p.relu) {
-          v0 = fmaxf(v0, 0.f);
-          v1 = fmaxf(v1, 0.f);
-        }
+#pragma unroll 1
+    for (int r = 0; r < ROWS; r++) {
+      uint32_t v[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + r * 16));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      const int x = x0 + warp * 32 + lane, y = y0 + r;
+      if (x < p.X && y < p.Y) {
+        const long long o = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16;
+        uint4 mk[2];
         if (p.mask) {
-          const float2 mf = __bfloat1622float2(m2[k]);
-          if (!(mf.x > 0.f)) v0 = 0.f;
-          if (!(mf.y > 0.f)) v1 = 0.f;
+          mk[0] = *reinterpret_cast<const uint4 *>(p.mask + o);
+          mk[1] = *reinterpret_cast<const uint4 *>(p.mask + o + 8);
         }
-        h[k] = __floats2bfloat162_rn(v0, v1);
+        uint4 outv[2];
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(outv);
+        const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          float v0 = __uint_as_float(v[2 * k]) + (p.bias ? p.bias[2 * k] : 0.f);
+          float v1 = __uint_as_float(v[2 * k + 1]) + (p.bias ? p.bias[2 * k + 1] : 0.f);
+          if (p.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          if (p.mask) {
+            const float2 mf = __bfloat1622float2(m2[k]);
+            if (!(mf.x > 0.f)) v0 = 0.f;
+            if (!(mf.y > 0.f)) v1 = 0.f;
+          }
+          h[k] = __floats2bfloat162_rn(v0, v1);
+        }
+        *reinterpret_cast<uint4 *>(p.y + o) = outv[0];
+        *reinterpret_cast<uint4 *>(p.y + o + 8) = outv[1];
       }
-      *reinterpret_cast<uint4 *>(p.y + o) = outv[0];
-      *reinterpret_cast<uint4 *>(p.y + o + 8) = outv[1];
     }
-    __syncthreads();   // TMEM and this patch buffer are reused two tiles on
-    buf ^= 1;
+    tc_fence_before();
+    __syncthreads();   // TMEM and the patch buffer are reused
+    if (NBUF == 2) buf ^= 1;
   }
   cp_wait<0>();
   if (!ok) {
@@ -640,7 +656,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
   }
 }
 
@@ -1136,34 +1152,45 @@ cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s) {
+template <int ROWS, int NBUF>
+static cudaError_t launch_tc16_rows(const ConvParams &p, cudaStream_t s) {
   static int grid_cap = 0;
-  const size_t smem = 27 * 512 + 4 * 9 * 130 * 16 + 16;
+  const size_t smem = 27 * 512 + (size_t)NBUF * 2 * 3 * (ROWS + 2) * 130 * 16 + 16;
   if (!grid_cap) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tc16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tc16<ROWS, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_conv3d_tc16, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    e = cudaFuncSetAttribute(k_conv3d_tc16<ROWS, NBUF>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     int per_sm = 0, dev = 0, sms = 0, smem_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc16, 128, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc16<ROWS, NBUF>, 128, smem);
     if (e != cudaSuccess) return e;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     const int by_smem = smem_sm > 0 ? (int)(smem_sm / (smem + 1024)) : 1;
     if (per_sm < by_smem) per_sm = by_smem;
-    // TMEM: 32 columns per CTA, 512 per SM
-    if (per_sm > 16) per_sm = 16;
-    cudaGetDevice(&dev);
+    // TMEM: at most 512 columns per SM
+    const int cols = ROWS * 16 <= 32 ? 32 : (ROWS * 16 <= 64 ? 64 : 128);
+    if (per_sm > 512 / cols) per_sm = 512 / cols;
+    if (per_sm < 1) per_sm = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grid_cap = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    grid_cap = per_sm * (sms > 0 ? sms : 1);
   }
   const long long M = (long long)p.B * p.Z * p.Y * p.X;
   if (M == 0) return cudaSuccess;
   const int tiles_x = (p.X + 127) / 128;
-  const long long ntiles = (long long)p.B * p.Z * p.Y * tiles_x;
+  const long long ntiles = (long long)p.B * p.Z * ((p.Y + ROWS - 1) / ROWS) * tiles_x;
   const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
-  k_conv3d_tc16<<<grid, 128, smem, s>>>(p, tiles_x, ntiles);
+  k_conv3d_tc16<ROWS, NBUF><<<grid, 128, smem, s>>>(p, tiles_x, ntiles);
   return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s) {
+  // p.splits selects the tile: 1 = 1 row x 128 (double-buffered), 4 = 4 rows (single buffer),
+  // 5 = 4 rows double-buffered
+  if (p.splits == 4) return launch_tc16_rows<4, 1>(p, s);
+  if (p.splits == 5) return launch_tc16_rows<4, 2>(p, s);
+  return launch_tc16_rows<1, 2>(p, s);
 }
 
 int net_status_read_and_clear() {

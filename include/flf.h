@@ -243,10 +243,11 @@ int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      void *stream);
 /* flf_conv3d_tc: flf_conv3d for 16 -> 16 channels on the tcgen05 tensor cores
- * (accumulator in TMEM; 128-voxel x rows per tile).  flf_net_status: FLF_OK, or
- * FLF_E_TIMEOUT when a bounded wait inside it gave up since the last call. */
+ * (accumulators in TMEM; tiles of `rows` (1 or 4) x 128 voxels, one
+ * accumulator per row).  flf_net_status: FLF_OK, or FLF_E_TIMEOUT when a
+ * bounded wait inside it gave up since the last call. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
-                  int X, int relu, void *stream);
+                  int X, int relu, int rows, void *stream);
 int flf_net_status(void);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
 int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream);
