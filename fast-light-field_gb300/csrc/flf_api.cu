@@ -89,6 +89,9 @@ struct flf_ctx {
   int opt_geometry_cache = 2;    // geometries of other image shapes kept resident (most recent first)
   std::vector<Geometry> parked;  // those geometries
   unsigned long long mem_epoch = 0;   // bumped whenever a workspace or geometry buffer is freed
+  int opt_streams = 2;           // transform groups alternate over this many streams (1 or 2)
+  cudaStream_t s2 = nullptr;     // the second stream, and the events that fork / chain / join it
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chain = nullptr;
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
   int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
@@ -650,6 +653,38 @@ void ws_needs(const flf_ctx *ctx, const PlaneSet &ps, int nt, bool fwd, size_t &
   }
 }
 
+// Workspace slots: one per stream the transform groups alternate over.
+int ws_slots(const flf_ctx *ctx) { return ctx->opt_streams > 1 ? 2 : 1; }
+size_t slot_bytes(size_t b) { return (b + 255) / 256 * 256; }
+
+// The second stream and its events (created on first use).
+int ensure_streams(flf_ctx *ctx) {
+  if (ctx->opt_streams < 2 || ctx->s2) return FLF_OK;
+  CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->s2, cudaStreamNonBlocking));
+  CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+  CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_chain, cudaEventDisableTiming));
+  return FLF_OK;
+}
+
+// Streams of a per-group loop: st[0] = s, st[1] = the second stream forked from s
+// (or s again with one stream).  join_streams makes s wait for the second.
+int fork_streams(flf_ctx *ctx, cudaStream_t s, cudaStream_t st[2]) {
+  st[0] = st[1] = s;
+  if (ctx->opt_streams < 2) return FLF_OK;
+  if (int rc = ensure_streams(ctx)) return rc;
+  CUDA_TRY(ctx, cudaEventRecord(ctx->ev_fork, s));
+  CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->s2, ctx->ev_fork, 0));
+  st[1] = ctx->s2;
+  return FLF_OK;
+}
+int join_streams(flf_ctx *ctx, cudaStream_t s) {
+  if (ctx->opt_streams < 2 || !ctx->s2) return FLF_OK;
+  CUDA_TRY(ctx, cudaEventRecord(ctx->ev_join, ctx->s2));
+  CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
+  return FLF_OK;
+}
+
 MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   MacParams mp{};
   mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
@@ -736,18 +771,30 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneS
   const int NN = L.NN, Y = Gm.Y, X = Gm.X;
   size_t sS, sO, sCv;
   ws_needs(ctx, ps, nt, true, sS, sO, sCv);
-  int rc = ensure_ws(ctx, ctx->wsS, sS);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, sCv);
+  sS = slot_bytes(sS), sO = slot_bytes(sO), sCv = slot_bytes(sCv);
+  const int nslot = ws_slots(ctx);
+  int rc = ensure_ws(ctx, ctx->wsS, nslot * sS);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, nslot * sO);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, nslot * sCv);
   if (rc != FLF_OK) return rc;
   int last = -1;
   for (size_t gi = 0; gi < Gm.groups.size(); gi++)
     if (ps.n[gi]) last = (int)gi;
   bool first = true;
-  float *cvol = (float *)ctx->wsCvol.p;
+  // groups alternate over two streams with their own workspace slots; the
+  // inverse transforms, which accumulate into chan, stay in group order
+  cudaStream_t st[2];
+  if ((rc = fork_streams(ctx, s, st))) return rc;
+  const cudaStream_t s_caller = s;
+  int k = 0;
   for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
     const int nplanes = ps.n[gi];
     if (!nplanes) continue;
+    const int slot = k & (nslot - 1);
+    const cudaStream_t s = st[k & 1];
+    float *cvol = (float *)((char *)ctx->wsCvol.p + slot * sCv);
+    void *wS = (char *)ctx->wsS.p + slot * sS;
+    float2 *wO = (float2 *)((char *)ctx->wsO.p + slot * sO);
     const Group &G = Gm.groups[gi];
     const int ffh = G.f * G.fh;
     const int zgroup = zgroup_for(ctx, nplanes, G.nkp);
@@ -757,24 +804,27 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneS
                                   nplanes, nt, cvol);
     LAUNCH(ctx, "k_split", chan_bytes(ctx, nt * nplanes) + 4.0 * Y * X * nt * nplanes, s, launch_split(sp, s));
 
-    Rfft2Params rp = rfft2_params(ctx, G, cvol, nt * nplanes * NN, ctx->wsS.p);
+    Rfft2Params rp = rfft2_params(ctx, G, cvol, nt * nplanes * NN, wS);
     LAUNCH(ctx, "k_rfft2", chan_bytes(ctx, nt * nplanes) + 8.0 * ffh * NN * nt * nplanes, s, launch_rfft2(rp, 0, s));
 
     const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
     MacParams mp = mac_params(ctx, G, FLF_DIR_FORWARD, nt);
     mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zgroup;
-    mp.S = (const float2 *)ctx->wsS.p; mp.nzS = nplanes; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nzg;
+    mp.S = (const float2 *)wS; mp.nzS = nplanes; mp.O = wO; mp.nzo = nzg;
     mp.nzo_grid = nzg;
     LAUNCH(ctx, "k_mac_fwd", pbytes + 8.0 * ffh * NN * nt * ((double)nplanes + nzg), s, launch_mac(mp, true, s));
 
-    Irfft2Params ip = irfft2_params(ctx, G, (const float2 *)ctx->wsO.p, nt * NN, chan);
+    if (k > 0 && nslot > 1) CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_chain, 0));
+    Irfft2Params ip = irfft2_params(ctx, G, wO, nt * NN, chan);
     ip.sum_stride = (long long)nt * NN * ffh; ip.nsum = nzg;
     ip.add = !first; ip.final_pass = (int)gi == last; ip.num = ip.final_pass ? num : nullptr;
     const double cb = chan_bytes(ctx, nt) * (1 + ip.add + (ip.num ? 1 : 0));
     LAUNCH(ctx, "k_irfft2", 8.0 * ffh * NN * nt * nzg + cb, s, launch_irfft2(ip, s));
+    if (nslot > 1) CUDA_TRY(ctx, cudaEventRecord(ctx->ev_chain, s));
     first = false;
+    k++;
   }
-  return FLF_OK;
+  return join_streams(ctx, s_caller);
 }
 
 // Back projection of frames [t0, t0+nt) of the channel-major image set
@@ -787,29 +837,42 @@ int backward_chunk(flf_ctx *ctx, const float *chan, const PlaneSet &ps, int nt, 
   const int NN = L.NN, Y = Gm.Y, X = Gm.X;
   size_t sS, sO, sCv;
   ws_needs(ctx, ps, nt, false, sS, sO, sCv);
-  int rc = ensure_ws(ctx, ctx->wsS, sS);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, sO);
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, sCv);
+  sS = slot_bytes(sS), sO = slot_bytes(sO), sCv = slot_bytes(sCv);
+  const int nslot = ws_slots(ctx);
+  int rc = ensure_ws(ctx, ctx->wsS, nslot * sS);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, nslot * sO);
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, nslot * sCv);
   if (rc != FLF_OK) return rc;
-  float *cvol = (float *)ctx->wsCvol.p;
+  // groups alternate over two streams with their own workspace slots (their
+  // planes, and so their outputs, are disjoint)
+  cudaStream_t st[2];
+  if ((rc = fork_streams(ctx, s, st))) return rc;
+  const cudaStream_t s_caller = s;
+  int k = 0;
   for (size_t gi = 0; gi < Gm.groups.size(); gi++) {
     const int nplanes = ps.n[gi];
     if (!nplanes) continue;
+    const int slot = k & (nslot - 1);
+    const cudaStream_t s = st[k & 1];
+    k++;
+    float *cvol = (float *)((char *)ctx->wsCvol.p + slot * sCv);
+    void *wS = (char *)ctx->wsS.p + slot * sS;
+    float2 *wO = (float2 *)((char *)ctx->wsO.p + slot * sO);
     const Group &G = Gm.groups[gi];
     const int ffh = G.f * G.fh;
 
-    Rfft2Params rp = rfft2_params(ctx, G, chan, nt * NN, ctx->wsS.p);
+    Rfft2Params rp = rfft2_params(ctx, G, chan, nt * NN, wS);
     LAUNCH(ctx, "k_rfft2", chan_bytes(ctx, nt) + 8.0 * ffh * NN * nt, s, launch_rfft2(rp, 0, s));
 
     const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
     const int zgb = zgroup_for(ctx, nplanes, G.nkp);
     MacParams mp = mac_params(ctx, G, FLF_DIR_BACKWARD, nt);
     mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zgb;
-    mp.S = (const float2 *)ctx->wsS.p; mp.nzS = 1; mp.O = (float2 *)ctx->wsO.p; mp.nzo = nplanes;
+    mp.S = (const float2 *)wS; mp.nzS = 1; mp.O = wO; mp.nzo = nplanes;
     mp.nzo_grid = (nplanes + zgb - 1) / zgb;
     LAUNCH(ctx, "k_mac_bwd", pbytes + 8.0 * ffh * NN * nt * (1.0 + nplanes), s, launch_mac(mp, false, s));
 
-    Irfft2Params ip = irfft2_params(ctx, G, (const float2 *)ctx->wsO.p, nt * nplanes * NN, cvol);
+    Irfft2Params ip = irfft2_params(ctx, G, wO, nt * nplanes * NN, cvol);
     ip.final_pass = 1;
     LAUNCH(ctx, "k_irfft2", 8.0 * ffh * NN * nt * nplanes + chan_bytes(ctx, nt * nplanes), s, launch_irfft2(ip, s));
 
@@ -818,7 +881,7 @@ int backward_chunk(flf_ctx *ctx, const float *chan, const PlaneSet &ps, int nt, 
     LAUNCH(ctx, "k_merge", chan_bytes(ctx, nt * nplanes) + 4.0 * npix * Y * X * nt * nplanes, s,
            launch_merge(mg, s));
   }
-  return FLF_OK;
+  return join_streams(ctx, s_caller);
 }
 
 // ----------------------------------------------------------------------------
@@ -912,6 +975,10 @@ int flf_ctx_destroy(flf_ctx *ctx) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
+  cudaEvent_t evs[] = {ctx->ev_fork, ctx->ev_join, ctx->ev_chain};
+  for (cudaEvent_t e : evs)
+    if (e) cudaEventDestroy(e);
+  if (ctx->s2) cudaStreamDestroy(ctx->s2);
   delete ctx;
   return FLF_OK;
 }
@@ -1116,9 +1183,11 @@ int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int 
   size_t a, b, c, a2, b2, c2;
   ws_needs(ctx, ps, nt, true, a, b, c);
   ws_needs(ctx, ps, nt, false, a2, b2, c2);
-  rc = ensure_ws(ctx, ctx->wsS, std::max(a, a2));
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, std::max(b, b2));
-  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, std::max(c, c2));
+  const int nslot = ws_slots(ctx);
+  rc = ensure_ws(ctx, ctx->wsS, nslot * slot_bytes(std::max(a, a2)));
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsO, nslot * slot_bytes(std::max(b, b2)));
+  if (rc == FLF_OK) rc = ensure_ws(ctx, ctx->wsCvol, nslot * slot_bytes(std::max(c, c2)));
+  if (rc == FLF_OK) rc = ensure_streams(ctx);
   return rc;
 }
 
@@ -1338,9 +1407,15 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     ctx->opt_geometry_cache = (int)value;
     while ((int)ctx->parked.size() > ctx->opt_geometry_cache) {
       cudaDeviceSynchronize();
+      ctx->mem_epoch++;
       free_geometry(ctx->parked.back());
       ctx->parked.pop_back();
     }
+    return FLF_OK;
+  }
+  if (!strcmp(name, "streams")) {
+    if (value != 1 && value != 2) return fail(ctx, FLF_E_ARG, "streams must be 1 or 2");
+    ctx->opt_streams = (int)value;
     return FLF_OK;
   }
   const bool cr_all = !strcmp(name, "mac_chunk_rows");

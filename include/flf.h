@@ -164,8 +164,11 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
  * transform its PSF allows, planes grouped by size - the default; 0: one
  * size for all planes) and "geometry_cache" (0..16, default 2: how many
  * transfer-matrix sets of other image shapes stay resident, most recent
- * first, so that a series alternating image sizes does not rebuild them).
- * Results agree to rounding whatever the values. */
+ * first, so that a series alternating image sizes does not rebuild them) and
+ * "streams" (1 or 2, default 2: the transform groups of a projection
+ * alternate over this many streams, so one group's transforms overlap the
+ * next group's multiply-accumulate).  Results agree to rounding whatever the
+ * values. */
 int flf_set_option(flf_ctx *ctx, const char *name, long long value);
 
 /* Wait for `stream` and report any failure of earlier launches, including a
