@@ -347,13 +347,16 @@ def run_gb300(args, rank, world, local):
     time.sleep(0.3)
     ms = timed(direct=False)
     clk = clocks.stop()
-    # per-kernel durations: the same steps again, launched directly with CUDA
-    # events around every kernel on the launching stream (a graph replay has
-    # no per-kernel events)
+    # per-kernel durations: the same steps again, launched directly on one
+    # stream with CUDA events around every kernel (a graph replay has no
+    # per-kernel events, and with two streams an event pair would also time the
+    # other stream's kernels running beside it)
+    ctx.set_option("streams", 1)
     ctx.profile(True)
     ms_direct = timed(direct=True)
     prof = ctx.profile_read()
     ctx.profile(False)
+    ctx.set_option("streams", 2)
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
