@@ -15,7 +15,10 @@ Differences from the reference, all in the caller's favour:
   (as with the reference's ``--volumes-on-gpu``); only the camera images go
   up and the finished volumes come down;
 * ``--mode`` and ``--cacheFH`` are accepted for compatibility: every mode runs
-  the GB300 path, and the transfer matrices always stay resident.
+  the GB300 path, and the transfer matrices always stay resident;
+* ``--warm-start NET`` (an addition) starts RL from the learned warm start of
+  warmstart.py (weights trained for one image size; frames of other sizes
+  start from Htf as usual).
 """
 
 import argparse
@@ -32,9 +35,10 @@ import projector as proj
 import tiffio
 
 
-def ProcessBatch(projector, hMatrix, timepoints, destDir, maxIter):
+def ProcessBatch(projector, hMatrix, timepoints, destDir, maxIter, warm=None):
     """Deconvolve the images `timepoints` (one shape) together and save the volumes
-    (deconvolve_time_series.py:9-37)."""
+    (deconvolve_time_series.py:9-37).  With `warm` (a warmstart.WarmStart for this
+    image size), RL starts from the network's volume instead of Htf."""
     os.makedirs(destDir, exist_ok=True)
     images = [lfimage.LoadLightFieldTiff(t) for t in timepoints]
     if any(im.shape != images[0].shape for im in images):
@@ -44,7 +48,8 @@ def ProcessBatch(projector, hMatrix, timepoints, destDir, maxIter):
     projector.storeVolumesOnGPU = True      # Htf stays on the device as the RL start and reference
     try:
         Htf = lfdeconv.BackwardProjectACC(hMatrix, images, progress=None, logPrint=False, projector=projector)
-        result = lfdeconv.DeconvRL(hMatrix, Htf, maxIter=maxIter, Xguess=Htf, logPrint=False,
+        x0 = warm.initial_volume(Htf) if warm is not None else Htf
+        result = lfdeconv.DeconvRL(hMatrix, Htf, maxIter=maxIter, Xguess=x0, logPrint=False,
                                    projector=projector)
     finally:
         projector.storeVolumesOnGPU = saved
@@ -84,6 +89,8 @@ def main(argv, maxIter=8, numParallel=32):
                         help="path to the PSF .mat file (its memmap folder is used when present)")
     parser.add_argument("-t", "--timepoints", dest="timepoints", metavar="IMG", required=True,
                         default=argparse.SUPPRESS, nargs="+", help="files to deconvolve")
+    parser.add_argument("-w", "--warm-start", dest="warmStart", metavar="NET", default=None,
+                        help="warm-start network (warmstart.py) for frames of the size it was trained for")
     args = parser.parse_args(argv)
     if args.numParallel < 1:
         raise SystemExit("ERROR: Invalid batch size: %d" % args.numParallel)
@@ -95,14 +102,21 @@ def main(argv, maxIter=8, numParallel=32):
     hMatrix = psfmatrix.LoadMatrix(args.psfFile, createPSF=True)
 
     groups = GroupByShape(args.timepoints)
+    warm_shape = None
+    if args.warmStart:
+        import warmstart
+        warm_shape = warmstart.WarmStart.trained_shape(args.warmStart)
     total = len(args.timepoints)
     done = 0
     t0 = time.time()
     written = []
     for shape, files in groups:
+        warm = None
+        if warm_shape is not None and tuple(shape[-2:]) == tuple(warm_shape[1:]):
+            warm = warmstart.WarmStart(projector, hMatrix, shape[-2], shape[-1]).load(args.warmStart)
         for b in range(0, len(files), args.numParallel):
             batch = files[b:b + args.numParallel]
-            written += ProcessBatch(projector, hMatrix, batch, args.destDir, args.numIter)
+            written += ProcessBatch(projector, hMatrix, batch, args.destDir, args.numIter, warm)
             done += len(batch)
             print("Deconvolved %d of %d files (%d x %d px)" % (done, total, shape[0], shape[1]), flush=True)
     print("Deconvolved %d files in %.1f s" % (total, time.time() - t0), flush=True)

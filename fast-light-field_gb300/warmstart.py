@@ -419,6 +419,32 @@ class WarmStart:
         return x0
 
 
+    def save(self, path):
+        """Network weights plus the image size and plane count they were trained for."""
+        d = self.net.state_dict()
+        d["meta.shape"] = np.array([self.Z, self.Y, self.X], np.int64)
+        d["meta.nnum"] = np.array([self.hm.Nnum], np.int64)
+        np.savez(path, **d)
+
+    def load(self, path):
+        """Weights saved by save(); the image size and plane count must match."""
+        with np.load(path) as f:
+            d = dict(f)
+        shape = tuple(int(v) for v in d.pop("meta.shape", np.array([self.Z, self.Y, self.X])))
+        nnum = int(d.pop("meta.nnum", np.array([self.hm.Nnum]))[0])
+        if shape != (self.Z, self.Y, self.X) or nnum != self.hm.Nnum:
+            raise ValueError("%s was trained for %d planes of %d x %d px at Nnum %d, not %d planes of %d x %d at %d"
+                             % (path, shape[0], shape[1], shape[2], nnum, self.Z, self.Y, self.X, self.hm.Nnum))
+        self.net.load_state_dict(d)
+        return self
+
+    @staticmethod
+    def trained_shape(path):
+        """(Z, Y, X) a saved network was trained for."""
+        with np.load(path) as f:
+            return tuple(int(v) for v in f["meta.shape"])
+
+
 def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):
     """RL from the network's start volume: back projection, warm start, ``maxIter``
     Prevedel iterations (the reference's default update), on the device; returns the
@@ -432,3 +458,36 @@ def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):
     if maxIter > 0:
         p.RichardsonLucy(warm.hm, x, htf if prevedel else img, maxIter, prevedel=prevedel)
     return x
+
+
+def main(argv=None):
+    """Command line: train a warm-start network for a PSF matrix and image size.
+
+    python warmstart.py -p PSF.mat -s Y X -o net.npz [--steps N] [--beads B] [--filaments F]
+    """
+    import argparse
+    import sys
+
+    import projector as proj
+    import psfmatrix
+
+    ap = argparse.ArgumentParser(description="Train the learned RL warm start for one PSF matrix and image size.")
+    ap.add_argument("-p", "--psf", required=True, help="PSF .mat path (its memmap folder is used when present)")
+    ap.add_argument("-s", "--size", required=True, nargs=2, type=int, metavar=("Y", "X"), help="image size in pixels")
+    ap.add_argument("-o", "--out", required=True, help="output .npz for the network weights")
+    ap.add_argument("--steps", type=int, default=1600, help="training steps")
+    ap.add_argument("--beads", type=int, default=200, help="beads per synthetic training volume")
+    ap.add_argument("--filaments", type=int, default=0, help="filaments per synthetic training volume")
+    ap.add_argument("--target-iters", type=int, default=32, help="plain-RL iterations the network learns to reach")
+    args = ap.parse_args(sys.argv[1:] if argv is None else argv)
+    hm = psfmatrix.LoadMatrix(args.psf, createPSF=True)
+    p = proj.Projector_gb300()
+    ws = WarmStart(p, hm, args.size[0], args.size[1], beads=args.beads, filaments=args.filaments)
+    sec = ws.train(steps=args.steps, target_iters=args.target_iters)
+    ws.save(args.out)
+    print("trained %d steps in %.1f s -> %s" % (args.steps, sec, args.out), flush=True)
+    return args.out
+
+
+if __name__ == "__main__":
+    main()

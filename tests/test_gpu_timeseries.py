@@ -61,3 +61,50 @@ def test_time_series_driver_rejects_bad_arguments(tmp_path, built_lib):
         dts.main(["-p", str(tmp_path / "psf.mat"), "-b", "0", "-t", "x.tif"])
     with pytest.raises(SystemExit):
         dts.main(["-p", str(tmp_path / "psf.mat"), "-i", "0", "-t", "x.tif"])
+
+
+def test_time_series_driver_with_warm_start(tmp_path, built_lib):
+    """--warm-start: a network trained for one frame size (warmstart.py command line)
+    starts RL for frames of that size; other sizes start from Htf; saved weights come
+    back unchanged and refuse another image size."""
+    import deconvolve_time_series as dts
+    import lfdeconv
+    import projector
+    import psfmatrix
+    import synthetic
+    import tiffio
+    import warmstart
+    N = 5
+    H, Ht = synthetic.synthetic_psf(N, [-10, 0, 10], 2)
+    psfmatrix.SaveReducedMatrices(str(tmp_path / "psf"), H, Ht)
+    net = str(tmp_path / "net.npz")
+    warmstart.main(["-p", str(tmp_path / "psf.mat"), "-s", "40", "40", "-o", net, "--steps", "40", "--beads", "20"])
+    assert warmstart.WarmStart.trained_shape(net) == (3, 40, 40)
+    hm = psfmatrix.LoadMatrix(str(tmp_path / "psf.mat"))
+    p = projector.Projector_gb300()
+    ws = warmstart.WarmStart(p, hm, 40, 40).load(net)
+    with np.load(net) as f:
+        assert np.array_equal(ws.net.state_dict()["e0a.w"], f["e0a.w"])
+    with pytest.raises(ValueError, match="trained for"):
+        warmstart.WarmStart(p, hm, 30, 30).load(net)
+    rng = np.random.default_rng(2)
+    files, images = [], []
+    for k, s in enumerate([(40, 40), (30, 30)]):
+        im = (rng.random(s) * 500 + 100).astype(np.uint16)
+        path = str(tmp_path / ("w%d.tif" % k))
+        tiffio.imwrite(path, im)
+        files.append(path)
+        images.append(im.astype(np.float32))
+    out = dts.main(["-p", str(tmp_path / "psf.mat"), "-t"] + files + ["-d", str(tmp_path / "out"), "-i", "2",
+                                                                     "-w", net])
+    vols = {os.path.basename(o): tiffio.imread(o) for o in out}
+    # the 40 x 40 frame: RL from the network's start volume
+    htf = lfdeconv.BackwardProjectACC(hm, images[0][None], None, projector=p, logPrint=False)
+    import torch
+    x0 = ws.initial_volume(torch.as_tensor(htf, device="cuda"))
+    want = lfdeconv.DeconvRL(hm, htf, 2, x0, logPrint=False, projector=p)
+    assert rel(vols["w0_deconvolved.tif"], want[:, 0]) < RL_TOL
+    # the 30 x 30 frame: RL from Htf, as without the option
+    htf1 = lfdeconv.BackwardProjectACC(hm, images[1][None], None, projector=p, logPrint=False)
+    want1 = lfdeconv.DeconvRL(hm, htf1, 2, htf1, logPrint=False, projector=p)
+    assert rel(vols["w1_deconvolved.tif"], want1[:, 0]) < RL_TOL
