@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--train-steps", type=int, default=1600, help="warm-start network training steps")
+    ap.add_argument("--target-iters", type=int, default=32,
+                    help="plain-RL iterations the warm-start network learns to reach")
     ap.add_argument("--tune-steps", type=int, default=0,
                     help="warm-start fine-tuning steps on the data-fit residual (whole volumes)")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
@@ -678,7 +680,7 @@ def run_warmstart(args):
     p = projector.Projector_gb300()
     ws = warmstart.WarmStart(p, hm, Y, X, beads=wl["beads"], filaments=wl.get("filaments", 0))
     refresh = 8 if Y * X * Z < 10_000_000 else 16
-    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=32, log_every=100,
+    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=args.target_iters, log_every=100,
                        refresh_every=refresh)
     tune_s = ws.finetune_residual(steps=args.tune_steps, log_every=50) if args.tune_steps > 0 else 0.0
     dev = ws.dev
@@ -767,6 +769,7 @@ def run_warmstart(args):
             "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": wl["Nnum"], "frames": 1,
                        "psf": psf_desc,
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
+                       "target_iters": args.target_iters,
                        "residual_finetune_steps": args.tune_steps, "finetune_s": round(tune_s, 1),
                        "losses": [[round(float(v), 6) if isinstance(v, float) else v for v in l]
                                   for l in ws.losses[-8:]],
