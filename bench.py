@@ -61,7 +61,7 @@ WORKLOADS = {
                                       "41 planes -100..100 um"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
-    # a time series of frames of three sizes (--frames per size), 500 drifting beads each
+    # a time series of frames of three sizes (--frames per size, default 32), 500 drifting beads each
     "timeseries": dict(Nnum=15, sizes=(30, 45, 67), z=(-75, 75, 5), img_size_ref=21, beads=500,
                        label="time series, Nnum 15, 31 planes -75..75 um, frames at 30x30, 45x45 and 67x67 "
                              "lenslets, RL from x0 = Htf"),
@@ -448,20 +448,23 @@ def run_gb300(args, rank, world, local):
 
 
 def run_timeseries(args):
-    """Mixed-size time series on one device: per size, T frames back projected and
-    deconvolved together (x0 = Htf, as the time-series driver does); one step =
+    """Mixed-size time series on one device (config 2: 32 frames of each size by
+    default): per size, T frames back projected and deconvolved together (x0 = Htf,
+    as the time-series driver does), the multiply-accumulate launch shape autotuned
+    per size and the RL iterations replayed from one CUDA graph per size; one step =
     every frame of every size.  The geometries of all sizes stay resident."""
     import torch
     import projector
     import psfmatrix
     import synthetic
+    import warmstart
     import _flf
     import build_lib
     build_lib.build()
     dev = torch.device("cuda", 0)
     wl = WORKLOADS["timeseries"]
     N = wl["Nnum"]
-    T = max(args.frames, 1)
+    T = args.frames if args.frames > 1 else 32
     z0, z1, dz = wl["z"]
     z = np.arange(z0, z1 + dz / 2, dz)
     Z = len(z)
@@ -472,31 +475,49 @@ def run_timeseries(args):
     ctx = p.context(hm)
     ctx.set_option("geometry_cache", len(wl["sizes"]))
     rng = np.random.default_rng(4321)
+    s = torch.cuda.current_stream(dev)
     data = []
     t_setup = time.time()
     for L in wl["sizes"]:
         Y = X = L * N
-        vol0, pos = synthetic.bead_volume((Z, Y, X), wl["beads"], seed=int(rng.integers(1 << 30)), sigma=1.0,
-                                          amp_range=(500.0, 1000.0))
-        frames = [vol0]
-        for _ in range(T - 1):       # drift N(0, 0.5 voxel) per frame
-            pos = pos + rng.normal(0.0, 0.5, pos.shape)
-            frames.append(synthetic.bead_volume((Z, Y, X), 0, positions=pos, sigma=1.0, amp_range=(500.0, 1000.0))[0])
-        gt = torch.as_tensor(np.stack(frames, axis=1), device=dev)
+        # drifting beads rendered on the device: positions move N(0, 0.5 voxel) per frame
+        pos = np.stack([rng.uniform(0, Z - 1, wl["beads"]), rng.uniform(0, Y - 1, wl["beads"]),
+                        rng.uniform(0, X - 1, wl["beads"])], axis=1)
+        amp = rng.uniform(500.0, 1000.0, wl["beads"])
+        gt = torch.zeros((T, Z, Y, X), device=dev)
+        for t in range(T):
+            if t:
+                pos = pos + rng.normal(0.0, 0.5, pos.shape)
+            pts = torch.as_tensor(np.concatenate([pos, amp[:, None]], axis=1).astype(np.float32), device=dev)
+            _flf.render_blobs(gt[t], pts, 1.0, s.cuda_stream)
+        gt = gt.permute(1, 0, 2, 3).contiguous()
         clean = p.ForwardProjectACC(hm, gt, None)
         img = torch.poisson((clean.double() + 100.0).clamp_min(0)).float()
         data.append((Y, X, img))
         del gt, clean
-    setup_s = time.time() - t_setup
-    s = torch.cuda.current_stream(dev)
     bufs = [(torch.empty((Z, T, Y, X), device=dev), torch.empty((Z, T, Y, X), device=dev)) for Y, X, _ in data]
+    tuned = {}
+    for (Y, X, _), _b in zip(data, bufs):
+        tuned["%dx%d" % (Y, X)] = p.autotune(hm, T, Y, X)
+    # one direct pass sizes every workspace before the graphs bake their addresses in
+    for (Y, X, img), (htf, x) in zip(data, bufs):
+        p._prepare(ctx, Y, X, hm)
+        ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
+        x.copy_(htf)
+        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    graphs = []
+    for (Y, X, img), (htf, x) in zip(data, bufs):
+        p._prepare(ctx, Y, X, hm)
+        graphs.append(ctx.rl_graph(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X))
+    setup_s = time.time() - t_setup
 
     def step():
-        for (Y, X, img), (htf, x) in zip(data, bufs):
+        for (Y, X, img), (htf, x), g in zip(data, bufs, graphs):
             p._prepare(ctx, Y, X, hm)
             ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
             x.copy_(htf)
-            ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=s.cuda_stream)
+            g.launch(s.cuda_stream)
 
     for _ in range(max(args.warmup, 1)):
         step()
@@ -519,10 +540,14 @@ def run_timeseries(args):
             "data": "synthetic",
             "config": {"workload": wl["label"], "frames_per_size": T, "sizes_px": [Y for Y, _, _ in data],
                        "planes": Z, "nnum": N, "rl_iterations": args.iters, "volumes_per_step": nvol,
-                       "device_gb": round(ctx.memory_usage() / 1e9, 2), "setup_s": round(setup_s, 1),
+                       "rl_launch": "one CUDA graph per size (%s kernels)" % [g.kernels for g in graphs],
+                       "autotuned": tuned, "device_gb": round(ctx.memory_usage() / 1e9, 2),
+                       "setup_s": round(setup_s, 1),
                        "l2": "inputs larger than L2 (transfer matrices of three geometries)"},
             "rl_iterations_per_s": nvol * args.iters / (ms / 1000.0), "clocks": clk}
     print(json.dumps(line), flush=True)
+    for g in graphs:
+        g.close()
 
 
 def run_rectify(args):
