@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--train-steps", type=int, default=1600, help="warm-start network training steps")
+    ap.add_argument("--held-out", type=int, default=0,
+                    help="held-out volumes of the warm-start evaluation (0: 256 at 450 x 450, 16 at full field)")
     ap.add_argument("--target-iters", type=int, default=32,
                     help="plain-RL iterations the warm-start network learns to reach")
     ap.add_argument("--tune-steps", type=int, default=0,
@@ -711,7 +713,7 @@ def run_warmstart(args):
     dev = ws.dev
     s = torch.cuda.current_stream(dev)
     rng = np.random.default_rng(2024)
-    nseed = 16
+    nseed = args.held_out if args.held_out > 0 else (256 if Y * X * Z < 10_000_000 else 16)
     ctx = ws.ctx
 
     def resid(x, img):
