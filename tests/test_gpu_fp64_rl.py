@@ -1,8 +1,7 @@
 """FP32 GPU Richardson-Lucy against the FP64 oracle at benchmark sizes.
 
-The spec accuracy statement: max and relative L2 error of the GPU's
-FP32 RL against an FP64 CPU restatement of the same iterations, per
-configuration.  Runs only with FLF_FP64_CHECK=1 (a few minutes of host CPU);
+The accuracy statement per configuration: max and relative L2 error of the
+GPU's FP32 RL against an FP64 CPU restatement of the same iterations.  Runs only with FLF_FP64_CHECK=1 (a few minutes of host CPU);
 ``python tests/test_gpu_fp64_rl.py`` prints the numbers.
 
 * config 0: 450 x 450 px, Nnum 15, 11 planes at -25..25 um, 8 Prevedel
