@@ -450,7 +450,7 @@ def run_gb300(args, rank, world, local):
 
 
 def run_timeseries(args):
-    """Mixed-size time series on one device (config 2: 32 frames of each size by
+    """Mixed-size time series on one device (32 frames of each size by
     default): per size, T frames back projected and deconvolved together (x0 = Htf,
     as the time-series driver does), the multiply-accumulate launch shape autotuned
     per size and the RL iterations replayed from one CUDA graph per size; one step =

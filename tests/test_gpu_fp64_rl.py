@@ -1,10 +1,11 @@
 """FP32 GPU Richardson-Lucy against the FP64 oracle at benchmark sizes.
 
 The accuracy statement per configuration: max and relative L2 error of the
-GPU's FP32 RL against an FP64 CPU restatement of the same iterations.  Runs only with FLF_FP64_CHECK=1 (a few minutes of host CPU);
+GPU's FP32 RL against an FP64 CPU restatement of the same iterations.  Runs
+only with FLF_FP64_CHECK=1 (a few minutes of host CPU);
 ``python tests/test_gpu_fp64_rl.py`` prints the numbers.
 
-* config 0: 450 x 450 px, Nnum 15, 11 planes at -25..25 um, 8 Prevedel
+* 450 x 450 px, Nnum 15, 11 planes at -25..25 um, 8 Prevedel
   iterations from a uniform volume;
 * full field, cut to 3 planes (z = -100, 0, 100 um, PSF sizes 841 / 61 / 841)
   of the 1005 x 1005 workload, 4 iterations.
@@ -119,7 +120,7 @@ def _pool():
     return mp.get_context("spawn").Pool(max(1, min(os.cpu_count() or 1, 32)))
 
 
-def test_config0_fp32_rl_matches_fp64(built_lib):
+def test_450px_11planes_fp32_rl_matches_fp64(built_lib):
     with _pool() as pool:
         r = compare("small", None, 8, pool)
     assert r["max_abs_rel"] < TOL and r["rel_l2"] < TOL, r

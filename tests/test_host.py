@@ -95,7 +95,7 @@ def test_check_planes():
 
 def test_psf_sizes_follow_reference_rule():
     import synthetic
-    # config 0 (M40, z -25..25 um): support sizes of the reference generator
+    # M40 optics, z -25..25 um: support sizes of the reference generator
     assert synthetic.psf_sizes(15, np.arange(-25, 26, 5), 7) == [211, 181, 151, 91, 61, 61, 61, 91, 151, 181, 211]
 
 
