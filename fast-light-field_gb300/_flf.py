@@ -60,6 +60,7 @@ _SIGS = {
     "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
+    "flf_net_conv16_tcgen05": (_I, [_I]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
     "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P]),
     "flf_pool2": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
@@ -190,13 +191,23 @@ def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
 
 
 def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):
-    """conv3d for 16 -> 16 channels on the tcgen05 tensor cores (tiles of rows x 128 voxels)."""
+    """conv3d for 16 -> 16 channels on the tcgen05 tensor cores.
+
+    rows = 0: the warp-specialised kernel with TMA-staged input slabs;
+    1, 4, 5: single-role kernels with tiles of rows x 128 voxels (5 = 4 rows,
+    double-buffered)."""
     lib = load_library()
     B, Z, Y, X, C = _vshape(x)
     if C != 16 or int(y.shape[-1]) != 16:
         raise ValueError("conv3d_tc takes 16 channels in and out")
     _check_global(lib.flf_conv3d_tc(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X,
                                     int(bool(relu)), int(rows), _ptr(stream)))
+
+
+def conv16_tcgen05(on):
+    """Select the kernel conv3d and ws_head use for 16 -> 16 channels (True: the
+    warp-specialised tcgen05 kernel, False: mma.sync); returns the previous choice."""
+    return bool(load_library().flf_net_conv16_tcgen05(int(bool(on))))
 
 
 def net_status():

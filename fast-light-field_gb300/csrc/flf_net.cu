@@ -22,6 +22,8 @@
 //                     ReLU mask, MSE loss gradient, Adam, bead rendering.
 #include "flf_internal.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 namespace flf {
@@ -660,6 +662,397 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// 16 -> 16 channels, warp-specialised on tcgen05 with TMA staging.  A work
+// item is a column of output, R rows (y) x 126 voxels (x), over a run of z
+// planes.  The CTA walks z: output plane z needs input slabs z-1, z, z+1, a
+// slab being (R+2) rows x 130 voxels of one plane (the x / y halo included).
+// Slabs sit in a ring of S shared-memory slots that TMA fills: a tensor map
+// over [B][Z][Y][X][16] BF16 with box 8 channels x 130 x (R+2) x 1 x 1, two
+// loads per slab for the two 8-channel planes, so a slab row is a canonical
+// K-major A operand (8-voxel x 16-byte core matrices, the planes one LBO
+// apart).  Coordinates outside the volume read zeros: the 'same' padding.
+// The three x taps are folded into N: for each (dz, dy) one
+//   tcgen05.mma  M 128 (slab voxels c) x N 48 (dx, co) x K 16 (ci)
+// accumulates D[c][dx][co] = sum over (dz, dy, ci) of in[c] w[dz][dy][dx][ci][co],
+// and the epilogue forms out[i][co] = D[i][0][co] + D[i+1][1][co] + D[i+2][2][co]
+// (warp shuffles; the two lanes past each 32-lane TMEM quarter come through
+// shared memory).  That is 9 MMAs per output row instead of 27 with N = 16,
+// a third of the operand traffic from shared memory, and 126 outputs per
+// 128-voxel MMA row.
+//   warp 0     producer: one thread issues the TMA loads;
+//   warp 1     MMA issuer: one thread issues 9 x R MMAs per output plane into
+//              one of two TMEM accumulator stages (R x 48 columns each),
+//              commits to the stage's full barrier, and releases the slab no
+//              longer needed;
+//   warps 2-17 epilogue: warp w reads TMEM lane quarter w % 4 (tcgen05.ld)
+//              for 8 of the 16 output channels and half of the rows, forms
+//              the tap sum, then bias / ReLU / mask and BF16 stores, or with
+//              HEAD the clamped, scaled start volume from output channel 0.
+// Every mbarrier wait is bounded (1 s).  A wait that gives up sets g_net_err
+// and a shared abort flag that every role polls; the epilogue warps decide
+// together (barrier.red.or), and the CTA waits (bounded) for its copies and
+// MMAs in flight before TMEM is released.
+// ---------------------------------------------------------------------------
+struct Tma16Grid {   // work items: [B][zchunks][yblocks][xsegs] columns of R x 126 voxels over zc planes
+  int xsegs, yblocks, zchunks, zc;
+  long long items;
+};
+
+namespace {
+
+constexpr int TMA16_XW = 126;   // output voxels per 128-lane MMA row
+
+__device__ __forceinline__ void net_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void net_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            int c4, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+// named barrier 1 over the 512 epilogue threads, OR of `pred` across them
+__device__ __forceinline__ bool epi_bar_or(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.red.or.pred q, 1, 512, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void epi_bar() { asm volatile("barrier.sync 1, 512;\n" ::: "memory"); }
+// bounded wait that also gives up when another role has aborted
+__device__ __forceinline__ bool role_wait(uint32_t bar, uint32_t parity, volatile int *abort_s, int code) {
+  unsigned long long t0 = 0;
+  for (int it = 0;; it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*abort_s) return false;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    if (it == 0) {
+      t0 = t;
+    } else if (t - t0 > 1000000000ULL) {
+      *abort_s = 1;
+      atomicExch(&g_net_err, code);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t addr, float *v) {
+  uint32_t u[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7])
+               : "r"(addr));
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = __uint_as_float(u[k]);
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, float *v) {
+  uint32_t u[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]),
+        "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
+      : "r"(addr));
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(u[k]);
+}
+
+}  // namespace
+
+template <int R, int S, bool HEAD>
+__global__ void __launch_bounds__(576, 1)
+    k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  constexpr int PXW = 130, PYH = R + 2;
+  constexpr uint32_t PLANE_TX = PYH * PXW * 16;              // bytes one TMA load writes
+  constexpr uint32_t PLANE = (PLANE_TX + 127) / 128 * 128;   // plane stride inside a slot
+  constexpr uint32_t SLOT = 2 * PLANE;
+  constexpr uint32_t BBLK = 48 * 16 * 2;                     // B operand of one (dz, dy): N 48 x K 16
+  constexpr uint32_t SLAB0 = (9 * BBLK + 1023) / 1024 * 1024;
+  constexpr uint32_t EDGE = 2 * 2 * 4 * R * 2 * 16 * 4;      // [stage][half][quarter][row][lane 0/1][dx 1..2 x 8] f32
+  constexpr uint32_t STAGE_COLS = R * 48;
+  constexpr uint32_t TCOLS = 2 * STAGE_COLS <= 256 ? 256 : 512;
+  static_assert(2 * STAGE_COLS <= 512, "two accumulator stages of R rows x 48 columns");
+  // layout: [B operands][S slots x 2 planes][edge exchange][mbarriers][tmem address][abort flag]
+  unsigned char *Wb = smem;
+  float *edge = reinterpret_cast<float *>(smem + SLAB0 + S * SLOT);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SLAB0 + S * SLOT + EDGE);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 5);
+  volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t wb_s = su32(Wb), slab_s = su32(smem + SLAB0), bar_s = su32(bars);
+  auto full = [&](uint32_t k) { return bar_s + 8u * k; };
+  auto empty = [&](uint32_t k) { return bar_s + 8u * (S + k); };
+  auto tfull = [&](uint32_t k) { return bar_s + 8u * (2 * S + k); };
+  auto tempty = [&](uint32_t k) { return bar_s + 8u * (2 * S + 2 + k); };
+  const uint32_t fin = bar_s + 8u * (2 * S + 4);
+
+  // B operands: block (dz, dy) holds B[n = dx*16 + co][k = ci] = w[tap = dz*9 + dy*3 + dx][ci][co],
+  // core matrix (n/8, ci/8) at (n/8)*256 + (ci/8)*128, row n%8 at 16 B, element ci%8 at 2 B
+  for (int i = tid; i < 9 * 48; i += 576) {
+    const int blk = i / 48, n = i % 48;
+    const int tap = blk * 3 + n / 16, co = n % 16;
+    uint32_t pk[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const unsigned short lo = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c) * 16 + co]);
+      const unsigned short hi = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c + 1) * 16 + co]);
+      pk[c] = (uint32_t)lo | ((uint32_t)hi << 16);
+    }
+    unsigned char *row = Wb + blk * BBLK + (n >> 3) * 256 + (n & 7) * 16;
+    *reinterpret_cast<uint4 *>(row) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    *reinterpret_cast<uint4 *>(row + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  }
+  if (tid == 0) {
+    for (int k = 0; k < S; k++) {
+      net_mbar_init(full(k), 1);
+      net_mbar_init(empty(k), 1);
+    }
+    for (int k = 0; k < 2; k++) {
+      net_mbar_init(tfull(k), 1);
+      net_mbar_init(tempty(k), 512);
+    }
+    net_mbar_init(fin, 1);
+    *abort_s = 0;
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // the B operands, for the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  auto decode = [&](long long it, int &b, int &zlo, int &nz, int &y0, int &x0) {
+    long long q = it;
+    x0 = (int)(q % g.xsegs) * TMA16_XW;
+    q /= g.xsegs;
+    y0 = (int)(q % g.yblocks) * R;
+    q /= g.yblocks;
+    zlo = (int)(q % g.zchunks) * g.zc;
+    b = (int)(q / g.zchunks);
+    nz = min(p.Z - zlo, g.zc);
+  };
+
+  uint32_t nload = 0;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- producer ----
+      for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
+        int b, zlo, nz, y0, x0;
+        decode(it, b, zlo, nz, y0, x0);
+        for (int k = 0; k < nz + 2; k++) {
+          const uint32_t slot = nload % S;
+          if (nload >= S && !role_wait(empty(slot), ((nload / S) - 1) & 1, abort_s, 4)) break;
+          net_expect_tx(full(slot), 2 * PLANE_TX);
+          const uint32_t dst = slab_s + slot * SLOT;
+          tma_load_5d(dst, &tx, 0, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
+          tma_load_5d(dst + PLANE, &tx, 8, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
+          nload++;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 48, M = 128
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
+      uint64_t bdesc[9];
+#pragma unroll
+      for (int blk = 0; blk < 9; blk++) bdesc[blk] = umma_desc(wb_s + blk * BBLK, 128, 256);
+      const uint64_t a_desc = umma_desc(slab_s, PLANE, 128);   // slot 0, row 0
+      const uint32_t a_lo = (uint32_t)a_desc, a_hi = (uint32_t)(a_desc >> 32);
+      uint32_t n = 0, q = 0;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
+        int b, zlo, nz, y0, x0;
+        decode(it, b, zlo, nz, y0, x0);
+        ok = role_wait(full(n % S), (n / S) & 1, abort_s, 5) &&
+             role_wait(full((n + 1) % S), ((n + 1) / S) & 1, abort_s, 5);
+        for (int zi = 0; zi < nz && ok; zi++) {
+          const uint32_t k2 = n + zi + 2;
+          const uint32_t stage = q & 1;
+          ok = role_wait(full(k2 % S), (k2 / S) & 1, abort_s, 5) &&
+               (q < 2 || role_wait(tempty(stage), ((q >> 1) - 1) & 1, abort_s, 6));
+          if (!ok) break;
+          tc_fence_after();
+          // low descriptor words (start address >> 4 | LBO >> 4 << 16) of the three slabs; a row
+          // of 130 voxels is 130 in units of 16 bytes
+          const uint32_t a0 = a_lo + ((n + zi) % S) * (SLOT >> 4), a1 = a_lo + ((n + zi + 1) % S) * (SLOT >> 4),
+                         a2 = a_lo + (k2 % S) * (SLOT >> 4);
+          const uint32_t dcol = tmem + stage * STAGE_COLS;
+#pragma unroll
+          for (int blk = 0; blk < 9; blk++) {
+            const int dz = blk / 3, dy = blk % 3;
+            const uint32_t al = dz == 0 ? a0 : (dz == 1 ? a1 : a2);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              const uint64_t ad = ((uint64_t)a_hi << 32) | (uint64_t)(al + (uint32_t)((r + dy) * PXW));
+              umma_f16(dcol + r * 48, ad, bdesc[blk], idesc, blk > 0 ? 1u : 0u);
+            }
+          }
+          umma_commit(tfull(stage));
+          umma_commit(empty((n + zi) % S));   // slab z-1 has no later user in this column
+          q++;
+        }
+        if (!ok) break;
+        umma_commit(empty((n + nz) % S));
+        umma_commit(empty((n + nz + 1) % S));
+        n += nz + 2;
+      }
+    }
+  } else {
+    // ---- epilogue: warps 2..17; warp w owns TMEM lane quarter w % 4, output channels 8*hf..8*hf+7
+    // and rows RW*rh..RW*rh+RW-1 ----
+    constexpr int RW = R / 2;
+    const int e = warp - 2, qd = warp & 3, hf = (e >> 2) & 1, rh = e >> 3;
+    const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
+    const int i = qd * 32 + lane;   // output voxel of the segment (valid for i < 126)
+    float bias[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) bias[c] = (!HEAD && p.bias) ? p.bias[hf * 8 + c] : 0.f;
+    uint32_t q = 0;
+    bool ok = true;
+    for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
+      int b, zlo, nz, y0, x0;
+      decode(it, b, zlo, nz, y0, x0);
+      const int x = x0 + i;
+      for (int zi = 0; zi < nz; zi++) {
+        const uint32_t stage = q & 1;
+        // tcgen05.ld is .sync.aligned and the edge exchange uses a named barrier:
+        // all epilogue warps take one decision
+        const bool late = !role_wait(tfull(stage), (q >> 1) & 1, abort_s, 7);
+        if (epi_bar_or(late)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        float d[RW][3][8];
+#pragma unroll
+        for (int rr = 0; rr < RW; rr++)
+#pragma unroll
+          for (int dx = 0; dx < 3; dx++)
+            tmem_ld8(tmem + lane_base + stage * STAGE_COLS + (rh * RW + rr) * 48 + dx * 16 + hf * 8, d[rr][dx]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        tc_fence_before();
+        net_arrive(tempty(stage));   // the accumulator stage is free for the next plane
+        q++;
+        // lanes 0 and 1 publish D[.][1] and D[.][2] for lanes 30 and 31 of the quarter below
+        float *eg = edge + (size_t)(((stage * 2 + hf) * 4 + qd) * R) * 32;
+        if (lane < 2) {
+#pragma unroll
+          for (int rr = 0; rr < RW; rr++) {
+            float4 *e4 = reinterpret_cast<float4 *>(eg + ((rh * RW + rr) * 2 + lane) * 16);
+            e4[0] = make_float4(d[rr][1][0], d[rr][1][1], d[rr][1][2], d[rr][1][3]);
+            e4[1] = make_float4(d[rr][1][4], d[rr][1][5], d[rr][1][6], d[rr][1][7]);
+            e4[2] = make_float4(d[rr][2][0], d[rr][2][1], d[rr][2][2], d[rr][2][3]);
+            e4[3] = make_float4(d[rr][2][4], d[rr][2][5], d[rr][2][6], d[rr][2][7]);
+          }
+        }
+        // out[i] = D[i][0] + D[i+1][1] + D[i+2][2]; lanes 30 and 31 are corrected below (a shuffle
+        // past lane 31 returns the lane's own value)
+        float o[RW][8];
+#pragma unroll
+        for (int rr = 0; rr < RW; rr++)
+#pragma unroll
+          for (int c = 0; c < 8; c++)
+            o[rr][c] = d[rr][0][c] + __shfl_down_sync(0xffffffffu, d[rr][1][c], 1) +
+                       __shfl_down_sync(0xffffffffu, d[rr][2][c], 2);
+        epi_bar();   // every quarter's edge values are in shared memory
+        if (lane >= 30) {
+          if (qd < 3) {
+            // lane 30 took its own D[2] for D[32(qd+1)][2]; lane 31 its own D[1] and D[2] for
+            // D[32(qd+1)][1] and D[32(qd+1)+1][2]
+            const float *en = edge + (size_t)(((stage * 2 + hf) * 4 + qd + 1) * R) * 32;
+#pragma unroll
+            for (int rr = 0; rr < RW; rr++) {
+              const float *l0 = en + ((rh * RW + rr) * 2) * 16, *l1 = l0 + 16;
+#pragma unroll
+              for (int c = 0; c < 8; c++) {
+                if (lane == 30) o[rr][c] += l0[8 + c] - d[rr][2][c];
+                else o[rr][c] += l0[c] + l1[8 + c] - d[rr][1][c] - d[rr][2][c];
+              }
+            }
+          }
+        }
+        const int z = zlo + zi;
+        if (i >= TMA16_XW) continue;
+#pragma unroll
+        for (int rr = 0; rr < RW; rr++) {
+          const int y = y0 + rh * RW + rr;
+          if (HEAD) {
+            if (hf == 0 && b < h.T && z < h.Zr && y < h.Yr && x < h.Xr) {
+              const float sc = h.sum_x1[b] / h.count;
+              h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[rr][0] + h.bias, h.floor) * sc;
+            }
+            continue;
+          }
+          if (x >= p.X || y >= p.Y) continue;
+          const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16 + hf * 8;
+          uint4 mk;
+          if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + off);
+          uint4 outv;
+          __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(&outv);
+          const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            float v0 = o[rr][2 * k] + bias[2 * k];
+            float v1 = o[rr][2 * k + 1] + bias[2 * k + 1];
+            if (p.relu) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            if (p.mask) {
+              const float2 mf = __bfloat1622float2(m2[k]);
+              if (!(mf.x > 0.f)) v0 = 0.f;
+              if (!(mf.y > 0.f)) v1 = 0.f;
+            }
+            hv[k] = __floats2bfloat162_rn(v0, v1);
+          }
+          *reinterpret_cast<uint4 *>(p.y + off) = outv;
+        }
+      }
+    }
+  }
+
+  __syncthreads();   // every role has left its loop (normally, or on an abort)
+  if (warp == 0 && lane == 0 && *abort_s) {
+    // copies still in flight land before the CTA exits: wait for the last load of every slot
+    for (uint32_t s = 0; s < (uint32_t)S && s < nload; s++) {
+      const uint32_t last = s + ((nload - 1 - s) / S) * S;
+      if (!net_mbar_wait(full(s), (last / S) & 1, 1000000000ULL)) atomicExch(&g_net_err, 8);
+    }
+  }
+  if (warp == 1 && lane == 0) {
+    // every MMA issued has completed before the accumulator is released
+    umma_commit(fin);
+    if (!net_mbar_wait(fin, 0, 1000000000ULL)) atomicExch(&g_net_err, 9);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+  }
+}
+
 // Weight gradient.  CTA = (voxel chunk, tap) x (ci tile CM, co tile CN); the 4
 // warps take alternate k16 steps of its voxels (split-K) and are summed in
 // shared memory at the end, then added to dW with FP32 atomics.
@@ -1096,11 +1489,90 @@ static cudaError_t launch_t16(const ConvParams &p, const HeadOut &h, cudaStream_
   return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }
+  return fn;
+}
+
+template <int R, int S, bool HEAD>
+static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
+  constexpr size_t PLANE = ((R + 2) * 130 * 16 + 127) / 128 * 128;
+  constexpr size_t SMEM = (9 * 1536 + 1023) / 1024 * 1024 + S * 2 * PLANE + 2 * 2 * 4 * R * 2 * 16 * 4 + (2 * S + 5) * 8 + 8;
+  static int sms = 0;
+  if (!sms) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3d_tma16<R, S, HEAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    if (e != cudaSuccess) return e;
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 1;
+  }
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  if (M == 0) return cudaSuccess;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  if (reinterpret_cast<uintptr_t>(p.x) % 16) return cudaErrorMisalignedAddress;
+  // [B][Z][Y][X][16] BF16, innermost first; one box = one 8-channel plane of a slab
+  CUtensorMap map;
+  const cuuint64_t dims[5] = {16, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
+  const cuuint64_t strides[4] = {32, 32ull * p.X, 32ull * p.X * p.Y, 32ull * p.X * p.Y * p.Z};
+  const cuuint32_t box[5] = {8, 130, (cuuint32_t)(R + 2), 1, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(p.x), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  Tma16Grid g;
+  g.xsegs = (p.X + TMA16_XW - 1) / TMA16_XW;
+  g.yblocks = (p.Y + R - 1) / R;
+  // split z into chunks when whole columns fill the GPU unevenly (each chunk reloads 2 halo slabs)
+  long long best = -1;
+  int zc_best = p.Z;
+  for (int c = 1; c <= 8 && c <= p.Z; c++) {
+    const int zc = (p.Z + c - 1) / c;
+    const long long items = (long long)p.B * ((p.Z + zc - 1) / zc) * g.yblocks * g.xsegs;
+    const long long cost = (items + sms - 1) / sms * (zc + 2);
+    if (best < 0 || cost < best) {
+      best = cost;
+      zc_best = zc;
+    }
+  }
+  g.zc = zc_best;
+  g.zchunks = (p.Z + g.zc - 1) / g.zc;
+  g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
+  const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
+  k_conv3d_tma16<R, S, HEAD><<<grid, 576, SMEM, s>>>(map, p, h, g);
+  return cudaGetLastError();
+}
+
+static int g_conv16_tc = 1;   // 16 -> 16 convolutions: 1 = tcgen05 with TMA staging (default), 0 = mma.sync tiles
+
+int net_set_conv16_tcgen05(int on) {
+  const int old = g_conv16_tc;
+  g_conv16_tc = on ? 1 : 0;
+  return old;
+}
+
+cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s) {
+  return launch_tma16<4, 6, false>(p, HeadOut{}, s);
+}
+
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
   const long long M = (long long)p.B * p.Z * p.Y * p.X;
   if (M == 0) return cudaSuccess;
   p.splits = 1;
-  if (p.Ci == 16 && p.Co == 16) return launch_t16<false>(p, HeadOut{}, s);
+  if (p.Ci == 16 && p.Co == 16)
+    return g_conv16_tc ? launch_tma16<4, 6, false>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
   if (p.Ci == 16 && p.Co == 32) return launch_tiled<16, 32>(p, s);
   if (p.Ci == 32 && p.Co == 16) return launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32) return launch_tiled<32, 32>(p, s);
@@ -1267,7 +1739,7 @@ cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor
                            int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s) {
   ConvParams p{(const bf16 *)d, (const bf16 *)w, nullptr, nullptr, nullptr, T, Zp, Yp, Xp, 16, 16, 0, nullptr, 1};
   HeadOut h{x0, sum_x1, (float)Z * Y * X, bias, floor_, T, Z, Y, X};
-  return launch_t16<true>(p, h, s);
+  return g_conv16_tc ? launch_tma16<4, 6, true>(p, h, s) : launch_t16<true>(p, h, s);
 }
 
 cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,

@@ -246,12 +246,19 @@ int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      void *stream);
 /* flf_conv3d_tc: flf_conv3d for 16 -> 16 channels on the tcgen05 tensor cores
- * (accumulators in TMEM; tiles of `rows` (1 or 4) x 128 voxels, one
- * accumulator per row).  flf_net_status: FLF_OK, or FLF_E_TIMEOUT when a
- * bounded wait inside it gave up since the last call. */
+ * (accumulators in TMEM).  rows = 0: the warp-specialised kernel (TMA loads
+ * of input slabs into a shared-memory ring, one MMA-issuing thread, two TMEM
+ * accumulator stages, 4 epilogue warps; 4 x 128-voxel tiles walking z);
+ * rows = 1, 4 or 5: single-role kernels with tiles of 1 or 4 rows x 128
+ * voxels (5 = 4 rows, double-buffered).  flf_net_status: FLF_OK, or
+ * FLF_E_TIMEOUT when a bounded wait inside one gave up since the last call.
+ * flf_net_conv16_tcgen05(on): the kernel flf_conv3d and flf_ws_head use for
+ * 16 -> 16 channels: 1 = the warp-specialised tcgen05 kernel, 0 = the
+ * mma.sync kernel; returns the previous setting. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream);
 int flf_net_status(void);
+int flf_net_conv16_tcgen05(int on);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
 int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream);
 int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);

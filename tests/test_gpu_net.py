@@ -159,11 +159,12 @@ def test_mse_adam_and_blobs(env):
     assert np.max(np.abs(vol.cpu().numpy() - ref)) < 1e-5
 
 
-@pytest.mark.parametrize("rows", [1, 4, 5])
+@pytest.mark.parametrize("rows", [0, 1, 4, 5])
 @pytest.mark.parametrize("shape,relu,masked", [((1, 2, 3, 5), True, False), ((2, 3, 4, 130), False, False),
                                                ((1, 4, 9, 300), True, True), ((2, 5, 6, 128), True, False)])
 def test_conv3d_tcgen05(env, shape, relu, masked, rows):
-    """The 16 -> 16 convolution on the tcgen05 tensor cores (TMEM accumulator)."""
+    """The 16 -> 16 convolution on the tcgen05 tensor cores (TMEM accumulator);
+    rows = 0 is the warp-specialised kernel with TMA-staged slabs."""
     torch, _flf = env
     g = torch.Generator().manual_seed(sum(shape))
     x = torch.randn(shape + (16,), generator=g).bfloat16()
@@ -180,3 +181,51 @@ def test_conv3d_tcgen05(env, shape, relu, masked, rows):
     if masked:
         ref = ref * (m.double() > 0)
     _close(torch, y, ref)
+
+
+@pytest.mark.parametrize("shape,relu,masked", [((1, 6, 200, 700), True, True), ((3, 9, 10, 130), False, False),
+                                               ((1, 1, 1, 1), True, False)])
+def test_conv3d_tcgen05_warp_specialised_many_items(env, shape, relu, masked):
+    """More work items than SMs (each CTA walks several columns through its slab
+    ring), z split into chunks, and a single voxel."""
+    torch, _flf = env
+    g = torch.Generator().manual_seed(shape[2])
+    x = torch.randn(shape + (16,), generator=g).bfloat16()
+    w = (torch.randn((27, 16, 16), generator=g) / np.sqrt(27 * 16)).bfloat16()
+    b = torch.randn(16, generator=g).float()
+    m = torch.randn(shape + (16,), generator=g).bfloat16() if masked else None
+    y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d_tc(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, mask=m.cuda() if masked else None, rows=0)
+    torch.cuda.synchronize()
+    _flf.net_status()
+    ref = _ref_conv(torch, x.double(), w.double(), b.double())
+    if relu:
+        ref = ref.clamp_min(0)
+    if masked:
+        ref = ref * (m.double() > 0)
+    _close(torch, y, ref)
+
+
+@pytest.mark.parametrize("shape", [(2, 4, 6, 10), (1, 5, 17, 260)])
+def test_conv3d_dispatch_to_tcgen05(env, shape):
+    """flf_conv3d routes 16 -> 16 channels to the tcgen05 kernel when selected; the
+    result agrees with the mma.sync kernel to the BF16 rounding of the output."""
+    torch, _flf = env
+    g = torch.Generator().manual_seed(17)
+    x = torch.randn(shape + (16,), generator=g).bfloat16().cuda()
+    w = (torch.randn((27, 16, 16), generator=g) / 20).bfloat16().cuda()
+    b = torch.randn(16, generator=g).float().cuda()
+    out = {}
+    for on in (False, True):
+        old = _flf.conv16_tcgen05(on)
+        try:
+            y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
+            _flf.conv3d(x, w, b, y, relu=True)
+            torch.cuda.synchronize()
+            _flf.net_status()
+            out[on] = y
+        finally:
+            _flf.conv16_tcgen05(old)
+    ref = _ref_conv(torch, x.double().cpu(), w.double().cpu(), b.double().cpu()).clamp_min(0)
+    _close(torch, out[True], ref)
+    assert float((out[True].float() - out[False].float()).abs().max()) <= 1e-2 * float(ref.abs().max())

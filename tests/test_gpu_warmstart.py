@@ -47,8 +47,18 @@ def _reference_forward(torch, ws_mod, net, x):
     return out.permute(0, 2, 3, 4, 1), P
 
 
-def test_network_gradients_match_float64(env):
+@pytest.mark.parametrize("tcgen05", [False, True])
+def test_network_gradients_match_float64(env, tcgen05):
     torch, ws_mod = env
+    import _flf
+    old = _flf.conv16_tcgen05(tcgen05)
+    try:
+        _gradients_match(torch, ws_mod)
+    finally:
+        _flf.conv16_tcgen05(old)
+
+
+def _gradients_match(torch, ws_mod):
     net = ws_mod.UNet3D(seed=3)
     g = torch.Generator().manual_seed(0)
     x = torch.zeros((2, 8, 16, 24, ws_mod.CIN))
@@ -111,10 +121,22 @@ def test_training_and_warm_started_rl(env):
     assert resid(xw) <= 1.01 * resid(xu)
 
 
-def test_fused_input_and_head_kernels(env):
-    """flf_ws_input / flf_ws_head against their torch formulas."""
+@pytest.mark.parametrize("tcgen05", [False, True])
+def test_fused_input_and_head_kernels(env, tcgen05):
+    """flf_ws_input / flf_ws_head against their torch formulas (head on the
+    mma.sync and on the warp-specialised tcgen05 kernel)."""
     torch, ws_mod = env
     import _flf
+    old = _flf.conv16_tcgen05(tcgen05)
+    try:
+        _input_and_head(torch, _flf)
+        torch.cuda.synchronize()
+        _flf.net_status()
+    finally:
+        _flf.conv16_tcgen05(old)
+
+
+def _input_and_head(torch, _flf):
     g = torch.Generator().manual_seed(11)
     Z, T, Y, X = 5, 2, 13, 21
     Zp, Yp, Xp = 8, 16, 24
