@@ -193,7 +193,8 @@ def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
 def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):
     """conv3d for 16 -> 16 channels on the tcgen05 tensor cores.
 
-    rows = 0: the warp-specialised kernel with TMA-staged input slabs;
+    rows = 0: the warp-specialised kernel with TMA-staged input slabs (-1: the
+    same with 32-byte swizzled slabs);
     1, 4, 5: single-role kernels with tiles of rows x 128 voxels (5 = 4 rows,
     double-buffered)."""
     lib = load_library()

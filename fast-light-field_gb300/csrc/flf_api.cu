@@ -1653,10 +1653,11 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
     return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
   ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
                (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16, relu ? 1 : 0, nullptr, rows};
-  if (rows != 0 && rows != 1 && rows != 4 && rows != 5)
+  if (rows != 0 && rows != -1 && rows != 1 && rows != 4 && rows != 5)
     return fail(nullptr, FLF_E_ARG,
-                "tile choice must be 0 (warp-specialised, TMA-staged), 1, 4 or 5 (4 rows, double-buffered)");
-  if (rows == 0) NET_CHECK(launch_conv3d_tma16(p, (cudaStream_t)stream));
+                "tile choice must be 0 or -1 (warp-specialised, TMA-staged; -1 with 32-byte swizzled slabs), "
+                "1, 4 or 5 (4 rows, double-buffered)");
+  if (rows <= 0) NET_CHECK(launch_conv3d_tma16(p, (cudaStream_t)stream, rows < 0));
   else NET_CHECK(launch_conv3d_tc16(p, (cudaStream_t)stream));
   return FLF_OK;
 }

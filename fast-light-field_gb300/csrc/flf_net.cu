@@ -664,44 +664,53 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 
 // ---------------------------------------------------------------------------
 // 16 -> 16 channels, warp-specialised on tcgen05 with TMA staging.  A work
-// item is a column of output, R rows (y) x 126 voxels (x), over a run of z
-// planes.  The CTA walks z: output plane z needs input slabs z-1, z, z+1, a
-// slab being (R+2) rows x 130 voxels of one plane (the x / y halo included).
-// Slabs sit in a ring of S shared-memory slots that TMA fills: a tensor map
-// over [B][Z][Y][X][16] BF16 with box 8 channels x 130 x (R+2) x 1 x 1, two
-// loads per slab for the two 8-channel planes, so a slab row is a canonical
-// K-major A operand (8-voxel x 16-byte core matrices, the planes one LBO
-// apart).  Coordinates outside the volume read zeros: the 'same' padding.
-// The three x taps are folded into N: for each (dz, dy) one
-//   tcgen05.mma  M 128 (slab voxels c) x N 48 (dx, co) x K 16 (ci)
-// accumulates D[c][dx][co] = sum over (dz, dy, ci) of in[c] w[dz][dy][dx][ci][co],
-// and the epilogue forms out[i][co] = D[i][0][co] + D[i+1][1][co] + D[i+2][2][co]
-// (warp shuffles; the two lanes past each 32-lane TMEM quarter come through
-// shared memory).  That is 9 MMAs per output row instead of 27 with N = 16,
-// a third of the operand traffic from shared memory, and 126 outputs per
-// 128-voxel MMA row.
+// item is a column of output, R rows (y) x 128 voxels (x), over a run of z
+// planes.  The CTA walks the input planes z' of the column: each is one slab,
+// (R+2) rows of the voxels x0-1 .. (the x / y halo included), that TMA loads
+// into a ring of S shared-memory slots through a tensor map over
+// [B][Z][Y][X][16] BF16.  Two slab layouts (SW32):
+//   true   one load per slab, box 16 channels x 136 x (R+2) x 1 x 1 with the
+//          32-byte swizzle: a voxel is one 32-byte row whose 16-byte halves
+//          are swapped where smem address bit 7 is set, rows 256-byte aligned,
+//          which is the 32-byte-swizzled K-major A layout (8-row groups 256
+//          bytes apart).  A tap's x shift moves the start 32 bytes per voxel;
+//          the tensor cores apply the swizzle to the absolute address, as TMA
+//          does, so shifted windows read correctly (checked by the tests);
+//   false  two loads per slab, box 8 channels x 130 x (R+2) x 1 x 1, one per
+//          8-channel plane: the canonical no-swizzle K-major layout, 8-voxel
+//          x 16-byte core matrices, the planes one LBO apart.
+// Coordinates outside the volume read zeros: the 'same' padding in x and y.
+// The three z taps are folded into N.  For output row r of slab z', one
+//   tcgen05.mma  M 128 (voxels x) x N 48 (dz, co) x K 16 (ci)
+// per (dy, dx), with A the slab row r+dy shifted by dx, accumulates
+//   D[z'][r][x][dz][co] = sum over (dy, dx, ci) of in[z'][r+dy][x+dx][ci] w[dz][dy][dx][ci][co]
+// into one of 5 TMEM accumulator slots (R x 48 columns each), and
+//   out[z][r][x][co] = D[z-1][r][x][0][co] + D[z][r][x][1][co] + D[z+1][r][x][2][co]
+// adds three column groups of the same TMEM lane: no data moves between
+// lanes.  A slab's shared memory is free as soon as its MMAs complete; its
+// accumulator slot is free after the last output plane that reads it.
+// Planes outside the volume contribute nothing: their MMAs are skipped and
+// the epilogue leaves their terms out.
 //   warp 0     producer: one thread issues the TMA loads;
-//   warp 1     MMA issuer: one thread issues 9 x R MMAs per output plane into
-//              one of two TMEM accumulator stages (R x 48 columns each),
-//              commits to the stage's full barrier, and releases the slab no
-//              longer needed;
-//   warps 2-17 epilogue: warp w reads TMEM lane quarter w % 4 (tcgen05.ld)
-//              for 8 of the 16 output channels and half of the rows, forms
-//              the tap sum, then bias / ReLU / mask and BF16 stores, or with
-//              HEAD the clamped, scaled start volume from output channel 0.
+//   warps 1-2  MMA issuers: one thread each issues the 9 MMAs of half of the
+//              rows per slab, then commits to the slab's accumulator barrier
+//              and to its shared-memory slot;
+//   warps 3-10 epilogue: warp w reads TMEM lane quarter w % 4 (tcgen05.ld)
+//              for 8 of the 16 output channels, sums the three z terms, then
+//              bias / ReLU / mask and BF16 stores, or with HEAD the clamped,
+//              scaled start volume from output channel 0.
 // Every mbarrier wait is bounded (1 s).  A wait that gives up sets g_net_err
-// and a shared abort flag that every role polls; the epilogue warps decide
-// together (barrier.red.or), and the CTA waits (bounded) for its copies and
-// MMAs in flight before TMEM is released.
+// and a shared abort flag that every role polls; the CTA then waits (bounded)
+// for its copies and MMAs in flight before TMEM is released.
 // ---------------------------------------------------------------------------
-struct Tma16Grid {   // work items: [B][zchunks][yblocks][xsegs] columns of R x 126 voxels over zc planes
+struct Tma16Grid {   // work items: [B][zchunks][yblocks][xsegs] columns of R x 128 voxels over zc planes
   int xsegs, yblocks, zchunks, zc;
   long long items;
 };
 
-namespace {
+constexpr int TMA16_NACC = 5;   // TMEM accumulator slots (R x 48 columns each)
 
-constexpr int TMA16_XW = 126;   // output voxels per 128-lane MMA row
+namespace {
 
 __device__ __forceinline__ void net_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
@@ -717,17 +726,6 @@ __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
       : "memory");
 }
-// named barrier 1 over the 512 epilogue threads, OR of `pred` across them
-__device__ __forceinline__ bool epi_bar_or(bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.red.or.pred q, 1, 512, p;\n selp.u32 %0, 1, 0, q;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)pred)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void epi_bar() { asm volatile("barrier.sync 1, 512;\n" ::: "memory"); }
 // bounded wait that also gives up when another role has aborted
 __device__ __forceinline__ bool role_wait(uint32_t bar, uint32_t parity, volatile int *abort_s, int code) {
   unsigned long long t0 = 0;
@@ -759,52 +757,46 @@ __device__ __forceinline__ void tmem_ld8(uint32_t addr, float *v) {
 #pragma unroll
   for (int k = 0; k < 8; k++) v[k] = __uint_as_float(u[k]);
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t addr, float *v) {
-  uint32_t u[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]),
-        "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
-      : "r"(addr));
-#pragma unroll
-  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(u[k]);
-}
 
 }  // namespace
 
-template <int R, int S, bool HEAD>
-__global__ void __launch_bounds__(576, 1)
+template <int R, int S, bool HEAD, bool SW32>
+__global__ void __launch_bounds__(352, 1)
     k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  constexpr int PXW = 130, PYH = R + 2;
-  constexpr uint32_t PLANE_TX = PYH * PXW * 16;              // bytes one TMA load writes
-  constexpr uint32_t PLANE = (PLANE_TX + 127) / 128 * 128;   // plane stride inside a slot
-  constexpr uint32_t SLOT = 2 * PLANE;
-  constexpr uint32_t BBLK = 48 * 16 * 2;                     // B operand of one (dz, dy): N 48 x K 16
+  constexpr int PYH = R + 2, NACC = TMA16_NACC;
+  // SW32: one load per slab of rows of 136 voxels x 32 bytes (16 channels), written with the
+  // 32-byte swizzle (16-byte halves of a voxel swapped where address bit 7 is set); otherwise two
+  // loads of 130-voxel rows x 16 bytes, one per 8-channel plane
+  constexpr int PXW = SW32 ? 136 : 130;
+  constexpr uint32_t PLANE_TX = SW32 ? PYH * PXW * 32 : PYH * PXW * 16;   // bytes one TMA load writes
+  constexpr uint32_t PLANE = SW32 ? (PLANE_TX + 1023) / 1024 * 1024 : (PLANE_TX + 127) / 128 * 128;
+  constexpr uint32_t SLOT = SW32 ? PLANE : 2 * PLANE;
+  constexpr uint32_t LOADS = SW32 ? 1 : 2;
+  constexpr uint32_t BBLK = 48 * 16 * 2;                     // B operand of one (dy, dx): N 48 x K 16
   constexpr uint32_t SLAB0 = (9 * BBLK + 1023) / 1024 * 1024;
-  constexpr uint32_t EDGE = 2 * 2 * 4 * R * 2 * 16 * 4;      // [stage][half][quarter][row][lane 0/1][dx 1..2 x 8] f32
-  constexpr uint32_t STAGE_COLS = R * 48;
-  constexpr uint32_t TCOLS = 2 * STAGE_COLS <= 256 ? 256 : 512;
-  static_assert(2 * STAGE_COLS <= 512, "two accumulator stages of R rows x 48 columns");
-  // layout: [B operands][S slots x 2 planes][edge exchange][mbarriers][tmem address][abort flag]
+  constexpr uint32_t ACOLS = R * 48;                         // one accumulator slot
+  constexpr uint32_t TCOLS = NACC * ACOLS <= 256 ? 256 : 512;
+  static_assert(NACC * ACOLS <= 512, "the accumulator slots fit the 512 TMEM columns");
+  static_assert(R % 2 == 0, "the two MMA issuers take half of the rows each");
+  // layout: [B operands][S slots x 2 planes][mbarriers][tmem address][abort flag]
   unsigned char *Wb = smem;
-  float *edge = reinterpret_cast<float *>(smem + SLAB0 + S * SLOT);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SLAB0 + S * SLOT + EDGE);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 5);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SLAB0 + S * SLOT);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 2 * NACC + 1);
   volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t wb_s = su32(Wb), slab_s = su32(smem + SLAB0), bar_s = su32(bars);
-  auto full = [&](uint32_t k) { return bar_s + 8u * k; };
-  auto empty = [&](uint32_t k) { return bar_s + 8u * (S + k); };
-  auto tfull = [&](uint32_t k) { return bar_s + 8u * (2 * S + k); };
-  auto tempty = [&](uint32_t k) { return bar_s + 8u * (2 * S + 2 + k); };
-  const uint32_t fin = bar_s + 8u * (2 * S + 4);
+  auto full = [&](uint32_t k) { return bar_s + 8u * k; };                  // slab k loaded
+  auto empty = [&](uint32_t k) { return bar_s + 8u * (S + k); };           // slab k's MMAs done
+  auto tfull = [&](uint32_t k) { return bar_s + 8u * (2 * S + k); };       // accumulator slot k written
+  auto tempty = [&](uint32_t k) { return bar_s + 8u * (2 * S + NACC + k); };   // accumulator slot k read
+  const uint32_t fin = bar_s + 8u * (2 * S + 2 * NACC);
 
-  // B operands: block (dz, dy) holds B[n = dx*16 + co][k = ci] = w[tap = dz*9 + dy*3 + dx][ci][co],
+  // B operands: block (dy, dx) holds B[n = dz*16 + co][k = ci] = w[tap = dz*9 + dy*3 + dx][ci][co],
   // core matrix (n/8, ci/8) at (n/8)*256 + (ci/8)*128, row n%8 at 16 B, element ci%8 at 2 B
-  for (int i = tid; i < 9 * 48; i += 576) {
+  for (int i = tid; i < 9 * 48; i += blockDim.x) {
     const int blk = i / 48, n = i % 48;
-    const int tap = blk * 3 + n / 16, co = n % 16;
+    const int tap = (n / 16) * 9 + blk, co = n % 16;
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
@@ -819,13 +811,13 @@ __global__ void __launch_bounds__(576, 1)
   if (tid == 0) {
     for (int k = 0; k < S; k++) {
       net_mbar_init(full(k), 1);
-      net_mbar_init(empty(k), 1);
+      net_mbar_init(empty(k), 2);
     }
-    for (int k = 0; k < 2; k++) {
-      net_mbar_init(tfull(k), 1);
-      net_mbar_init(tempty(k), 512);
+    for (int k = 0; k < NACC; k++) {
+      net_mbar_init(tfull(k), 2);
+      net_mbar_init(tempty(k), 256);
     }
-    net_mbar_init(fin, 1);
+    net_mbar_init(fin, 2);
     *abort_s = 0;
   }
   if (warp == 1) {
@@ -842,7 +834,7 @@ __global__ void __launch_bounds__(576, 1)
 
   auto decode = [&](long long it, int &b, int &zlo, int &nz, int &y0, int &x0) {
     long long q = it;
-    x0 = (int)(q % g.xsegs) * TMA16_XW;
+    x0 = (int)(q % g.xsegs) * 128;
     q /= g.xsegs;
     y0 = (int)(q % g.yblocks) * R;
     q /= g.yblocks;
@@ -854,153 +846,114 @@ __global__ void __launch_bounds__(576, 1)
   uint32_t nload = 0;
   if (warp == 0) {
     if (lane == 0) {
-      // ---- producer ----
+      // ---- producer: slabs zlo-1 .. zlo+nz of every item ----
       for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
         int b, zlo, nz, y0, x0;
         decode(it, b, zlo, nz, y0, x0);
         for (int k = 0; k < nz + 2; k++) {
           const uint32_t slot = nload % S;
           if (nload >= S && !role_wait(empty(slot), ((nload / S) - 1) & 1, abort_s, 4)) break;
-          net_expect_tx(full(slot), 2 * PLANE_TX);
+          net_expect_tx(full(slot), LOADS * PLANE_TX);
           const uint32_t dst = slab_s + slot * SLOT;
           tma_load_5d(dst, &tx, 0, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
-          tma_load_5d(dst + PLANE, &tx, 8, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
+          if (!SW32) tma_load_5d(dst + PLANE, &tx, 8, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
           nload++;
         }
       }
     }
-  } else if (warp == 1) {
+  } else if (warp <= 2) {
     if (lane == 0) {
-      // ---- MMA issuer ----
+      // ---- MMA issuers: warp 1 rows 0 .. R/2-1, warp 2 rows R/2 .. R-1 ----
+      const int r0 = (warp - 1) * (R / 2);
       // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 48, M = 128
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
       uint64_t bdesc[9];
 #pragma unroll
       for (int blk = 0; blk < 9; blk++) bdesc[blk] = umma_desc(wb_s + blk * BBLK, 128, 256);
-      const uint64_t a_desc = umma_desc(slab_s, PLANE, 128);   // slot 0, row 0
+      // A: slot 0, row 0.  SW32: K-major with the 32-byte swizzle (layout type 6 in bits 61-63),
+      // 8-row groups 256 bytes apart, K within one swizzle row (leading offset unused, 16 bytes);
+      // otherwise canonical no-swizzle, the two 8-channel planes one LBO apart
+      const uint64_t a_desc = SW32 ? (umma_desc(slab_s, 16, 256) | (6ull << 61)) : umma_desc(slab_s, PLANE, 128);
       const uint32_t a_lo = (uint32_t)a_desc, a_hi = (uint32_t)(a_desc >> 32);
-      uint32_t n = 0, q = 0;
+      constexpr uint32_t VOX = SW32 ? 2 : 1;   // one voxel in 16-byte units
+      uint32_t n = 0;   // slabs consumed (= accumulator slots written)
       bool ok = true;
       for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
         int b, zlo, nz, y0, x0;
         decode(it, b, zlo, nz, y0, x0);
-        ok = role_wait(full(n % S), (n / S) & 1, abort_s, 5) &&
-             role_wait(full((n + 1) % S), ((n + 1) / S) & 1, abort_s, 5);
-        for (int zi = 0; zi < nz && ok; zi++) {
-          const uint32_t k2 = n + zi + 2;
-          const uint32_t stage = q & 1;
-          ok = role_wait(full(k2 % S), (k2 / S) & 1, abort_s, 5) &&
-               (q < 2 || role_wait(tempty(stage), ((q >> 1) - 1) & 1, abort_s, 6));
+        for (int k = 0; k < nz + 2; k++, n++) {
+          const uint32_t acc = n % NACC;
+          ok = role_wait(full(n % S), (n / S) & 1, abort_s, 5) &&
+               (n < NACC || role_wait(tempty(acc), ((n / NACC) - 1) & 1, abort_s, 6));
           if (!ok) break;
-          tc_fence_after();
-          // low descriptor words (start address >> 4 | LBO >> 4 << 16) of the three slabs; a row
-          // of 130 voxels is 130 in units of 16 bytes
-          const uint32_t a0 = a_lo + ((n + zi) % S) * (SLOT >> 4), a1 = a_lo + ((n + zi + 1) % S) * (SLOT >> 4),
-                         a2 = a_lo + (k2 % S) * (SLOT >> 4);
-          const uint32_t dcol = tmem + stage * STAGE_COLS;
+          const int zin = zlo - 1 + k;
+          if (zin >= 0 && zin < p.Z) {
+            tc_fence_after();
+            // low descriptor word of the slab (start address >> 4 | LBO >> 4 << 16); a slab row of
+            // 130 voxels is 130 units of 16 bytes
+            const uint32_t al = a_lo + (n % S) * (SLOT >> 4);
+            const uint32_t dcol = tmem + acc * ACOLS;
 #pragma unroll
-          for (int blk = 0; blk < 9; blk++) {
-            const int dz = blk / 3, dy = blk % 3;
-            const uint32_t al = dz == 0 ? a0 : (dz == 1 ? a1 : a2);
+            for (int blk = 0; blk < 9; blk++) {
+              const int dy = blk / 3, dx = blk % 3;
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-              const uint64_t ad = ((uint64_t)a_hi << 32) | (uint64_t)(al + (uint32_t)((r + dy) * PXW));
-              umma_f16(dcol + r * 48, ad, bdesc[blk], idesc, blk > 0 ? 1u : 0u);
+              for (int r = 0; r < R / 2; r++) {
+                const uint64_t ad =
+                    ((uint64_t)a_hi << 32) | (uint64_t)(al + (uint32_t)(((r0 + r + dy) * PXW + dx) * VOX));
+                umma_f16(dcol + (r0 + r) * 48, ad, bdesc[blk], idesc, blk > 0 ? 1u : 0u);
+              }
             }
           }
-          umma_commit(tfull(stage));
-          umma_commit(empty((n + zi) % S));   // slab z-1 has no later user in this column
-          q++;
+          umma_commit(tfull(acc));
+          umma_commit(empty(n % S));   // the slab's shared memory is free
         }
-        if (!ok) break;
-        umma_commit(empty((n + nz) % S));
-        umma_commit(empty((n + nz + 1) % S));
-        n += nz + 2;
       }
     }
   } else {
-    // ---- epilogue: warps 2..17; warp w owns TMEM lane quarter w % 4, output channels 8*hf..8*hf+7
-    // and rows RW*rh..RW*rh+RW-1 ----
-    constexpr int RW = R / 2;
-    const int e = warp - 2, qd = warp & 3, hf = (e >> 2) & 1, rh = e >> 3;
+    // ---- epilogue: warps 3..10; warp w owns TMEM lane quarter w % 4 and output channels 8*hf..8*hf+7 ----
+    const int qd = warp & 3, hf = (warp - 3) >> 2;
     const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
-    const int i = qd * 32 + lane;   // output voxel of the segment (valid for i < 126)
     float bias[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) bias[c] = (!HEAD && p.bias) ? p.bias[hf * 8 + c] : 0.f;
-    uint32_t q = 0;
+    uint32_t n = 0;   // first slab of the current item
     bool ok = true;
     for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
       int b, zlo, nz, y0, x0;
       decode(it, b, zlo, nz, y0, x0);
-      const int x = x0 + i;
-      for (int zi = 0; zi < nz; zi++) {
-        const uint32_t stage = q & 1;
-        // tcgen05.ld is .sync.aligned and the edge exchange uses a named barrier:
-        // all epilogue warps take one decision
-        const bool late = !role_wait(tfull(stage), (q >> 1) & 1, abort_s, 7);
-        if (epi_bar_or(late)) {
+      const int x = x0 + qd * 32 + lane;
+      for (int i = 0; i < nz; i++) {
+        // output plane z = zlo + i reads slabs n+i (dz 0), n+i+1 (dz 1), n+i+2 (dz 2); each issuer's
+        // commits complete in order, so slab n+i+2's barrier covers the other two
+        const uint32_t m = n + i + 2;
+        // tcgen05.ld is .sync.aligned: the whole warp takes one decision
+        if (!__all_sync(0xffffffffu, role_wait(tfull(m % NACC), (m / NACC) & 1, abort_s, 7) ? 1 : 0)) {
           ok = false;
           break;
         }
         tc_fence_after();
-        float d[RW][3][8];
+        const int z = zlo + i;
+        float d[R][3][8];
 #pragma unroll
-        for (int rr = 0; rr < RW; rr++)
+        for (int r = 0; r < R; r++)
 #pragma unroll
-          for (int dx = 0; dx < 3; dx++)
-            tmem_ld8(tmem + lane_base + stage * STAGE_COLS + (rh * RW + rr) * 48 + dx * 16 + hf * 8, d[rr][dx]);
+          for (int dz = 0; dz < 3; dz++)
+            tmem_ld8(tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + r * 48 + dz * 16 + hf * 8, d[r][dz]);
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         tc_fence_before();
-        net_arrive(tempty(stage));   // the accumulator stage is free for the next plane
-        q++;
-        // lanes 0 and 1 publish D[.][1] and D[.][2] for lanes 30 and 31 of the quarter below
-        float *eg = edge + (size_t)(((stage * 2 + hf) * 4 + qd) * R) * 32;
-        if (lane < 2) {
+        net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
+        const bool lo_in = z > 0, hi_in = z + 1 < p.Z;
 #pragma unroll
-          for (int rr = 0; rr < RW; rr++) {
-            float4 *e4 = reinterpret_cast<float4 *>(eg + ((rh * RW + rr) * 2 + lane) * 16);
-            e4[0] = make_float4(d[rr][1][0], d[rr][1][1], d[rr][1][2], d[rr][1][3]);
-            e4[1] = make_float4(d[rr][1][4], d[rr][1][5], d[rr][1][6], d[rr][1][7]);
-            e4[2] = make_float4(d[rr][2][0], d[rr][2][1], d[rr][2][2], d[rr][2][3]);
-            e4[3] = make_float4(d[rr][2][4], d[rr][2][5], d[rr][2][6], d[rr][2][7]);
-          }
-        }
-        // out[i] = D[i][0] + D[i+1][1] + D[i+2][2]; lanes 30 and 31 are corrected below (a shuffle
-        // past lane 31 returns the lane's own value)
-        float o[RW][8];
-#pragma unroll
-        for (int rr = 0; rr < RW; rr++)
+        for (int r = 0; r < R; r++) {
+          const int y = y0 + r;
+          float o[8];
 #pragma unroll
           for (int c = 0; c < 8; c++)
-            o[rr][c] = d[rr][0][c] + __shfl_down_sync(0xffffffffu, d[rr][1][c], 1) +
-                       __shfl_down_sync(0xffffffffu, d[rr][2][c], 2);
-        epi_bar();   // every quarter's edge values are in shared memory
-        if (lane >= 30) {
-          if (qd < 3) {
-            // lane 30 took its own D[2] for D[32(qd+1)][2]; lane 31 its own D[1] and D[2] for
-            // D[32(qd+1)][1] and D[32(qd+1)+1][2]
-            const float *en = edge + (size_t)(((stage * 2 + hf) * 4 + qd + 1) * R) * 32;
-#pragma unroll
-            for (int rr = 0; rr < RW; rr++) {
-              const float *l0 = en + ((rh * RW + rr) * 2) * 16, *l1 = l0 + 16;
-#pragma unroll
-              for (int c = 0; c < 8; c++) {
-                if (lane == 30) o[rr][c] += l0[8 + c] - d[rr][2][c];
-                else o[rr][c] += l0[c] + l1[8 + c] - d[rr][1][c] - d[rr][2][c];
-              }
-            }
-          }
-        }
-        const int z = zlo + zi;
-        if (i >= TMA16_XW) continue;
-#pragma unroll
-        for (int rr = 0; rr < RW; rr++) {
-          const int y = y0 + rh * RW + rr;
+            o[c] = (lo_in ? d[r][0][c] : 0.f) + d[r][1][c] + (hi_in ? d[r][2][c] : 0.f);
           if (HEAD) {
             if (hf == 0 && b < h.T && z < h.Zr && y < h.Yr && x < h.Xr) {
               const float sc = h.sum_x1[b] / h.count;
-              h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[rr][0] + h.bias, h.floor) * sc;
+              h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[0] + h.bias, h.floor) * sc;
             }
             continue;
           }
@@ -1013,8 +966,8 @@ __global__ void __launch_bounds__(576, 1)
           const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
 #pragma unroll
           for (int k = 0; k < 4; k++) {
-            float v0 = o[rr][2 * k] + bias[2 * k];
-            float v1 = o[rr][2 * k + 1] + bias[2 * k + 1];
+            float v0 = o[2 * k] + bias[2 * k];
+            float v1 = o[2 * k + 1] + bias[2 * k + 1];
             if (p.relu) {
               v0 = fmaxf(v0, 0.f);
               v1 = fmaxf(v1, 0.f);
@@ -1029,6 +982,11 @@ __global__ void __launch_bounds__(576, 1)
           *reinterpret_cast<uint4 *>(p.y + off) = outv;
         }
       }
+      if (!ok) break;
+      // the item's last two slabs have no later reader
+      net_arrive(tempty((n + nz) % NACC));
+      net_arrive(tempty((n + nz + 1) % NACC));
+      n += nz + 2;
     }
   }
 
@@ -1040,8 +998,8 @@ __global__ void __launch_bounds__(576, 1)
       if (!net_mbar_wait(full(s), (last / S) & 1, 1000000000ULL)) atomicExch(&g_net_err, 8);
     }
   }
-  if (warp == 1 && lane == 0) {
-    // every MMA issued has completed before the accumulator is released
+  if ((warp == 1 || warp == 2) && lane == 0) {
+    // every MMA issued has completed before the accumulators are released
     umma_commit(fin);
     if (!net_mbar_wait(fin, 0, 1000000000ULL)) atomicExch(&g_net_err, 9);
   }
@@ -1503,14 +1461,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-template <int R, int S, bool HEAD>
+template <int R, int S, bool HEAD, bool SW32>
 static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
-  constexpr size_t PLANE = ((R + 2) * 130 * 16 + 127) / 128 * 128;
-  constexpr size_t SMEM = (9 * 1536 + 1023) / 1024 * 1024 + S * 2 * PLANE + 2 * 2 * 4 * R * 2 * 16 * 4 + (2 * S + 5) * 8 + 8;
+  constexpr size_t SLOT = SW32 ? ((R + 2) * 136 * 32 + 1023) / 1024 * 1024 : 2 * (((R + 2) * 130 * 16 + 127) / 128 * 128);
+  constexpr size_t SMEM = (9 * 1536 + 1023) / 1024 * 1024 + S * SLOT + (2 * S + 2 * TMA16_NACC + 1) * 8 + 8;
   static int sms = 0;
   if (!sms) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_conv3d_tma16<R, S, HEAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<R, S, HEAD, SW32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -1526,14 +1484,15 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   CUtensorMap map;
   const cuuint64_t dims[5] = {16, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
   const cuuint64_t strides[4] = {32, 32ull * p.X, 32ull * p.X * p.Y, 32ull * p.X * p.Y * p.Z};
-  const cuuint32_t box[5] = {8, 130, (cuuint32_t)(R + 2), 1, 1};
+  const cuuint32_t box[5] = {SW32 ? 16u : 8u, SW32 ? 136u : 130u, (cuuint32_t)(R + 2), 1, 1};
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(p.x), dims, strides, box, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, SW32 ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return cudaErrorInvalidValue;
   Tma16Grid g;
-  g.xsegs = (p.X + TMA16_XW - 1) / TMA16_XW;
+  g.xsegs = (p.X + 127) / 128;
   g.yblocks = (p.Y + R - 1) / R;
   // split z into chunks when whole columns fill the GPU unevenly (each chunk reloads 2 halo slabs)
   long long best = -1;
@@ -1551,7 +1510,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   g.zchunks = (p.Z + g.zc - 1) / g.zc;
   g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
-  k_conv3d_tma16<R, S, HEAD><<<grid, 576, SMEM, s>>>(map, p, h, g);
+  k_conv3d_tma16<R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g);
   return cudaGetLastError();
 }
 
@@ -1563,8 +1522,8 @@ int net_set_conv16_tcgen05(int on) {
   return old;
 }
 
-cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s) {
-  return launch_tma16<4, 6, false>(p, HeadOut{}, s);
+cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32) {
+  return sw32 ? launch_tma16<2, 8, false, true>(p, HeadOut{}, s) : launch_tma16<2, 8, false, false>(p, HeadOut{}, s);
 }
 
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
@@ -1572,7 +1531,7 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
   if (M == 0) return cudaSuccess;
   p.splits = 1;
   if (p.Ci == 16 && p.Co == 16)
-    return g_conv16_tc ? launch_tma16<4, 6, false>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
+    return g_conv16_tc ? launch_tma16<2, 8, false, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
   if (p.Ci == 16 && p.Co == 32) return launch_tiled<16, 32>(p, s);
   if (p.Ci == 32 && p.Co == 16) return launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32) return launch_tiled<32, 32>(p, s);
@@ -1739,7 +1698,7 @@ cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor
                            int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s) {
   ConvParams p{(const bf16 *)d, (const bf16 *)w, nullptr, nullptr, nullptr, T, Zp, Yp, Xp, 16, 16, 0, nullptr, 1};
   HeadOut h{x0, sum_x1, (float)Z * Y * X, bias, floor_, T, Z, Y, X};
-  return g_conv16_tc ? launch_tma16<4, 6, true>(p, h, s) : launch_t16<true>(p, h, s);
+  return g_conv16_tc ? launch_tma16<2, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
 }
 
 cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,

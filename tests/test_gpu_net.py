@@ -159,12 +159,13 @@ def test_mse_adam_and_blobs(env):
     assert np.max(np.abs(vol.cpu().numpy() - ref)) < 1e-5
 
 
-@pytest.mark.parametrize("rows", [0, 1, 4, 5])
+@pytest.mark.parametrize("rows", [0, -1, 1, 4, 5])
 @pytest.mark.parametrize("shape,relu,masked", [((1, 2, 3, 5), True, False), ((2, 3, 4, 130), False, False),
                                                ((1, 4, 9, 300), True, True), ((2, 5, 6, 128), True, False)])
 def test_conv3d_tcgen05(env, shape, relu, masked, rows):
     """The 16 -> 16 convolution on the tcgen05 tensor cores (TMEM accumulator);
-    rows = 0 is the warp-specialised kernel with TMA-staged slabs."""
+    rows = 0 is the warp-specialised kernel with TMA-staged slabs, -1 the same
+    with 32-byte swizzled slabs."""
     torch, _flf = env
     g = torch.Generator().manual_seed(sum(shape))
     x = torch.randn(shape + (16,), generator=g).bfloat16()
@@ -183,9 +184,10 @@ def test_conv3d_tcgen05(env, shape, relu, masked, rows):
     _close(torch, y, ref)
 
 
+@pytest.mark.parametrize("rows", [0, -1])
 @pytest.mark.parametrize("shape,relu,masked", [((1, 6, 200, 700), True, True), ((3, 9, 10, 130), False, False),
                                                ((1, 1, 1, 1), True, False)])
-def test_conv3d_tcgen05_warp_specialised_many_items(env, shape, relu, masked):
+def test_conv3d_tcgen05_warp_specialised_many_items(env, shape, relu, masked, rows):
     """More work items than SMs (each CTA walks several columns through its slab
     ring), z split into chunks, and a single voxel."""
     torch, _flf = env
@@ -195,7 +197,7 @@ def test_conv3d_tcgen05_warp_specialised_many_items(env, shape, relu, masked):
     b = torch.randn(16, generator=g).float()
     m = torch.randn(shape + (16,), generator=g).bfloat16() if masked else None
     y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
-    _flf.conv3d_tc(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, mask=m.cuda() if masked else None, rows=0)
+    _flf.conv3d_tc(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, mask=m.cuda() if masked else None, rows=rows)
     torch.cuda.synchronize()
     _flf.net_status()
     ref = _ref_conv(torch, x.double(), w.double(), b.double())
