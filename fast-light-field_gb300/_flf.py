@@ -206,8 +206,9 @@ def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):
 
 
 def conv16_tcgen05(on):
-    """Select the kernel conv3d and ws_head use for 16 -> 16 channels (True: the
-    warp-specialised tcgen05 kernel, False: mma.sync); returns the previous choice."""
+    """Select the kernels conv3d and ws_head use for 16 / 32 -> 16 / 32 channels
+    (True: the warp-specialised tcgen05 kernel, False: mma.sync); returns the
+    previous choice."""
     return bool(load_library().flf_net_conv16_tcgen05(int(bool(on))))
 
 

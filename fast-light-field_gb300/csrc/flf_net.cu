@@ -749,6 +749,16 @@ __device__ __forceinline__ bool role_wait(uint32_t bar, uint32_t parity, volatil
     }
   }
 }
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, float *v) {
+  uint32_t u[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]),
+        "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
+      : "r"(addr));
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(u[k]);
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t addr, float *v) {
   uint32_t u[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
@@ -760,26 +770,32 @@ __device__ __forceinline__ void tmem_ld8(uint32_t addr, float *v) {
 
 }  // namespace
 
-template <int R, int S, bool HEAD, bool SW32>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32>
 __global__ void __launch_bounds__(352, 1)
     k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
   extern __shared__ __align__(1024) unsigned char smem[];
   constexpr int PYH = R + 2, NACC = TMA16_NACC;
-  // SW32: one load per slab of rows of 136 voxels x 32 bytes (16 channels), written with the
-  // 32-byte swizzle (16-byte halves of a voxel swapped where address bit 7 is set); otherwise two
-  // loads of 130-voxel rows x 16 bytes, one per 8-channel plane
+  constexpr int KS = CI / 16;                 // K steps of 16 input channels
+  constexpr int NN = 3 * CO;                  // N of one MMA: (dz, co)
+  constexpr int NISS = R % 2 == 0 ? 2 : 1;    // MMA-issuing threads (warps 1 .. NISS)
+  constexpr int CH = CO / 2;                  // output channels per epilogue warp
+  static_assert((CI == 16 || CI == 32) && (CO == 16 || CO == 32), "16 or 32 channels in and out");
+  static_assert(SW32 || CI == 16, "the unswizzled slab layout is for 16 input channels");
+  static_assert(!HEAD || (CI == 16 && CO == 16), "the head is a 16 -> 16 convolution");
+  // SW32: per slab one load per 16 input channels of rows of 136 voxels x 32 bytes, written with
+  // the 32-byte swizzle (16-byte halves of a voxel swapped where address bit 7 is set); otherwise
+  // two loads of 130-voxel rows x 16 bytes, one per 8-channel plane
   constexpr int PXW = SW32 ? 136 : 130;
   constexpr uint32_t PLANE_TX = SW32 ? PYH * PXW * 32 : PYH * PXW * 16;   // bytes one TMA load writes
   constexpr uint32_t PLANE = SW32 ? (PLANE_TX + 1023) / 1024 * 1024 : (PLANE_TX + 127) / 128 * 128;
-  constexpr uint32_t SLOT = SW32 ? PLANE : 2 * PLANE;
-  constexpr uint32_t LOADS = SW32 ? 1 : 2;
-  constexpr uint32_t BBLK = 48 * 16 * 2;                     // B operand of one (dy, dx): N 48 x K 16
-  constexpr uint32_t SLAB0 = (9 * BBLK + 1023) / 1024 * 1024;
-  constexpr uint32_t ACOLS = R * 48;                         // one accumulator slot
+  constexpr uint32_t LOADS = SW32 ? KS : 2;
+  constexpr uint32_t SLOT = LOADS * PLANE;
+  constexpr uint32_t BBLK = NN * 16 * 2;                     // B operand of one (dy, dx, K step)
+  constexpr uint32_t SLAB0 = (9 * KS * BBLK + 1023) / 1024 * 1024;
+  constexpr uint32_t ACOLS = R * NN;                         // one accumulator slot
   constexpr uint32_t TCOLS = NACC * ACOLS <= 256 ? 256 : 512;
   static_assert(NACC * ACOLS <= 512, "the accumulator slots fit the 512 TMEM columns");
-  static_assert(R % 2 == 0, "the two MMA issuers take half of the rows each");
-  // layout: [B operands][S slots x 2 planes][mbarriers][tmem address][abort flag]
+  // layout: [B operands][S slots][mbarriers][tmem address][abort flag]
   unsigned char *Wb = smem;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SLAB0 + S * SLOT);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 2 * NACC + 1);
@@ -792,32 +808,35 @@ __global__ void __launch_bounds__(352, 1)
   auto tempty = [&](uint32_t k) { return bar_s + 8u * (2 * S + NACC + k); };   // accumulator slot k read
   const uint32_t fin = bar_s + 8u * (2 * S + 2 * NACC);
 
-  // B operands: block (dy, dx) holds B[n = dz*16 + co][k = ci] = w[tap = dz*9 + dy*3 + dx][ci][co],
-  // core matrix (n/8, ci/8) at (n/8)*256 + (ci/8)*128, row n%8 at 16 B, element ci%8 at 2 B
-  for (int i = tid; i < 9 * 48; i += blockDim.x) {
-    const int blk = i / 48, n = i % 48;
-    const int tap = (n / 16) * 9 + blk, co = n % 16;
+  // B operands: block (dy, dx, K step kh) holds B[n = dz*CO + co][k = ci - 16 kh] =
+  // w[tap = dz*9 + dy*3 + dx][ci][co]; core matrix (n/8, k/8) at (n/8)*256 + (k/8)*128, row n%8 at
+  // 16 B, element k%8 at 2 B
+  for (int i = tid; i < 9 * KS * NN; i += blockDim.x) {
+    const int bk = i / NN, n = i % NN;
+    const int blk = bk / KS, kh = bk % KS;
+    const int tap = (n / CO) * 9 + blk, co = n % CO;
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const unsigned short lo = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c) * 16 + co]);
-      const unsigned short hi = __bfloat16_as_ushort(p.w[((long long)tap * 16 + 2 * c + 1) * 16 + co]);
+      const int ci = kh * 16 + 2 * c;
+      const unsigned short lo = __bfloat16_as_ushort(p.w[((long long)tap * CI + ci) * CO + co]);
+      const unsigned short hi = __bfloat16_as_ushort(p.w[((long long)tap * CI + ci + 1) * CO + co]);
       pk[c] = (uint32_t)lo | ((uint32_t)hi << 16);
     }
-    unsigned char *row = Wb + blk * BBLK + (n >> 3) * 256 + (n & 7) * 16;
+    unsigned char *row = Wb + bk * BBLK + (n >> 3) * 256 + (n & 7) * 16;
     *reinterpret_cast<uint4 *>(row) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     *reinterpret_cast<uint4 *>(row + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
   }
   if (tid == 0) {
     for (int k = 0; k < S; k++) {
       net_mbar_init(full(k), 1);
-      net_mbar_init(empty(k), 2);
+      net_mbar_init(empty(k), NISS);
     }
     for (int k = 0; k < NACC; k++) {
-      net_mbar_init(tfull(k), 2);
+      net_mbar_init(tfull(k), NISS);
       net_mbar_init(tempty(k), 256);
     }
-    net_mbar_init(fin, 2);
+    net_mbar_init(fin, NISS);
     *abort_s = 0;
   }
   if (warp == 1) {
@@ -855,21 +874,23 @@ __global__ void __launch_bounds__(352, 1)
           if (nload >= S && !role_wait(empty(slot), ((nload / S) - 1) & 1, abort_s, 4)) break;
           net_expect_tx(full(slot), LOADS * PLANE_TX);
           const uint32_t dst = slab_s + slot * SLOT;
-          tma_load_5d(dst, &tx, 0, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
-          if (!SW32) tma_load_5d(dst + PLANE, &tx, 8, x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
+#pragma unroll
+          for (int l = 0; l < (int)LOADS; l++)
+            tma_load_5d(dst + l * PLANE, &tx, l * (SW32 ? 16 : 8), x0 - 1, y0 - 1, zlo - 1 + k, b, full(slot));
           nload++;
         }
       }
     }
   } else if (warp <= 2) {
-    if (lane == 0) {
-      // ---- MMA issuers: warp 1 rows 0 .. R/2-1, warp 2 rows R/2 .. R-1 ----
-      const int r0 = (warp - 1) * (R / 2);
-      // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 48, M = 128
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
-      uint64_t bdesc[9];
-#pragma unroll
-      for (int blk = 0; blk < 9; blk++) bdesc[blk] = umma_desc(wb_s + blk * BBLK, 128, 256);
+    if (lane == 0 && warp <= NISS) {
+      // ---- MMA issuers: warp 1 + j takes rows j*R/NISS .. (j+1)*R/NISS - 1 ----
+      constexpr int RI = R / NISS;
+      const int r0 = (warp - 1) * RI;
+      // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 3 CO, M = 128
+      const uint32_t idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NN >> 3) << 17) | ((128u >> 4) << 24);
+      const uint64_t b_desc = umma_desc(wb_s, 128, 256);
+      const uint32_t b_lo = (uint32_t)b_desc, b_hi = (uint32_t)(b_desc >> 32);
       // A: slot 0, row 0.  SW32: K-major with the 32-byte swizzle (layout type 6 in bits 61-63),
       // 8-row groups 256 bytes apart, K within one swizzle row (leading offset unused, 16 bytes);
       // otherwise canonical no-swizzle, the two 8-channel planes one LBO apart
@@ -890,17 +911,22 @@ __global__ void __launch_bounds__(352, 1)
           if (zin >= 0 && zin < p.Z) {
             tc_fence_after();
             // low descriptor word of the slab (start address >> 4 | LBO >> 4 << 16); a slab row of
-            // 130 voxels is 130 units of 16 bytes
+            // PXW voxels is PXW * VOX units of 16 bytes
             const uint32_t al = a_lo + (n % S) * (SLOT >> 4);
             const uint32_t dcol = tmem + acc * ACOLS;
 #pragma unroll
             for (int blk = 0; blk < 9; blk++) {
               const int dy = blk / 3, dx = blk % 3;
 #pragma unroll
-              for (int r = 0; r < R / 2; r++) {
-                const uint64_t ad =
-                    ((uint64_t)a_hi << 32) | (uint64_t)(al + (uint32_t)(((r0 + r + dy) * PXW + dx) * VOX));
-                umma_f16(dcol + (r0 + r) * 48, ad, bdesc[blk], idesc, blk > 0 ? 1u : 0u);
+              for (int kh = 0; kh < KS; kh++) {
+                const uint64_t bd = ((uint64_t)b_hi << 32) | (uint64_t)(b_lo + (blk * KS + kh) * (BBLK >> 4));
+#pragma unroll
+                for (int r = 0; r < RI; r++) {
+                  const uint64_t ad = ((uint64_t)a_hi << 32) |
+                                      (uint64_t)(al + kh * (PLANE >> 4) +
+                                                 (uint32_t)(((r0 + r + dy) * PXW + dx) * VOX));
+                  umma_f16(dcol + (r0 + r) * NN, ad, bd, idesc, (blk > 0 || kh > 0) ? 1u : 0u);
+                }
               }
             }
           }
@@ -910,12 +936,12 @@ __global__ void __launch_bounds__(352, 1)
       }
     }
   } else {
-    // ---- epilogue: warps 3..10; warp w owns TMEM lane quarter w % 4 and output channels 8*hf..8*hf+7 ----
+    // ---- epilogue: warps 3..10; warp w owns TMEM lane quarter w % 4 and output channels CH*hf .. ----
     const int qd = warp & 3, hf = (warp - 3) >> 2;
     const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
-    float bias[8];
+    float bias[CH];
 #pragma unroll
-    for (int c = 0; c < 8; c++) bias[c] = (!HEAD && p.bias) ? p.bias[hf * 8 + c] : 0.f;
+    for (int c = 0; c < CH; c++) bias[c] = (!HEAD && p.bias) ? p.bias[hf * CH + c] : 0.f;
     uint32_t n = 0;   // first slab of the current item
     bool ok = true;
     for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
@@ -933,12 +959,15 @@ __global__ void __launch_bounds__(352, 1)
         }
         tc_fence_after();
         const int z = zlo + i;
-        float d[R][3][8];
+        float d[R][3][CH];
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll
-          for (int dz = 0; dz < 3; dz++)
-            tmem_ld8(tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + r * 48 + dz * 16 + hf * 8, d[r][dz]);
+          for (int dz = 0; dz < 3; dz++) {
+            const uint32_t a = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + r * NN + dz * CO + hf * CH;
+            if constexpr (CH == 16) tmem_ld16(a, d[r][dz]);
+            else tmem_ld8(a, d[r][dz]);
+          }
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         tc_fence_before();
         net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
@@ -946,9 +975,9 @@ __global__ void __launch_bounds__(352, 1)
 #pragma unroll
         for (int r = 0; r < R; r++) {
           const int y = y0 + r;
-          float o[8];
+          float o[CH];
 #pragma unroll
-          for (int c = 0; c < 8; c++)
+          for (int c = 0; c < CH; c++)
             o[c] = (lo_in ? d[r][0][c] : 0.f) + d[r][1][c] + (hi_in ? d[r][2][c] : 0.f);
           if (HEAD) {
             if (hf == 0 && b < h.T && z < h.Zr && y < h.Yr && x < h.Xr) {
@@ -958,28 +987,31 @@ __global__ void __launch_bounds__(352, 1)
             continue;
           }
           if (x >= p.X || y >= p.Y) continue;
-          const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * 16 + hf * 8;
-          uint4 mk;
-          if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + off);
-          uint4 outv;
-          __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(&outv);
-          const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
+          const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO + hf * CH;
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
-            float v0 = o[2 * k] + bias[2 * k];
-            float v1 = o[2 * k + 1] + bias[2 * k + 1];
-            if (p.relu) {
-              v0 = fmaxf(v0, 0.f);
-              v1 = fmaxf(v1, 0.f);
+          for (int v = 0; v < CH / 8; v++) {
+            uint4 mk;
+            if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + off + v * 8);
+            uint4 outv;
+            __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(&outv);
+            const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              float v0 = o[v * 8 + 2 * k] + bias[v * 8 + 2 * k];
+              float v1 = o[v * 8 + 2 * k + 1] + bias[v * 8 + 2 * k + 1];
+              if (p.relu) {
+                v0 = fmaxf(v0, 0.f);
+                v1 = fmaxf(v1, 0.f);
+              }
+              if (p.mask) {
+                const float2 mf = __bfloat1622float2(m2[k]);
+                if (!(mf.x > 0.f)) v0 = 0.f;
+                if (!(mf.y > 0.f)) v1 = 0.f;
+              }
+              hv[k] = __floats2bfloat162_rn(v0, v1);
             }
-            if (p.mask) {
-              const float2 mf = __bfloat1622float2(m2[k]);
-              if (!(mf.x > 0.f)) v0 = 0.f;
-              if (!(mf.y > 0.f)) v1 = 0.f;
-            }
-            hv[k] = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<uint4 *>(p.y + off + v * 8) = outv;
           }
-          *reinterpret_cast<uint4 *>(p.y + off) = outv;
         }
       }
       if (!ok) break;
@@ -993,12 +1025,12 @@ __global__ void __launch_bounds__(352, 1)
   __syncthreads();   // every role has left its loop (normally, or on an abort)
   if (warp == 0 && lane == 0 && *abort_s) {
     // copies still in flight land before the CTA exits: wait for the last load of every slot
-    for (uint32_t s = 0; s < (uint32_t)S && s < nload; s++) {
-      const uint32_t last = s + ((nload - 1 - s) / S) * S;
-      if (!net_mbar_wait(full(s), (last / S) & 1, 1000000000ULL)) atomicExch(&g_net_err, 8);
+    for (uint32_t sl = 0; sl < (uint32_t)S && sl < nload; sl++) {
+      const uint32_t last = sl + ((nload - 1 - sl) / S) * S;
+      if (!net_mbar_wait(full(sl), (last / S) & 1, 1000000000ULL)) atomicExch(&g_net_err, 8);
     }
   }
-  if ((warp == 1 || warp == 2) && lane == 0) {
+  if (warp >= 1 && warp <= NISS && lane == 0) {
     // every MMA issued has completed before the accumulators are released
     umma_commit(fin);
     if (!net_mbar_wait(fin, 0, 1000000000ULL)) atomicExch(&g_net_err, 9);
@@ -1461,14 +1493,18 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-template <int R, int S, bool HEAD, bool SW32>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32>
 static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
-  constexpr size_t SLOT = SW32 ? ((R + 2) * 136 * 32 + 1023) / 1024 * 1024 : 2 * (((R + 2) * 130 * 16 + 127) / 128 * 128);
-  constexpr size_t SMEM = (9 * 1536 + 1023) / 1024 * 1024 + S * SLOT + (2 * S + 2 * TMA16_NACC + 1) * 8 + 8;
+  constexpr int KS = CI / 16;
+  constexpr size_t SLOT = SW32 ? KS * (((R + 2) * 136 * 32 + 1023) / 1024 * 1024)
+                               : 2 * (((R + 2) * 130 * 16 + 127) / 128 * 128);
+  constexpr size_t SMEM =
+      (9 * KS * 3 * CO * 32 + 1023) / 1024 * 1024 + S * SLOT + (2 * S + 2 * TMA16_NACC + 1) * 8 + 8;
+  static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
   static int sms = 0;
   if (!sms) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<R, S, HEAD, SW32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -1480,10 +1516,11 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return cudaErrorNotSupported;
   if (reinterpret_cast<uintptr_t>(p.x) % 16) return cudaErrorMisalignedAddress;
-  // [B][Z][Y][X][16] BF16, innermost first; one box = one 8-channel plane of a slab
+  // [B][Z][Y][X][CI] BF16, innermost first; one box = 16 channels (SW32) or one 8-channel plane of a slab
   CUtensorMap map;
-  const cuuint64_t dims[5] = {16, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
-  const cuuint64_t strides[4] = {32, 32ull * p.X, 32ull * p.X * p.Y, 32ull * p.X * p.Y * p.Z};
+  const cuuint64_t vb = 2ull * CI;   // bytes per voxel
+  const cuuint64_t dims[5] = {(cuuint64_t)CI, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
+  const cuuint64_t strides[4] = {vb, vb * p.X, vb * p.X * p.Y, vb * p.X * p.Y * p.Z};
   const cuuint32_t box[5] = {SW32 ? 16u : 8u, SW32 ? 136u : 130u, (cuuint32_t)(R + 2), 1, 1};
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(p.x), dims, strides, box, estr,
@@ -1510,11 +1547,12 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   g.zchunks = (p.Z + g.zc - 1) / g.zc;
   g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
-  k_conv3d_tma16<R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g);
+  k_conv3d_tma16<CI, CO, R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g);
   return cudaGetLastError();
 }
 
-static int g_conv16_tc = 1;   // 16 -> 16 convolutions: 1 = tcgen05 with TMA staging (default), 0 = mma.sync tiles
+// 16 / 32 -> 16 / 32 channel convolutions: 1 = tcgen05 with TMA staging (default), 0 = mma.sync tiles
+static int g_conv16_tc = 1;
 
 int net_set_conv16_tcgen05(int on) {
   const int old = g_conv16_tc;
@@ -1523,7 +1561,8 @@ int net_set_conv16_tcgen05(int on) {
 }
 
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32) {
-  return sw32 ? launch_tma16<2, 8, false, true>(p, HeadOut{}, s) : launch_tma16<2, 8, false, false>(p, HeadOut{}, s);
+  return sw32 ? launch_tma16<16, 16, 2, 8, false, true>(p, HeadOut{}, s)
+              : launch_tma16<16, 16, 2, 8, false, false>(p, HeadOut{}, s);
 }
 
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
@@ -1531,10 +1570,13 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
   if (M == 0) return cudaSuccess;
   p.splits = 1;
   if (p.Ci == 16 && p.Co == 16)
-    return g_conv16_tc ? launch_tma16<2, 8, false, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
-  if (p.Ci == 16 && p.Co == 32) return launch_tiled<16, 32>(p, s);
-  if (p.Ci == 32 && p.Co == 16) return launch_tiled<32, 16>(p, s);
-  if (p.Ci == 32 && p.Co == 32) return launch_tiled<32, 32>(p, s);
+    return g_conv16_tc ? launch_tma16<16, 16, 2, 8, false, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
+  if (p.Ci == 16 && p.Co == 32)
+    return g_conv16_tc ? launch_tma16<16, 32, 1, 8, false, true>(p, HeadOut{}, s) : launch_tiled<16, 32>(p, s);
+  if (p.Ci == 32 && p.Co == 16)
+    return g_conv16_tc ? launch_tma16<32, 16, 2, 4, false, true>(p, HeadOut{}, s) : launch_tiled<32, 16>(p, s);
+  if (p.Ci == 32 && p.Co == 32)
+    return g_conv16_tc ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
   const int BN = p.Co >= 64 ? 64 : p.Co;
   const long long ctas = (M + 127) / 128 * (p.Co / BN);
   const int KT = 27 * (p.Ci / 16);
@@ -1698,7 +1740,7 @@ cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor
                            int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s) {
   ConvParams p{(const bf16 *)d, (const bf16 *)w, nullptr, nullptr, nullptr, T, Zp, Yp, Xp, 16, 16, 0, nullptr, 1};
   HeadOut h{x0, sum_x1, (float)Z * Y * X, bias, floor_, T, Z, Y, X};
-  return g_conv16_tc ? launch_tma16<2, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
+  return g_conv16_tc ? launch_tma16<16, 16, 2, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
 }
 
 cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,

@@ -252,9 +252,10 @@ int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int
  * rows = 1, 4 or 5: single-role kernels with tiles of 1 or 4 rows x 128
  * voxels (5 = 4 rows, double-buffered).  flf_net_status: FLF_OK, or
  * FLF_E_TIMEOUT when a bounded wait inside one gave up since the last call.
- * flf_net_conv16_tcgen05(on): the kernel flf_conv3d and flf_ws_head use for
- * 16 -> 16 channels: 1 = the warp-specialised tcgen05 kernel, 0 = the
- * mma.sync kernel; returns the previous setting. */
+ * flf_net_conv16_tcgen05(on): the kernels flf_conv3d and flf_ws_head use for
+ * 16 / 32 -> 16 / 32 channels: 1 = the warp-specialised tcgen05 kernel (32-byte
+ * swizzled TMA slabs, z taps folded into N), 0 = the mma.sync kernels;
+ * returns the previous setting. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream);
 int flf_net_status(void);

@@ -208,20 +208,22 @@ def test_conv3d_tcgen05_warp_specialised_many_items(env, shape, relu, masked, ro
     _close(torch, y, ref)
 
 
-@pytest.mark.parametrize("shape", [(2, 4, 6, 10), (1, 5, 17, 260)])
-def test_conv3d_dispatch_to_tcgen05(env, shape):
-    """flf_conv3d routes 16 -> 16 channels to the tcgen05 kernel when selected; the
-    result agrees with the mma.sync kernel to the BF16 rounding of the output."""
+@pytest.mark.parametrize("ci,co", [(16, 16), (16, 32), (32, 16), (32, 32)])
+@pytest.mark.parametrize("shape", [(2, 4, 6, 10), (1, 5, 17, 260), (1, 6, 40, 300)])
+def test_conv3d_dispatch_to_tcgen05(env, shape, ci, co):
+    """flf_conv3d routes 16 / 32 -> 16 / 32 channels to the tcgen05 kernel when
+    selected; the result agrees with float64 and with the mma.sync kernels to the
+    BF16 rounding of the output (the largest shape has more work items than SMs)."""
     torch, _flf = env
-    g = torch.Generator().manual_seed(17)
-    x = torch.randn(shape + (16,), generator=g).bfloat16().cuda()
-    w = (torch.randn((27, 16, 16), generator=g) / 20).bfloat16().cuda()
-    b = torch.randn(16, generator=g).float().cuda()
+    g = torch.Generator().manual_seed(17 + ci + co)
+    x = torch.randn(shape + (ci,), generator=g).bfloat16().cuda()
+    w = (torch.randn((27, ci, co), generator=g) / np.sqrt(27 * ci)).bfloat16().cuda()
+    b = torch.randn(co, generator=g).float().cuda()
     out = {}
     for on in (False, True):
         old = _flf.conv16_tcgen05(on)
         try:
-            y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
+            y = torch.empty(shape + (co,), dtype=torch.bfloat16, device="cuda")
             _flf.conv3d(x, w, b, y, relu=True)
             torch.cuda.synchronize()
             _flf.net_status()
