@@ -233,3 +233,31 @@ def test_conv3d_dispatch_to_tcgen05(env, shape, ci, co):
     ref = _ref_conv(torch, x.double().cpu(), w.double().cpu(), b.double().cpu()).clamp_min(0)
     _close(torch, out[True], ref)
     assert float((out[True].float() - out[False].float()).abs().max()) <= 1e-2 * float(ref.abs().max())
+
+
+@pytest.mark.parametrize("ci,co", [(16, 16), (16, 32), (32, 16), (32, 32)])
+@pytest.mark.parametrize("shape", [(4, 24, 128, 128), (4, 12, 64, 64)])
+def test_conv3d_tcgen05_training_shapes(env, shape, ci, co):
+    """The network's training batches (4 crops of 24 x 128 x 128 and their level-1
+    halves) with a gradient mask: every work item of every CTA agrees with the
+    mma.sync kernels to the BF16 rounding of the output."""
+    torch, _flf = env
+    g = torch.Generator(device="cuda").manual_seed(ci * 3 + co + shape[1])
+    x = torch.randn(shape + (ci,), generator=g, device="cuda").bfloat16()
+    w = (torch.randn((27, ci, co), generator=g, device="cuda") / np.sqrt(27 * ci)).bfloat16()
+    m = torch.randn(shape + (co,), generator=g, device="cuda").bfloat16()
+    out = {}
+    for on in (False, True):
+        old = _flf.conv16_tcgen05(on)
+        try:
+            y = torch.full(shape + (co,), float("nan"), dtype=torch.bfloat16, device="cuda")
+            _flf.conv3d(x, w, None, y, mask=m)
+            torch.cuda.synchronize()
+            _flf.net_status()
+            out[on] = y.float()
+        finally:
+            _flf.conv16_tcgen05(old)
+    assert bool(torch.isfinite(out[True]).all())
+    err = (out[True] - out[False]).abs()
+    lim = 1e-2 * out[False].abs() + 1e-3 * float(out[False].abs().max())
+    assert bool((err <= lim).all()), (float(err.max()), int((err > lim).sum()))
