@@ -1662,7 +1662,7 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
   return FLF_OK;
 }
 
-int flf_net_conv16_tcgen05(int on) { return net_set_conv16_tcgen05(on); }
+int flf_net_conv16_tcgen05(int mode) { return net_set_conv16_tcgen05(mode); }
 
 int flf_net_status(void) {
   const int v = net_status_read_and_clear();

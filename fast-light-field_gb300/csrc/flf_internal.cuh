@@ -272,7 +272,7 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
 cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms);
 cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s);
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32);
-int net_set_conv16_tcgen05(int on);
+int net_set_conv16_tcgen05(int mode);
 int net_status_read_and_clear();
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s);
 cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s);

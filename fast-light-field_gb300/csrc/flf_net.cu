@@ -1551,12 +1551,13 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   return cudaGetLastError();
 }
 
-// 16 / 32 -> 16 / 32 channel convolutions: 1 = tcgen05 with TMA staging (default), 0 = mma.sync tiles
+// kernels of the 16 / 32-channel convolutions: 0 = mma.sync tiles; 1 (default) = tcgen05 with TMA
+// staging for 16 -> 16, mma.sync for the 32-channel layers; 2 = tcgen05 for all of them
 static int g_conv16_tc = 1;
 
-int net_set_conv16_tcgen05(int on) {
+int net_set_conv16_tcgen05(int mode) {
   const int old = g_conv16_tc;
-  g_conv16_tc = on ? 1 : 0;
+  g_conv16_tc = mode < 0 ? 0 : (mode > 2 ? 2 : mode);
   return old;
 }
 
@@ -1572,11 +1573,11 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
   if (p.Ci == 16 && p.Co == 16)
     return g_conv16_tc ? launch_tma16<16, 16, 2, 8, false, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
   if (p.Ci == 16 && p.Co == 32)
-    return g_conv16_tc ? launch_tma16<16, 32, 1, 8, false, true>(p, HeadOut{}, s) : launch_tiled<16, 32>(p, s);
+    return g_conv16_tc == 2 ? launch_tma16<16, 32, 1, 8, false, true>(p, HeadOut{}, s) : launch_tiled<16, 32>(p, s);
   if (p.Ci == 32 && p.Co == 16)
-    return g_conv16_tc ? launch_tma16<32, 16, 2, 4, false, true>(p, HeadOut{}, s) : launch_tiled<32, 16>(p, s);
+    return g_conv16_tc == 2 ? launch_tma16<32, 16, 2, 4, false, true>(p, HeadOut{}, s) : launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32)
-    return g_conv16_tc ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
+    return g_conv16_tc == 2 ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
   const int BN = p.Co >= 64 ? 64 : p.Co;
   const long long ctas = (M + 127) / 128 * (p.Co / BN);
   const int KT = 27 * (p.Ci / 16);

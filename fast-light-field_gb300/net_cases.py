@@ -1,6 +1,6 @@
 """Timing cases for the warm-start network kernels (CUDA events, no profiler).
 
-    python net_cases.py conv16 [Z Y X] [--kernel tcgen05|tcgen05-noswizzle|mma.sync] [--reps N]
+    python net_cases.py conv16 [Z Y X] [--kernel tcgen05|tcgen05-all|tcgen05-noswizzle|mma.sync] [--reps N]
     python net_cases.py unet   [Z Y X] [--kernel ...] [--reps N]
 
 ``conv16`` runs the 16 -> 16 channel 3x3x3 convolution (flf_conv3d, or
@@ -37,7 +37,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("case", choices=["conv16", "unet"])
     ap.add_argument("shape", nargs="*", type=int, default=[24, 456, 456], help="Z Y X")
-    ap.add_argument("--kernel", default="tcgen05", choices=["tcgen05", "tcgen05-noswizzle", "mma.sync"])
+    ap.add_argument("--kernel", default="tcgen05", choices=["tcgen05", "tcgen05-all", "tcgen05-noswizzle", "mma.sync"],
+                    help="tcgen05: 16->16 layers on tcgen05 (the default); tcgen05-all: the 32-channel layers too")
     ap.add_argument("--reps", type=int, default=10)
     args = ap.parse_args(argv)
     if len(args.shape) != 3:
@@ -45,7 +46,7 @@ def main(argv=None):
     import torch
     import _flf
     _flf.load_library()
-    _flf.conv16_tcgen05(args.kernel != "mma.sync")
+    _flf.conv16_tcgen05({"mma.sync": 0, "tcgen05-all": 2}.get(args.kernel, 1))
     Z, Y, X = args.shape
     g = torch.Generator(device="cuda").manual_seed(0)
     if args.case == "conv16":

@@ -333,20 +333,19 @@ class WarmStart:
         return x
 
     def train(self, steps=1500, batch=4, crop=128, volumes_per_refresh=8, refresh_every=8, lr=1e-3, seed=1,
-              target_iters=32, log_every=0, tcgen05=False):
+              target_iters=32, log_every=0, kernels=None):
         """Train on crops of freshly generated synthetic volumes; returns seconds taken.
 
-        tcgen05 selects the 16 / 32-channel convolution kernels used while training
-        (forward and data gradients): False keeps the mma.sync kernels, with which the
-        networks of the measured runs were trained; inference afterwards uses the
-        library's default (the tcgen05 kernels).  Both agree to the BF16 rounding of
-        each layer's output, but training follows a different rounding path with each."""
-        old = _flf.conv16_tcgen05(tcgen05)
+        kernels selects the 16 / 32-channel convolution kernels used while training
+        (forward and data gradients; a mode of _flf.conv16_tcgen05), None keeps the
+        library's current choice."""
+        old = _flf.conv16_tcgen05(kernels) if kernels is not None else None
         try:
             return self._train(steps, batch, crop, volumes_per_refresh, refresh_every, lr, seed, target_iters,
                                log_every)
         finally:
-            _flf.conv16_tcgen05(old)
+            if old is not None:
+                _flf.conv16_tcgen05(old)
 
     def _train(self, steps, batch, crop, volumes_per_refresh, refresh_every, lr, seed, target_iters, log_every):
         rng = np.random.default_rng(seed)

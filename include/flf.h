@@ -252,14 +252,15 @@ int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int
  * rows = 1, 4 or 5: single-role kernels with tiles of 1 or 4 rows x 128
  * voxels (5 = 4 rows, double-buffered).  flf_net_status: FLF_OK, or
  * FLF_E_TIMEOUT when a bounded wait inside one gave up since the last call.
- * flf_net_conv16_tcgen05(on): the kernels flf_conv3d and flf_ws_head use for
- * 16 / 32 -> 16 / 32 channels: 1 = the warp-specialised tcgen05 kernel (32-byte
- * swizzled TMA slabs, z taps folded into N), 0 = the mma.sync kernels;
- * returns the previous setting. */
+ * flf_net_conv16_tcgen05(mode): the kernels flf_conv3d and flf_ws_head use for
+ * 16 / 32 -> 16 / 32 channels: 0 = the mma.sync kernels; 1 (default) = the
+ * warp-specialised tcgen05 kernel (32-byte swizzled TMA slabs, z taps folded
+ * into N) for 16 -> 16 and mma.sync for the 32-channel layers; 2 = tcgen05
+ * for all of them.  Returns the previous setting. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream);
 int flf_net_status(void);
-int flf_net_conv16_tcgen05(int on);
+int flf_net_conv16_tcgen05(int mode);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
 int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream);
 int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);

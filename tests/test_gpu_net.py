@@ -261,3 +261,31 @@ def test_conv3d_tcgen05_training_shapes(env, shape, ci, co):
     err = (out[True] - out[False]).abs()
     lim = 1e-2 * out[False].abs() + 1e-3 * float(out[False].abs().max())
     assert bool((err <= lim).all()), (float(err.max()), int((err > lim).sum()))
+
+
+@pytest.mark.parametrize("ci,co", [(16, 32), (32, 16), (32, 32)])
+def test_conv3d_tcgen05_inference_level1_shape(env, ci, co):
+    """The network's level-1 layers at inference size (12 x 228 x 228: a partial
+    second x segment, three or more items per CTA) with bias and ReLU: the tcgen05
+    kernels agree with the mma.sync kernels to the BF16 rounding of the output."""
+    torch, _flf = env
+    shape = (1, 12, 228, 228)
+    g = torch.Generator(device="cuda").manual_seed(ci + 2 * co)
+    x = torch.randn(shape + (ci,), generator=g, device="cuda").bfloat16()
+    w = (torch.randn((27, ci, co), generator=g, device="cuda") / np.sqrt(27 * ci)).bfloat16()
+    b = torch.randn(co, generator=g, device="cuda")
+    out = {}
+    for mode in (0, 2):
+        old = _flf.conv16_tcgen05(mode)
+        try:
+            y = torch.full(shape + (co,), float("nan"), dtype=torch.bfloat16, device="cuda")
+            _flf.conv3d(x, w, b, y, relu=True)
+            torch.cuda.synchronize()
+            _flf.net_status()
+            out[mode] = y.float()
+        finally:
+            _flf.conv16_tcgen05(old)
+    assert bool(torch.isfinite(out[2]).all())
+    err = (out[2] - out[0]).abs()
+    lim = 1e-2 * out[0].abs() + 1e-3 * float(out[0].abs().max())
+    assert bool((err <= lim).all()), (float(err.max()), int((err > lim).sum()))
