@@ -796,7 +796,7 @@ def run_warmstart(args):
             "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": wl["Nnum"], "frames": 1,
                        "psf": psf_desc,
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
-                       "conv_kernels": "tcgen05 for 16->16 channels, mma.sync for the 32-channel layers",
+                       "conv_kernels": "tcgen05 for the 16/32-channel layers, mma.sync for 64/128 channels",
                        "target_iters": args.target_iters,
                        "residual_finetune_steps": args.tune_steps, "finetune_s": round(tune_s, 1),
                        "losses": [[round(float(v), 6) if isinstance(v, float) else v for v in l]

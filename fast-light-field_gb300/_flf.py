@@ -207,9 +207,9 @@ def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):
 
 def conv16_tcgen05(mode):
     """Select the kernels conv3d and ws_head use for 16 / 32 -> 16 / 32 channels and
-    return the previous mode: 0 or False = mma.sync; 1 (the default) = the
-    warp-specialised tcgen05 kernel for 16 -> 16, mma.sync for the 32-channel
-    layers; 2 or True = tcgen05 for all of them."""
+    return the previous mode: 0 or False = mma.sync; 1 = the warp-specialised
+    tcgen05 kernel for 16 -> 16, mma.sync for the 32-channel layers; 2 or True
+    (the default) = tcgen05 for all of them."""
     if type(mode) is bool:
         mode = 2 if mode else 0
     return int(load_library().flf_net_conv16_tcgen05(int(mode)))

@@ -1551,9 +1551,9 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   return cudaGetLastError();
 }
 
-// kernels of the 16 / 32-channel convolutions: 0 = mma.sync tiles; 1 (default) = tcgen05 with TMA
-// staging for 16 -> 16, mma.sync for the 32-channel layers; 2 = tcgen05 for all of them
-static int g_conv16_tc = 1;
+// kernels of the 16 / 32-channel convolutions: 0 = mma.sync tiles; 1 = tcgen05 with TMA staging
+// for 16 -> 16, mma.sync for the 32-channel layers; 2 (default) = tcgen05 for all of them
+static int g_conv16_tc = 2;
 
 int net_set_conv16_tcgen05(int mode) {
   const int old = g_conv16_tc;

@@ -1,6 +1,6 @@
 """Timing cases for the warm-start network kernels (CUDA events, no profiler).
 
-    python net_cases.py conv16 [Z Y X] [--kernel tcgen05|tcgen05-all|tcgen05-noswizzle|mma.sync] [--reps N]
+    python net_cases.py conv16 [Z Y X] [--kernel tcgen05-all|tcgen05|tcgen05-noswizzle|mma.sync] [--reps N]
     python net_cases.py unet   [Z Y X] [--kernel ...] [--reps N]
 
 ``conv16`` runs the 16 -> 16 channel 3x3x3 convolution (flf_conv3d, or
@@ -37,8 +37,10 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("case", choices=["conv16", "unet"])
     ap.add_argument("shape", nargs="*", type=int, default=[24, 456, 456], help="Z Y X")
-    ap.add_argument("--kernel", default="tcgen05", choices=["tcgen05", "tcgen05-all", "tcgen05-noswizzle", "mma.sync"],
-                    help="tcgen05: 16->16 layers on tcgen05 (the default); tcgen05-all: the 32-channel layers too")
+    ap.add_argument("--kernel", default="tcgen05-all",
+                    choices=["tcgen05", "tcgen05-all", "tcgen05-noswizzle", "mma.sync"],
+                    help="tcgen05: the 16->16 layers on tcgen05; tcgen05-all (the default): the 32-channel "
+                         "layers too")
     ap.add_argument("--reps", type=int, default=10)
     args = ap.parse_args(argv)
     if len(args.shape) != 3:

@@ -253,10 +253,10 @@ int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int
  * voxels (5 = 4 rows, double-buffered).  flf_net_status: FLF_OK, or
  * FLF_E_TIMEOUT when a bounded wait inside one gave up since the last call.
  * flf_net_conv16_tcgen05(mode): the kernels flf_conv3d and flf_ws_head use for
- * 16 / 32 -> 16 / 32 channels: 0 = the mma.sync kernels; 1 (default) = the
+ * 16 / 32 -> 16 / 32 channels: 0 = the mma.sync kernels; 1 = the
  * warp-specialised tcgen05 kernel (32-byte swizzled TMA slabs, z taps folded
- * into N) for 16 -> 16 and mma.sync for the 32-channel layers; 2 = tcgen05
- * for all of them.  Returns the previous setting. */
+ * into N) for 16 -> 16 and mma.sync for the 32-channel layers; 2 (default) =
+ * tcgen05 for all of them.  Returns the previous setting. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream);
 int flf_net_status(void);
