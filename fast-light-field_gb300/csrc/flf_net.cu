@@ -14,6 +14,11 @@
 //   k_conv3d_t16      16 -> 16 channels: 16 x 16-voxel tiles, 4 rows per warp,
 //                     one z slice of weight fragments in registers at a time;
 //                     with HEAD, the warm-start head writing the start volume.
+//   k_conv3d_tma16    16 / 32 -> 16 / 32 channels on tcgen05 (the default for
+//                     these layers): warp-specialised producer / MMA /
+//                     epilogue roles, TMA-staged input slabs, the z taps
+//                     folded into N and summed from a TMEM accumulator ring.
+//   k_conv3d_tc16     the first single-role tcgen05 16 -> 16 kernel.
 //   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
 //                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
 //                     split-K over its 4 warps, FP32 atomics into dW.
@@ -663,7 +668,9 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 }
 
 // ---------------------------------------------------------------------------
-// 16 -> 16 channels, warp-specialised on tcgen05 with TMA staging.  A work
+// 16 / 32 -> 16 / 32 channels, warp-specialised on tcgen05 with TMA staging
+// (written here for CI = CO = 16; CI = 32 adds a second K step of 16
+// channels, CO = 32 makes N = 96 and an item one row).  A work
 // item is a column of output, R rows (y) x 128 voxels (x), over a run of z
 // planes.  The CTA walks the input planes z' of the column: each is one slab,
 // (R+2) rows of the voxels x0-1 .. (the x / y halo included), that TMA loads
@@ -684,7 +691,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 //   tcgen05.mma  M 128 (voxels x) x N 48 (dz, co) x K 16 (ci)
 // per (dy, dx), with A the slab row r+dy shifted by dx, accumulates
 //   D[z'][r][x][dz][co] = sum over (dy, dx, ci) of in[z'][r+dy][x+dx][ci] w[dz][dy][dx][ci][co]
-// into one of 5 TMEM accumulator slots (R x 48 columns each), and
+// into one of 5 TMEM accumulator slots (R x N columns each), and
 //   out[z][r][x][co] = D[z-1][r][x][0][co] + D[z][r][x][1][co] + D[z+1][r][x][2][co]
 // adds three column groups of the same TMEM lane: no data moves between
 // lanes.  A slab's shared memory is free as soon as its MMAs complete; its
@@ -708,7 +715,7 @@ struct Tma16Grid {   // work items: [B][zchunks][yblocks][xsegs] columns of R x 
   long long items;
 };
 
-constexpr int TMA16_NACC = 5;   // TMEM accumulator slots (R x 48 columns each)
+constexpr int TMA16_NACC = 5;   // TMEM accumulator slots (R x 3 CO columns each)
 
 namespace {
 
