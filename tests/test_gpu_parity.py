@@ -151,7 +151,7 @@ def test_zero_image_rl_gives_zero(mods):
 
 
 def test_full_size_linearity_and_adjointness(mods):
-    """Config-0 sizes (450x450, Nnum 15, 11 planes): size-independent properties."""
+    """The 450 x 450 px, Nnum 15, 11-plane workload: size-independent properties."""
     projector, lfdeconv, psfmatrix = mods
     import synthetic
     z = np.arange(-25, 26, 5)

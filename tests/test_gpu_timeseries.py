@@ -28,7 +28,7 @@ def test_time_series_driver_mixed_sizes(tmp_path, built_lib):
     import tiffio
     N, iters = 5, 3
     H, Ht = synthetic.synthetic_psf(N, [-10, 0, 10], 2)
-    # the driver takes the .mat path; its memmap folder (same name, no extension) is read
+    # the time-series CLI takes the .mat path; its memmap folder (same name, no extension) is read
     psfmatrix.SaveReducedMatrices(str(tmp_path / "psf"), H, Ht)
     rng = np.random.default_rng(11)
     shapes = [(40, 35), (30, 30), (40, 35), (30, 30), (40, 35)]     # interleaved sizes
