@@ -28,6 +28,7 @@ import time
 
 import numpy as np
 
+import _flf
 import lfdeconv
 import lfimage
 import psfmatrix
@@ -53,6 +54,8 @@ def ProcessBatch(projector, hMatrix, timepoints, destDir, maxIter, warm=None):
                                    projector=projector)
     finally:
         projector.storeVolumesOnGPU = saved
+    if warm is not None:
+        _flf.net_status()   # the result is on the host: raise if a network kernel's bounded wait gave up
     paths = []
     for i, t in enumerate(timepoints):
         dest = os.path.join(destDir, "%s_deconvolved.tif" % os.path.splitext(os.path.basename(t))[0])

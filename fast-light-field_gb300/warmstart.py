@@ -376,6 +376,7 @@ class WarmStart:
             if log_every and (step % log_every == 0 or step == steps - 1):
                 self.losses.append((step, float(loss)))
         torch.cuda.synchronize(self.dev)
+        _flf.net_status()   # raise if a bounded wait in a tensor-core convolution gave up
         return time.time() - t0
 
     def finetune_residual(self, steps=200, lr=1e-4, frames=1, seed=7, floor=1e-3, log_every=0):
@@ -409,6 +410,7 @@ class WarmStart:
                 self.losses.append(("residual", step, loss))
             del cache, out
         torch.cuda.synchronize(self.dev)
+        _flf.net_status()   # raise if a bounded wait in a tensor-core convolution gave up
         return time.time() - t0
 
     def initial_volume(self, htf, floor=1e-3):
