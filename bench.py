@@ -61,6 +61,10 @@ WORKLOADS = {
                                       "41 planes -100..100 um"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
+    # the warm-start network's kernels alone on a random BF16 volume (--shape Z Y X, default 24 456 456,
+    # the padded 450 x 450 px x 21-plane volume): one 16 -> 16 channel 3x3x3 convolution, or the U-Net forward
+    "conv16": dict(label="warm-start network: one 16->16 channel 3x3x3 BF16 convolution"),
+    "unet": dict(label="warm-start network: U-Net forward (16-32-64-128 channels) with its head"),
     # a time series of frames of three sizes (--frames per size, default 32), 500 drifting beads each
     "timeseries": dict(Nnum=15, sizes=(30, 45, 67), z=(-75, 75, 5), img_size_ref=21, beads=500,
                        label="time series, Nnum 15, 31 planes -75..75 um, frames at 30x30, 45x45 and 67x67 "
@@ -88,6 +92,12 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-planes", type=int, default=5)
+    ap.add_argument("--shape", type=int, nargs=3, default=[24, 456, 456], metavar=("Z", "Y", "X"),
+                    help="volume of the conv16 / unet network workloads")
+    ap.add_argument("--kernel", default="tcgen05-all",
+                    choices=["tcgen05", "tcgen05-all", "tcgen05-noswizzle", "mma.sync"],
+                    help="conv16 / unet: tcgen05 = the 16->16 layers on tcgen05; tcgen05-all (the default) = "
+                         "the 32-channel layers too")
     ap.add_argument("--planes", default=None,
                     help="comma-separated z indices of the workload to keep (smaller cases for profiling)")
     return ap.parse_args()
@@ -265,7 +275,7 @@ def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload in ("timeseries", "rectify", "psf", "warmstart", "warmstart_fullfield"):
+    if args.workload in ("timeseries", "rectify", "psf", "warmstart", "warmstart_fullfield", "conv16", "unet"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
                           "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
@@ -814,6 +824,58 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
+def run_network_case(args):
+    """The warm-start network's kernels on a random BF16 volume [1][Z][Y][X][C]
+    (inputs larger than L2 at the default 24 x 456 x 456): one 16 -> 16 channel
+    3x3x3 convolution with bias and ReLU (``conv16``), or the U-Net forward with
+    its head (``unet``); CUDA-event time per call after the warm-up calls.  These
+    are the cases the network kernel profiles are captured on."""
+    import torch
+    import build_lib
+    import _flf
+    build_lib.build()
+    _flf.load_library()
+    _flf.conv16_tcgen05({"mma.sync": 0, "tcgen05-all": 2}.get(args.kernel, 1))
+    Z, Y, X = args.shape
+    g = torch.Generator(device="cuda").manual_seed(0)
+    if args.workload == "conv16":
+        x = torch.randn((1, Z, Y, X, 16), generator=g, device="cuda").bfloat16()
+        w = (torch.randn((27, 16, 16), generator=g, device="cuda") / 20).bfloat16()
+        b = torch.randn(16, generator=g, device="cuda")
+        y = torch.empty_like(x)
+        if args.kernel == "tcgen05-noswizzle":
+            fn = lambda: _flf.conv3d_tc(x, w, b, y, relu=True, rows=0)   # noqa: E731
+        else:
+            fn = lambda: _flf.conv3d(x, w, b, y, relu=True)   # noqa: E731
+        flop = 2.0 * Z * Y * X * 27 * 16 * 16
+    else:
+        import warmstart
+        net = warmstart.UNet3D(seed=1)
+        x = torch.zeros((1, Z, Y, X, warmstart.CIN), device="cuda").bfloat16()
+        x[..., :4] = torch.rand((1, Z, Y, X, 4), generator=g, device="cuda").bfloat16()
+        fn = lambda: net.forward(x)   # noqa: E731
+        flop = None
+    for _ in range(max(args.warmup, 3)):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    _flf.net_status()
+    line = {"metric": "ms per call, %s" % WORKLOADS[args.workload]["label"], "value": ms, "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulation)",
+            "data": "synthetic", "config": {"workload": WORKLOADS[args.workload]["label"], "shape": [Z, Y, X],
+                                            "kernel": args.kernel, "l2": "activations larger than L2"}}
+    if flop:
+        line["tflops"] = flop / ms / 1e9
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -827,6 +889,8 @@ def main():
         run_psf(args)
     elif args.workload in ("warmstart", "warmstart_fullfield"):
         run_warmstart(args)
+    elif args.workload in ("conv16", "unet"):
+        run_network_case(args)
     else:
         run_gb300(args, rank, world, local)
 

@@ -387,7 +387,13 @@ class Context:
         del keep
 
     def backward_noalloc(self, img, vol, T, Y, X, stream=None):
-        """Back projection over all planes that allocates no device memory (see include/flf.h)."""
+        """Back projection over all planes that allocates no device memory.
+
+        For callers that must not allocate while they run; its scratch is a
+        fixed 16 MiB device array set up when the context was created.  The
+        call only enqueues work: call ``synchronize`` (which raises on a
+        bounded device wait that gave up) before using ``vol``.
+        """
         self._check(self._lib.flf_backward_noalloc(self._h, _ptr(img), _ptr(vol), int(T), int(Y), int(X),
                                                    _ptr(stream)))
 

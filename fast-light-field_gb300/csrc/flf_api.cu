@@ -92,6 +92,7 @@ struct flf_ctx {
   int opt_streams = 2;           // transform groups alternate over this many streams (1 or 2)
   cudaStream_t s2 = nullptr;     // the second stream, and the events that fork / chain / join it
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chain = nullptr;
+  void *noalloc_scratch = nullptr;   // device address of the fixed scratch of flf_backward_noalloc
   int *h_err = nullptr;          // host-mapped flag set by bounded device waits
   int *d_err = nullptr;
   // per-kernel launch statistics; event timing when profiling is on
@@ -886,28 +887,25 @@ int backward_chunk(flf_ctx *ctx, const float *chan, const PlaneSet &ps, int nt, 
 
 // ----------------------------------------------------------------------------
 // Fixed scratch for flf_backward_noalloc: a file-scope device array, so that
-// entry point never asks the driver for memory.  Every GPU that loads this
-// library holds FLF_NOALLOC_SCRATCH_BYTES of it until the process exits.
+// entry point never asks the driver for memory.  With CUDA's lazy module
+// loading the array is committed when this file's module loads, which
+// flf_ctx_create forces by looking up the array's address (below): from then
+// on the GPU holds FLF_NOALLOC_SCRATCH_BYTES of it until the process exits.
 // ----------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_noalloc_scratch[FLF_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-void *g_noalloc_ptr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (`device`).
-// The host-side symbol is only a stand-in and must never reach a kernel; the
-// real address is looked up once per device, with that device current.
-int noalloc_scratch(flf_ctx *ctx, int device, void **out) {
-  if (device < 0 || device >= kMaxDevices)
-    return fail(ctx, FLF_E_ARG, "device %d beyond the %d devices the fixed scratch supports", device, kMaxDevices);
-  if (!g_noalloc_ptr[device]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr)
-      return fail(ctx, FLF_E_CUDA, "cudaGetSymbolAddress of the fixed scratch failed: %s", cudaGetErrorString(e));
-    g_noalloc_ptr[device] = ptr;
+// Device address of the scratch array in the current CUDA context.  The
+// host-side symbol is only a stand-in and must never reach a kernel.  Called
+// by flf_ctx_create with the context's device current; the address is kept in
+// the context, which is valid only in the primary context of that device.
+int noalloc_scratch_lookup(flf_ctx *ctx) {
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) {
+    cudaGetLastError();
+    return fail(ctx, FLF_E_CUDA, "cudaGetSymbolAddress of the fixed scratch failed: %s", cudaGetErrorString(e));
   }
-  *out = g_noalloc_ptr[device];
+  ctx->noalloc_scratch = ptr;
   return FLF_OK;
 }
 
@@ -951,6 +949,7 @@ int flf_ctx_create(flf_ctx **out, int device, int nnum, int num_planes) {
     *ctx->h_err = 0;
   }
   if (rc == FLF_OK) rc = build_tables(ctx);
+  if (rc == FLF_OK) rc = noalloc_scratch_lookup(ctx);
   if (rc != FLF_OK) {
     g_create_error = ctx->err;
     flf_ctx_destroy(ctx);
@@ -1114,9 +1113,8 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
                 "flf_backward_noalloc needs %zu bytes of scratch for this geometry (Nnum %d, transform %d), "
                 "more than its fixed %u bytes; use flf_backward", need, ctx->N, Gm.max_f(),
                 (unsigned)FLF_NOALLOC_SCRATCH_BYTES);
-  void *scratch = nullptr;
-  int rc = noalloc_scratch(ctx, ctx->device, &scratch);
-  if (rc != FLF_OK) return rc;
+  void *scratch = ctx->noalloc_scratch;
+  if (!scratch) return fail(ctx, FLF_E_STATE, "the fixed scratch was not set up by flf_ctx_create");
   cudaStream_t s = (cudaStream_t)stream;
   const long long YX = (long long)Y * X;
   char *base = (char *)scratch;

@@ -112,12 +112,21 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
  *    (2 * (Nnum^2 * f * (f/2+1) * 8 + Nnum^2 * Ly * Lxp * 4) bytes, Lxp =
  *    ceil(X/Nnum) rounded up to 4; e.g. the 1005 x 1005 full field) are
  *    rejected with FLF_E_ARG; use flf_backward.
- *  - The first call on each device looks up the array's device address (a
- *    one-time set-up with that device current); make that first call before
- *    any stream capture.
+ *  - The array is set up when the context is created: flf_ctx_create looks
+ *    up its device address with the context's device current, which (under
+ *    CUDA's lazy module loading) is also when the 16 MiB is committed on that
+ *    GPU.  The call itself does no set-up, but under lazy loading its first
+ *    launch of each kernel makes the driver load that kernel's code into
+ *    device memory: make one call at set-up time (or run with
+ *    CUDA_MODULE_LOADING=EAGER) before the loop that must not allocate.
+ *    The address belongs to the device's primary context; after
+ *    cudaDeviceReset create a new context.
  *  - All calls share the one array and nothing in it needs to start at zero
  *    (every element read is written first by the same call); calls whose
- *    work overlaps on the GPU, on any stream or context, race on it. */
+ *    work overlaps on the GPU, on any stream or context, race on it.
+ *  - Like flf_backward, the call only enqueues work: a bounded device wait
+ *    that gave up is reported by the next flf_synchronize (FLF_E_TIMEOUT),
+ *    so check that before using the result. */
 int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y,
                          int X, void *stream);
 

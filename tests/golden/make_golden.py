@@ -1,7 +1,7 @@
 """Generate tests/golden/reference_vectors.npz by running the reference itself.
 
-Runs in a container that holds the reference sources (jmtayloruk/fast-light-field)
-at /root/reference; the GPU test machines never read them.  It imports the
+Runs in a container that holds the reference sources (jmtayloruk/fast-light-field),
+whose folder is the one argument; the GPU test machines never read them.  It imports the
 reference's own Python modules and uses its pure-python projector
 ``Projector_python`` (projector.py:1017) and RL driver ``lfdeconv.DeconvRL``
 (lfdeconv.py:72) - the code the reference's self-test trusts as its oracle
@@ -9,7 +9,7 @@ reference's own Python modules and uses its pure-python projector
 extension ``py_light_field``, h5py, tifffile, the Cython PSF integrands) are
 replaced by empty stand-ins so that the imports succeed.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/reference
 """
 
 import os
@@ -49,7 +49,9 @@ def make_hmatrix(psfmatrix, H, Ht, tmp):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    ref_dir = sys.argv[1]
     projector, lfdeconv, psfmatrix = import_reference(ref_dir)
     out = {}
     noprog = lambda w, desc=None, leave=True, **k: w  # noqa: E731

@@ -1,14 +1,14 @@
 """Generate tests/golden/psf_vectors.npz by running the reference's GeneratePSF.
 
-Runs in a container that holds the reference sources (default /root/reference;
-the GPU machines never read them).  The reference's Cython integrand module
+Runs in a container that holds the reference sources, whose folder is the one
+argument (the GPU machines never read them).  The reference's Cython integrand module
 (light-field-integrands: one .pyx plus bessel.c) is compiled into a temporary
 folder; h5py, which is not installed, is replaced by a stand-in whose File
 object records what GeneratePSF saves.  For every case of psf_inputs.py the
 fixture keeps H and Ht (as saved: transposed, [Z, b, a, y, x]), CAindex and
 Hmax.
 
-Usage:  python tests/golden/make_golden_psf.py [/path/to/reference]
+Usage:  python tests/golden/make_golden_psf.py /path/to/reference
 """
 
 import os
@@ -59,7 +59,9 @@ def build_integrands(ref_dir, work):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    ref_dir = sys.argv[1]
     work = tempfile.mkdtemp(prefix="flf_psf_golden_")
     build_integrands(ref_dir, work)
     h5 = types.ModuleType("h5py")

@@ -1,11 +1,11 @@
 """Generate tests/golden/rectify_vectors.npz by running the reference's RectifyImage.
 
-Runs in a container that holds the reference sources at /root/reference (the GPU
-machines never read them); tifffile, which RectifyImage does not call, is replaced
+Runs in a container that holds the reference sources, whose folder is the one
+argument (the GPU machines never read them); tifffile, which RectifyImage does not call, is replaced
 by an empty stand-in.  Inputs are regenerated from the seeds in rectify_inputs.py;
 only the outputs are stored.
 
-Usage:  python tests/golden/make_golden_rectify.py [/path/to/reference]
+Usage:  python tests/golden/make_golden_rectify.py /path/to/reference
 """
 
 import os
@@ -20,7 +20,9 @@ from rectify_inputs import RECTIFY_CASES, rectify_input  # noqa: E402
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    ref_dir = sys.argv[1]
     sys.modules.setdefault("tifffile", types.ModuleType("tifffile"))
     sys.path.insert(0, ref_dir)
     import rectify
