@@ -1,16 +1,27 @@
-"""Benchmark: Richardson-Lucy light-field deconvolution volumes/s on one GB300.
+"""Benchmark: learned warm start + Richardson-Lucy light-field deconvolution on one GB300.
 
-Workload (default "fullfield"): Nnum 15, 67 x 67 lenslets (1005 x 1005 px),
-41 z planes at -100..+100 um (step 5), one frame; synthetic seeded inputs
-(2000 Gaussian beads + 50 random-walk filaments, forward projected, +100
-background, Poisson noise) and a synthetic PSF set with the shapes of that
-optical configuration.  One step = one deconvolved volume at the accuracy of
-8 plain-RL iterations: back projection Htf of the image, a uniform start
-volume, 8 Prevedel RL iterations (the reference's default update).
+Default workload ("warmstart", the metric's configuration): Nnum 15, 30 x 30
+lenslets (450 x 450 px), 21 z planes at -50..50 um, PSF generated on the GPU
+for M40 / NA 0.95 / 150 um lenslets / f_ml 3000 um / 520 nm.  A 3-D U-Net is
+trained on the GPU on synthetic bead + filament volumes (forward projected,
++100 background, Poisson noise); 256 held-out volumes decide how many RL
+iterations after the network reach the data-fit residual of 8 plain-RL
+iterations from a uniform volume.  One step = one deconvolved volume at that
+accuracy: back projection Htf, the network's start volume, those RL
+iterations.  ``value`` is that arm's volumes/s; the plain-RL arm (Htf, uniform
+start, 8 Prevedel iterations), both arms' errors against the ground truth, the
+roofline of the multiply-accumulate kernel, the FP32-vs-FP64 error (committed
+FP64-oracle fixture) and the reference's own C++/FFTW CPU path on the same
+geometry are reported in the same JSON line.
 
-Prints one JSON line (rank 0).  ``--impl reference`` times the reference's
-CPU algorithm (the oracle port, numpy/scipy on all host cores) on bounded
-samples of the same workload instead.
+Other workloads (``--workload``): "small" (plain RL, 450 x 450, 11 planes),
+"fullfield" (plain RL, 1005 x 1005, 41 planes), "timeseries" (mixed-size
+frames), "psf", "rectify", "conv16" / "unet" (network kernels alone),
+"warmstart_fullfield".
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the reference's own
+C++/FFTW CPU path (Projector_allC + DeconvRL, built from the reference's
+sources by oracle/ref_build.py) on the workload's geometry with all host cores.
 """
 
 import argparse
@@ -41,8 +52,10 @@ UNIT = "volumes/s"
 WORKLOADS = {
     # name: (Nnum, lenslets, z_min, z_max, z_step, psf size ref (lenslets at z_max), beads, filaments)
     "fullfield": dict(Nnum=15, lenslets=67, z=(-100, 100, 5), img_size_ref=28, beads=2000, filaments=50,
+                      fp64_case="1005px_41planes",
                       label="full-field 1005x1005 px, Nnum 15, 41 planes -100..100 um, plain RL"),
     "small": dict(Nnum=15, lenslets=30, z=(-25, 25, 5), img_size_ref=7, beads=200, filaments=0,
+                  fp64_case="450px_11planes",
                   label="450x450 px, Nnum 15, 11 planes -25..25 um, plain RL"),
     # GPU PSF generation for the optics of the 450 x 450 workload (M40 / NA 0.95 water, 150 um
     # lenslets, f_ml 3000 um, 520 nm, OSR 3)
@@ -51,9 +64,13 @@ WORKLOADS = {
                 label="PSF generation, Nnum 15, M40 NA 0.95, OSR 3, 11 planes -25..25 um"),
     # learned warm start (450 x 450 px, Nnum 15, 21 planes at -50..50 um, PSF generated on the GPU for
     # the M40 / NA 0.95 optics); 200 beads per volume, background 100, Poisson noise
-    "warmstart": dict(Nnum=15, lenslets=30, z=(-50, 50, 5), beads=200,
+    # (img_size_ref 14: the PSF sizes, 61..421, the generator derives for these optics; the reference CPU
+    # arm uses a synthetic set of those sizes)
+    "warmstart": dict(Nnum=15, lenslets=30, z=(-50, 50, 5), beads=200, filaments=10, img_size_ref=14,
                       optics=dict(M=40, NA=0.95, MLPitch=150e-6, OSR=3, n=1.33, fml=3000e-6, lam=520e-9),
-                      label="learned warm start + RL vs plain RL(8 it), 450x450 px, Nnum 15, 21 planes -50..50 um"),
+                      fp64_case="450px_21planes",
+                      label="learned warm start + RL vs plain RL(8 it): 450x450 px (30x30 lenslets), Nnum 15, "
+                            "21 planes -50..50 um, bead + filament volumes, 256 held-out seeds"),
     # the learned warm start on the full-field workload (synthetic PSF of the default workload)
     "warmstart_fullfield": dict(Nnum=15, lenslets=67, z=(-100, 100, 5), img_size_ref=28, beads=2000, filaments=50,
                                 psf="synthetic",
@@ -78,7 +95,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fullfield", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="warmstart", choices=sorted(WORKLOADS))
     ap.add_argument("--iters", type=int, default=8)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
@@ -91,7 +108,6 @@ def parse():
                     help="warm-start fine-tuning steps on the data-fit residual (whole volumes)")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-planes", type=int, default=5)
     ap.add_argument("--shape", type=int, nargs=3, default=[24, 456, 456], metavar=("Z", "Y", "X"),
                     help="volume of the conv16 / unet network workloads")
     ap.add_argument("--kernel", default="tcgen05-all",
@@ -186,114 +202,194 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(hm, H, Ht, z, Y, X, N, iters, nplanes_sample, cores):
-    """Reference CPU algorithm (oracle port) on a bounded sample, extrapolated to one volume."""
-    from oracle import lf_oracle as O
-    rng = np.random.default_rng(7)
-    img = rng.random((1, Y, X)).astype(np.float32)
+def survey_psf_bytes(N, Y, X, hs):
+    """Compulsory PSF-spectrum bytes of one projection: sum over planes of
+    K * F_z * (F_z / 2 + 1) * 8, K = n_h (n_h + 1) / 2 stored PSFs per plane,
+    F_z = Nnum * ceil((max(Y, X) + h_z - 1) / Nnum) (the reference's GPU padding)."""
+    nh = (N + 1) // 2
+    K = nh * (nh + 1) // 2
+    tot = 0
+    for h in hs:
+        F = N * (-(-(max(Y, X) + h - 1) // N))
+        tot += K * F * (F // 2 + 1) * 8
+    return float(tot)
+
+
+def mac_roofline(prof, survey_bytes, what):
+    """Roofline of k_mac from a per-kernel profile pass: achieved = the compulsory
+    PSF-spectrum bytes of the projections profiled (survey_psf_bytes) over the
+    kernel's total CUDA-event time, against the measured HBM copy peak; the
+    kernel's own streamed bytes and their fraction beside it."""
+    peak, peak_kind = measured_peaks()
+    mac = {k: v for k, v in prof.items() if k.startswith("k_mac")}
+    tot_ms = sum(v["ms"] for v in mac.values())
+    own = sum(v["bytes"] for v in mac.values())
+    n = max(1, sum(v["launches"] for v in mac.values()))
+    ach = survey_bytes / (tot_ms / 1000.0) / 1e9 if tot_ms > 0 else 0.0
+    own_ach = own / (tot_ms / 1000.0) / 1e9 if tot_ms > 0 else 0.0
+    tot_all = sum(w["ms"] for w in prof.values()) or 1.0
+    return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
+            "traffic": round(own / n * MAC_TRAFFIC_RATIO),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_mac launch, as a ratio to "
+                              "the kernel's own streamed bytes (%.3f), times this run's own bytes per launch"
+                              % MAC_TRAFFIC_RATIO,
+            "kernel": "k_mac_fwd+k_mac_bwd", "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "launches": n, "avg_launch_ms": tot_ms / n,
+            "algorithmic_bytes_per_launch": survey_bytes / n,
+            "algorithmic_bytes": "sum over planes of K F_z (F_z/2+1) 8 B per projection, K = 36 stored PSFs, "
+                                 "F_z = Nnum ceil((Y + h_z - 1) / Nnum); %s" % what,
+            "own_bytes_per_launch": own / n, "own_achieved": round(own_ach, 1),
+            "own_frac": round(own_ach / peak, 4),
+            "kernel_share": {k: round(v["ms"] / tot_all, 4) for k, v in prof.items()}}
+
+
+def reference_geometry(wl):
+    """(Nnum, z planes, PSF sizes, Y, X) of a projection workload."""
+    import synthetic
+    N = wl["Nnum"]
+    z0, z1, dz = wl["z"]
+    z = np.arange(z0, z1 + dz / 2, dz)
+    hs = synthetic.psf_sizes(N, z, wl["img_size_ref"])
+    return N, z, hs, wl["lenslets"] * N, wl["lenslets"] * N
+
+
+# Reference CPU arm: one step is one RL iteration (forward + back projection +
+# update) where that takes seconds on the host, one back projection on the
+# larger workloads.
+REF_STEP = {"warmstart": "iteration", "small": "iteration", "fullfield": "projection",
+            "warmstart_fullfield": "projection"}
+
+
+def reference_line(workload, steps, warmup, iters, n_gpus):
+    """Time the reference's own C++/FFTW CPU path (Projector_allC + DeconvRL, built
+    from the reference's sources by oracle/ref_build.py) on the workload's geometry,
+    with all host cores.  The PSF values are a synthetic set with the workload's PSF
+    sizes (the work depends only on the shapes).  Falls back to the oracle's numpy
+    restatement of the same algorithm ("port") when the reference cannot be built."""
+    import shutil
+    import tempfile
+    import synthetic
+    wl = WORKLOADS[workload]
+    N, z, hs, Y, X = reference_geometry(wl)
     Z = len(z)
-    # sample planes spanning the PSF sizes (evenly spaced in support size),
-    # repeated until the sample holds about 10 s of CPU work
-    hs = np.array([h.shape[-1] for h in Ht])
-    order = np.argsort(hs)
-    k = max(2, min(nplanes_sample, len(order)))
-    picks = sorted(set(int(order[int(round(i * (len(order) - 1) / (k - 1)))]) for i in range(k)))
-    times = {zi: [] for zi in picks}
-    t_all = time.time()
-    while True:
-        for zi in picks:
-            t0 = time.time()
-            O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
-            times[zi].append(time.time() - t0)
-        if time.time() - t_all > 10.0 or len(times[picks[0]]) >= 5:
-            break
-    sample_s = time.time() - t_all
-    times = {zi: float(np.median(v)) for zi, v in times.items()}
-    # cost per plane ~ F_z * RX_z (the spectral multiply-accumulate and FFT sizes)
-
-    def cost(zi):
-        (FY, FX), _ = O.convolution_shape((Y, X), (hs[zi], hs[zi]), N, True)
-        return FY * (FX // 2 + 1)
-
-    xs = np.array([cost(p) for p in picks], dtype=np.float64)
-    ys = np.array([times[p] for p in picks])
-    if len(picks) >= 2 and xs.max() > xs.min():
-        a, b = np.polyfit(xs, ys, 1)
-    else:
-        a, b = ys[0] / xs[0], 0.0
-    per_projection = float(sum(max(a * cost(zi) + b, 0.0) for zi in range(Z)))
-    projections = 1 + 2 * iters
-    vol_s = per_projection * projections
-    return {
-        "value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": "port",
-        "sample": "back projections of planes %s (PSF sizes %s) of the workload on %d threads, %.1f s in total; "
-                  "one volume = %d projections x %d planes, extrapolated linearly in the per-plane "
-                  "spectrum size" % (picks, [int(hs[p]) for p in picks], cores, sample_s, projections, Z),
-        "seconds_per_volume": vol_s,
-    }
-
-
-def reference_steps(Ht, z, Y, X, N, iters, cores, warmup, steps):
-    """Each step back-projects one sample plane (cycling largest / smallest / middle PSF);
-    the timed samples fit the per-plane cost model that extrapolates one volume."""
-    from oracle import lf_oracle as O
-    rng = np.random.default_rng(7)
-    img = rng.random((1, Y, X)).astype(np.float32)
-    hs = np.array([h.shape[-1] for h in Ht])
-    order = np.argsort(hs)
-    cycle = [int(order[-1]), int(order[0]), int(order[len(order) // 2])]
-
-    def cost(zi):
-        (FY, FX), _ = O.convolution_shape((Y, X), (hs[zi], hs[zi]), N, True)
-        return FY * (FX // 2 + 1)
-
-    xs, ys = [], []
-    t_all = time.time()
-    for i in range(warmup + steps):
-        zi = cycle[i % len(cycle)]
+    cores = os.cpu_count() or 1
+    H, Ht = synthetic.synthetic_psf(N, z, wl["img_size_ref"])
+    img = synthetic.poisson_image(np.full((1, Y, X), 50.0, np.float32), 100.0, seed=3)
+    kind, why = "reference", None
+    try:
+        from oracle import ref_build
         t0 = time.time()
-        O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores)
-        dt = time.time() - t0
-        if i >= warmup:
-            xs.append(cost(zi))
-            ys.append(dt)
-    xs, ys = np.array(xs, float), np.array(ys, float)
-    if len(set(xs)) >= 2:
-        a, b = np.polyfit(xs, ys, 1)
+        rprojector, rlfdeconv, rpsfmatrix, _ = ref_build.load()
+        build_s = time.time() - t0
+    except Exception as e:          # no C++ toolchain result: the numpy restatement
+        kind, why, build_s = "port", "%s: %s" % (type(e).__name__, e), 0.0
+    step_kind = REF_STEP[workload]
+    cwd = os.getcwd()
+    tmp = tempfile.mkdtemp(prefix="flf_ref_")
+    os.chdir(tmp)       # the reference writes overall.txt / mutex_report_static.txt into the working directory
+    noprog = lambda w, desc=None, leave=True, **k: w   # noqa: E731
+    try:
+        if kind == "reference":
+            shapes = []
+            for zi, (h, ht) in enumerate(zip(H, Ht)):
+                for nm, arr in (("H", h), ("Ht", ht)):
+                    m = np.memmap(os.path.join(tmp, "%s%02d.array" % (nm, zi)), dtype="float32", mode="w+",
+                                  shape=arr.shape)
+                    m[...] = arr
+                    m.flush()
+                    del m
+                shapes.append(h.shape)
+            hm = rpsfmatrix.HMatrix(os.path.join(tmp, "H{z:02d}.array"), os.path.join(tmp, "Ht{z:02d}.array"), shapes)
+            proj = rprojector.Projector_allC()
+
+            def backward():
+                return proj.BackwardProjectACC(hm, img, range(Z), noprog, False, cores)
+
+            def iteration(htf, x):
+                return rlfdeconv.DeconvRL(hm, htf, 1, x, logPrint=False, numjobs=cores, projector=proj,
+                                          progress=noprog)
+            impl = "reference C++/FFTW path (Projector_allC, DeconvRL), built from the reference's sources"
+        else:
+            from oracle import lf_oracle as O
+
+            def backward():
+                return np.stack([O.project_plane_ref_cpu(img, Ht[zi], N, workers=cores) for zi in range(Z)])
+
+            def iteration(htf, x):
+                hx = sum(O.project_plane_ref_cpu(x[zi], H[zi], N, workers=cores) for zi in range(Z))
+                bp = np.stack([O.project_plane_ref_cpu(hx, Ht[zi], N, workers=cores) for zi in range(Z)])
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    x = x * (htf / bp)
+                x[np.isnan(x)] = 0
+                return x
+            impl = "oracle numpy restatement of the reference's CPU algorithm (%s)" % why
+        t0 = time.time()
+        htf = backward()                     # first call: FFTW planning, memmaps paged in
+        first_s = time.time() - t0
+        t0 = time.time()
+        htf = backward()
+        t_bwd = time.time() - t0
+        x = np.ones_like(htf)
+        times = []
+        for i in range(warmup + steps):
+            t0 = time.time()
+            if step_kind == "iteration":
+                x = iteration(htf, x)
+            else:
+                backward()
+            if i >= warmup:
+                times.append(time.time() - t0)
+    finally:
+        os.chdir(cwd)
+        shutil.rmtree(tmp, ignore_errors=True)
+    t_step = float(np.mean(times))
+    if step_kind == "iteration":
+        vol_s = t_bwd + iters * t_step
+        sample = ("%d timed RL iterations (each a forward and a back projection of all %d planes and the update) "
+                  "after %d warm-up iterations; one volume = back projection %.2f s + %d iterations" %
+                  (steps, Z, warmup, t_bwd, iters))
     else:
-        a, b = float(np.mean(ys / xs)), 0.0
-    per_projection = float(sum(max(a * cost(zi) + b, 0.0) for zi in range(len(z))))
-    vol_s = per_projection * (1 + 2 * iters)
-    return {"value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d timed single-plane back projections (PSF sizes %s) on %d threads, %.1f s total; "
-                      "one volume = %d projections x %d planes, extrapolated linearly in the per-plane "
-                      "spectrum size" % (steps, sorted(set(int(hs[c]) for c in cycle)), cores,
-                                         time.time() - t_all, 1 + 2 * iters, len(z)),
-            "seconds_per_volume": vol_s}
+        vol_s = (1 + 2 * iters) * t_step
+        sample = ("%d timed back projections of all %d planes after %d warm-up; one volume = %d projections "
+                  "(a forward projection streams the same spectra)" % (steps, Z, warmup, 1 + 2 * iters))
+    return {"impl": "reference", "metric": METRIC if workload == "warmstart" else
+            "volumes/s to plain-RL(8 it) accuracy, CPU", "value": 1.0 / vol_s, "unit": UNIT,
+            "n_gpus": n_gpus, "steps": steps, "warmup": warmup, "ms_per_step": t_step * 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "psf_sizes": hs,
+                       "rl_iterations": iters, "frames": 1, "implementation": impl,
+                       "step": step_kind, "first_call_s": round(first_s, 2), "build_or_load_s": round(build_s, 1)},
+            "rl_iterations_per_s": iters / vol_s,
+            "cpu_baseline": {"value": 1.0 / vol_s, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                             "seconds_per_volume": vol_s},
+            "e2e": {"value": 1.0 / vol_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def cpu_baseline_subprocess(workload, iters, steps=2, warmup=1, timeout=900):
+    """The reference CPU arm on a bounded sample, in a separate process (the
+    reference's modules share names with this package's); None if it fails."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
+           "--steps", str(steps), "--warmup", str(warmup), "--iters", str(iters)]
+    try:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=timeout,
+                           cwd=ROOT)
+        line = json.loads(r.stdout.strip().splitlines()[-1])
+        cb = dict(line["cpu_baseline"])
+        cb["implementation"] = line["config"]["implementation"]
+        return cb
+    except Exception as e:
+        return {"value": None, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": None,
+                "sample": "reference CPU arm failed: %s" % (str(e)[:200])}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload in ("timeseries", "rectify", "psf", "warmstart", "warmstart_fullfield", "conv16", "unet"):
+    if args.workload not in REF_STEP:
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm is timed on the projection "
                           "workloads; this workload reports its CPU oracle inside the GB300 line"}), flush=True)
         return
-    wl = WORKLOADS[args.workload]
-    N = wl["Nnum"]
-    hm, H, Ht, z, gt, Y, X = build_problem(wl)
-    cores = os.cpu_count() or 1
-    cb = reference_steps(Ht, z, Y, X, N, args.iters, cores, args.warmup, args.steps)
-    v = cb["value"]
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": wl["label"], "rl_iterations": args.iters, "frames": 1,
-                       "implementation": "reference CPU algorithm, numpy/scipy port (oracle)"},
-            "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(reference_line(args.workload, args.steps, args.warmup, args.iters, args.gpus)), flush=True)
 
 
 def run_gb300(args, rank, world, local):
@@ -393,22 +489,9 @@ def run_gb300(args, rank, world, local):
                "d2h_bytes_per_step": int(r.nbytes), "ms_per_step": e2e_s * 1000.0}
 
     # roofline of the dominant kernel (the spectral multiply-accumulate)
-    peak, peak_kind = measured_peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    mac = {k: v for k, v in prof.items() if k.startswith("k_mac")}
-    tot_ms = sum(v["ms"] for v in mac.values())
-    tot_bytes = sum(v["bytes"] for v in mac.values())
-    n_mac = sum(v["launches"] for v in mac.values())
-    achieved = tot_bytes / (tot_ms / 1000.0) / 1e9 if tot_ms > 0 else 0.0
-    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": round(tot_bytes / max(n_mac, 1) * MAC_TRAFFIC_RATIO),
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, as a ratio to the "
-                              "algorithmic bytes (%.3f), times this run's algorithmic bytes per launch"
-                              % MAC_TRAFFIC_RATIO,
-            "kernel": "k_mac_fwd+k_mac_bwd",
-            "peak_source": peak_kind, "launches": n_mac,
-            "bytes_per_launch": tot_bytes / max(n_mac, 1), "avg_launch_ms": tot_ms / max(n_mac, 1),
-            "kernel_share": {k: round(v["ms"] / sum(w["ms"] for w in prof.values()), 4) for k, v in prof.items()}}
+    hs = [int(hm.PSFShape(c)[-1]) for c in range(Z)]
+    roof = mac_roofline(prof, survey_psf_bytes(N, Y, X, hs) * args.steps * (1 + 2 * args.iters),
+                        "%s, %d projections per step" % (wl["label"], 1 + 2 * args.iters))
     launches = sum(v["launches"] for v in prof.values()) // args.steps
 
     # accuracy of the volume the timed step produced (outside the timed region):
@@ -427,10 +510,12 @@ def run_gb300(args, rank, world, local):
                 "truth_rel_l2_scaled": float(torch.linalg.vector_norm(scale * x64 - g64) / torch.linalg.vector_norm(g64)),
                 "reductions": "f64"}
     del hx, y64, x64, g64
+    if wl.get("fp64_case") and keep is None:
+        accuracy["fp64"] = fp64_accuracy(wl["fp64_case"], local)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_baseline(hm, H, Ht, z, Y, X, N, args.iters, args.cpu_sample_planes, os.cpu_count() or 1)
+        cb = cpu_baseline_subprocess(args.workload, args.iters)
 
     if rank == 0:
         gb = ctx.memory_usage() / 1e9
@@ -445,7 +530,8 @@ def run_gb300(args, rank, world, local):
                            "precompute_fp64": geo["fp64"], "device_gb": round(gb, 2),
                            "setup_s": round(setup_s, 1),
                            "l2": "inputs larger than L2: %.1f GB of transfer matrices streamed per "
-                                 "projection, %.0f MB volume" % (tot_bytes / args.steps / (1 + 2 * args.iters) / 1e9,
+                                 "projection, %.0f MB volume" % (roof["own_bytes_per_launch"] * roof["launches"]
+                                                                / args.steps / (1 + 2 * args.iters) / 1e9,
                                                                 Z * T * Y * X * 4 / 1e6),
                            "parallelism": "replicas" if world > 1 else "single",
                            "rl_launch": "direct" if graph is None else
@@ -497,11 +583,12 @@ def run_timeseries(args):
                         rng.uniform(0, X - 1, wl["beads"])], axis=1)
         amp = rng.uniform(500.0, 1000.0, wl["beads"])
         gt = torch.zeros((T, Z, Y, X), device=dev)
+        acc = torch.empty(Z * Y * X, dtype=torch.int64, device=dev)
         for t in range(T):
             if t:
                 pos = pos + rng.normal(0.0, 0.5, pos.shape)
             pts = torch.as_tensor(np.concatenate([pos, amp[:, None]], axis=1).astype(np.float32), device=dev)
-            _flf.render_blobs(gt[t], pts, 1.0, s.cuda_stream)
+            _flf.render_blobs(gt[t], pts, 1.0, s.cuda_stream, acc=acc)
         gt = gt.permute(1, 0, 2, 3).contiguous()
         clean = p.ForwardProjectACC(hm, gt, None)
         img = torch.poisson((clean.double() + 100.0).clamp_min(0)).float()
@@ -687,10 +774,51 @@ def run_psf(args):
     print(json.dumps(line), flush=True)
 
 
+def fp64_accuracy(case, p_dev=0):
+    """FP32 GPU Htf and Prevedel RL against the committed FP64-oracle fixture of a
+    case (tests/golden/fp64_<case>.npz; same inputs regenerated from
+    tests/golden/fp64_inputs.py): largest sampled error over the FP64 maximum and
+    sampled relative L2 error.  None when the fixture is absent."""
+    import torch
+    import _flf
+    import psfmatrix
+    import projector
+    gold = os.path.join(ROOT, "tests", "golden")
+    if not os.path.exists(os.path.join(gold, "fp64_%s.npz" % case)):
+        return None
+    if gold not in sys.path:
+        sys.path.insert(0, gold)
+    import fp64_inputs as F
+    c = F.CASES[case]
+    H, Ht = F.psf(case)
+    p = projector.Projector_gb300(device=p_dev)
+    ctx = p.context(psfmatrix.HMatrixArrays(H, Ht))
+    Z, Y, X = len(H), c["Y"], c["X"]
+    dev = torch.device("cuda", p_dev)
+    img = torch.as_tensor(F.image(case), device=dev)
+    htf = torch.empty((Z, 1, Y, X), device=dev)
+    s = torch.cuda.current_stream(dev).cuda_stream
+    ctx.backward(img, htf, 1, Y, X, None, stream=s)
+    x = torch.ones_like(htf)
+    ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, c["iters"], 1, Y, X, stream=s)
+    ctx.synchronize(s)
+    e = F.compare(case, htf[:, 0].cpu().numpy(), x[:, 0].cpu().numpy())
+    ctx.close()
+    del p, htf, x
+    torch.cuda.empty_cache()
+    e.update({"case": case, "rl_iterations": int(c["iters"]), "checked_planes": F.checked_planes(case),
+              "samples": F.SAMPLES, "psf": "synthetic set with the configuration's PSF sizes",
+              "oracle": "float64 restatement of the reference's CPU algorithm (tests/golden/make_fp64_fixtures.py)"})
+    return e
+
+
 def run_warmstart(args):
     """Volumes/s to the data-fit residual of 8 plain-RL iterations: plain RL from a
     uniform volume against the learned warm start plus as many RL iterations as the
-    held-out volumes need (the largest over them)."""
+    held-out volumes need (the largest over them).  ``value`` is the warm-start arm;
+    the plain-RL arm, both arms' errors against the ground-truth volumes, the k_mac
+    roofline, the network convolution's tensor roofline, the FP32-vs-FP64 error and
+    the reference's CPU path are reported beside it."""
     import warnings
     import torch
     import build_lib
@@ -698,10 +826,13 @@ def run_warmstart(args):
     import psfmatrix
     import projector
     import warmstart
+    import _flf
     build_lib.build()
     warnings.simplefilter("ignore")
     wl = WORKLOADS[args.workload]
     z0, z1, dz = wl["z"]
+    # the reference's CPU path first, in its own process, before this one holds the GPU busy
+    cb = None if args.no_cpu_baseline else cpu_baseline_subprocess(args.workload, 8)
     t0 = time.time()
     if wl.get("psf") == "synthetic":
         hm = build_problem(wl)[0]
@@ -712,12 +843,14 @@ def run_warmstart(args):
         hm = psfmatrix.HMatrixArrays(r["H"], r["Ht"], name="bench-warmstart")
         psf_desc = "generated on the GPU (generate_psf.py), sizes %s" % [int(h.shape[-1]) for h in r["H"]]
     psf_s = time.time() - t0
-    Y = X = wl["lenslets"] * wl["Nnum"]
+    N = wl["Nnum"]
+    Y = X = wl["lenslets"] * N
     Z = hm.numZ
+    hs = [int(hm.PSFShape(c)[-1]) for c in range(Z)]
     p = projector.Projector_gb300()
     ws = warmstart.WarmStart(p, hm, Y, X, beads=wl["beads"], filaments=wl.get("filaments", 0))
     refresh = 8 if Y * X * Z < 10_000_000 else 16
-    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=args.target_iters, log_every=100,
+    train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=args.target_iters, log_every=1,
                        refresh_every=refresh)
     tune_s = ws.finetune_residual(steps=args.tune_steps, log_every=50) if args.tune_steps > 0 else 0.0
     dev = ws.dev
@@ -733,29 +866,43 @@ def run_warmstart(args):
         d = (img.double() - hx.double()).reshape(T, -1)
         return (d.norm(dim=1) / img.double().reshape(T, -1).norm(dim=1)).cpu().numpy()
 
+    def truth_err(x, truth):
+        """Relative L2 error against the ground-truth volume after the best scale
+        (RL recovers a volume up to the PSF's normalisation), per frame."""
+        xs = x.double().permute(1, 0, 2, 3).reshape(x.shape[1], -1)
+        g = truth.double().permute(1, 0, 2, 3).reshape(truth.shape[1], -1)
+        a = (xs * g).sum(dim=1) / (xs * xs).sum(dim=1).clamp_min(1e-300)
+        return ((a[:, None] * xs - g).norm(dim=1) / g.norm(dim=1)).cpu().numpy()
+
     # held-out volumes in chunks that keep the network's activations small
     chunk = max(1, min(nseed, 40_000_000 // (Z * Y * X)))
-    r_plain, curves, need = [], [], []
+    r_plain, t_plain, curves, tcurves, need = [], [], [], [], []
     for c0 in range(0, nseed, chunk):
-        _, imgs, htfs = ws.make_batch(min(chunk, nseed - c0), rng)
+        truth, imgs, htfs = ws.make_batch(min(chunk, nseed - c0), rng)
         xu = torch.ones_like(htfs)
         p.RichardsonLucy(hm, xu, htfs, 8)
         rp = resid(xu, imgs)
+        t_plain.append(truth_err(xu, truth))
         x = ws.initial_volume(htfs)
         nd = np.full(len(rp), -1)
-        cv = []
+        cv, tv = [], []
         for k in range(0, 9):
             if k > 0:
                 p.RichardsonLucy(hm, x, htfs, 1)
             rk = resid(x, imgs)
             cv.append(rk)
+            tv.append(truth_err(x, truth))
             nd[(nd < 0) & (rk <= rp)] = k
         r_plain.append(rp)
         curves.append(np.stack(cv))
+        tcurves.append(np.stack(tv))
         need.append(nd)
-        del xu, x
+        del xu, x, truth
     r_plain = np.concatenate(r_plain)
-    curve = [float(v) for v in np.concatenate(curves, axis=1).mean(axis=1)]
+    t_plain = np.concatenate(t_plain)
+    curves = np.concatenate(curves, axis=1)
+    tcurves = np.concatenate(tcurves, axis=1)
+    curve = [float(v) for v in curves.mean(axis=1)]
     need = np.concatenate(need)
     k_warm = None if (need < 0).any() else int(need.max())
     img1 = imgs[:1].contiguous()
@@ -791,36 +938,103 @@ def run_warmstart(args):
     ms_warm = timed(warm_step) if k_warm is not None else None
     clk = clocks.stop()
     net_ms = timed(lambda: ws.initial_volume(htf1))
+
+    # kernel launches of one warm-start step: the projection kernels (launch
+    # counters of the context) and the network's kernels, with the RL iterations
+    # launched directly instead of from a graph
+    p.useGraphs = False
+    ctx.profile(False)
+    n0 = _flf.net_launches()
+    for _ in range(args.steps):
+        warm_step()
+    torch.cuda.synchronize()
+    launches_warm = (sum(v["launches"] for v in ctx.profile_read().values()) + _flf.net_launches() - n0) / args.steps
+    p.useGraphs = True
+
+    # per-kernel times of the plain-RL arm: the same steps with every kernel
+    # between CUDA events, on one stream (roofline of the multiply-accumulate)
+    ctx.set_option("streams", 1)
+    ctx.profile(True)
+    for _ in range(args.steps):
+        ctx.backward(img1, htf1, 1, Y, X, None, stream=s.cuda_stream)
+        xp.fill_(1.0)
+        ctx.rl_iterate(xp, htf1, None, _flf.FLF_RL_PREVEDEL, 8, 1, Y, X, stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    ctx.set_option("streams", 2)
+    roof = mac_roofline(prof, survey_psf_bytes(N, Y, X, hs) * args.steps * 17,
+                        "plain-RL arm, 17 projections per volume")
+
+    # the network's dominant convolution (16 -> 16 channels at full resolution)
+    # against the measured dense BF16 peak
+    Zp, Yp, Xp = ws.pad
+    g = torch.Generator(device=dev).manual_seed(0)
+    xa = torch.randn((1, Zp, Yp, Xp, 16), generator=g, device=dev).bfloat16()
+    wa = (torch.randn((27, 16, 16), generator=g, device=dev) / 20).bfloat16()
+    ba = torch.zeros(16, device=dev)
+    ya = torch.empty_like(xa)
+    conv_ms = timed(lambda: _flf.conv3d(xa, wa, ba, ya, relu=True, stream=s.cuda_stream))
+    _flf.net_status()
+    flop = 2.0 * Zp * Yp * Xp * 27 * 16 * 16
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak, bf16_kind = float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops)"
+    except Exception:
+        bf16_peak, bf16_kind = 1900.0, "fallback"
+    roof_net = {"bound": "tensor", "kernel": "k_conv3d_tma16 (16 -> 16 channels, tcgen05)", "unit": "TFLOP/s",
+                "achieved": round(flop / conv_ms / 1e9, 1), "peak": bf16_peak, "peak_source": bf16_kind,
+                "frac": round(flop / conv_ms / 1e9 / bf16_peak, 4), "avg_launch_ms": conv_ms,
+                "flop_per_launch": flop, "shape": [Zp, Yp, Xp, 16]}
+    del xa, ya
+
+    # end to end through the public API: host image in, host volume out
     img_h = img1.cpu().numpy()
     warmstart.DeconvRLWarm(ws, img_h, k_warm or 0)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     ne = 5
+    t0 = time.perf_counter()
     for _ in range(ne):
         out = warmstart.DeconvRLWarm(ws, img_h, k_warm or 0).cpu().numpy()
     e2e_s = (time.perf_counter() - t0) / ne
-    line = {"metric": "volumes/s to plain-RL(8 it) accuracy: learned warm-start vs plain RL, 1 GB300",
-            "value": 1000.0 / ms_warm if ms_warm else None, "unit": "volumes/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms_warm, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16 network (fp32 accumulation), f32 projections", "data": "synthetic",
-            "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": wl["Nnum"], "frames": 1,
-                       "psf": psf_desc,
+    fp64 = fp64_accuracy(wl["fp64_case"]) if wl.get("fp64_case") else None
+
+    losses = [l for _, l in ws.losses]
+    k_use = k_warm if k_warm is not None else 8
+    line = {"metric": METRIC,
+            "value": 1000.0 / ms_warm if ms_warm else 1000.0 / ms_plain, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_warm or ms_plain,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network (fp32 accumulation), f32 projections", "data": "synthetic",
+            "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "frames": 1,
+                       "psf": psf_desc, "beads": wl["beads"], "filaments": wl.get("filaments", 0),
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
                        "conv_kernels": "tcgen05 for the 16/32-channel layers, mma.sync for 64/128 channels",
-                       "target_iters": args.target_iters,
-                       "residual_finetune_steps": args.tune_steps, "finetune_s": round(tune_s, 1),
-                       "losses": [[round(float(v), 6) if isinstance(v, float) else v for v in l]
-                                  for l in ws.losses[-8:]],
+                       "target_iters": args.target_iters, "residual_finetune_steps": args.tune_steps,
+                       "finetune_s": round(tune_s, 1),
+                       "train_loss_mean_last_100": float(np.mean(losses[-100:])) if losses else None,
+                       "train_loss_mean_first_100": float(np.mean(losses[:100])) if losses else None,
                        "network_parameters": ws.net.num_parameters(), "held_out_volumes": nseed,
-                       "l2": "transfer matrices and volumes larger than L2"},
+                       "value_arm": "warm start" if ms_warm else "plain RL (the warm start missed the residual)",
+                       "device_gb": round(ctx.memory_usage() / 1e9, 2),
+                       "l2": "transfer matrices (%.2f GB per projection) and volumes larger than L2"
+                             % (roof["own_bytes_per_launch"] * roof["launches"] / args.steps / 17 / 1e9)},
             "plain_rl": {"volumes_per_s": 1000.0 / ms_plain, "ms_per_volume": ms_plain, "iterations": 8,
-                         "residual_rel_l2_mean": float(r_plain.mean())},
+                         "residual_rel_l2_mean": float(r_plain.mean()),
+                         "truth_rel_l2_scaled_mean": float(t_plain.mean())},
             "warm_start": {"rl_iterations_needed": k_warm, "network_ms": net_ms,
                            "residual_after_k_mean": [round(v, 5) for v in curve],
+                           "truth_rel_l2_scaled_mean_after_k": [round(float(v), 5) for v in tcurves.mean(axis=1)],
+                           "truth_rel_l2_scaled_mean": float(tcurves[k_use].mean()),
                            "speedup_vs_plain": (ms_plain / ms_warm) if ms_warm else None},
-            "e2e": {"value": 1.0 / e2e_s, "unit": "volumes/s", "h2d_bytes_per_step": int(img_h.nbytes),
-                    "d2h_bytes_per_step": int(out.nbytes)},
-            "clocks": clk}
+            "rl_iterations_per_s": 8 * 1000.0 / ms_plain,
+            "accuracy": {"fp64": fp64, "residual_rel_l2_plain8_mean": float(r_plain.mean()),
+                         "residual_rel_l2_warm_mean": float(curves[k_use].mean()), "reductions": "f64"},
+            "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(img_h.nbytes),
+                    "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": e2e_s * 1000.0,
+                    "path": "warmstart.DeconvRLWarm on a host image, volume copied back"},
+            "gpu_launches": int(round(launches_warm)), "roofline": roof, "roofline_network": roof_net,
+            "cpu_baseline": cb, "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

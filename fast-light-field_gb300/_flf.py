@@ -57,19 +57,20 @@ _SIGS = {
     "flf_psf_lf_bin": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
-    "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
     "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
     "flf_net_conv16_tcgen05": (_I, [_I]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
-    "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P]),
+    "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P, ctypes.c_longlong, _P]),
     "flf_pool2": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_pool2_bwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_up2_add": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_up2_bwd": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_mse_grad": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _I, _P]),
     "flf_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, _F, _F, _F, _F, _F, _F, _F, _P]),
-    "flf_render_blobs": (_I, [_P, _I, _I, _I, _P, _I, _F, _P]),
+    "flf_render_blobs": (_I, [_P, _I, _I, _I, _P, _I, _F, _P, _P]),
+    "flf_net_launches": (ctypes.c_longlong, []),
     "flf_ws_input": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _F, _F, _P]),
     "flf_ws_head": (_I, [_P, _P, _F, _F, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
 }
@@ -181,7 +182,7 @@ def _vshape(t):
 
 def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
     """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16;
-    ws: optional float32 workspace (at least B*Z*Y*X*Co elements) for split-K layers."""
+    ws: optional float32 workspace for split-K layers (one B*Z*Y*X*Co slice per split, at least two)."""
     lib = load_library()
     B, Z, Y, X, Ci = _vshape(x)
     Co = int(y.shape[-1])
@@ -215,17 +216,25 @@ def conv16_tcgen05(mode):
     return int(load_library().flf_net_conv16_tcgen05(int(mode)))
 
 
+def net_launches():
+    """Kernel launches made by the network entry points since the library was loaded."""
+    return int(load_library().flf_net_launches())
+
+
 def net_status():
     """Raise FlfError if a bounded wait in a tensor-core convolution gave up."""
     _check_global(load_library().flf_net_status())
 
 
-def conv3d_wgrad(x, dy, dw, stream=None):
-    """dw [27,Ci,Co] float32 += weight gradient of conv3d(x, .) for output gradient dy."""
+def conv3d_wgrad(x, dy, dw, stream=None, ws=None):
+    """dw [27,Ci,Co] float32 += weight gradient of conv3d(x, .) for output gradient dy.
+
+    ws: float32 workspace for the per-chunk partial gradients (27*Ci*Co floats per
+    chunk; more chunks spread the voxels over more CTAs), summed in a fixed order."""
     lib = load_library()
     B, Z, Y, X, Ci = _vshape(x)
     _check_global(lib.flf_conv3d_wgrad(_ptr(x), _ptr(dy), _ptr(dw), B, Z, Y, X, Ci, int(dy.shape[-1]),
-                                       _ptr(stream)))
+                                       _ptr(ws), int(ws.numel()) if ws is not None else 0, _ptr(stream)))
 
 
 def conv3d_flip(w, w2, stream=None):
@@ -233,10 +242,13 @@ def conv3d_flip(w, w2, stream=None):
     _check_global(lib.flf_conv3d_flip(_ptr(w), _ptr(w2), int(w.shape[1]), int(w.shape[2]), _ptr(stream)))
 
 
-def bias_grad(g, db, stream=None):
+def bias_grad(g, db, stream=None, ws=None):
+    """db [C] += sums of g [..., C] over all rows; ws: float32 workspace for the
+    per-block sums (C floats per block of 2048 rows), added in block order."""
     lib = load_library()
     C = int(g.shape[-1])
-    _check_global(lib.flf_bias_grad(_ptr(g), _ptr(db), int(g.numel() // C), C, _ptr(stream)))
+    _check_global(lib.flf_bias_grad(_ptr(g), _ptr(db), int(g.numel() // C), C, _ptr(ws),
+                                    int(ws.numel()) if ws is not None else 0, _ptr(stream)))
 
 
 def pool2(x, out, stream=None):
@@ -272,12 +284,17 @@ def adam(w, g, m, v, wb, lr, b1, b2, eps, c1, c2, wd, stream=None):
                                c2, wd, _ptr(stream)))
 
 
-def render_blobs(vol, pts, sigma, stream=None):
-    """vol [Z,Y,X] float32 += Gaussian blobs at pts [n,4] = (z, y, x, amplitude)."""
+def render_blobs(vol, pts, sigma, stream=None, acc=None):
+    """vol [Z,Y,X] float32 += Gaussian blobs at pts [n,4] = (z, y, x, amplitude).
+
+    acc: int64 scratch of Z*Y*X elements; with it the blob terms are summed as
+    fixed-point integers, so the volume is the same bits on every run."""
     lib = load_library()
     Z, Y, X = (int(v) for v in vol.shape)
+    if acc is not None and acc.numel() < Z * Y * X:
+        raise ValueError("render_blobs: acc needs %d elements" % (Z * Y * X))
     _check_global(lib.flf_render_blobs(_ptr(vol), Z, Y, X, _ptr(pts), int(pts.shape[0]), float(sigma),
-                                       _ptr(stream)))
+                                       _ptr(acc), _ptr(stream)))
 
 
 def ws_input(htf, hth1, ht1, sum_x1, out, c2, c3, stream=None):

@@ -1662,6 +1662,8 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
 
 int flf_net_conv16_tcgen05(int mode) { return net_set_conv16_tcgen05(mode); }
 
+long long flf_net_launches(void) { return net_launches(); }
+
 int flf_net_status(void) {
   const int v = net_status_read_and_clear();
   if (v < 0) return fail(nullptr, FLF_E_CUDA, "reading the network status flag failed");
@@ -1670,13 +1672,14 @@ int flf_net_status(void) {
 }
 
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
-                     void *stream) {
+                     float *ws, long long ws_elems, void *stream) {
   if (!x || !dy || !dw) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
   if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
   if (!aligned16(x) || !aligned16(dy)) return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
-  WgradParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)dy, dw, B, Z, Y, X, Ci, Co, 0};
-  NET_CHECK(launch_conv3d_wgrad(p, (cudaStream_t)stream, net_sms()));
+  if (ws && ws_elems < 0) return fail(nullptr, FLF_E_ARG, "negative workspace size");
+  WgradParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)dy, dw, B, Z, Y, X, Ci, Co, 0, ws};
+  NET_CHECK(launch_conv3d_wgrad(p, ws ? ws_elems : 0, (cudaStream_t)stream, net_sms()));
   return FLF_OK;
 }
 
@@ -1686,9 +1689,10 @@ int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream) {
   return FLF_OK;
 }
 
-int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream) {
-  if (!g || !db || M < 0 || C <= 0 || C > 128) return fail(nullptr, FLF_E_ARG, "invalid bias gradient arguments");
-  if (M > 0) NET_CHECK(launch_bias_grad(g, db, M, C, (cudaStream_t)stream));
+int flf_bias_grad(const void *g, float *db, long long M, int C, float *ws, long long ws_elems, void *stream) {
+  if (!g || !db || M < 0 || C <= 0 || C > 128 || (ws && ws_elems < 0))
+    return fail(nullptr, FLF_E_ARG, "invalid bias gradient arguments");
+  if (M > 0) NET_CHECK(launch_bias_grad(g, db, ws, ws ? ws_elems : 0, M, C, (cudaStream_t)stream));
   return FLF_OK;
 }
 
@@ -1740,11 +1744,13 @@ int flf_adam(float *w, const float *g, float *m, float *v, void *wb, long long n
   return FLF_OK;
 }
 
-int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *stream) {
+int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *acc,
+                     void *stream) {
   if (!vol || (!pts && npts > 0) || Z <= 0 || Y <= 0 || X <= 0 || npts < 0 || !(sigma > 0) || sigma > 8)
     return fail(nullptr, FLF_E_ARG, "invalid blob rendering arguments");
   if (!aligned16(pts)) return fail(nullptr, FLF_E_ARG, "blob array must be 16-byte aligned");
-  NET_CHECK(launch_render_blobs(vol, Z, Y, X, pts, npts, sigma, (cudaStream_t)stream));
+  if (acc && (reinterpret_cast<uintptr_t>(acc) & 7)) return fail(nullptr, FLF_E_ARG, "accumulator must be 8-byte aligned");
+  NET_CHECK(launch_render_blobs(vol, acc, Z, Y, X, pts, npts, sigma, (cudaStream_t)stream));
   return FLF_OK;
 }
 

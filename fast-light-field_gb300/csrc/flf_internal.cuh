@@ -258,7 +258,7 @@ struct ConvParams {          // y = act(conv3x3x3(x, w) + bias) (* (mask > 0))
   const __nv_bfloat16 *mask; // [M][Co] or null
   __nv_bfloat16 *y;          // [M][Co]
   int B, Z, Y, X, Ci, Co, relu;
-  float *ws;                 // [M][Co] FP32 partial sums when the K loop is split (splits > 1)
+  float *ws;                 // [splits][M][Co] FP32 partial sums when the K loop is split (splits > 1)
   int splits;
 };
 struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co]
@@ -267,15 +267,18 @@ struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co
   float *dw;
   int B, Z, Y, X, Ci, Co;
   long long chunk;           // voxels per CTA (set by the launcher)
+  float *part;               // [chunks][27][Ci][Co] partial gradients, reduced in chunk order (or null)
 };
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
-cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms);
+long long net_launches();
+cudaError_t launch_conv3d_wgrad(WgradParams p, long long ws_elems, cudaStream_t s, int num_sms);
 cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s);
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32);
 int net_set_conv16_tcgen05(int mode);
 int net_status_read_and_clear();
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s);
-cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s);
+cudaError_t launch_bias_grad(const void *g, float *db, float *ws, long long ws_elems, long long M, int C,
+                             cudaStream_t s);
 cudaError_t launch_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, cudaStream_t s);
 cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y,
                              int X, int C, cudaStream_t s);
@@ -287,7 +290,7 @@ cudaError_t launch_mse_grad(const void *y, const float *target, void *g, float *
                             cudaStream_t s);
 cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
                         float b2, float eps, float c1, float c2, float wd, cudaStream_t s);
-cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,
+cudaError_t launch_render_blobs(float *vol, void *acc, int Z, int Y, int X, const float *pts, int npts, float sigma,
                                 cudaStream_t s);
 struct WsInputParams {        // warm-start network input from Htf
   const float *htf;           // [Z][T][Y][X]

@@ -27,11 +27,23 @@
 //                     ReLU mask, MSE loss gradient, Adam, bead rendering.
 #include "flf_internal.cuh"
 
+#include <atomic>
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 namespace flf {
+
+// Kernel launches made by this file since the library was loaded (flf_net_launches).
+static std::atomic<long long> g_net_launches{0};
+#define FLF_NET_LAUNCH(...)  \
+  do {                       \
+    __VA_ARGS__;             \
+    ++g_net_launches;        \
+  } while (0)
+
+long long net_launches() { return g_net_launches.load(); }
 
 namespace {
 
@@ -167,7 +179,8 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
   }
   cp_wait<0>();
 
-  if (p.splits > 1) {   // partial sums of this CTA's K range
+  if (p.splits > 1) {   // partial sums of this CTA's K range, in its own slice of ws
+    float *slice = p.ws + (long long)blockIdx.z * M * p.Co;
 #pragma unroll
     for (int mt = 0; mt < 2; mt++)
 #pragma unroll
@@ -177,8 +190,7 @@ __global__ void __launch_bounds__(128) k_conv3d(ConvParams p) {
           const long long row = m0 + warp * 32 + mt * 16 + (lane >> 2) + 8 * h;
           if (row >= M) continue;
           const int col = n0 + nt * 8 + 2 * (lane & 3);
-          atomicAdd(reinterpret_cast<float2 *>(p.ws + row * p.Co + col),
-                    make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
+          *reinterpret_cast<float2 *>(slice + row * p.Co + col) = make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]);
         }
     return;
   }
@@ -1052,7 +1064,10 @@ __global__ void __launch_bounds__(352, 1)
 
 // Weight gradient.  CTA = (voxel chunk, tap) x (ci tile CM, co tile CN); the 4
 // warps take alternate k16 steps of its voxels (split-K) and are summed in
-// shared memory at the end, then added to dW with FP32 atomics.
+// shared memory at the end.  The tile goes to its chunk's slice of p.part,
+// and k_wgrad_reduce adds the chunks to dW in chunk order, so the gradient is
+// the same bits on every run; with one chunk (p.part null) the CTA adds its
+// tile to dW itself (one writer per element).
 template <int CM, int CN>
 __global__ void __launch_bounds__(128) k_conv3d_wgrad(WgradParams p) {
   constexpr int BK = 64, NS = 3, RA = CM / 8, RBc = CN / 8;
@@ -1157,9 +1172,21 @@ __global__ void __launch_bounds__(128) k_conv3d_wgrad(WgradParams p) {
     }
     __syncthreads();
   }
+  const long long nw = 27LL * p.Ci * p.Co;
   for (int i = tid; i < CM * CN; i += 128) {
     const int ci = i / CN, co = i - ci * CN;
-    atomicAdd(p.dw + ((long long)tap * p.Ci + ci0 + ci) * p.Co + co0 + co, red[i]);
+    const long long o = ((long long)tap * p.Ci + ci0 + ci) * p.Co + co0 + co;
+    if (p.part) p.part[chunk * nw + o] = red[i];
+    else p.dw[o] += red[i];
+  }
+}
+
+// dw[i] += sum over the chunks of part[chunk][i], in chunk order.
+__global__ void k_wgrad_reduce(const float *part, float *dw, long long n, int chunks) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int c = 0; c < chunks; c++) s += part[(long long)c * n + i];
+    dw[i] += s;
   }
 }
 
@@ -1174,15 +1201,26 @@ __global__ void k_conv3d_flip_weights(const bf16 *w, bf16 *w2, int Ci, int Co) {
   }
 }
 
-// db[c] += sum over rows of g[M][C]
-__global__ void k_bias_grad(const bf16 *g, float *db, long long M, int C, long long rows_per_block) {
+// Sums over rows of g[M][C], one row block per CTA: into part[block][c] (then
+// k_bias_reduce adds the blocks in order), or with a single block (part null)
+// straight into db[c].
+__global__ void k_bias_grad(const bf16 *g, float *db, float *part, long long M, int C, long long rows_per_block) {
   const int c = threadIdx.x;
   if (c >= C) return;
   const long long r0 = (long long)blockIdx.x * rows_per_block;
   const long long r1 = r0 + rows_per_block < M ? r0 + rows_per_block : M;
   float s = 0.f;
   for (long long r = r0; r < r1; r++) s += __bfloat162float(g[r * C + c]);
-  atomicAdd(db + c, s);
+  if (part) part[(long long)blockIdx.x * C + c] = s;
+  else db[c] += s;
+}
+
+__global__ void k_bias_reduce(const float *part, float *db, int blocks, int C) {
+  const int c = threadIdx.x;
+  if (c >= C) return;
+  float s = 0.f;
+  for (int b = 0; b < blocks; b++) s += part[(long long)b * C + c];
+  db[c] += s;
 }
 
 // Epilogue of a split convolution: y = act(ws + bias) (* (mask > 0)), 8 channels per thread.
@@ -1192,9 +1230,14 @@ __global__ void k_conv3d_finish(ConvParams p, long long M) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int c0 = (int)(i % G) * 8;
     const long long o = (i / G) * p.Co + c0;
-    const float4 a = *reinterpret_cast<const float4 *>(p.ws + o);
-    const float4 b = *reinterpret_cast<const float4 *>(p.ws + o + 4);
-    float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int sp = 0; sp < p.splits; sp++) {   // the K slices in order
+      const float *src = p.ws + (long long)sp * M * p.Co + o;
+      const float4 a = *reinterpret_cast<const float4 *>(src);
+      const float4 b = *reinterpret_cast<const float4 *>(src + 4);
+      v[0] += a.x; v[1] += a.y; v[2] += a.z; v[3] += a.w;
+      v[4] += b.x; v[5] += b.y; v[6] += b.z; v[7] += b.w;
+    }
     uint4 mk;
     if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + o);
     const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
@@ -1373,8 +1416,12 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, bf16 *wb, l
 }
 
 // Gaussian blobs: vol[z][y][x] += amp exp(-|p - c|^2 / (2 sigma^2)) within 3 sigma;
-// pts[k] = (z, y, x, amp), one warp per blob.
-__global__ void k_render_blobs(float *vol, int Z, int Y, int X, const float4 *pts, int npts, float sigma) {
+// pts[k] = (z, y, x, amp), one warp per blob.  With acc (an int64 per voxel,
+// zeroed) the terms are added as 32.32 fixed-point integers, whose sum does
+// not depend on the order the warps arrive in; k_blobs_add then adds the
+// totals to vol.  Without acc they go to vol through FP32 atomics.
+__global__ void k_render_blobs(float *vol, unsigned long long *acc, int Z, int Y, int X, const float4 *pts, int npts,
+                               float sigma) {
   const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (k >= npts) return;
   const float4 q = pts[k];
@@ -1386,13 +1433,23 @@ __global__ void k_render_blobs(float *vol, int Z, int Y, int X, const float4 *pt
     const int z = (int)floorf(q.x + 0.5f) + dz, y = (int)floorf(q.y + 0.5f) + dy, x = (int)floorf(q.z + 0.5f) + dx;
     if (z < 0 || z >= Z || y < 0 || y >= Y || x < 0 || x >= X) continue;
     const float d2 = (z - q.x) * (z - q.x) + (y - q.y) * (y - q.y) + (x - q.z) * (x - q.z);
-    atomicAdd(vol + ((long long)z * Y + y) * X + x, q.w * __expf(-d2 * inv));
+    const float v = q.w * __expf(-d2 * inv);
+    const long long o = ((long long)z * Y + y) * X + x;
+    if (acc) atomicAdd(acc + o, (unsigned long long)__double2ll_rn((double)v * 4294967296.0));
+    else atomicAdd(vol + o, v);
   }
 }
 
-// Frame sums of the first RL iterate Htf / HtH1 (Htf [Z][T][Y][X], HtH1 [Z][Y][X]).
-__global__ void __launch_bounds__(256) k_ws_sum(const float *htf, const float *hth1, float *sum, int T, long long V,
-                                                long long YX) {
+__global__ void k_blobs_add(float *vol, const unsigned long long *acc, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    vol[i] += (float)((double)(long long)acc[i] * (1.0 / 4294967296.0));
+}
+
+// Frame sums of the first RL iterate Htf / HtH1 (Htf [Z][T][Y][X], HtH1 [Z][Y][X]):
+// one partial per (block, frame) into part[t][block]; k_ws_sum_final adds them
+// in block order.
+__global__ void __launch_bounds__(256) k_ws_sum(const float *htf, const float *hth1, float *partial, int T,
+                                                long long V, long long YX) {
   __shared__ float red[8];
   const int t = blockIdx.y;
   float part = 0.f;
@@ -1406,8 +1463,16 @@ __global__ void __launch_bounds__(256) k_ws_sum(const float *htf, const float *h
   if (threadIdx.x == 0) {
     float b = 0.f;
     for (int w = 0; w < 8; w++) b += red[w];
-    atomicAdd(sum + t, b);
+    partial[(long long)t * gridDim.x + blockIdx.x] = b;
   }
+}
+
+__global__ void k_ws_sum_final(const float *part, float *sum, int T, int blocks) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  float s = 0.f;
+  for (int b = 0; b < blocks; b++) s += part[(long long)t * blocks + b];
+  sum[t] = s;
 }
 
 // Network input, channels-last [T][Zp][Yp][Xp][16] from Htf [Z][T][Y][X]:
@@ -1461,7 +1526,7 @@ static cudaError_t launch_tiled(const ConvParams &p, cudaStream_t s) {
   const int tiles_x = (p.X + 15) / 16, tiles_y = (p.Y + 7) / 8;
   const long long ntiles = (long long)p.B * p.Z * tiles_y * tiles_x;
   const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
-  k_conv3d_tiled<CI, CO><<<grid, 128, smem, s>>>(p, tiles_x, tiles_y, ntiles);
+  FLF_NET_LAUNCH(k_conv3d_tiled<CI, CO><<<grid, 128, smem, s>>>(p, tiles_x, tiles_y, ntiles));
   return cudaGetLastError();
 }
 
@@ -1482,7 +1547,7 @@ static cudaError_t launch_t16(const ConvParams &p, const HeadOut &h, cudaStream_
   const int tiles_x = (p.X + 15) / 16, tiles_y = (p.Y + 15) / 16;
   const long long ntiles = (long long)p.B * p.Z * tiles_y * tiles_x;
   const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
-  k_conv3d_t16<HEAD><<<grid, 128, smem, s>>>(p, h, tiles_x, tiles_y, ntiles);
+  FLF_NET_LAUNCH(k_conv3d_t16<HEAD><<<grid, 128, smem, s>>>(p, h, tiles_x, tiles_y, ntiles));
   return cudaGetLastError();
 }
 
@@ -1554,7 +1619,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   g.zchunks = (p.Z + g.zc - 1) / g.zc;
   g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
-  k_conv3d_tma16<CI, CO, R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g);
+  FLF_NET_LAUNCH(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g));
   return cudaGetLastError();
 }
 
@@ -1595,41 +1660,43 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  // few CTAs with long K loops (the coarse levels): split K over up to 3 waves
-  if (p.ws && ws_elems >= M * p.Co && ctas < 2LL * sms) {
+  // few CTAs with long K loops (the coarse levels): split K over up to 3 waves,
+  // each split writing its own [M][Co] slice of ws (as many as ws holds)
+  if (p.ws && ws_elems >= 2 * M * p.Co && ctas < 2LL * sms) {
     long long sp = (3LL * sms + ctas - 1) / ctas;
     if (sp > KT / 8) sp = KT / 8;
+    if (sp > ws_elems / (M * p.Co)) sp = ws_elems / (M * p.Co);
     if (sp > 1) p.splits = (int)sp;
   }
-  if (p.splits > 1) {
-    cudaError_t e = cudaMemsetAsync(p.ws, 0, sizeof(float) * M * p.Co, s);
-    if (e != cudaSuccess) return e;
-  }
   dim3 grid((unsigned)((M + 127) / 128), (unsigned)(p.Co / BN), (unsigned)p.splits);
-  if (BN == 64) k_conv3d<64><<<grid, 128, 0, s>>>(p);
-  else if (BN == 32) k_conv3d<32><<<grid, 128, 0, s>>>(p);
-  else k_conv3d<16><<<grid, 128, 0, s>>>(p);
-  if (p.splits > 1) k_conv3d_finish<<<grid_for(M * p.Co / 8, 256), 256, 0, s>>>(p, M);
+  if (BN == 64) FLF_NET_LAUNCH(k_conv3d<64><<<grid, 128, 0, s>>>(p));
+  else if (BN == 32) FLF_NET_LAUNCH(k_conv3d<32><<<grid, 128, 0, s>>>(p));
+  else FLF_NET_LAUNCH(k_conv3d<16><<<grid, 128, 0, s>>>(p));
+  if (p.splits > 1) FLF_NET_LAUNCH(k_conv3d_finish<<<grid_for(M * p.Co / 8, 256), 256, 0, s>>>(p, M));
   return cudaGetLastError();
 }
 
-cudaError_t launch_conv3d_wgrad(WgradParams p, cudaStream_t s, int num_sms) {
+cudaError_t launch_conv3d_wgrad(WgradParams p, long long ws_elems, cudaStream_t s, int num_sms) {
   const long long M = (long long)p.B * p.Z * p.Y * p.X;
   if (M == 0) return cudaSuccess;
   const int CM = p.Ci >= 32 ? 32 : 16, CN = p.Co >= 64 ? 64 : p.Co;
   const int tiles = (p.Ci / CM) * (p.Co / CN);
+  const long long nw = 27LL * p.Ci * p.Co;
   long long chunks = (4LL * num_sms + 27 * tiles - 1) / (27 * tiles);
+  if (p.part && chunks > ws_elems / nw) chunks = ws_elems / nw;   // partial tiles must fit the workspace
   if (chunks < 1) chunks = 1;
   long long per = (M + chunks - 1) / chunks;
   per = (per + 63) / 64 * 64;
   chunks = (M + per - 1) / per;
   p.chunk = per;
+  if (chunks == 1) p.part = nullptr;
   dim3 grid((unsigned)(chunks * 27), (unsigned)tiles);
-#define FLF_WG(a, b) else if (CM == a && CN == b) k_conv3d_wgrad<a, b><<<grid, 128, 0, s>>>(p);
+#define FLF_WG(a, b) else if (CM == a && CN == b) FLF_NET_LAUNCH(k_conv3d_wgrad<a, b><<<grid, 128, 0, s>>>(p));
   if (false) {
   }
   FLF_WG(16, 16) FLF_WG(16, 32) FLF_WG(16, 64) FLF_WG(32, 16) FLF_WG(32, 32) FLF_WG(32, 64)
 #undef FLF_WG
+  if (p.part) FLF_NET_LAUNCH(k_wgrad_reduce<<<grid_for(nw, 256), 256, 0, s>>>(p.part, p.dw, nw, (int)chunks));
   return cudaGetLastError();
 }
 
@@ -1662,7 +1729,7 @@ static cudaError_t launch_tc16_rows(const ConvParams &p, cudaStream_t s) {
   const int tiles_x = (p.X + 127) / 128;
   const long long ntiles = (long long)p.B * p.Z * ((p.Y + ROWS - 1) / ROWS) * tiles_x;
   const unsigned grid = (unsigned)(ntiles < grid_cap ? ntiles : grid_cap);
-  k_conv3d_tc16<ROWS, NBUF><<<grid, 128, smem, s>>>(p, tiles_x, ntiles);
+  FLF_NET_LAUNCH(k_conv3d_tc16<ROWS, NBUF><<<grid, 128, smem, s>>>(p, tiles_x, ntiles));
   return cudaGetLastError();
 }
 
@@ -1682,65 +1749,74 @@ int net_status_read_and_clear() {
 }
 
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s) {
-  k_conv3d_flip_weights<<<grid_for(27LL * Ci * Co, 256), 256, 0, s>>>((const bf16 *)w, (bf16 *)w2, Ci, Co);
+  FLF_NET_LAUNCH(k_conv3d_flip_weights<<<grid_for(27LL * Ci * Co, 256), 256, 0, s>>>((const bf16 *)w, (bf16 *)w2, Ci, Co));
   return cudaGetLastError();
 }
 
-cudaError_t launch_bias_grad(const void *g, float *db, long long M, int C, cudaStream_t s) {
-  const long long rows = 2048;
-  k_bias_grad<<<(unsigned)((M + rows - 1) / rows), 128, 0, s>>>((const bf16 *)g, db, M, C, rows);
+cudaError_t launch_bias_grad(const void *g, float *db, float *ws, long long ws_elems, long long M, int C,
+                             cudaStream_t s) {
+  long long blocks = (M + 2047) / 2048;
+  if (!ws || blocks > ws_elems / C) blocks = ws ? ws_elems / C : 1;
+  if (blocks > 65535) blocks = 65535;
+  if (blocks < 1) blocks = 1;
+  const long long rows = (M + blocks - 1) / blocks;
+  blocks = (M + rows - 1) / rows;
+  float *part = blocks > 1 ? ws : nullptr;
+  FLF_NET_LAUNCH(k_bias_grad<<<(unsigned)blocks, 128, 0, s>>>((const bf16 *)g, db, part, M, C, rows));
+  if (part) FLF_NET_LAUNCH(k_bias_reduce<<<1, 128, 0, s>>>(part, db, (int)blocks, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, cudaStream_t s) {
-  k_pool2<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)in, (bf16 *)out, B, Z, Y, X, C);
+  FLF_NET_LAUNCH(k_pool2<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)in, (bf16 *)out, B, Z, Y, X, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y,
                              int X, int C, cudaStream_t s) {
-  k_pool2_bwd<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>(
-      (const bf16 *)gpool, (const bf16 *)gskip, (const bf16 *)act, (bf16 *)gin, B, Z, Y, X, C);
+  FLF_NET_LAUNCH(k_pool2_bwd<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>(
+      (const bf16 *)gpool, (const bf16 *)gskip, (const bf16 *)act, (bf16 *)gin, B, Z, Y, X, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C,
                            cudaStream_t s) {
-  k_up2_add<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
-                                                                          (bf16 *)out, B, Z, Y, X, C);
+  FLF_NET_LAUNCH(k_up2_add<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
+                                                                          (bf16 *)out, B, Z, Y, X, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y, int X, int C,
                            cudaStream_t s) {
-  k_up2_bwd<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)g, (const bf16 *)act,
-                                                                              (bf16 *)glow, B, Z, Y, X, C);
+  FLF_NET_LAUNCH(k_up2_bwd<<<grid_for((long long)B * Z * Y * X * C / 64, 256), 256, 0, s>>>((const bf16 *)g, (const bf16 *)act,
+                                                                              (bf16 *)glow, B, Z, Y, X, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C,
                             cudaStream_t s) {
-  k_mse_grad<<<grid_for(M, 256), 256, 0, s>>>((const bf16 *)y, target, (bf16 *)g, loss, M, C);
+  FLF_NET_LAUNCH(k_mse_grad<<<grid_for(M, 256), 256, 0, s>>>((const bf16 *)y, target, (bf16 *)g, loss, M, C));
   return cudaGetLastError();
 }
 
 cudaError_t launch_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
                         float b2, float eps, float c1, float c2, float wd, cudaStream_t s) {
-  k_adam<<<grid_for(n, 256), 256, 0, s>>>(w, g, m, v, (bf16 *)wb, n, lr, b1, b2, eps, c1, c2, wd);
+  FLF_NET_LAUNCH(k_adam<<<grid_for(n, 256), 256, 0, s>>>(w, g, m, v, (bf16 *)wb, n, lr, b1, b2, eps, c1, c2, wd));
   return cudaGetLastError();
 }
 
 cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s) {
   const long long n = (long long)p.T * p.Zp * p.Yp * p.Xp;
   if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(p.sum_x1, 0, sizeof(float) * p.T, s);
-  if (e != cudaSuccess) return e;
   const long long V = (long long)p.Z * p.Y * p.X;
   long long blocks = (V + 2047) / 2048;
   if (blocks > 1024) blocks = 1024;
-  k_ws_sum<<<dim3((unsigned)blocks, (unsigned)p.T), 256, 0, s>>>(p.htf, p.hth1, p.sum_x1, p.T, V,
-                                                                  (long long)p.Y * p.X);
-  k_ws_input<<<grid_for(n, 256), 256, 0, s>>>(p);
+  // the per-block partial sums go to the start of `out` (T * blocks floats fit:
+  // out holds 32 bytes per padded voxel), which k_ws_input overwrites afterwards
+  float *part = reinterpret_cast<float *>(p.out);
+  FLF_NET_LAUNCH(k_ws_sum<<<dim3((unsigned)blocks, (unsigned)p.T), 256, 0, s>>>(p.htf, p.hth1, part, p.T, V, (long long)p.Y * p.X));
+  FLF_NET_LAUNCH(k_ws_sum_final<<<(p.T + 127) / 128, 128, 0, s>>>(part, p.sum_x1, p.T, (int)blocks));
+  FLF_NET_LAUNCH(k_ws_input<<<grid_for(n, 256), 256, 0, s>>>(p));
   return cudaGetLastError();
 }
 
@@ -1751,10 +1827,17 @@ cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor
   return g_conv16_tc ? launch_tma16<16, 16, 2, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
 }
 
-cudaError_t launch_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma,
+cudaError_t launch_render_blobs(float *vol, void *acc, int Z, int Y, int X, const float *pts, int npts, float sigma,
                                 cudaStream_t s) {
   if (npts <= 0) return cudaSuccess;
-  k_render_blobs<<<(unsigned)((npts * 32 + 255) / 256), 256, 0, s>>>(vol, Z, Y, X, (const float4 *)pts, npts, sigma);
+  const long long n = (long long)Z * Y * X;
+  if (acc) {
+    cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * n, s);
+    if (e != cudaSuccess) return e;
+  }
+  FLF_NET_LAUNCH(k_render_blobs<<<(unsigned)((npts * 32 + 255) / 256), 256, 0, s>>>(vol, (unsigned long long *)acc, Z, Y, X,
+                                                                      (const float4 *)pts, npts, sigma));
+  if (acc) FLF_NET_LAUNCH(k_blobs_add<<<grid_for(n, 256), 256, 0, s>>>(vol, (const unsigned long long *)acc, n));
   return cudaGetLastError();
 }
 

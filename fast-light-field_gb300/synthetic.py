@@ -49,19 +49,24 @@ def _profiles(Nnum, h, spread_lenslets, sigma, gamma, alpha, n_terms):
     return u
 
 
-def synthetic_psf(Nnum, z_um, img_size_ref, dtype=np.float32):
+def synthetic_psf(Nnum, z_um, img_size_ref, dtype=np.float32, only=None):
     """Stand-in PSF set: lists of per-plane ``H`` and ``Ht`` quadrants ``[n_h, n_h, h, h]``.
 
     ``Hfull[b][a] = sum_r u^r_b (x) u^r_a`` with mirror-symmetric profiles, so the
     reference's symmetry map reproduces the full set exactly; ``Ht`` is built
     by the adjoint relation ``Ht_ba(y, x) = H_{(b+y-ch)%N, (a+x-ch)%N}(2ch-y, 2ch-x)``.
+    ``only``: plane indices to compute (the others are None in the lists).
     """
     N = int(Nnum)
     nh = (N + 1) // 2
     hs = psf_sizes(N, z_um, img_size_ref)
     zmax = float(np.max(np.abs(z_um))) or 1.0
     H_list, Ht_list = [], []
-    for zz, h in zip(z_um, hs):
+    for zi, (zz, h) in enumerate(zip(z_um, hs)):
+        if only is not None and zi not in only:
+            H_list.append(None)
+            Ht_list.append(None)
+            continue
         ch = (h - 1) // 2
         rel = abs(zz) / zmax
         spread = img_size_ref * rel

@@ -100,7 +100,8 @@ class UNet3D:
         y = out if out is not None else _bf(tuple(x.shape[:4]) + (co,), self.dev)
         if relu is None:
             relu = q["relu"] and not flip       # a data gradient is linear
-        need = y.numel()
+        # split-K layers (few output tiles: the coarse levels) write one slice per split
+        need = y.numel() * (4 if y.numel() < (1 << 22) else 1)
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
         _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,
@@ -150,8 +151,11 @@ class UNet3D:
     def _wgrad(self, name, x, g):
         q = self.p[name]
         s = torch.cuda.current_stream(self.dev).cuda_stream
-        _flf.conv3d_wgrad(x, g, q["gw"], s)
-        _flf.bias_grad(g, q["gb"], s)
+        need = max(64 * q["w"].numel(), g.numel() // 2048 + q["co"])   # wgrad chunks / bias row blocks
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
+        _flf.conv3d_wgrad(x, g, q["gw"], s, ws=self._ws)
+        _flf.bias_grad(g, q["gb"], s, ws=self._ws)
 
     def backward(self, a, dout):
         """Gradients of all parameters (accumulated into gw / gb) for dL/d(out) = dout."""
@@ -313,10 +317,11 @@ class WarmStart:
     def make_batch(self, T, rng):
         """T synthetic (truth [Z, T, Y, X], noisy image [T, Y, X], Htf [Z, T, Y, X])."""
         truth = torch.zeros((T, self.Z, self.Y, self.X), device=self.dev)
+        acc = torch.empty(self.Z * self.Y * self.X, dtype=torch.int64, device=self.dev)
         for t in range(T):
             pts = torch.as_tensor(synthetic_volume_points((self.Z, self.Y, self.X), self.beads, self.filaments, rng),
                                   device=self.dev)
-            _flf.render_blobs(truth[t], pts, self.sigma, self._s())
+            _flf.render_blobs(truth[t], pts, self.sigma, self._s(), acc=acc)
         truth = truth.permute(1, 0, 2, 3).contiguous()
         clean = torch.empty((T, self.Y, self.X), device=self.dev)
         self.ctx.forward(truth, clean, T, self.Y, self.X, None, stream=self._s())

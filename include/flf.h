@@ -232,12 +232,22 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), bias [Co] float or NULL, act = ReLU
  *   when relu != 0; with mask != NULL ([..][Co] bf16) entries whose mask is
  *   not > 0 are zeroed (the ReLU derivative in a backward pass).  ws (float,
- *   ws_elems >= B Z Y X Co, or NULL) lets layers with few output tiles split
- *   their K loop across CTAs; it must not be shared by concurrent calls.
+ *   or NULL) lets layers with few output tiles split their K loop across
+ *   CTAs, each split into its own B Z Y X Co slice (as many splits as fit,
+ *   at least 2), summed in split order; it must not be shared by concurrent
+ *   calls.
  * flf_conv3d_wgrad: dw [27][Ci][Co] float += sum_v x[v + tap][ci] dy[v][co].
+ *   The voxels are cut into chunks whose partial gradients go to ws (float,
+ *   27 Ci Co per chunk; as many chunks as ws holds, one without ws) and are
+ *   added to dw in chunk order.
+ * Every reduction of these kernels runs in a fixed order (no floating-point
+ *   atomics), so training repeats bit for bit on the same device; the loss
+ *   value of flf_mse_grad alone is summed with atomics.
  * flf_conv3d_flip: w2[26 - tap][co][ci] = w[tap][ci][co]; conv3d with w2 is
  *   the data gradient.
- * flf_bias_grad: db[c] += sum over the M rows of g[M][C] (C <= 128).
+ * flf_bias_grad: db[c] += sum over the M rows of g[M][C] (C <= 128); row
+ *   blocks of 2048 have their sums in ws (float, C per block; as many blocks as
+ *   ws holds, one without ws), added in block order.
  * flf_pool2 / flf_pool2_bwd: 2x2x2 average pooling (Z, Y, X even) and its
  *   adjoint plus an optional second gradient gskip, times (act > 0) if act.
  * flf_up2_add / flf_up2_bwd: out = nearest 2x upsampling of low (+ skip);
@@ -249,11 +259,14 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   (bias corrections c1, c2, decoupled weight decay wd); writes the BF16
  *   copy wb when not NULL.
  * flf_render_blobs: vol [Z][Y][X] float += amp exp(-d^2 / 2 sigma^2) within
- *   3 sigma of each pts[k] = (z, y, x, amp) (float4 array). */
+ *   3 sigma of each pts[k] = (z, y, x, amp) (float4 array).  With acc (Z Y X
+ *   int64, 8-byte aligned, overwritten) the terms are summed exactly as 32.32
+ *   fixed-point integers, so the result does not depend on the order of
+ *   arrival (per-voxel totals below 2^31); without it, FP32 atomics. */
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
                int Ci, int Co, int relu, float *ws, long long ws_elems, void *stream);
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
-                     void *stream);
+                     float *ws, long long ws_elems, void *stream);
 /* flf_conv3d_tc: flf_conv3d for 16 -> 16 channels on the tcgen05 tensor cores
  * (accumulators in TMEM).  rows = 0: the warp-specialised kernel (TMA loads
  * of input slabs into a shared-memory ring, one MMA-issuing thread, two TMEM
@@ -270,8 +283,11 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
                   int X, int relu, int rows, void *stream);
 int flf_net_status(void);
 int flf_net_conv16_tcgen05(int mode);
+/* Number of kernel launches the network entry points above have made since
+ * the library was loaded (all threads). */
+long long flf_net_launches(void);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
-int flf_bias_grad(const void *g, float *db, long long M, int C, void *stream);
+int flf_bias_grad(const void *g, float *db, long long M, int C, float *ws, long long ws_elems, void *stream);
 int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);
 int flf_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y, int X, int C,
                   void *stream);
@@ -280,7 +296,8 @@ int flf_up2_bwd(const void *g, const void *act, void *glow, int B, int Z, int Y,
 int flf_mse_grad(const void *y, const float *target, void *g, float *loss, long long M, int C, void *stream);
 int flf_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1, float b2,
              float eps, float c1, float c2, float wd, void *stream);
-int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *stream);
+int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts, float sigma, void *acc,
+                     void *stream);
 /* Warm-start inference glue.  flf_ws_input: network input [T][Zp][Yp][Xp][16]
  * bf16 from Htf [Z][T][Y][X] float and the sensitivity maps HtH1, Ht1
  * [Z][Y][X]: channel 0 = Htf / HtH1 / m_t (m_t = frame mean of Htf / HtH1,

@@ -282,10 +282,9 @@ def deconv_rl(H_planes, Ht_planes, Nnum, max_iter, im=None, Htf=None, x0=None,
 # CPU baseline: the reference's production algorithm with its symmetry reuse
 # ---------------------------------------------------------------------------
 
-def project_plane_ref_cpu(src, Hred, Nnum, workers=-1):
+def project_plane_ref_cpu(src, Hred, Nnum, workers=-1, dtype=np.float32):
     """One plane of the reference's CPU projection, as ``Projector_allC`` computes it.
 
-    Single precision throughout (py_light_field.cpp works in complex<float>).
     Per plane: one real FFT per stored quadrant PSF (``FHWorkItem``,
     py_light_field.cpp:781-812; transposed quadrant positions FFT the
     transposed PSF, :1526-1541), mirrored offsets reuse those spectra with
@@ -294,41 +293,39 @@ def project_plane_ref_cpu(src, Hred, Nnum, workers=-1):
     offset the strided sub-image FFT is tiled with phase ramps and
     multiply-accumulated (``ConvolveWorkItem``, :1001-1087); one inverse real
     FFT and a centred crop finish the plane (:925-950, projector.py:792-796).
-    FFTs use scipy with ``workers`` threads (the reference's FFTW thread pool).
+    The offsets are visited grouped by the stored spectrum they use, so only one
+    spectrum is held at a time.  ``dtype`` float32 is the reference's single
+    precision (py_light_field.cpp works in complex<float>); float64 is the same
+    algorithm in double precision.  FFTs use scipy with ``workers`` threads
+    (the reference's FFTW thread pool).
     """
     import scipy.fft as sfft
-    src = np.asarray(src, dtype=np.float32)
+    cdt = np.complex64 if dtype == np.float32 else np.complex128
+    src = np.asarray(src, dtype=dtype)
     if src.ndim == 2:
         src = src[np.newaxis]
     T, Y, X = src.shape
     N = int(Nnum)
     c = N // 2
-    Hred = np.asarray(Hred, dtype=np.float32)
+    Hred = np.asarray(Hred, dtype=dtype)
     h = Hred.shape[-1]
     (FY, FX), full = convolution_shape((Y, X), (h, h), N, True)
     fy, fx = FY // N, FX // N
     RX = FX // 2 + 1
     ky = np.arange(FY)
     kx = np.arange(RX)
-    ph_y = np.exp(-2j * np.pi * ky * (h - 1) / FY).astype(np.complex64)     # row flip
-    ph_x = np.exp(-2j * np.pi * kx * (h - 1) / FX).astype(np.complex64)     # column flip
-    ey = [np.exp(-2j * np.pi * b * ky / FY).astype(np.complex64) for b in range(N)]
-    ex = [np.exp(-2j * np.pi * a * kx / FX).astype(np.complex64) for a in range(N)]
+    ph_y = np.exp(-2j * np.pi * ky * (h - 1) / FY).astype(cdt)     # row flip
+    ph_x = np.exp(-2j * np.pi * kx * (h - 1) / FX).astype(cdt)     # column flip
     yflip = (-ky) % FY
-    accum = np.zeros((T, FY, RX), dtype=np.complex64)
-    cache = {}
-
-    def base_spectrum(bb, aa):
-        key = (bb, aa)
-        if key not in cache:
-            P = Hred[bb, aa] if aa >= bb else Hred[aa, bb].T
-            cache[key] = sfft.rfft2(P, s=(FY, FX), workers=workers).astype(np.complex64)
-        return cache[key]
-
+    accum = np.zeros((T, FY, RX), dtype=cdt)
+    groups = {}
     for b in range(N):
         for a in range(N):
-            bb, aa = min(b, N - 1 - b), min(a, N - 1 - a)
-            Fb = base_spectrum(bb, aa)
+            groups.setdefault((min(b, N - 1 - b), min(a, N - 1 - a)), []).append((b, a))
+    for (bb, aa), offsets in groups.items():
+        P = Hred[bb, aa] if aa >= bb else Hred[aa, bb].T
+        Fb = sfft.rfft2(P, s=(FY, FX), workers=workers).astype(cdt)
+        for b, a in offsets:
             if b > c and a > c:
                 FH = np.conj(Fb) * (ph_y[:, None] * ph_x[None, :])
             elif b > c:
@@ -337,10 +334,12 @@ def project_plane_ref_cpu(src, Hred, Nnum, workers=-1):
                 FH = np.conj(Fb[yflip]) * ph_x[None, :]
             else:
                 FH = Fb
-            Ss = sfft.fft2(src[:, b::N, a::N], s=(fy, fx), axes=(1, 2), workers=workers).astype(np.complex64)
-            Sx = Ss[:, :, kx % fx] * ex[a][None, None, :]
-            Sf = Sx[:, ky % fy, :] * ey[b][None, :, None]
+            ey = np.exp(-2j * np.pi * b * ky / FY).astype(cdt)
+            ex = np.exp(-2j * np.pi * a * kx / FX).astype(cdt)
+            Ss = sfft.fft2(src[:, b::N, a::N], s=(fy, fx), axes=(1, 2), workers=workers).astype(cdt)
+            Sx = Ss[:, :, kx % fx] * ex[None, None, :]
+            Sf = Sx[:, ky % fy, :] * ey[None, :, None]
             accum += Sf * FH[None]
-    img = sfft.irfft2(accum, s=(FY, FX), axes=(1, 2), workers=workers).astype(np.float32)
+    img = sfft.irfft2(accum, s=(FY, FX), axes=(1, 2), workers=workers).astype(dtype)
     img = img[:, :full[0], :full[1]]
-    return _centered(img, (Y, X)).astype(np.float32)
+    return _centered(img, (Y, X)).astype(dtype)

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     text = open(os.path.join(ROOT, "include", "flf.h")).read()
-    return sorted(set(re.findall(r"^int\s+\**\s*(flf_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|long long)\s+\**\s*(flf_\w+)\s*\(", text, re.M)))
 
 
 def test_header_matches_binding():

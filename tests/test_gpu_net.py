@@ -51,12 +51,16 @@ def test_conv3d_forward(env, shape, Ci, Co, relu):
     w = (torch.randn((27, Ci, Co), generator=g) / np.sqrt(27 * Ci)).bfloat16()
     b = torch.randn(Co, generator=g).float()
     y = torch.empty(shape + (Co,), dtype=torch.bfloat16, device="cuda")
-    ws = torch.empty(int(np.prod(shape)) * Co, device="cuda")
+    ws = torch.empty(4 * int(np.prod(shape)) * Co, device="cuda")    # room for 4 K slices
     _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws)
     ref = _ref_conv(torch, x.double(), w.double(), b.double())
     if relu:
         ref = ref.clamp_min(0)
     _close(torch, y, ref)
+    # split layers add their K slices in a fixed order: the same bits again
+    y2 = torch.empty_like(y)
+    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y2, relu=relu, ws=ws)
+    assert torch.equal(y, y2)
 
 
 @pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 32, 16), ((1, 3, 6, 6), 64, 128)])
@@ -73,7 +77,7 @@ def test_conv3d_mask_and_data_gradient(env, shape, Ci, Co):
     w2 = torch.empty((27, Co, Ci), dtype=torch.bfloat16, device="cuda")
     _flf.conv3d_flip(w.cuda(), w2)
     dx = torch.empty(shape + (Ci,), dtype=torch.bfloat16, device="cuda")
-    ws = torch.empty(int(np.prod(shape)) * Ci, device="cuda")
+    ws = torch.empty(4 * int(np.prod(shape)) * Ci, device="cuda")
     _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws)
     _close(torch, dx, ref)
 
@@ -88,12 +92,18 @@ def test_conv3d_weight_and_bias_gradient(env, shape, Ci, Co):
     b = torch.zeros(Co, dtype=torch.float64, requires_grad=True)
     dy = torch.randn(shape + (Co,), generator=g).bfloat16()
     _ref_conv(torch, x.double(), w, b).backward(dy.double())
-    dw = torch.zeros((27, Ci, Co), dtype=torch.float32, device="cuda")
-    db = torch.zeros(Co, dtype=torch.float32, device="cuda")
-    _flf.conv3d_wgrad(x.cuda(), dy.cuda(), dw)
-    _flf.bias_grad(dy.cuda(), db)
-    assert float((dw.double().cpu() - w.grad).abs().max()) <= 1e-4 * float(w.grad.abs().max())
-    assert float((db.double().cpu() - b.grad).abs().max()) <= 1e-4 * float(b.grad.abs().max())
+    ws = torch.empty(64 * 27 * Ci * Co, dtype=torch.float32, device="cuda")
+    runs = []
+    for use_ws in (False, True, True):
+        dw = torch.zeros((27, Ci, Co), dtype=torch.float32, device="cuda")
+        db = torch.zeros(Co, dtype=torch.float32, device="cuda")
+        _flf.conv3d_wgrad(x.cuda(), dy.cuda(), dw, ws=ws if use_ws else None)
+        _flf.bias_grad(dy.cuda(), db, ws=ws if use_ws else None)
+        assert float((dw.double().cpu() - w.grad).abs().max()) <= 1e-4 * float(w.grad.abs().max())
+        assert float((db.double().cpu() - b.grad).abs().max()) <= 1e-4 * float(b.grad.abs().max())
+        runs.append((dw.cpu(), db.cpu()))
+    # the partial sums are added in a fixed order: the same bits on every run
+    assert torch.equal(runs[1][0], runs[2][0]) and torch.equal(runs[1][1], runs[2][1])
 
 
 def test_pool_upsample_and_their_adjoints(env):
@@ -157,6 +167,15 @@ def test_mse_adam_and_blobs(env):
         near = (np.abs(zz - cz) <= 3) & (np.abs(yy - cy) <= 3) & (np.abs(xx - cx) <= 3)
         ref += near * a * np.exp(-((zz - z0) ** 2 + (yy - y0) ** 2 + (xx - x0) ** 2) / 2)
     assert np.max(np.abs(vol.cpu().numpy() - ref)) < 1e-5
+    # fixed-point accumulation: the same volume, bit for bit on every run
+    acc = torch.empty(6 * 20 * 30, dtype=torch.int64, device="cuda")
+    outs = []
+    for _ in range(2):
+        v2 = torch.zeros((6, 20, 30), device="cuda")
+        _flf.render_blobs(v2, pts, 1.0, acc=acc)
+        assert np.max(np.abs(v2.cpu().numpy() - ref)) < 1e-5
+        outs.append(v2.cpu())
+    assert torch.equal(outs[0], outs[1])
 
 
 @pytest.mark.parametrize("rows", [0, -1, 1, 4, 5])

@@ -1,9 +1,12 @@
 """The learned warm start: the whole network's gradients against a torch CPU
 float64 restatement, training, and RL from the warm start.
 
-Gradient check: the device network keeps activations in BF16, so each
-parameter gradient must agree with the float64 restatement (same BF16 weights
-and input, FP64 activations) in direction (cosine >= 0.99) and to 10 % in
+Gradient check: the device network keeps activations and activation
+gradients in BF16.  The float64 restatement does the same: every activation
+is rounded to BF16 in the forward pass and its gradient is rounded to BF16 in
+the backward pass (the tensors the device kernels write), with everything else
+in float64.  What is left is the device's FP32 accumulation order, so each
+parameter gradient must agree in direction (cosine >= 0.9999) and to 1 % in
 norm.
 """
 
@@ -20,9 +23,27 @@ def env(built_lib):
     return torch, warmstart
 
 
+def _bf16_round(torch):
+    """Identity that rounds its value to BF16 going forward and its gradient to
+    BF16 going back: the activations and activation gradients the device keeps."""
+
+    class R(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return t.to(torch.bfloat16).double()
+
+        @staticmethod
+        def backward(ctx, g):
+            return g.to(torch.bfloat16).double()
+
+    return R.apply
+
+
 def _reference_forward(torch, ws_mod, net, x):
-    """The network in float64 on the CPU with the device network's BF16 weights."""
+    """The network in float64 on the CPU with the device network's BF16 weights,
+    with BF16 rounding of every activation and activation gradient."""
     F = torch.nn.functional
+    R = _bf16_round(torch)
     P = {n: (q["wb"].double().cpu().requires_grad_(), q["b"].double().cpu().requires_grad_())
          for n, q in net.p.items()}
 
@@ -30,19 +51,22 @@ def _reference_forward(torch, ws_mod, net, x):
         w, b = P[name]
         ci, co = w.shape[1], w.shape[2]
         y = F.conv3d(t, w.reshape(3, 3, 3, ci, co).permute(4, 3, 0, 1, 2), b, padding=1)
-        return F.relu(y) if relu else y
+        return R(F.relu(y) if relu else y)
 
     def up(t):
         return t.repeat_interleave(2, 2).repeat_interleave(2, 3).repeat_interleave(2, 4)
 
-    t = x.double().cpu().permute(0, 4, 1, 2, 3)
+    def pool(t):
+        return R(F.avg_pool3d(t, 2))
+
+    t = R(x.double().cpu().permute(0, 4, 1, 2, 3))
     e0 = conv("e0b", conv("e0a", t, True), True)
-    e1 = conv("e1b", conv("e1a", F.avg_pool3d(e0, 2), True), True)
-    e2 = conv("e2b", conv("e2a", F.avg_pool3d(e1, 2), True), True)
-    e3 = conv("e3b", conv("e3a", F.avg_pool3d(e2, 2), True), True)
-    d2 = conv("d2", up(conv("u2", e3, True)) + e2, True)
-    d1 = conv("d1", up(conv("u1", d2, True)) + e1, True)
-    d0 = conv("d0", up(conv("u0", d1, True)) + e0, True)
+    e1 = conv("e1b", conv("e1a", pool(e0), True), True)
+    e2 = conv("e2b", conv("e2a", pool(e1), True), True)
+    e3 = conv("e3b", conv("e3a", pool(e2), True), True)
+    d2 = conv("d2", R(up(conv("u2", e3, True)) + e2), True)
+    d1 = conv("d1", R(up(conv("u1", d2, True)) + e1), True)
+    d0 = conv("d0", R(up(conv("u0", d1, True)) + e0), True)
     out = conv("head", d0, False)
     return out.permute(0, 2, 3, 4, 1), P
 
@@ -67,13 +91,16 @@ def _gradients_match(torch, ws_mod):
     target = torch.rand((2, 8, 16, 24), generator=g)
     out, cache = net.forward(x.cuda())
     ref, P = _reference_forward(torch, ws_mod, net, x)
-    assert float((out.double().cpu() - ref.detach()).abs().max()) <= 0.05 * float(ref.detach().abs().max())
+    # outputs differ only where FP32 and FP64 sums round to neighbouring BF16 values
+    assert float((out.double().cpu() - ref.detach()).abs().max()) <= 0.02 * float(ref.detach().abs().max())
     dout = torch.empty_like(out)
     loss = torch.zeros(1, device="cuda")
     import _flf
     _flf.mse_grad(out, target.cuda(), dout, loss)
-    ((ref[..., 0] - target.double()) ** 2).mean().backward()
+    R = _bf16_round(torch)
+    ((R(ref[..., 0]) - target.double()) ** 2).mean().backward()
     net.backward(cache, dout)
+    worst = []
     for name, q in net.p.items():
         for key, gref in (("gw", P[name][0].grad), ("gb", P[name][1].grad)):
             gd = q[key].double().cpu()
@@ -85,8 +112,11 @@ def _gradients_match(torch, ws_mod):
             if nr == 0:
                 continue
             cos = float((gd * gref).sum() / (gd.norm() * gref.norm() + 1e-300))
-            assert cos >= 0.99, (name, key, cos)
-            assert abs(float(gd.norm()) - nr) <= 0.1 * nr, (name, key, float(gd.norm()), nr)
+            worst.append((1 - cos, abs(float(gd.norm()) - nr) / nr, name, key))
+            assert cos >= 0.9999, (name, key, cos)
+            assert abs(float(gd.norm()) - nr) <= 0.01 * nr, (name, key, float(gd.norm()), nr)
+    print("largest 1 - cosine %.2e (%s %s), largest norm difference %.2e (%s %s)"
+          % (max(worst)[0], max(worst)[2], max(worst)[3], *max(worst, key=lambda w: w[1])[1:]))
 
 
 def test_training_and_warm_started_rl(env):
@@ -115,10 +145,21 @@ def test_training_and_warm_started_rl(env):
         ws.ctx.forward(x, hx, 2, Y, X, None, stream=s)
         return float(torch.linalg.vector_norm(img.double() - hx.double()) / torch.linalg.vector_norm(img.double()))
 
+    # what the network gains: RL from its start volume reaches the data-fit
+    # residual of 8 plain-RL iterations from a uniform volume in fewer iterations
     xu = torch.ones_like(htf)
     p.RichardsonLucy(hm, xu, htf, 8)
-    xw = ws_mod.DeconvRLWarm(ws, img, 8)
-    assert resid(xw) <= 1.01 * resid(xu)
+    r_plain = resid(xu)
+    xw = ws.initial_volume(htf)
+    need = None
+    for k in range(9):
+        if k:
+            p.RichardsonLucy(hm, xw, htf, 1)
+        if resid(xw) <= r_plain:
+            need = k
+            break
+    print("plain RL-8 residual %.5f; warm start reaches it after %s RL iterations" % (r_plain, need))
+    assert need is not None and need < 8, need
 
 
 @pytest.mark.parametrize("tcgen05", [False, True])
