@@ -29,11 +29,11 @@ struct Workspace {
 // smallest size its own kernel radius allows; planes with equal sizes share
 // one group (one set of launches per projection).
 struct Group {
-  int f = 0, fh = 0, fq = 0, nkp = 0, R = 0;
+  int f = 0, fh = 0, fq = 0, nkp = 0, nquads = 0, R = 0;   // nkp = fq^2 half blocks, nquads = fq(fq+1)/2
   FftPlan plan{};
   float2 *tw = nullptr;       // float twiddles [f]
   double2 *tw64 = nullptr;    // double twiddles [f]
-  float2 *P[2] = {nullptr, nullptr};   // packed matrices [slot][nkp][nrow][RS]
+  float2 *P[2] = {nullptr, nullptr};   // packed matrices [slot][nkp half blocks][nrow][RS]
   bool built[2] = {false, false};
   std::vector<int> planes;    // plane ids of the group, ascending (slot = index)
   int *d_ids = nullptr;       // device copy of `planes`
@@ -68,7 +68,8 @@ struct flf_ctx {
   std::vector<int> h[2];
   Geometry geo;
   // index tables (device)
-  short4 *d_rowS = nullptr;
+  short4 *d_rowS = nullptr, *d_oslots = nullptr;
+  short *d_rowF = nullptr;
   short *d_slotcol = nullptr, *d_colslot = nullptr;
   int *d_rep_ch = nullptr, *d_rep_row = nullptr, *d_rep_kind = nullptr;
   int *d_planes_all = nullptr;
@@ -289,33 +290,77 @@ int build_tables(flf_ctx *ctx) {
   std::vector<short> colslot(NN, -1);
   for (int s = 0; s < NN; s++) colslot[slotcol[s]] = s;
 
-  std::vector<short4> rowS;
-  ctx->rep_ch.clear(); ctx->rep_row.clear(); ctx->rep_kind.clear();
-  int row = 0;
-  for (int b = 0; b < c; b++)
-    for (int a = 0; a < N; a++) {
-      if (a == c) continue;
-      int i = b * N + a;
-      rowS.push_back(make_short4(i, Mxy(i), NN + My(i), NN + Mx(i)));
-      ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row++); ctx->rep_kind.push_back(0);
+  auto Tr = [&](int i) { return (i % N) * N + i / N; };
+  // virtual slots [q, My q, Mx q, Mxy q] of each output orbit (degenerate orbits
+  // repeat their entries) and the slots of the transposed channels in the same order
+  std::vector<short4> oslots(2 * L.nthr);
+  for (int o = 0; o < L.nthr; o++) {
+    int off[4];
+    if (o < c2) {
+      off[0] = o; off[1] = c2 + o; off[2] = 2 * c2 + o; off[3] = 3 * c2 + o;
+    } else if (o < c2 + c) {
+      const int j = o - c2;
+      off[0] = off[2] = 4 * c2 + j; off[1] = off[3] = 4 * c2 + c + j;
+    } else if (o < c2 + 2 * c) {
+      const int j = o - c2 - c;
+      off[0] = off[1] = 4 * c2 + 2 * c + j; off[2] = off[3] = 4 * c2 + 3 * c + j;
+    } else {
+      off[0] = off[1] = off[2] = off[3] = NN - 1;
     }
-  for (int k = 0; k < L.nrep; k++) {
-    int i, kind;
-    if (k < c) { i = k * N + c; kind = 1; }
-    else if (k < 2 * c) { i = c * N + (k - c); kind = 2; }
-    else { i = c * N + c; kind = 3; }
-    short4 s;
-    if (kind == 1) s = make_short4(i, NN + i, NN + My(i), My(i));
-    else if (kind == 2) s = make_short4(i, NN + i, NN + Mx(i), Mx(i));
-    else s = make_short4(i, NN + i, 0, 0);
-    rowS.push_back(s);
-    ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row); ctx->rep_kind.push_back(kind);
-    row += 2;
+    int offT[4];
+    for (int k = 0; k < 4; k++) offT[k] = colslot[Tr(slotcol[off[k]])];
+    oslots[o] = make_short4(off[0], off[1], off[2], off[3]);
+    oslots[L.nthr + o] = make_short4(offT[0], offT[1], offT[2], offT[3]);
   }
-  if (row != L.nrow) return fail(ctx, FLF_E_STATE, "internal: row table size");
+  // row groups of a half block with their operands for the own frequency pair
+  // (use 0) and, through the transpose, for the other one of the quad (use 1)
+  std::vector<short4> rowS(2 * L.ngrp, make_short4(0, 0, 0, 0));
+  std::vector<short> rowF(2 * L.ngrp, 0);
+  ctx->rep_ch.clear(); ctx->rep_row.clear(); ctx->rep_kind.clear();
+  auto generic_ops = [&](int x, bool mxrow, short4 &si, short &fl) {
+    si = make_short4(x, Mxy(x), NN + My(x), NN + Mx(x));
+    fl = (short)((1 << 1) | (1 << 3) | (mxrow ? 0xF0 : 0));
+  };
+  int row = 0, grp = 0;
+  for (int b = 0; b < c; b++)
+    for (int ap = 0; ap <= b; ap++)
+      for (int a : {ap, N - 1 - ap}) {
+        const int i = b * N + a;
+        const bool trans = ap < b, mxrow = a > c;
+        generic_ops(i, mxrow, rowS[grp], rowF[grp]);
+        if (trans) {
+          generic_ops(Tr(i), mxrow, rowS[L.ngrp + grp], rowF[L.ngrp + grp]);
+          rowF[grp] |= kRowTransposable;
+          rowF[L.ngrp + grp] |= kRowTransposable;
+        }
+        ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row); ctx->rep_kind.push_back(0);
+        row++; grp++;
+      }
+  if (row != L.nrowG) return fail(ctx, FLF_E_STATE, "internal: generic row table size");
+  for (int k = 0; k <= c; k++) {
+    const bool centre = k == c;
+    const int i = centre ? c * N + c : k * N + c;
+    if (centre) {
+      rowS[grp] = make_short4(i, NN + i, 0, 0);
+      rowF[grp] = (short)((1 << 5) | (1 << 10) | (1 << 11));
+    } else {
+      rowS[grp] = make_short4(i, NN + i, NN + My(i), My(i));
+      rowF[grp] = (short)((1 << 5) | (1 << 7) | kRowTransposable);
+      const int x = Tr(i);   // (c, b): the row pair read through the transpose, conjugated u* terms
+      rowS[L.ngrp + grp] = make_short4(x, NN + x, NN + Mx(x), Mx(x));
+      rowF[L.ngrp + grp] = (short)((1 << 1) | (1 << 2) | (1 << 5) | (1 << 7) | kRowTransposable);
+    }
+    ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row); ctx->rep_kind.push_back(1);
+    row += 2; grp++;
+  }
+  if (row != L.nrow || grp != L.ngrp) return fail(ctx, FLF_E_STATE, "internal: row table size");
   const int nrepAll = (int)ctx->rep_ch.size();
   CUDA_TRY(ctx, cudaMalloc(&ctx->d_rowS, sizeof(short4) * rowS.size()));
   CUDA_TRY(ctx, cudaMemcpy(ctx->d_rowS, rowS.data(), sizeof(short4) * rowS.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_rowF, sizeof(short) * rowF.size()));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_rowF, rowF.data(), sizeof(short) * rowF.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(ctx, cudaMalloc(&ctx->d_oslots, sizeof(short4) * oslots.size()));
+  CUDA_TRY(ctx, cudaMemcpy(ctx->d_oslots, oslots.data(), sizeof(short4) * oslots.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(ctx, cudaMalloc(&ctx->d_slotcol, sizeof(short) * NN));
   CUDA_TRY(ctx, cudaMemcpy(ctx->d_slotcol, slotcol.data(), sizeof(short) * NN, cudaMemcpyHostToDevice));
   CUDA_TRY(ctx, cudaMalloc(&ctx->d_colslot, sizeof(short) * NN));
@@ -494,7 +539,7 @@ int prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
   sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
   for (int f : sizes) {
     Group g;
-    g.f = f; g.fh = f / 2 + 1; g.fq = f / 2 + 1; g.nkp = g.fq * g.fq;
+    g.f = f; g.fh = f / 2 + 1; g.fq = f / 2 + 1; g.nkp = g.fq * g.fq; g.nquads = g.fq * (g.fq + 1) / 2;
     g.plan = make_plan(f);
     for (int z = 0; z < nz; z++)
       if (fz[z] == f) {
@@ -620,9 +665,11 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
 // (a few waves at the kernel's occupancy), as few plane groups as that allows.
 // Planes per multiply-accumulate CTA: enough CTAs for 32 per SM, at most
 // kMacMaxZgroup planes each.
-int zgroup_for(const flf_ctx *ctx, int nz, int nkp) {
-  const int target = 32 * std::max(1, ctx->num_sms);
-  const int nzg_needed = std::min(nz, std::max(1, (target + nkp - 1) / nkp));
+// Planes per multiply-accumulate CTA: enough plane groups to give about 16
+// CTAs per SM over the nquads frequency quads.
+int zgroup_for(const flf_ctx *ctx, int nz, int nquads) {
+  const int target = 16 * std::max(1, ctx->num_sms);
+  const int nzg_needed = std::min(nz, std::max(1, (target + nquads - 1) / nquads));
   return std::min(kMacMaxZgroup, std::max(1, (nz + nzg_needed - 1) / nzg_needed));
 }
 
@@ -644,7 +691,7 @@ void ws_needs(const flf_ctx *ctx, const PlaneSet &ps, int nt, bool fwd, size_t &
     const int n = ps.n[g];
     sCv = std::max(sCv, cset * nt * n);
     if (fwd) {
-      const int zg = zgroup_for(ctx, n, G.groups[g].nkp);
+      const int zg = zgroup_for(ctx, n, G.groups[g].nquads);
       sS = std::max(sS, spec * nt * n);
       sO = std::max(sO, spec * nt * ((n + zg - 1) / zg));
     } else {
@@ -688,13 +735,15 @@ int join_streams(flf_ctx *ctx, cudaStream_t s) {
 
 MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   MacParams mp{};
-  mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.T = nt;
+  mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.nquads = G.nquads; mp.T = nt;
   mp.P = G.P[dir];
-  mp.rowS = ctx->d_rowS; mp.slotcol = ctx->d_slotcol;
+  mp.rowS = ctx->d_rowS; mp.rowF = ctx->d_rowF; mp.oslots = ctx->d_oslots; mp.slotcol = ctx->d_slotcol;
   const int *tn = ctx->geo.tuned;
   mp.stages = tn[0] ? tn[0] : ctx->opt_stages;
   mp.chunk_rows = tn[1 + dir] ? tn[1 + dir] : ctx->opt_chunk_rows[dir];
   mp.split = tn[3] ? tn[3] : ctx->opt_split;
+  const int ntp = (ctx->L.nthr + 31) / 32 * 32;
+  while (mp.split > 1 && 2 * mp.split * ntp > 256) mp.split--;   // at most 256 threads per block
   mp.err = ctx->d_err;
   return mp;
 }
@@ -705,7 +754,7 @@ cudaError_t mac_group_launch(flf_ctx *ctx, size_t gi, int dir, int nt, const Pla
                              int split, cudaStream_t s) {
   const Group &G = ctx->geo.groups[gi];
   const int nplanes = ps.n[gi];
-  const int zg = zgroup_for(ctx, nplanes, G.nkp);
+  const int zg = zgroup_for(ctx, nplanes, G.nquads);
   MacParams mp = mac_params(ctx, G, dir, nt);
   mp.stages = stages; mp.chunk_rows = chunk; mp.split = split;
   mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zg;
@@ -798,7 +847,7 @@ int forward_chunk(flf_ctx *ctx, const float *vol, long long vol_sz, const PlaneS
     float2 *wO = (float2 *)((char *)ctx->wsO.p + slot * sO);
     const Group &G = Gm.groups[gi];
     const int ffh = G.f * G.fh;
-    const int zgroup = zgroup_for(ctx, nplanes, G.nkp);
+    const int zgroup = zgroup_for(ctx, nplanes, G.nquads);
     const int nzg = (nplanes + zgroup - 1) / zgroup;
 
     SplitParams sp = split_params(ctx, vol + (long long)t0 * Y * X, vol_sz, (long long)Y * X, ps.ids[gi],
@@ -866,7 +915,7 @@ int backward_chunk(flf_ctx *ctx, const float *chan, const PlaneSet &ps, int nt, 
     LAUNCH(ctx, "k_rfft2", chan_bytes(ctx, nt) + 8.0 * ffh * NN * nt, s, launch_rfft2(rp, 0, s));
 
     const double pbytes = (double)nplanes * G.nkp * L.nrow * L.RS * sizeof(float2);
-    const int zgb = zgroup_for(ctx, nplanes, G.nkp);
+    const int zgb = zgroup_for(ctx, nplanes, G.nquads);
     MacParams mp = mac_params(ctx, G, FLF_DIR_BACKWARD, nt);
     mp.planes = ps.slots[gi]; mp.nz = nplanes; mp.zgroup = zgb;
     mp.S = (const float2 *)wS; mp.nzS = 1; mp.O = wO; mp.nzo = nplanes;
@@ -968,7 +1017,7 @@ int flf_ctx_destroy(flf_ctx *ctx) {
   resolve_pending(ctx);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
   free_all_geometries(ctx);
-  void *ptrs[] = {ctx->d_rowS, ctx->d_slotcol, ctx->d_colslot, ctx->d_rep_ch, ctx->d_rep_row,
+  void *ptrs[] = {ctx->d_rowS, ctx->d_rowF, ctx->d_oslots, ctx->d_slotcol, ctx->d_colslot, ctx->d_rep_ch, ctx->d_rep_row,
                   ctx->d_rep_kind, ctx->d_planes_all, ctx->d_planes_user, ctx->d_zero,
                   ctx->wsS.p, ctx->wsO.p, ctx->wsCvol.p, ctx->wsCimg.p, ctx->wsCy.p};
   for (void *p : ptrs)
@@ -1134,7 +1183,7 @@ int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int
       e = launch_rfft2(rfft2_params(ctx, G, C, NN, S), 0, s);
       for (int z0 = 0; z0 < ng && e == cudaSuccess; z0 += zb) {
         const int nzl = std::min(zb, ng - z0);
-        const int zg = zgroup_for(ctx, nzl, G.nkp);
+        const int zg = zgroup_for(ctx, nzl, G.nquads);
         MacParams mp = mac_params(ctx, G, FLF_DIR_BACKWARD, 1);
         mp.planes = G.d_slots + z0; mp.nz = nzl; mp.zgroup = zg;
         mp.S = S; mp.nzS = 1; mp.O = O; mp.nzo = nzl; mp.nzo_grid = (nzl + zg - 1) / zg;
@@ -1427,8 +1476,9 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     for (int cr : {crf, crb})
       if (cr < 2 || cr > 64 || (cr & 1)) return fail(ctx, FLF_E_ARG, "mac_chunk_rows must be even, in [2, 64]");
     const int ntp = (ctx->L.nthr + 31) / 32 * 32;
-    if (sp < 1 || sp > 4 || sp * ntp > 256)
-      return fail(ctx, FLF_E_ARG, "mac_split must be in [1, 4] with at most 256 threads per block");
+    if (sp < 1 || sp > 4 || 2 * sp * ntp > 256)
+      return fail(ctx, FLF_E_ARG, "mac_split must be in [1, 4] with at most 256 threads per block "
+                                  "(2 frequency pairs x split x %d orbit threads)", ntp);
     for (int cr : {crf, crb})
       if (mac_smem_bytes(ctx->L, mac_max_frames(), st, cr, sp, true) > 227 * 1024)
         return fail(ctx, FLF_E_ARG, "pipeline of %d stages x %d rows exceeds shared memory", st, cr);
@@ -1486,7 +1536,7 @@ int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream) {
   for (int d = 0; d < 2 && e == cudaSuccess; d++)
     for (int a = 0; a < 2 && e == cudaSuccess; a++)
       for (int b = 0; b < 2 && e == cudaSuccess; b++) {
-        if (split_c[b] * ntp > 256) continue;
+        if (2 * split_c[b] * ntp > 256) continue;
         for (int ch : chunk_c) {
           if (mac_smem_bytes(ctx->L, mac_max_frames(), stages_c[a], ch, split_c[b], true) > 227 * 1024) continue;
           e = mac_group_launch(ctx, gi, d, nt, ps, stages_c[a], ch, split_c[b], s);   // warm-up

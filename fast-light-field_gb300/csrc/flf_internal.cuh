@@ -16,8 +16,9 @@
 //    T_{My i, My j}[u] = T_ij[u*]           (b != c), u* = (-uy, ux)
 //    T_{Mx i, Mx j}[u] = conj T_ij[u*]      (a != c)
 //    T_{Mxy i, Mxy j}[u] = conj T_ij[u]     (b != c and a != c)
-//    so the stored matrices cover a quarter of the frequencies and about
-//    half of the rows; see the packed layout below.
+//    and the transpose of the PSF set gives T_{Tr i, Tr j}[(uy, ux)] =
+//    T_ij[(ux, uy)], so the stored matrices cover a quarter of the
+//    frequencies and about a quarter of the rows; see the packed layout below.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -37,34 +38,52 @@ struct FftPlan {
   int rad[kMaxStages];   // radices, each in {2,3,4,5,7}
 };
 
-// Packed transfer-matrix layout for one (plane, direction):
-//   P[kpair][row][slot], kpair = uy*fq + ux over uy, ux in [0, f/2],
-//   fq = f/2 + 1; rows = 2*n_h^2; slot stride RS = N*N rounded up to even.
-// Rows: 2c^2 "generic" input channels (b < c, a != c) stored at u, then for
-// each of the 2c+1 centre-cross channels (b < c, a = c), (b = c, a < c),
-// (c, c) a pair of rows holding u and u*.  Slots: output channels of the
-// mirror orbits, slot-major: the c^2 generic orbits [q, My q, Mx q, Mxy q]
-// as four blocks of c^2, the c orbits [q, My q] (alpha = c) and the c orbits
-// [q, Mx q] (beta = c) as two blocks of c each, then the centre.
+// Packed transfer-matrix layout for one (plane, direction), using the mirror
+// symmetries above and the transpose symmetry of the reference's PSF set
+// (offset (a, b) uses the transpose of offset (b, a)'s PSF when their folded
+// indices differ, projector.py:176-179), which on the lenslet grid reads
+//   T_{Tr i, Tr j}[(uy, ux)] = T_ij[(ux, uy)],   Tr(b, a) = (a, b).
+// Frequency pairs (uy, ux), uy, ux in [0, f/2], come in quads {(uy, ux), (ux,
+// uy)}, uy <= ux, ordered ux-major: quad k = ux(ux+1)/2 + uy.  Each quad holds
+// one half block per frequency pair (one for a diagonal quad uy = ux): half
+// blocks 2k - ux and 2k - ux + 1, so a plane has fq^2 half blocks in all.
+//   P[half block][row][slot], rows = (c+1)(c+2) per half block, slot stride RS.
+// Rows of a half block: the generic input orbits (b, a'), a' <= b < c, as their
+// rows i = (b, a') and Mx i = (b, N-1-a') at u (c(c+1) rows); then row pairs
+// (u, u*) of the centre-cross representatives (b, c), b < c, and of the centre.
+// Orbits with a' < b and the (b, c) pairs also stand for their transposes
+// (a', b) and (c, b), which have no rows: a thread of the other frequency pair
+// reads them at the slots of its transposed output orbit.  Slots: output
+// channels of the mirror orbits, slot-major: the c^2 generic orbits [q, My q,
+// Mx q, Mxy q] as four blocks of c^2, the c orbits [q, My q] (alpha = c) and
+// the c orbits [q, Mx q] (beta = c) as two blocks of c each, then the centre.
 struct Layout {
   int N, NN, c, nh;
-  int nrowG;      // 2c^2
-  int nrep;       // 2c+1
-  int nrow;       // 2 nh^2
+  int nrowG;      // c(c+1) generic rows per half block
+  int nrep;       // c+1 row pairs per half block
+  int nrow;       // (c+1)(c+2) rows per half block
+  int ngrp;       // (c+1)^2 row groups (generic rows and row pairs) per half block
   int RS;         // row stride in complex elements
-  int nthr;       // nh^2: threads (orbits) per row group
+  int nthr;       // nh^2: output orbits (threads per row share)
 };
 
 inline Layout make_layout(int N) {
   Layout L;
   L.N = N; L.NN = N * N; L.c = N / 2; L.nh = L.c + 1;
-  L.nrowG = 2 * L.c * L.c;
-  L.nrep = 2 * L.c + 1;
-  L.nrow = 2 * L.nh * L.nh;
+  L.nrowG = L.c * (L.c + 1);
+  L.nrep = L.c + 1;
+  L.nrow = L.nrowG + 2 * L.nrep;
+  L.ngrp = L.nrowG + L.nrep;
   L.RS = (L.NN + 1) & ~1;
   L.nthr = L.nh * L.nh;
   return L;
 }
+
+// Row-group flags (MacParams::rowF): bits 0-3 conjugate operand j, bits 4-7
+// zero operand j when the receiving frequency pair is self-paired (u = u*),
+// bits 8-11 operand j always zero, bit 12 the group also feeds the other
+// frequency pair of its quad through the transpose.
+constexpr int kRowTransposable = 1 << 12;
 
 // ----------------------------------------------------------------------------
 // Runtime division by an invariant divisor d (1 <= d < 2^16) for n < 2^16:
@@ -169,9 +188,10 @@ struct ResampleParams {     // bilinear resample of img [H][W] at yq [ny] x xq [
 
 struct MacParams {
   Layout L;
-  int f, fh, fq, nkp;       // transform size, f/2+1, f/2+1, fq*fq
+  int f, fh, fq, nkp;       // transform size, f/2+1, f/2+1, fq*fq half blocks per plane
+  int nquads;               // fq(fq+1)/2 frequency quads (grid.x)
   int T;                    // frames in this launch (<= template TF)
-  const float2 *P;          // packed matrices [plane][nkp][nrow][RS]
+  const float2 *P;          // packed matrices [plane][half block][nrow][RS]
   const int *planes;        // plane id per z index
   int nz;                   // planes in the list
   int zgroup;               // forward: planes per CTA group
@@ -180,7 +200,10 @@ struct MacParams {
   float2 *O;                // output spectra
   int nzo;                  // forward: number of z groups (output sets); backward: nz
   int nzo_grid;             // grid.y: number of z groups of this launch
-  const short4 *rowS;       // per-row S gather indices into [su | ss]
+  const short4 *rowS;       // [2][ngrp]: operand channels of each row group for its own frequency
+                            // pair (use 0) and through the transpose (use 1); + NN: at u*
+  const short *rowF;        // [2][ngrp]: operand flags (kRowTransposable, conj / zero bits)
+  const short4 *oslots;     // [2][nthr]: an orbit's four virtual slots, own and transposed
   const short *slotcol;     // slot -> output channel
   int stages;               // shared-memory ring stages of the bulk-copy pipeline
   int chunk_rows;           // stored rows per stage (even)
@@ -199,14 +222,14 @@ struct BuildKParams {       // lenslet-grid kernels K_iq for the precompute
 
 struct PackParams {
   Layout L;
-  int f, fh, fq, nkp;
+  int f, fh, fq, nkp;       // nkp = fq * fq frequency pairs (half blocks)
   const void *spec;         // Complex<Real> [nrep_chunk][NN][f][fh]
   int rep0, nrep_chunk;
   const int *rep_row;       // packed row of representative (first row)
-  const int *rep_kind;      // 0 generic, 1 cc, 2 cr, 3 ctr
+  const int *rep_kind;      // 0 generic row, otherwise a row pair (u, u*)
   const int *rep_ch;
   const short *col_slot;    // channel -> slot
-  float2 *P;                // this plane's packed block [nkp][nrow][RS]
+  float2 *P;                // this plane's packed blocks [fq * fq][nrow][RS]
   double scale;             // 1/f^2
   int fp64;
 };

@@ -287,31 +287,32 @@ __device__ __forceinline__ f2x pk(float lo, float hi) { return make_float2(lo, h
 __device__ __forceinline__ float2 unpk(f2x v) { return v; }
 __device__ __forceinline__ void ffma2(f2x &acc, f2x a, f2x b) { acc = __ffma2_rn(a, b, acc); }
 
-// Per stored row, the input spectra enter as four packed operand pairs
+// Per row group, the input spectra enter as four packed operand pairs
 // (A_j, B_j), j = 0..3.  Each complex accumulator is kept as two lane pairs
 // P and Q with value (P.x - Q.y, P.y + Q.x), so that with t = (t.x, t.y)
 //   acc += t * s        is  P = fma2(t, (s.x, s.x)), Q = fma2(t, (s.y, s.y))
 //   acc += conj(t) * s  is  P = fma2(t, (s.x,-s.x)), Q = fma2(t, (s.y,-s.y))
-// and no lane swap of t is needed.  sv[tf][row][j] = float4(A_j, B_j); built
-// from comb once per plane.
-__device__ void build_sv(float4 *sv, const float2 *comb, const short4 *rowS, const Layout &L, int TF) {
-  const int nrowT = L.nrowG + L.nrep, NN2 = 2 * L.NN;
-  for (int idx = threadIdx.x; idx < TF * nrowT * 4; idx += blockDim.x) {
+// and no lane swap of t is needed.  sv[tf][side][use][group][j] = float4(A_j, B_j)
+// for the threads of frequency pair `side` reading a group of their own half
+// block (use 0) or of the other half block through the transpose (use 1);
+// built from comb once per plane.  An operand is zero where its flags say so,
+// or where the receiving pair is self-paired (u = u*) and the term would be
+// counted twice.
+__device__ void build_sv(float4 *sv, const float2 *comb, const short4 *rowS, const short *rowF, const Layout &L,
+                         int TF, bool selfp0, bool selfp1) {
+  const int G = L.ngrp, NN2 = 2 * L.NN;
+  for (int idx = threadIdx.x; idx < TF * 4 * G * 4; idx += blockDim.x) {
     const int j = idx & 3;
-    const int r = (idx >> 2) % nrowT;
-    const int tf = (idx >> 2) / nrowT;
-    const short4 si = rowS[r];
+    const int g = (idx >> 2) % G;
+    const int su = ((idx >> 2) / G) & 3;          // side * 2 + use
+    const int tf = (idx >> 2) / (4 * G);
+    const int side = su >> 1, use = su & 1;
+    const short4 si = rowS[use * G + g];
+    const int fl = rowF[use * G + g];
     const int ci = (j == 0) ? si.x : (j == 1) ? si.y : (j == 2) ? si.z : si.w;
-    bool conj = false, zero = false;
-    if (r < L.nrowG) {
-      conj = (j & 1);                          // s1, s3 multiply conjugated rows
-    } else {
-      const int k2 = r - L.nrowG;
-      const int rk = (k2 < L.c) ? 1 : ((k2 < 2 * L.c) ? 2 : 3);
-      if (rk == 2) conj = (j >= 2);
-      if (rk == 3 && j >= 2) zero = true;
-    }
-    const float2 sc = zero ? make_float2(0.f, 0.f) : comb[tf * NN2 + ci];
+    const bool conj = (fl >> j) & 1;
+    const bool zero = ((fl >> (8 + j)) & 1) || ((side ? selfp1 : selfp0) && ((fl >> (4 + j)) & 1));
+    const float2 sc = zero ? make_float2(0.f, 0.f) : comb[(tf * 2 + side) * NN2 + ci];
     sv[idx] = conj ? make_float4(sc.x, -sc.x, sc.y, -sc.y) : make_float4(sc.x, sc.x, sc.y, sc.y);
   }
 }
@@ -403,36 +404,41 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Stage the input spectra of plane slot `zs` at frequencies u and u* into
-// shared memory: comb[t][i] = S_i[u], comb[t][NN + i] = S_i[u*].
-__device__ __forceinline__ void stage_comb(float2 *comb, const MacParams &p, int TF, int zs, int uy,
-                                           int us, int ux) {
+// Stage the input spectra of plane slot `zs` at the four frequencies of the
+// quad into shared memory: comb[t][side][i] = S_i[u_side], comb[t][side][NN + i]
+// = S_i[u_side*], with u_0 = (uy, ux), u_1 = (ux, uy) (rows py, ps; column px).
+__device__ __forceinline__ void stage_comb(float2 *comb, const MacParams &p, int TF, int zs, int uy, int ux) {
+  const int us = uy ? p.f - uy : 0, vs = ux ? p.f - ux : 0;
   const int NN = p.L.NN, ffh = p.f * p.fh;
-  for (int idx = threadIdx.x; idx < TF * NN; idx += blockDim.x) {
-    const int t = idx / NN, i = idx % NN;
+  for (int idx = threadIdx.x; idx < TF * 2 * NN; idx += blockDim.x) {
+    const int i = idx % NN;
+    const int side = (idx / NN) & 1;
+    const int t = idx / (2 * NN);
+    float2 *dst = comb + (t * 2 + side) * 2 * NN;
     if (t < p.T) {
       const float2 *sb = p.S + ((long long)(t * p.nzS + zs) * NN + i) * ffh;
-      cp_async8(comb + t * 2 * NN + i, sb + uy * p.fh + ux);
-      cp_async8(comb + t * 2 * NN + NN + i, sb + us * p.fh + ux);
+      const int fy = side ? ux : uy, fys = side ? vs : us, fx = side ? uy : ux;
+      cp_async8(dst + i, sb + fy * p.fh + fx);
+      cp_async8(dst + NN + i, sb + fys * p.fh + fx);
     } else {
-      comb[t * 2 * NN + i] = make_float2(0.f, 0.f);
-      comb[t * 2 * NN + NN + i] = make_float2(0.f, 0.f);
+      dst[i] = make_float2(0.f, 0.f);
+      dst[NN + i] = make_float2(0.f, 0.f);
     }
   }
   cp_async_commit();
 }
 
 // Shared memory of k_mac: ring | sv | scratch (comb staging, later the
-// row-split reduction) | rowS | mbarriers.
+// share and side reduction) | rowS | rowF | mbarriers.
 __host__ __device__ inline size_t mac_scratch_elems(const Layout &L, int TF, int split, bool fwd) {
-  const size_t comb = (size_t)(fwd ? 2 : 1) * TF * 2 * L.NN;               // float2
-  const size_t red = (size_t)(split - 1) * ((L.nthr + 31) / 32 * 32) * 8 * TF;  // f2x = 8 B
+  const size_t comb = (size_t)(fwd ? 2 : 1) * TF * 2 * 2 * L.NN;                    // float2
+  const size_t red = (size_t)(2 * split - 1) * ((L.nthr + 31) / 32 * 32) * 8 * TF;   // f2x = 8 B
   return comb > red ? comb : red;
 }
 
 size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int split, bool fwd) {
   return sizeof(float2) * ((size_t)stages * chunk_rows * L.RS + mac_scratch_elems(L, TF, split, fwd)) +
-         sizeof(float4) * (size_t)TF * (L.nrowG + L.nrep) * 4 + sizeof(short4) * (L.nrowG + L.nrep) +
+         sizeof(float4) * (size_t)TF * 4 * L.ngrp * 4 + sizeof(short4) * 2 * L.ngrp + sizeof(short) * 2 * L.ngrp +
          2 * sizeof(unsigned long long) * stages + 16;
 }
 
@@ -441,21 +447,27 @@ size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int s
 // budget is sized for.
 template <int TF, bool WIDE> struct MacOcc {
   static constexpr int threads = WIDE ? 256 : 128;
-  static constexpr int v = WIDE ? (TF == 1 ? 2 : 1) : (TF == 1 ? 5 : (TF == 2 ? 3 : 2));
+  static constexpr int v = WIDE ? (TF == 1 ? 2 : 1) : (TF == 1 ? 4 : (TF == 2 ? 3 : 2));
 };
 
-// One CTA = one frequency pair and a group of planes.  Thread (h, o) owns the
-// mirror orbit o of output channels for the rows of its share h (rows are
-// dealt round-robin to the `split` threads of an orbit; their partial sums
-// are added through shared memory when a plane's output is due), so there is
-// no atomic and every output is written by exactly one thread.
+// One CTA = one frequency quad {(uy, ux), (ux, uy)} and a group of planes.
+// The threads form two sides, one per frequency pair of the quad; thread
+// (side, h, o) owns the mirror orbit o of output channels at its pair's
+// frequencies u and u* for the rows of its share h (rows are dealt round-robin
+// to the `split` threads of an orbit).  Every stored row of the quad's half
+// blocks streams through shared memory once and feeds both sides: the side it
+// belongs to through the thread's own orbit slots, and (for transposable
+// groups) the other side through the slots of the transposed orbit, since
+// T_{Tr i, Tr j}[(uy, ux)] = T_ij[(ux, uy)].  Shares (and, for a diagonal quad,
+// whose two sides are the same pair, the sides) are added through shared
+// memory when a plane's output is due, so there is no atomic and every output
+// is written by exactly one thread.
 // The stored rows stream through a ring of shared-memory stages filled by
-// bulk copies (thread 0 issues them `stages-1` chunks ahead, crossing plane
-// boundaries); consumers read their orbit's slots with shared loads.
-// Forward projection accumulates the planes of the group (the group sums are
-// added by the inverse transform); back projection writes each plane's
-// spectra when the plane is done.  The spectra of the next plane are staged
-// with cp.async while the current plane streams.
+// bulk copies (crossing plane boundaries).  Forward projection accumulates the
+// planes of the group (the group sums are added by the inverse transform);
+// back projection writes each plane's spectra when the plane is done.  The
+// spectra of the next plane are staged with cp.async while the current plane
+// streams.
 template <int TF, bool FWD, bool WIDE>
 __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v) k_mac(MacParams p) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -464,16 +476,17 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   __shared__ int s_plane[kMacMaxZgroup];        // plane slots of this CTA's z range
   volatile int *abortf = &s_abort;
   const Layout &L = p.L;
-  const int NN = L.NN, NT = L.nthr, c = L.c, c2 = c * c, RS = L.RS, NN2 = 2 * L.NN;
+  const int NN = L.NN, NT = L.nthr, RS = L.RS, NN2 = 2 * L.NN, G = L.ngrp, c = L.c;
   const int CH = p.chunk_rows, NST = p.stages, H = p.split;
   const int NTP = (NT + 31) / 32 * 32;
-  const int nrowT = L.nrowG + L.nrep;
   float2 *ring = reinterpret_cast<float2 *>(smraw);                          // [NST][CH*RS]
-  float4 *sv = reinterpret_cast<float4 *>(ring + (size_t)NST * CH * RS);     // [TF][nrowT][4]
-  float2 *scratch = reinterpret_cast<float2 *>(sv + TF * nrowT * 4);        // comb [1|2][TF][2NN] / red
-  f2x *red = reinterpret_cast<f2x *>(scratch);                              // [H-1][NTP][TF][8]
+  float4 *sv = reinterpret_cast<float4 *>(ring + (size_t)NST * CH * RS);     // [TF][2][2][G][4]
+  float2 *scratch = reinterpret_cast<float2 *>(sv + TF * 4 * G * 4);        // comb [1|2][TF][2][2NN] / red
+  f2x *red = reinterpret_cast<f2x *>(scratch);                              // [2H-1][NTP][TF][8]
   short4 *rowS = reinterpret_cast<short4 *>(scratch + mac_scratch_elems(L, TF, H, FWD));
-  unsigned long long *full = reinterpret_cast<unsigned long long *>(rowS + nrowT);
+  short *rowF = reinterpret_cast<short *>(rowS + 2 * G);
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(
+      (reinterpret_cast<uintptr_t>(rowF + 2 * G) + 7) & ~(uintptr_t)7);
   int *released = reinterpret_cast<int *>(full + NST);   // [NST] warps done with each slot, ever
 
   const int tid = threadIdx.x;
@@ -487,49 +500,55 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
     s_issued = 0;
     fence_mbar_init();
   }
-  for (int i = tid; i < nrowT; i += blockDim.x) rowS[i] = p.rowS[i];
+  for (int i = tid; i < 2 * G; i += blockDim.x) {
+    rowS[i] = p.rowS[i];
+    rowF[i] = p.rowF[i];
+  }
   {
     const int zb = blockIdx.y * p.zgroup, nzl = min(p.zgroup, p.nz - zb);
     for (int i = tid; i < nzl; i += blockDim.x) s_plane[i] = p.planes[zb + i];
   }
 
-  const int kp = blockIdx.x;
-  const int uy = kp / p.fq, ux = kp % p.fq;
-  const int us = uy ? p.f - uy : 0;
-  const bool selfp = (us == uy);
+  // quad k = ux (ux + 1) / 2 + uy, uy <= ux
+  const int kq = blockIdx.x;
+  int ux = (int)((sqrtf(8.f * (float)kq + 1.f) - 1.f) * 0.5f);
+  while ((ux + 1) * (ux + 2) / 2 <= kq) ux++;
+  while (ux * (ux + 1) / 2 > kq) ux--;
+  const int uy = kq - ux * (ux + 1) / 2;
+  const bool diag = (uy == ux);
+  const int hb0 = 2 * kq - ux;                   // first half block of the quad
+  const int nhalf = diag ? 1 : 2;
+  const bool selfp0 = (uy == 0) || (2 * uy == p.f), selfp1 = (ux == 0) || (2 * ux == p.f);
   const int ffh = p.f * p.fh;
-  const int h = tid / NTP, o = tid - h * NTP;
+  const int HS = H * NTP;                        // threads per side
+  const int ts = tid / HS;                       // side of this thread
+  const int h = (tid - ts * HS) / NTP, o = tid - ts * HS - h * NTP;
   const bool active = o < NT;
-  const int kind = (o < c2) ? 0 : ((o < c2 + c) ? 1 : ((o < c2 + 2 * c) ? 2 : 3));
-  // slot offsets of the orbit's virtual slots in a stored row (slot-major layout)
-  int off[4];
-  if (!active) {
-    off[0] = off[1] = off[2] = off[3] = 0;
-  } else if (kind == 0) {
-    off[0] = o; off[1] = c2 + o; off[2] = 2 * c2 + o; off[3] = 3 * c2 + o;
-  } else if (kind == 1) {
-    const int j = o - c2;
-    off[0] = off[2] = 4 * c2 + j; off[1] = off[3] = 4 * c2 + c + j;
-  } else if (kind == 2) {
-    const int j = o - c2 - c;
-    off[0] = off[1] = 4 * c2 + 2 * c + j; off[2] = off[3] = 4 * c2 + 3 * c + j;
-  } else {
-    off[0] = off[1] = off[2] = off[3] = NN - 1;
+  const int kind = (o < c * c) ? 0 : ((o < c * c + c) ? 1 : ((o < c * c + 2 * c) ? 2 : 3));
+  // own and transposed virtual slots of the orbit
+  int off[4], offT[4];
+  {
+    const short4 a = p.oslots[active ? o : 0], b = p.oslots[NT + (active ? o : 0)];
+    off[0] = a.x; off[1] = a.y; off[2] = a.z; off[3] = a.w;
+    offT[0] = b.x; offT[1] = b.y; offT[2] = b.z; offT[3] = b.w;
   }
   const int ns = (kind == 0) ? 4 : ((kind == 3) ? 1 : 2);
   const int z0 = blockIdx.y * p.zgroup;
   const int z1 = min(z0 + p.zgroup, p.nz);
-  const int cpb = (L.nrow + CH - 1) / CH;            // chunks per (frequency pair, plane) block
+  const int nrq = nhalf * L.nrow;                // stored rows of the quad per plane
+  const int cpb = (nrq + CH - 1) / CH;           // chunks per (quad, plane)
   const int total = (z1 - z0) * cpb;
-  const size_t blockElems = (size_t)L.nrow * RS;
+  const size_t halfElems = (size_t)L.nrow * RS;
+  const int combStride = TF * 2 * NN2;           // one plane's staged spectra (float2)
+  const int svs = 4 * G * 4;                     // sv stride between frames (float4)
 
   MacAcc<TF> acc;
   acc.zero();
 
-  stage_comb(scratch, p, TF, FWD ? z0 : 0, uy, us, ux);
+  stage_comb(scratch, p, TF, FWD ? z0 : 0, uy, ux);
   cp_async_wait_all();
-  __syncthreads();   // barriers initialised, rowS and first spectra staged
-  build_sv(sv, scratch, rowS, L, TF);
+  __syncthreads();   // barriers initialised, row tables and first spectra staged
+  build_sv(sv, scratch, rowS, rowF, L, TF, selfp0, selfp1);
   __syncthreads();   // (back projection: the staging area is free for the reduction)
 
   // Chunk g goes to ring slot g % NST.  Thread 0 fills the whole ring; after
@@ -539,8 +558,8 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   auto issue = [&](int gn) {
     const int zl_n = gn / cpb, ch_n = gn - zl_n * cpb, sl = gn % NST;
     const int r0 = ch_n * CH;
-    const int nr = min(CH, L.nrow - r0);
-    const float2 *src = p.P + ((long long)s_plane[zl_n] * p.nkp + kp) * (long long)blockElems + (long long)r0 * RS;
+    const int nr = min(CH, nrq - r0);
+    const float2 *src = p.P + ((long long)s_plane[zl_n] * p.nkp + hb0) * (long long)halfElems + (long long)r0 * RS;
     const unsigned bytes = (unsigned)(nr * RS * sizeof(float2));
     mbar_arrive_expect_tx(full + sl, bytes);
     bulk_g2s(ring + (size_t)sl * CH * RS, src, bytes, full + sl);
@@ -560,10 +579,10 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
       if (zl > 0) {
         cp_async_wait_all();
         __syncthreads();   // spectra of plane zi staged; all threads done with plane zi-1
-        build_sv(sv, scratch + (zl & 1) * TF * NN2, rowS, L, TF);
+        build_sv(sv, scratch + (zl & 1) * combStride, rowS, rowF, L, TF, selfp0, selfp1);
         __syncthreads();
       }
-      if (zi + 1 < z1) stage_comb(scratch + ((zl + 1) & 1) * TF * NN2, p, TF, zi + 1, uy, us, ux);
+      if (zi + 1 < z1) stage_comb(scratch + ((zl + 1) & 1) * combStride, p, TF, zi + 1, uy, ux);
     }
     if (*abortf) dead = true;
     if (!dead && !mbar_wait(full + slot, round & 1, kWaitLimitNs)) {
@@ -573,25 +592,43 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
     }
     if (!dead && active) {
       const int r0 = ch * CH;
-      const int r1 = min(L.nrow, r0 + CH);
+      const int r1 = min(nrq, r0 + CH);
       const float2 *stage = ring + (size_t)slot * CH * RS;
-      const int rg = min(r1, L.nrowG);
-      const int svs = nrowT * 4;
+      // the chunk's rows, one half block at a time
+      for (int bs = r0 / L.nrow; bs * L.nrow < r1; bs++) {
+        const int base = bs * L.nrow;
+        const int lo = max(r0, base) - base, hi = min(r1, base + L.nrow) - base;   // half-block rows
+        const int use = (bs == ts) ? 0 : 1;       // warp-uniform: a side is whole warps
+        const float4 *svb = sv + (ts * 2 + use) * G * 4;
+        const float2 *srow = stage + (base - r0) * RS;
+        const int rg = min(hi, L.nrowG);
 #pragma unroll 2
-      for (int r = r0 + h; r < rg; r += H) {
-        float2 t[4];
-        load_slots(stage + (size_t)(r - r0) * RS, off, t);
-        mac_generic_row<TF>(t, sv + r * 4, svs, acc);
-      }
-      // centre-cross row pairs of this chunk, dealt round-robin over the split
-      const int pr0 = max(r0, L.nrowG);
-      for (int r = pr0 + 2 * h; r < r1; r += 2 * H) {
-        const int k2 = (r - L.nrowG) >> 1;
-        float2 t[4], s2[4];
-        load_slots(stage + (size_t)(r - r0) * RS, off, t);
-        load_slots(stage + (size_t)(r + 1 - r0) * RS, off, s2);
-        const int rk = (k2 < c) ? 1 : ((k2 < 2 * c) ? 2 : 3);
-        mac_pair_rows<TF>(t, s2, rk, sv + (L.nrowG + k2) * 4, svs, acc);
+        for (int r = lo + h; r < rg; r += H) {
+          if (use && !(rowF[G + r] & kRowTransposable)) continue;
+          float2 t[4];
+          if (use) load_slots(srow + (size_t)r * RS, offT, t);
+          else load_slots(srow + (size_t)r * RS, off, t);
+          mac_generic_row<TF>(t, svb + r * 4, svs, acc);
+        }
+        // row pairs of this chunk, dealt round-robin over the split
+        const int pr0 = max(lo, L.nrowG);
+        for (int r = pr0 + 2 * h; r < hi; r += 2 * H) {
+          const int k2 = (r - L.nrowG) >> 1;
+          int rk = (k2 < c) ? 1 : 3;
+          if (use) {
+            if (rk == 3) continue;
+            rk = 2;                               // a (b, c) pair read as its transpose (c, b)
+          }
+          float2 t[4], s2[4];
+          if (use) {
+            load_slots(srow + (size_t)r * RS, offT, t);
+            load_slots(srow + (size_t)(r + 1) * RS, offT, s2);
+          } else {
+            load_slots(srow + (size_t)r * RS, off, t);
+            load_slots(srow + (size_t)(r + 1) * RS, off, s2);
+          }
+          mac_pair_rows<TF>(t, s2, rk, svb + (L.nrowG + k2) * 4, svs, acc);
+        }
       }
     }
     __syncwarp();
@@ -616,21 +653,25 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
           U[tf][k] = pq_value(acc.UP[tf][k], acc.UQ[tf][k]);
           V[tf][k] = pq_value(acc.VP[tf][k], acc.VQ[tf][k]);
         }
-      if (H > 1) {
-        // add the partial sums of the other row shares into share 0
+      // writers: share 0 of each side, or of side 0 only for a diagonal quad
+      // (its two sides are the same frequency pair); the others add into them
+      const bool writer = (h == 0) && (!diag || ts == 0);
+      if (H > 1 || diag) {
         if (FWD) cp_async_wait_all();   // the staging area doubles as reduction buffer
         __syncthreads();
-        if (h > 0 && active) {
-          f2x *rp = red + ((size_t)(h - 1) * NTP + o) * TF * 8;
+        if (!writer && active) {
+          const int idx = diag ? ts * H + h - 1 : ts * (H - 1) + h - 1;
+          f2x *rp = red + ((size_t)idx * NTP + o) * TF * 8;
 #pragma unroll
           for (int tf = 0; tf < TF; tf++)
 #pragma unroll
             for (int k = 0; k < 4; k++) { rp[tf * 8 + k] = U[tf][k]; rp[tf * 8 + 4 + k] = V[tf][k]; }
         }
         __syncthreads();
-        if (h == 0 && active) {
-          for (int hh = 1; hh < H; hh++) {
-            const f2x *rp = red + ((size_t)(hh - 1) * NTP + o) * TF * 8;
+        if (writer && active) {
+          const int n0 = diag ? 0 : ts * (H - 1), n1 = diag ? 2 * H - 1 : n0 + H - 1;
+          for (int idx = n0; idx < n1; idx++) {
+            const f2x *rp = red + ((size_t)idx * NTP + o) * TF * 8;
 #pragma unroll
             for (int tf = 0; tf < TF; tf++)
 #pragma unroll
@@ -643,7 +684,10 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
           }
         }
       }
-      if (h == 0 && active && !dead) {
+      if (writer && active && !dead) {
+        const int oy = ts ? ux : uy, ox = ts ? uy : ux;
+        const int osy = oy ? p.f - oy : 0;
+        const bool sp = ts ? selfp1 : selfp0;
 #pragma unroll
         for (int tf = 0; tf < TF; tf++) {
           if (tf >= p.T) break;
@@ -663,18 +707,18 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
 #pragma unroll
               for (int m = 1; m < 4; m++)
                 if (m == vk) { u = unpk(U[tf][m]); v = unpk(V[tf][m]); }
-              if (selfp) {
-                op[uy * p.fh + ux] = make_float2(u.x + v.x, u.y + v.y);
+              if (sp) {
+                op[oy * p.fh + ox] = make_float2(u.x + v.x, u.y + v.y);
               } else {
-                op[uy * p.fh + ux] = u;
-                op[us * p.fh + ux] = v;
+                op[oy * p.fh + ox] = u;
+                op[osy * p.fh + ox] = v;
               }
             }
           }
         }
       }
       acc.zero();
-      if (H > 1) __syncthreads();   // the reduction buffer is free again
+      if (H > 1 || diag) __syncthreads();   // the reduction buffer is free again
     }
     if (++ch == cpb) { ch = 0; zl++; }
     if (++slot == NST) { slot = 0; round++; }
@@ -724,6 +768,9 @@ __global__ void k_build_k(BuildKParams p) {
   }
 }
 
+// Packed matrices of a chunk of representatives: the value of frequency pair
+// (py, px) goes to its half block (quad (py, px) side 0 when py <= px, quad
+// (px, py) side 1 otherwise); a row pair also stores the row at (f - py, px).
 template <typename R>
 __global__ void k_pack(PackParams p) {
   typedef typename CT<R>::T C;
@@ -736,25 +783,22 @@ __global__ void k_pack(PackParams p) {
     const long long r2 = idx / NN;
     const int rl = (int)(r2 % p.nrep_chunk);
     const int kp = (int)(r2 / p.nrep_chunk);
-    const int uy = kp / p.fq, ux = kp % p.fq;
-    const int us = uy ? p.f - uy : 0;
-    const bool selfp = (us == uy);
+    const int fy = kp / p.fq, fx = kp % p.fq;       // frequency pair (fy, fx)
+    const int lo = min(fy, fx), hi = max(fy, fx);
+    const int hb = 2 * (hi * (hi + 1) / 2 + lo) - hi + (fy > fx ? 1 : 0);
+    const int fs = fy ? p.f - fy : 0;
     const int rep = p.rep0 + rl;
     const int kind = p.rep_kind[rep];
     const int row = p.rep_row[rep];
-    const int ch = p.rep_ch[rep];
     const C *sp = reinterpret_cast<const C *>(p.spec) + ((long long)rl * NN + q) * ffh;
     const int slot = p.col_slot[q];
-    float2 *dst = p.P + ((long long)kp * L.nrow + row) * L.RS + slot;
+    float2 *dst = p.P + ((long long)hb * L.nrow + row) * L.RS + slot;
     const R sc = (R)p.scale;
-    const C a = sp[uy * p.fh + ux];
-    if (kind == 0) {
-      const bool zero = selfp && ((ch % L.N) > L.c);
-      dst[0] = zero ? make_float2(0.f, 0.f) : make_float2((float)(a.x * sc), (float)(a.y * sc));
-    } else {
-      dst[0] = make_float2((float)(a.x * sc), (float)(a.y * sc));
-      const C b = sp[us * p.fh + ux];
-      dst[L.RS] = selfp ? make_float2(0.f, 0.f) : make_float2((float)(b.x * sc), (float)(b.y * sc));
+    const C a = sp[fy * p.fh + fx];
+    dst[0] = make_float2((float)(a.x * sc), (float)(a.y * sc));
+    if (kind != 0) {
+      const C b = sp[fs * p.fh + fx];
+      dst[L.RS] = make_float2((float)(b.x * sc), (float)(b.y * sc));
     }
   }
 }
@@ -964,8 +1008,8 @@ int mac_max_frames() { return 4; }
 template <int TF>
 static cudaError_t launch_mac_tf(const MacParams &p, bool fwd, cudaStream_t s) {
   const size_t sm = mac_smem_bytes(p.L, TF, p.stages, p.chunk_rows, p.split, fwd);
-  dim3 grid(p.nkp, p.nzo_grid);
-  const int block = p.split * (((p.L.nthr + 31) / 32) * 32);
+  dim3 grid(p.nquads, p.nzo_grid);
+  const int block = 2 * p.split * (((p.L.nthr + 31) / 32) * 32);
   const void *fn = block <= 128 ? (fwd ? (const void *)k_mac<TF, true, false> : (const void *)k_mac<TF, false, false>)
                                 : (fwd ? (const void *)k_mac<TF, true, true> : (const void *)k_mac<TF, false, true>);
   cudaError_t e = set_smem(fn, sm);

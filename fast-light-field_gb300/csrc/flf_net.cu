@@ -1683,7 +1683,8 @@ cudaError_t launch_conv3d_wgrad(WgradParams p, long long ws_elems, cudaStream_t 
   const int tiles = (p.Ci / CM) * (p.Co / CN);
   const long long nw = 27LL * p.Ci * p.Co;
   long long chunks = (4LL * num_sms + 27 * tiles - 1) / (27 * tiles);
-  if (p.part && chunks > ws_elems / nw) chunks = ws_elems / nw;   // partial tiles must fit the workspace
+  if (!p.part) chunks = 1;                                         // no workspace: one writer per element
+  else if (chunks > ws_elems / nw) chunks = ws_elems / nw;         // partial tiles must fit the workspace
   if (chunks < 1) chunks = 1;
   long long per = (M + chunks - 1) / chunks;
   per = (per + 63) / 64 * 64;

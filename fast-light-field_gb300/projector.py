@@ -139,18 +139,11 @@ class Projector_gb300(Projector_base):
         self._shape_key = None
         return ctx
 
-    # Double-precision precompute budget for fp64_precompute=None: GB300's FP64
-    # rate is a small fraction of its FP32 rate, so large PSF sets use FP32.
-    FP64_AUTO_GFLOP = 2.0
-
     def _auto_fp64(self, hMatrix, Y, X):
-        N = hMatrix.Nnum
-        Ly, Lx = -(-Y // N), -(-X // N)
-        R = max((((hMatrix.PSFShape(cc)[0] - 1) // 2 + N - 1) // N) for cc in range(hMatrix.numZ))
-        f = max(max(Ly, Lx) + R, 2 * R + 1)
-        reps = (N * N + 1) // 2
-        gflop = 2 * hMatrix.numZ * reps * N * N * 2.5 * f * f * np.log2(max(f * f, 2)) / 1e9
-        return gflop <= self.FP64_AUTO_GFLOP
+        """fp64_precompute=None: the transfer matrices are computed in double
+        precision; the library falls back to single precision for transform sizes
+        whose double-precision FFT does not fit shared memory (f > 112)."""
+        return True
 
     def _prepare(self, ctx, Y, X, hMatrix=None):
         fp64 = self.fp64_precompute

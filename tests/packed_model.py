@@ -2,8 +2,8 @@
 
 Mirrors, index for index, what libflf.so computes: the lenslet-grid kernels
 K_iq built from the stored PSF quadrant (k_build_k), their f x f spectra,
-the packed [freq pair][row][slot] layout with zeroed duplicates (k_pack), and
-the symmetric multiply-accumulate (k_mac).  Tests compare it with the oracle
+the packed [frequency quad][row][slot] layout (k_pack), and the symmetric
+multiply-accumulate that uses the mirror and transpose symmetries (k_mac).  Tests compare it with the oracle
 so that the mathematics of the kernels is checked on the CPU.
 """
 
@@ -62,12 +62,22 @@ def kernel_image(Hred, N, i, q, f):
 
 
 def tables(N):
+    """Index tables of the packed layout.
+
+    Output side (slots of a stored row): the mirror orbits of output channels,
+    slot-major as in the kernel.  Input side (stored rows of one half block):
+    the generic orbits (b, a'), a' <= b < c, as their two rows i = (b, a') and
+    Mx i = (b, N-1-a'); then the centre-cross representatives (b, c), b < c,
+    and the centre (c, c) as row pairs (u, u*).  Orbits with a' < b and the
+    (b, c) pairs are transposable: their transposes (a', b) and (c, b) get no
+    rows of their own."""
     c = N // 2
     NN = N * N
     My = lambda i: (N - 1 - i // N) * N + i % N  # noqa: E731
     Mx = lambda i: (i // N) * N + (N - 1 - i % N)  # noqa: E731
     Mxy = lambda i: NN - 1 - i  # noqa: E731
-    slotcol, okind = [], []
+    Tr = lambda i: (i % N) * N + i // N  # noqa: E731
+    slotcol, okind, offs = [], [], []
     for be in range(c):
         for al in range(c):
             q = be * N + al
@@ -83,105 +93,164 @@ def tables(N):
         okind.append(2)
     slotcol.append(c * N + c)
     okind.append(3)
-    reps = []   # (channel, kind, first row)
+    colslot = np.empty(NN, int)
+    colslot[slotcol] = np.arange(NN)
+    # virtual slots [q, My q, Mx q, Mxy q] of every output orbit (degenerate orbits repeat)
+    s0 = 0
+    for ok in okind:
+        if ok == 0:
+            off = [s0, s0 + 1, s0 + 2, s0 + 3]
+        elif ok == 1:
+            off = [s0, s0 + 1, s0, s0 + 1]
+        elif ok == 2:
+            off = [s0, s0, s0 + 1, s0 + 1]
+        else:
+            off = [s0] * 4
+        ns = {0: 4, 1: 2, 2: 2, 3: 1}[ok]
+        offT = [int(colslot[Tr(slotcol[o])]) for o in off]
+        offs.append((off, offT, ns, ok))
+        s0 += ns
+    groups = []     # (channel, kind, first row, transposable, mx_row)
     row = 0
     for b in range(c):
-        for a in range(N):
-            if a != c:
-                reps.append((b * N + a, 0, row))
+        for ap in range(b + 1):
+            for a in (ap, N - 1 - ap):
+                groups.append((b * N + a, 0, row, ap < b, a > c))
                 row += 1
-    for k in range(2 * c + 1):
-        if k < c:
-            reps.append((k * N + c, 1, row))
-        elif k < 2 * c:
-            reps.append((c * N + (k - c), 2, row))
-        else:
-            reps.append((c * N + c, 3, row))
+    for b in range(c):
+        groups.append((b * N + c, 1, row, True, False))
         row += 2
-    return dict(slotcol=slotcol, okind=okind, reps=reps, nrow=row, My=My, Mx=Mx, Mxy=Mxy, c=c)
+    groups.append((c * N + c, 3, row, False, False))
+    row += 2
+    return dict(slotcol=slotcol, colslot=colslot, okind=okind, offs=offs, groups=groups, nrow=row,
+                My=My, Mx=Mx, Mxy=Mxy, Tr=Tr, c=c)
+
+
+def quads(fq):
+    """Frequency quads in kernel order: k -> (uy, ux), uy <= ux, ux-major; and the
+    first stored row of each (in half blocks: a diagonal quad holds one)."""
+    out = []
+    for ux in range(fq):
+        for uy in range(ux + 1):
+            k = len(out)
+            out.append((uy, ux, 2 * k - ux))
+    return out
 
 
 def packed_matrices(Hred, N, f):
-    """P[kpair, row, slot] for one plane: the layout k_pack writes (scaled by 1/f^2)."""
+    """P[half block, row, slot] for one plane: the layout k_pack writes (scaled by 1/f^2).
+
+    Quad (uy, ux), uy < ux, holds two half blocks: rows of frequency pair
+    (uy, ux) then rows of (ux, uy); a diagonal quad (uy = ux) holds one."""
     tb = tables(N)
     NN = N * N
     fq = f // 2 + 1
     P = np.zeros((fq * fq, tb["nrow"], NN), np.complex128)
-    colslot = np.empty(NN, int)
-    colslot[tb["slotcol"]] = np.arange(NN)
-    for ch, kind, row in tb["reps"]:
+    colslot = tb["colslot"]
+    for ch, kind, row, _, _ in tb["groups"]:
         spec = np.stack([np.fft.rfft2(kernel_image(Hred, N, ch, q, f)) for q in range(NN)]) / (f * f)
-        for uy in range(fq):
-            us = (-uy) % f
-            for ux in range(fq):
-                kp = uy * fq + ux
-                selfp = us == uy
-                if kind == 0:
-                    if not (selfp and ch % N > N // 2):
-                        P[kp, row, colslot] = spec[:, uy, ux]
-                else:
-                    P[kp, row, colslot] = spec[:, uy, ux]
-                    if not selfp:
-                        P[kp, row + 1, colslot] = spec[:, us, ux]
+        for uy, ux, hb in quads(fq):
+            for side, (py, px) in enumerate(((uy, ux), (ux, uy))):
+                if side == 1 and uy == ux:
+                    continue
+                ps = (-py) % f
+                P[hb + side, row, colslot] = spec[:, py, px]
+                if kind != 0:
+                    P[hb + side, row + 1, colslot] = spec[:, ps, px]
     return P
 
 
-SIG = {0: dict(y=[1, 0, 3, 2], x=[2, 3, 0, 1], xy=[3, 2, 1, 0]),
-       1: dict(y=[1, 0], x=[0, 1], xy=[1, 0]),
-       2: dict(y=[0, 1], x=[1, 0], xy=[1, 0]),
-       3: dict(y=[0], x=[0], xy=[0])}
+SIG = dict(y=[1, 0, 3, 2], x=[2, 3, 0, 1], xy=[3, 2, 1, 0])
+
+
+def _operands(tb, ch, kind, mxrow, use, recv_self):
+    """Input channels (with the frequency: 0 = u, 1 = u*) and conjugation of the
+    four operand pairs of a row group, for its own side (use 0) or the other side
+    of the quad through the transpose (use 1); zero operands where the receiving
+    frequency pair is self-paired and the term would count twice."""
+    My, Mx, Mxy, Tr = tb["My"], tb["Mx"], tb["Mxy"], tb["Tr"]
+    if use == 1:
+        ch = Tr(ch)
+    if kind == 0:
+        ops = [(ch, 0, False), (Mxy(ch), 0, True), (My(ch), 1, False), (Mx(ch), 1, True)]
+        zero = [mxrow and recv_self] * 4
+    elif kind == 1 and use == 0:
+        ops = [(ch, 0, False), (ch, 1, False), (My(ch), 1, False), (My(ch), 0, False)]
+        zero = [False, recv_self, False, recv_self]
+    elif kind == 1:     # transposed (b, c) row pair: a (c, b) channel, conjugated u* terms
+        ops = [(ch, 0, False), (ch, 1, True), (Mx(ch), 1, True), (Mx(ch), 0, False)]
+        zero = [False, recv_self, False, recv_self]
+    else:
+        ops = [(ch, 0, False), (ch, 1, False), (ch, 0, False), (ch, 0, False)]
+        zero = [False, recv_self, True, True]
+    return ops, zero
 
 
 def packed_mac(Ps, Ss, N, f):
-    """out[j, uy, ux] = sum over planes of T_z S_z, evaluated from packed matrices."""
+    """out[j, uy, ux] = sum over planes of T_z S_z, evaluated as the kernel does:
+    per quad, side-0 and side-1 threads (frequency pairs (uy, ux) and (ux, uy)),
+    each owning one output orbit, stream the quad's stored rows; a row feeds its
+    own side through the thread's orbit slots and the other side through the
+    slots of the transposed orbit (transposable rows only)."""
     tb = tables(N)
     NN = N * N
     fq = f // 2 + 1
-    My, Mx, Mxy = tb["My"], tb["Mx"], tb["Mxy"]
     out = np.zeros((NN, f, fq), np.complex128)
-    for uy in range(fq):
-        us = (-uy) % f
-        for ux in range(fq):
-            kp = uy * fq + ux
-            s0 = 0
-            accs = []
-            for ok in tb["okind"]:
-                ns = {0: 4, 1: 2, 2: 2, 3: 1}[ok]
-                accs.append((s0, ns, ok, np.zeros(ns, complex), np.zeros(ns, complex)))
-                s0 += ns
-            for P, S in zip(Ps, Ss):
-                Su, Ss_ = S[:, uy, ux], S[:, us, ux]
-                for ch, kind, row in tb["reps"]:
-                    for s0, ns, ok, U, V in accs:
-                        sg = SIG[ok]
-                        t = P[kp, row, s0:s0 + ns]
-                        if kind == 0:
-                            sv = (Su[ch], Su[Mxy(ch)], Ss_[My(ch)], Ss_[Mx(ch)])
-                            for k in range(ns):
-                                U[k] += t[k] * sv[0] + np.conj(t[sg["xy"][k]]) * sv[1]
-                                V[sg["y"][k]] += t[k] * sv[2]
-                                V[sg["x"][k]] += np.conj(t[k]) * sv[3]
-                        else:
-                            s = P[kp, row + 1, s0:s0 + ns]
-                            M = My if kind == 1 else Mx
-                            sv = (Su[ch], Ss_[ch], Ss_[M(ch)], Su[M(ch)])
-                            for k in range(ns):
-                                U[k] += t[k] * sv[0]
-                                V[k] += s[k] * sv[1]
-                                if kind == 1:
-                                    V[sg["y"][k]] += t[k] * sv[2]
-                                    U[sg["y"][k]] += s[k] * sv[3]
-                                elif kind == 2:
-                                    V[sg["x"][k]] += np.conj(t[k]) * sv[2]
-                                    U[sg["x"][k]] += np.conj(s[k]) * sv[3]
-            for s0, ns, ok, U, V in accs:
+    for uy, ux, hb in quads(fq):
+        diag = uy == ux
+        freqs = [(uy, ux), (ux, uy)]
+        selfp = [(-p[0]) % f == p[0] for p in freqs]
+        acc = [[(np.zeros(4, complex), np.zeros(4, complex)) for _ in tb["offs"]] for _ in range(2)]
+        for P, S in zip(Ps, Ss):
+            comb = [(S[:, p[0], p[1]], S[:, (-p[0]) % f, p[1]]) for p in freqs]
+            for bs in range(1 if diag else 2):
+                for ch, kind, row, trans, mxrow in tb["groups"]:
+                    for ts in range(2):
+                        use = 0 if ts == bs else 1
+                        if use == 1 and not trans:
+                            continue
+                        ops, zero = _operands(tb, ch, kind, mxrow, use, selfp[ts])
+                        sv = [0 if z else (np.conj(comb[ts][st][ci]) if False else comb[ts][st][ci])
+                              for (ci, st, cj), z in zip(ops, zero)]
+                        for o, (off, offT, ns, ok) in enumerate(tb["offs"]):
+                            sl = off if use == 0 else offT
+                            U, V = acc[ts][o]
+                            t = P[hb + bs, row, sl]
+                            cj = lambda v, k: np.conj(v) if ops[k][2] else v  # noqa: E731
+                            if kind == 0:
+                                for k in range(4):
+                                    U[k] += cj(t[k], 0) * sv[0] + cj(t[SIG["xy"][k]], 1) * sv[1]
+                                    V[SIG["y"][k]] += cj(t[k], 2) * sv[2]
+                                    V[SIG["x"][k]] += cj(t[k], 3) * sv[3]
+                            else:
+                                s = P[hb + bs, row + 1, sl]
+                                for k in range(4):
+                                    U[k] += cj(t[k], 0) * sv[0]
+                                    V[k] += cj(s[k], 1) * sv[1]
+                                    if kind == 1 and use == 0:
+                                        V[SIG["y"][k]] += cj(t[k], 2) * sv[2]
+                                        U[SIG["y"][k]] += cj(s[k], 3) * sv[3]
+                                    elif kind == 1:
+                                        V[SIG["x"][k]] += cj(t[k], 2) * sv[2]
+                                        U[SIG["x"][k]] += cj(s[k], 3) * sv[3]
+        for ts in range(2):
+            if diag and ts == 1:
+                break
+            py, px = freqs[ts]
+            ps = (-py) % f
+            for o, (off, offT, ns, ok) in enumerate(tb["offs"]):
+                U, V = acc[ts][o]
+                if diag:
+                    U = U + acc[1][o][0]
+                    V = V + acc[1][o][1]
                 for k in range(ns):
-                    q = tb["slotcol"][s0 + k]
-                    if us == uy:
-                        out[q, uy, ux] = U[k] + V[k]
+                    vk = {0: k, 1: k, 2: 2 * k, 3: 0}[ok]
+                    q = tb["slotcol"][off[vk]]
+                    if selfp[ts]:
+                        out[q, py, px] = U[vk] + V[vk]
                     else:
-                        out[q, uy, ux] = U[k]
-                        out[q, us, ux] = V[k]
+                        out[q, py, px] = U[vk]
+                        out[q, ps, px] = V[vk]
     return out
 
 

@@ -37,8 +37,21 @@ def test_packed_rows_and_slots():
         tb = M.tables(N)
         c = N // 2
         assert sorted(tb["slotcol"]) == list(range(N * N))
-        assert tb["nrow"] == 2 * (c + 1) ** 2
+        # one half block: c(c+1) generic rows, c + 1 row pairs (mirror + transpose symmetry)
+        assert tb["nrow"] == (c + 1) * (c + 2)
         assert len(tb["okind"]) == (c + 1) ** 2
+        # every input channel is a stored row, a mirror image of one, or the transpose of one
+        seen = set()
+        for ch, kind, row, trans, mx in tb["groups"]:
+            orbit = {ch, tb["My"](ch), tb["Mx"](ch), tb["Mxy"](ch)}
+            seen |= orbit
+            if trans:
+                seen |= {tb["Tr"](i) for i in orbit}
+        assert seen == set(range(N * N))
+    # stored rows per frequency pair: 72 of the 128 of the mirror-only layout at Nnum 15
+    fq = 25
+    q = M.quads(fq)
+    assert len(q) == fq * (fq + 1) // 2 and q[-1][2] + 1 == fq * fq
 
 
 def test_transform_size_rule():
