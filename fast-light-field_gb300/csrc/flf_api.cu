@@ -322,9 +322,13 @@ int build_tables(flf_ctx *ctx) {
     fl = (short)((1 << 1) | (1 << 3) | (mxrow ? 0xF0 : 0));
   };
   int row = 0, grp = 0;
+  std::vector<std::pair<int, int>> orbits;   // transposable orbits (a' < b) first, then the diagonal ones
   for (int b = 0; b < c; b++)
-    for (int ap = 0; ap <= b; ap++)
-      for (int a : {ap, N - 1 - ap}) {
+    for (int ap = 0; ap < b; ap++) orbits.push_back({b, ap});
+  for (int b = 0; b < c; b++) orbits.push_back({b, b});
+  for (const auto &ob : orbits) {
+    const int b = ob.first, ap = ob.second;
+    for (int a : {ap, N - 1 - ap}) {
         const int i = b * N + a;
         const bool trans = ap < b, mxrow = a > c;
         generic_ops(i, mxrow, rowS[grp], rowF[grp]);
@@ -336,6 +340,7 @@ int build_tables(flf_ctx *ctx) {
         ctx->rep_ch.push_back(i); ctx->rep_row.push_back(row); ctx->rep_kind.push_back(0);
         row++; grp++;
       }
+  }
   if (row != L.nrowG) return fail(ctx, FLF_E_STATE, "internal: generic row table size");
   for (int k = 0; k <= c; k++) {
     const bool centre = k == c;

@@ -49,17 +49,21 @@ struct FftPlan {
 // blocks 2k - ux and 2k - ux + 1, so a plane has fq^2 half blocks in all.
 //   P[half block][row][slot], rows = (c+1)(c+2) per half block, slot stride RS.
 // Rows of a half block: the generic input orbits (b, a'), a' <= b < c, as their
-// rows i = (b, a') and Mx i = (b, N-1-a') at u (c(c+1) rows); then row pairs
-// (u, u*) of the centre-cross representatives (b, c), b < c, and of the centre.
-// Orbits with a' < b and the (b, c) pairs also stand for their transposes
-// (a', b) and (c, b), which have no rows: a thread of the other frequency pair
-// reads them at the slots of its transposed output orbit.  Slots: output
-// channels of the mirror orbits, slot-major: the c^2 generic orbits [q, My q,
-// Mx q, Mxy q] as four blocks of c^2, the c orbits [q, My q] (alpha = c) and
-// the c orbits [q, Mx q] (beta = c) as two blocks of c each, then the centre.
+// rows i = (b, a') and Mx i = (b, N-1-a') at u (c(c+1) rows, the c(c-1) rows
+// of the orbits with a' < b first); then row pairs (u, u*) of the centre-cross
+// representatives (b, c), b < c, and of the centre.  Orbits with a' < b and the
+// (b, c) pairs also stand for their transposes (a', b) and (c, b), which have
+// no rows.  Slots: output channels of the mirror orbits, slot-major: the c^2
+// generic orbits [q, My q, Mx q, Mxy q] as four blocks of c^2, the c orbits
+// [q, My q] (alpha = c) and the c orbits [q, Mx q] (beta = c) as two blocks of
+// c each, then the centre.  The second half block of a quad keeps its columns
+// in transposed order (the slot of channel j holds channel Tr j); thread t of
+// the second frequency pair owns the transposed orbit of t, so both sides read
+// both half blocks at the slots of orbit t: consecutive for a warp.
 struct Layout {
   int N, NN, c, nh;
   int nrowG;      // c(c+1) generic rows per half block
+  int nrowGT;     // c(c-1) of them (stored first) stand for their transposes too
   int nrep;       // c+1 row pairs per half block
   int nrow;       // (c+1)(c+2) rows per half block
   int ngrp;       // (c+1)^2 row groups (generic rows and row pairs) per half block
@@ -71,6 +75,7 @@ inline Layout make_layout(int N) {
   Layout L;
   L.N = N; L.NN = N * N; L.c = N / 2; L.nh = L.c + 1;
   L.nrowG = L.c * (L.c + 1);
+  L.nrowGT = L.c * (L.c - 1);
   L.nrep = L.c + 1;
   L.nrow = L.nrowG + 2 * L.nrep;
   L.ngrp = L.nrowG + L.nrep;

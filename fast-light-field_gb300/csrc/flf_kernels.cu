@@ -335,7 +335,9 @@ __device__ __forceinline__ float2 pq_value(f2x P, f2x Q) { return make_float2(P.
 
 // One generic stored row t (input channel i at u): feeds channel i at u,
 // Mxy i at u, My i at u*, Mx i at u*.
-template <int TF>
+// SW: the thread's virtual slots are those of a transposed orbit, [r, Mx r,
+// My r, Mxy r], so the My and Mx slot permutations trade places.
+template <int TF, bool SW>
 __device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const float4 *svr, int svstride,
                                                 MacAcc<TF> &a) {
 #pragma unroll
@@ -350,16 +352,16 @@ __device__ __forceinline__ void mac_generic_row(const float2 (&t)[4], const floa
       ffma2(a.UQ[tf][k], t[k], B0);
       ffma2(a.UP[tf][k], t[sxy(k)], A1);
       ffma2(a.UQ[tf][k], t[sxy(k)], B1);
-      ffma2(a.VP[tf][sy(k)], t[k], A2);
-      ffma2(a.VQ[tf][sy(k)], t[k], B2);
-      ffma2(a.VP[tf][sx(k)], t[k], A3);
-      ffma2(a.VQ[tf][sx(k)], t[k], B3);
+      ffma2(a.VP[tf][SW ? sx(k) : sy(k)], t[k], A2);
+      ffma2(a.VQ[tf][SW ? sx(k) : sy(k)], t[k], B2);
+      ffma2(a.VP[tf][SW ? sy(k) : sx(k)], t[k], A3);
+      ffma2(a.VQ[tf][SW ? sy(k) : sx(k)], t[k], B3);
     }
   }
 }
 
 // A centre-cross row pair (t at u, s at u*) of representative kind rk.
-template <int TF>
+template <int TF, bool SW>
 __device__ __forceinline__ void mac_pair_rows(const float2 (&t)[4], const float2 (&s)[4], int rk,
                                               const float4 *svr, int svstride, MacAcc<TF> &a) {
 #pragma unroll
@@ -376,7 +378,7 @@ __device__ __forceinline__ void mac_pair_rows(const float2 (&t)[4], const float2
     if (rk != 3) {
       const float4 q2 = svr[tf * svstride + 2], q3 = svr[tf * svstride + 3];
       const f2x A2 = pk(q2.x, q2.y), B2 = pk(q2.z, q2.w), A3 = pk(q3.x, q3.y), B3 = pk(q3.z, q3.w);
-      if (rk == 1) {
+      if ((rk == 1) != SW) {   // My partner (rk 1) or Mx partner (rk 2), in this thread's slot order
 #pragma unroll
         for (int k = 0; k < 4; k++) {
           ffma2(a.VP[tf][sy(k)], t[k], A2);
@@ -525,12 +527,12 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   const int h = (tid - ts * HS) / NTP, o = tid - ts * HS - h * NTP;
   const bool active = o < NT;
   const int kind = (o < c * c) ? 0 : ((o < c * c + c) ? 1 : ((o < c * c + 2 * c) ? 2 : 3));
-  // own and transposed virtual slots of the orbit
-  int off[4], offT[4];
+  // virtual slots of orbit o: every half block is read at these (side 1 owns
+  // the transposed orbit, its half block is stored in transposed column order)
+  int off[4];
   {
-    const short4 a = p.oslots[active ? o : 0], b = p.oslots[NT + (active ? o : 0)];
+    const short4 a = p.oslots[active ? o : 0];
     off[0] = a.x; off[1] = a.y; off[2] = a.z; off[3] = a.w;
-    offT[0] = b.x; offT[1] = b.y; offT[2] = b.z; offT[3] = b.w;
   }
   const int ns = (kind == 0) ? 4 : ((kind == 3) ? 1 : 2);
   const int z0 = blockIdx.y * p.zgroup;
@@ -601,33 +603,38 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
         const int use = (bs == ts) ? 0 : 1;       // warp-uniform: a side is whole warps
         const float4 *svb = sv + (ts * 2 + use) * G * 4;
         const float2 *srow = stage + (base - r0) * RS;
-        const int rg = min(hi, L.nrowG);
-#pragma unroll 2
-        for (int r = lo + h; r < rg; r += H) {
-          if (use && !(rowF[G + r] & kRowTransposable)) continue;
-          float2 t[4];
-          if (use) load_slots(srow + (size_t)r * RS, offT, t);
-          else load_slots(srow + (size_t)r * RS, off, t);
-          mac_generic_row<TF>(t, svb + r * 4, svs, acc);
-        }
-        // row pairs of this chunk, dealt round-robin over the split
+        // generic rows (through the transpose only the first nrowGT), then row pairs
+        const int rg = min(hi, use ? L.nrowGT : L.nrowG);
+        const int pr1 = min(hi, use ? L.nrowG + 2 * c : L.nrow);
         const int pr0 = max(lo, L.nrowG);
-        for (int r = pr0 + 2 * h; r < hi; r += 2 * H) {
-          const int k2 = (r - L.nrowG) >> 1;
-          int rk = (k2 < c) ? 1 : 3;
-          if (use) {
-            if (rk == 3) continue;
-            rk = 2;                               // a (b, c) pair read as its transpose (c, b)
+        if (ts == 0) {
+#pragma unroll 2
+          for (int r = lo + h; r < rg; r += H) {
+            float2 t[4];
+            load_slots(srow + (size_t)r * RS, off, t);
+            mac_generic_row<TF, false>(t, svb + r * 4, svs, acc);
           }
-          float2 t[4], s2[4];
-          if (use) {
-            load_slots(srow + (size_t)r * RS, offT, t);
-            load_slots(srow + (size_t)(r + 1) * RS, offT, s2);
-          } else {
+          for (int r = pr0 + 2 * h; r < pr1; r += 2 * H) {
+            const int k2 = (r - L.nrowG) >> 1;
+            float2 t[4], s2[4];
             load_slots(srow + (size_t)r * RS, off, t);
             load_slots(srow + (size_t)(r + 1) * RS, off, s2);
+            mac_pair_rows<TF, false>(t, s2, use ? 2 : ((k2 < c) ? 1 : 3), svb + (L.nrowG + k2) * 4, svs, acc);
           }
-          mac_pair_rows<TF>(t, s2, rk, svb + (L.nrowG + k2) * 4, svs, acc);
+        } else {
+#pragma unroll 2
+          for (int r = lo + h; r < rg; r += H) {
+            float2 t[4];
+            load_slots(srow + (size_t)r * RS, off, t);
+            mac_generic_row<TF, true>(t, svb + r * 4, svs, acc);
+          }
+          for (int r = pr0 + 2 * h; r < pr1; r += 2 * H) {
+            const int k2 = (r - L.nrowG) >> 1;
+            float2 t[4], s2[4];
+            load_slots(srow + (size_t)r * RS, off, t);
+            load_slots(srow + (size_t)(r + 1) * RS, off, s2);
+            mac_pair_rows<TF, true>(t, s2, use ? 2 : ((k2 < c) ? 1 : 3), svb + (L.nrowG + k2) * 4, svs, acc);
+          }
         }
       }
     }
@@ -661,11 +668,22 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
         __syncthreads();
         if (!writer && active) {
           const int idx = diag ? ts * H + h - 1 : ts * (H - 1) + h - 1;
-          f2x *rp = red + ((size_t)idx * NTP + o) * TF * 8;
+          // in a diagonal quad, side 1's orbit is the transposed orbit T(o) of side 0,
+          // with its My and Mx slots swapped
+          int ot = o;
+          if (diag && ts) {
+            const int c2 = c * c;
+            ot = (o < c2) ? (o % c) * c + o / c : ((o < c2 + c) ? o + c : ((o < c2 + 2 * c) ? o - c : o));
+          }
+          f2x *rp = red + ((size_t)idx * NTP + ot) * TF * 8;
 #pragma unroll
           for (int tf = 0; tf < TF; tf++)
 #pragma unroll
-            for (int k = 0; k < 4; k++) { rp[tf * 8 + k] = U[tf][k]; rp[tf * 8 + 4 + k] = V[tf][k]; }
+            for (int k = 0; k < 4; k++) {
+              const int kk = (diag && ts) ? ((k == 1) ? 2 : ((k == 2) ? 1 : k)) : k;
+              rp[tf * 8 + kk] = U[tf][k];
+              rp[tf * 8 + 4 + kk] = V[tf][k];
+            }
         }
         __syncthreads();
         if (writer && active) {
@@ -701,7 +719,8 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
 #pragma unroll
               for (int m = 1; m < 4; m++)
                 if (m == vk) sl = off[m];
-              const int q = p.slotcol[sl];
+              int q = p.slotcol[sl];
+              if (ts) q = (q % L.N) * L.N + q / L.N;   // side 1: the transposed channel
               float2 *op = p.O + obase + (long long)q * ffh;
               float2 u = unpk(U[tf][0]), v = unpk(V[tf][0]);
 #pragma unroll
@@ -791,7 +810,8 @@ __global__ void k_pack(PackParams p) {
     const int kind = p.rep_kind[rep];
     const int row = p.rep_row[rep];
     const C *sp = reinterpret_cast<const C *>(p.spec) + ((long long)rl * NN + q) * ffh;
-    const int slot = p.col_slot[q];
+    // the second half block of a quad holds channel Tr q at the slot of q
+    const int slot = p.col_slot[fy > fx ? (q % L.N) * L.N + q / L.N : q];
     float2 *dst = p.P + ((long long)hb * L.nrow + row) * L.RS + slot;
     const R sc = (R)p.scale;
     const C a = sp[fy * p.fh + fx];

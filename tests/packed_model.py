@@ -68,9 +68,9 @@ def tables(N):
     slot-major as in the kernel.  Input side (stored rows of one half block):
     the generic orbits (b, a'), a' <= b < c, as their two rows i = (b, a') and
     Mx i = (b, N-1-a'); then the centre-cross representatives (b, c), b < c,
-    and the centre (c, c) as row pairs (u, u*).  Orbits with a' < b and the
-    (b, c) pairs are transposable: their transposes (a', b) and (c, b) get no
-    rows of their own."""
+    and the centre (c, c) as row pairs (u, u*).  Orbits with a' < b (stored
+    first) and the (b, c) pairs are transposable: their transposes (a', b) and
+    (c, b) get no rows of their own."""
     c = N // 2
     NN = N * N
     My = lambda i: (N - 1 - i // N) * N + i % N  # noqa: E731
@@ -112,11 +112,11 @@ def tables(N):
         s0 += ns
     groups = []     # (channel, kind, first row, transposable, mx_row)
     row = 0
-    for b in range(c):
-        for ap in range(b + 1):
-            for a in (ap, N - 1 - ap):
-                groups.append((b * N + a, 0, row, ap < b, a > c))
-                row += 1
+    orbits = [(b, ap) for b in range(c) for ap in range(b)] + [(b, b) for b in range(c)]
+    for b, ap in orbits:
+        for a in (ap, N - 1 - ap):
+            groups.append((b * N + a, 0, row, ap < b, a > c))
+            row += 1
     for b in range(c):
         groups.append((b * N + c, 1, row, True, False))
         row += 2
@@ -141,12 +141,16 @@ def packed_matrices(Hred, N, f):
     """P[half block, row, slot] for one plane: the layout k_pack writes (scaled by 1/f^2).
 
     Quad (uy, ux), uy < ux, holds two half blocks: rows of frequency pair
-    (uy, ux) then rows of (ux, uy); a diagonal quad (uy = ux) holds one."""
+    (uy, ux) then rows of (ux, uy); a diagonal quad (uy = ux) holds one.  The
+    second half block keeps its columns in transposed order (the slot of output
+    channel j holds channel Tr j), so that both sides of a quad read every half
+    block at their own slots."""
     tb = tables(N)
     NN = N * N
     fq = f // 2 + 1
     P = np.zeros((fq * fq, tb["nrow"], NN), np.complex128)
     colslot = tb["colslot"]
+    colslotT = colslot[[tb["Tr"](q) for q in range(NN)]]
     for ch, kind, row, _, _ in tb["groups"]:
         spec = np.stack([np.fft.rfft2(kernel_image(Hred, N, ch, q, f)) for q in range(NN)]) / (f * f)
         for uy, ux, hb in quads(fq):
@@ -154,9 +158,10 @@ def packed_matrices(Hred, N, f):
                 if side == 1 and uy == ux:
                     continue
                 ps = (-py) % f
-                P[hb + side, row, colslot] = spec[:, py, px]
+                cs = colslotT if side else colslot
+                P[hb + side, row, cs] = spec[:, py, px]
                 if kind != 0:
-                    P[hb + side, row + 1, colslot] = spec[:, ps, px]
+                    P[hb + side, row + 1, cs] = spec[:, ps, px]
     return P
 
 
@@ -187,15 +192,22 @@ def _operands(tb, ch, kind, mxrow, use, recv_self):
 
 
 def packed_mac(Ps, Ss, N, f):
-    """out[j, uy, ux] = sum over planes of T_z S_z, evaluated as the kernel does:
-    per quad, side-0 and side-1 threads (frequency pairs (uy, ux) and (ux, uy)),
-    each owning one output orbit, stream the quad's stored rows; a row feeds its
-    own side through the thread's orbit slots and the other side through the
-    slots of the transposed orbit (transposable rows only)."""
+    """out[j, uy, ux] = sum over planes of T_z S_z, evaluated as the kernel does.
+
+    Per quad, side-0 and side-1 threads handle frequency pairs (uy, ux) and
+    (ux, uy).  Thread t of side 0 owns output orbit t (virtual slots [q, My q,
+    Mx q, Mxy q]); thread t of side 1 owns the transposed orbit, virtual slots
+    [Tr q, Tr My q, Tr Mx q, Tr Mxy q] = [r, Mx r, My r, Mxy r] (r = Tr q), so
+    its My and Mx slot permutations trade places.  Both read every row at the
+    slots of orbit t: a row feeds its own side, and transposable rows also feed
+    the other side through the transpose.  A diagonal quad adds side 1 into
+    side 0 (thread T(t), My / Mx slots swapped)."""
     tb = tables(N)
     NN = N * N
     fq = f // 2 + 1
+    Tr = tb["Tr"]
     out = np.zeros((NN, f, fq), np.complex128)
+    swap = [0, 2, 1, 3]
     for uy, ux, hb in quads(fq):
         diag = uy == ux
         freqs = [(uy, ux), (ux, uy)]
@@ -210,29 +222,39 @@ def packed_mac(Ps, Ss, N, f):
                         if use == 1 and not trans:
                             continue
                         ops, zero = _operands(tb, ch, kind, mxrow, use, selfp[ts])
-                        sv = [0 if z else (np.conj(comb[ts][st][ci]) if False else comb[ts][st][ci])
-                              for (ci, st, cj), z in zip(ops, zero)]
+                        sv = [0 if z else comb[ts][st][ci] for (ci, st, cj), z in zip(ops, zero)]
+                        sy = SIG["x"] if ts else SIG["y"]
+                        sx = SIG["y"] if ts else SIG["x"]
                         for o, (off, offT, ns, ok) in enumerate(tb["offs"]):
-                            sl = off if use == 0 else offT
                             U, V = acc[ts][o]
-                            t = P[hb + bs, row, sl]
+                            t = P[hb + bs, row, off]
                             cj = lambda v, k: np.conj(v) if ops[k][2] else v  # noqa: E731
                             if kind == 0:
                                 for k in range(4):
                                     U[k] += cj(t[k], 0) * sv[0] + cj(t[SIG["xy"][k]], 1) * sv[1]
-                                    V[SIG["y"][k]] += cj(t[k], 2) * sv[2]
-                                    V[SIG["x"][k]] += cj(t[k], 3) * sv[3]
+                                    V[sy[k]] += cj(t[k], 2) * sv[2]
+                                    V[sx[k]] += cj(t[k], 3) * sv[3]
                             else:
-                                s = P[hb + bs, row + 1, sl]
+                                s = P[hb + bs, row + 1, off]
                                 for k in range(4):
                                     U[k] += cj(t[k], 0) * sv[0]
                                     V[k] += cj(s[k], 1) * sv[1]
                                     if kind == 1 and use == 0:
-                                        V[SIG["y"][k]] += cj(t[k], 2) * sv[2]
-                                        U[SIG["y"][k]] += cj(s[k], 3) * sv[3]
+                                        V[sy[k]] += cj(t[k], 2) * sv[2]
+                                        U[sy[k]] += cj(s[k], 3) * sv[3]
                                     elif kind == 1:
-                                        V[SIG["x"][k]] += cj(t[k], 2) * sv[2]
-                                        U[SIG["x"][k]] += cj(s[k], 3) * sv[3]
+                                        V[sx[k]] += cj(t[k], 2) * sv[2]
+                                        U[sx[k]] += cj(s[k], 3) * sv[3]
+        if diag:
+            # side-1 thread t holds the transposed orbit of t, i.e. the orbit of thread T(t)
+            for o, (off, offT, ns, ok) in enumerate(tb["offs"]):
+                q = tb["slotcol"][off[0]]
+                o2 = [i for i, ent in enumerate(tb["offs"]) if tb["slotcol"][ent[0][0]] == Tr(q)][0]
+                U1, V1 = acc[1][o]
+                U0, V0 = acc[0][o2]
+                for k in range(4):
+                    U0[swap[k]] += U1[k]
+                    V0[swap[k]] += V1[k]
         for ts in range(2):
             if diag and ts == 1:
                 break
@@ -240,12 +262,11 @@ def packed_mac(Ps, Ss, N, f):
             ps = (-py) % f
             for o, (off, offT, ns, ok) in enumerate(tb["offs"]):
                 U, V = acc[ts][o]
-                if diag:
-                    U = U + acc[1][o][0]
-                    V = V + acc[1][o][1]
                 for k in range(ns):
                     vk = {0: k, 1: k, 2: 2 * k, 3: 0}[ok]
                     q = tb["slotcol"][off[vk]]
+                    if ts:
+                        q = Tr(q)
                     if selfp[ts]:
                         out[q, py, px] = U[vk] + V[vk]
                     else:
