@@ -76,6 +76,12 @@ WORKLOADS = {
                                 psf="synthetic",
                                 label="learned warm start + RL vs plain RL(8 it), full field 1005x1005 px, Nnum 15, "
                                       "41 planes -100..100 um"),
+    # Nnum 19, 101 x 101 lenslets, 51 planes at -125..125 um (125 um lenslets, f_ml 2500 um, M40, NA 0.95:
+    # the reference's size rule gives PSFs of 41 lenslets at the deepest plane, sides up to 1559 px), 16 frames
+    # per launch, 5000 beads + 200 filaments per volume; synthetic PSF set of those sizes
+    "config4": dict(Nnum=19, lenslets=101, z=(-125, 125, 5), img_size_ref=41, beads=5000, filaments=200,
+                    label="Nnum 19, 101x101 lenslets (1919x1919 px), 51 planes -125..125 um, 16 frames per launch, "
+                          "plain RL(8 it), 5000 beads + 200 filaments"),
     # rectification of raw 2048 x 2048 16-bit camera images (lenslet period 14.73 px) to Nnum 15
     "rectify": dict(Nnum=15, raw=(2048, 2048), dx=14.73, label="rectify 2048x2048 uint16 raw images to Nnum 15"),
     # the warm-start network's kernels alone on a random BF16 volume (--shape Z Y X, default 24 456 456,
@@ -106,6 +112,8 @@ def parse():
                     help="plain-RL iterations the warm-start network learns to reach")
     ap.add_argument("--tune-steps", type=int, default=0,
                     help="warm-start fine-tuning steps on the data-fit residual (whole volumes)")
+    ap.add_argument("--streams", type=int, default=2, choices=[1, 2],
+                    help="streams the transform groups alternate over (config4)")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--shape", type=int, nargs=3, default=[24, 456, 456], metavar=("Z", "Y", "X"),
@@ -1038,6 +1046,137 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
+def run_config4(args):
+    """Plain RL (8 Prevedel iterations from a uniform volume, after the back
+    projection) of 16 frames per launch at Nnum 19 on 1919 x 1919 px images and
+    51 planes, with the memory plan measured: the transfer matrices of both
+    directions stay resident, the uploaded PSF quadrants are released after the
+    precompute, and the volumes of the 16 frames are the only other large
+    buffers.  One step = 16 deconvolved volumes."""
+    import torch
+    import _flf
+    import build_lib
+    import psfmatrix
+    import projector
+    import synthetic
+    import warmstart
+    build_lib.build()
+    wl = WORKLOADS["config4"]
+    N = wl["Nnum"]
+    T = args.frames if args.frames > 1 else 16
+    z0, z1, dz = wl["z"]
+    z = np.arange(z0, z1 + dz / 2, dz)
+    Z = len(z)
+    Y = X = wl["lenslets"] * N
+    dev = torch.device("cuda", 0)
+    s = torch.cuda.current_stream(dev)
+    t0 = time.time()
+    hs = synthetic.psf_sizes(N, z, wl["img_size_ref"])
+    nh = (N + 1) // 2
+
+    class LazyPsf(psfmatrix.HMatrix):
+        """The synthetic PSF set generated one plane at a time as the projector
+        uploads it (the whole set is 36 GB of host memory)."""
+
+        def __init__(self):
+            super().__init__("mem:bench-config4/H{z:02d}", "mem:bench-config4/Ht{z:02d}",
+                             [(nh, nh, h, h) for h in hs], cacheMMap=False)
+            self._plane = (None, None)
+
+        def Hcc(self, cc, useHt):
+            if self._plane[0] != cc:
+                H1, Ht1 = synthetic.synthetic_psf(N, z, wl["img_size_ref"], only=[cc])
+                self._plane = (cc, (H1[cc], Ht1[cc]))
+            return self._plane[1][1 if useHt else 0]
+
+    hm = LazyPsf()
+    psf_gb = 2 * sum(nh * nh * h * h * 4 for h in hs) / 1e9
+    p = projector.Projector_gb300()
+    p.storeVolumesOnGPU = True
+    ctx = p.context(hm)
+    hm._plane = (None, None)
+    ctx.set_option("release_psf", 1)
+    ctx.set_option("streams", args.streams)
+    psf_s = time.time() - t0
+    t1 = time.time()
+    p._prepare(ctx, Y, X, hm)
+    torch.cuda.synchronize()
+    prep_s = time.time() - t1
+    geo = ctx.geometry()
+    mat_gb = ctx.memory_usage() / 1e9
+    # synthetic frames rendered on the device and forward projected one at a time, Poisson noise
+    rng = np.random.default_rng(4444)
+    img = torch.empty((T, Y, X), device=dev)
+    acc = torch.empty(Z * Y * X, dtype=torch.int64, device=dev)
+    gt1 = None
+    for t in range(T):
+        g = torch.zeros((Z, 1, Y, X), device=dev)
+        pts = torch.as_tensor(warmstart.synthetic_volume_points((Z, Y, X), wl["beads"], wl["filaments"], rng),
+                              device=dev)
+        _flf.render_blobs(g[:, 0], pts, 1.0, s.cuda_stream, acc=acc)
+        ctx.forward(g, img[t:t + 1], 1, Y, X, None, stream=s.cuda_stream)
+        if t == 0:
+            gt1 = g[:, 0].cpu()
+        del g
+    del acc
+    gen = torch.Generator(device=dev).manual_seed(55)
+    img = torch.poisson((img + 100.0).clamp_min(0), generator=gen)
+    htf = torch.empty((Z, T, Y, X), device=dev)
+    x = torch.empty((Z, T, Y, X), device=dev)
+    setup_s = time.time() - t0
+
+    def step():
+        ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
+        x.fill_(1.0)
+        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=s.cuda_stream)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    free_b, total_b = torch.cuda.mem_get_info(dev)
+    clocks = ClockSampler(0)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ctx.synchronize(s.cuda_stream)
+    # accuracy of frame 0: data-fit residual and error against its ground truth (FP64 reductions)
+    hx = torch.empty((T, Y, X), device=dev)
+    ctx.forward(x, hx, T, Y, X, None, stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    y64, h64 = img[0].double(), hx[0].double()
+    resid = float(torch.linalg.vector_norm(y64 - h64) / torch.linalg.vector_norm(y64))
+    x0 = x[:, 0].double().cpu()
+    g0 = gt1.double()
+    a = float((x0 * g0).sum() / (x0 * x0).sum())
+    truth = float(torch.linalg.vector_norm(a * x0 - g0) / torch.linalg.vector_norm(g0))
+    line = {"metric": "volumes/s to plain-RL(8 it) accuracy, Nnum 19 full field, 16 frames per launch, 1 GB300",
+            "value": T / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": max(1, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "frames": T,
+                       "rl_iterations": args.iters, "psf_sizes_max": max(hs),
+                       "psf": "synthetic set with the sizes of these optics (41 lenslets at 125 um)",
+                       "transform_sizes": geo["f"], "precompute_fp64": geo["fp64"],
+                       "psf_upload_s": round(psf_s, 1), "precompute_s": round(prep_s, 1),
+                       "setup_s": round(setup_s, 1), "streams": args.streams,
+                       "l2": "transfer matrices (%.0f GB per direction) streamed per projection" % (mat_gb / 2)},
+            "memory": {"transfer_matrices_gb": round(mat_gb, 1), "psf_quadrants_gb_released": round(psf_gb, 1),
+                       "library_gb_after_run": round(ctx.memory_usage() / 1e9, 1),
+                       "device_used_gb": round((total_b - free_b) / 1e9, 1),
+                       "torch_peak_allocated_gb": round(torch.cuda.max_memory_allocated(dev) / 1e9, 1),
+                       "device_total_gb": round(total_b / 1e9, 1)},
+            "rl_iterations_per_s": T * args.iters / (ms / 1000.0),
+            "accuracy": {"frame": 0, "residual_rel_l2": resid, "truth_rel_l2_scaled": truth, "reductions": "f64"},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_network_case(args):
     """The warm-start network's kernels on a random BF16 volume [1][Z][Y][X][C]
     (inputs larger than L2 at the default 24 x 456 x 456): one 16 -> 16 channel
@@ -1105,6 +1244,8 @@ def main():
         run_warmstart(args)
     elif args.workload in ("conv16", "unet"):
         run_network_case(args)
+    elif args.workload == "config4":
+        run_config4(args)
     else:
         run_gb300(args, rank, world, local)
 

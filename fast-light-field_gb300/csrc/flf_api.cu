@@ -84,13 +84,15 @@ struct flf_ctx {
   int num_sms = 0;
   int req_f = 0, req_fp64 = 0;   // transform size / precision asked for by flf_prepare
   int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
-  int opt_chunk_rows[2] = {16, 12};   // tunable: stored rows per pipeline stage (forward, backward)
-  int opt_split = 2;             // tunable: threads sharing one orbit's rows
+  int opt_chunk_rows[2] = {12, 12};   // tunable: stored rows per pipeline stage (forward, backward)
+  int opt_split = 1;             // tunable: threads sharing one orbit's rows
   int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
   int opt_geometry_cache = 2;    // geometries of other image shapes kept resident (most recent first)
   std::vector<Geometry> parked;  // those geometries
   unsigned long long mem_epoch = 0;   // bumped whenever a workspace or geometry buffer is freed
   int opt_streams = 2;           // transform groups alternate over this many streams (1 or 2)
+  int opt_release_psf = 0;       // free the PSF quadrants after the precompute of both directions
+  bool psf_released = false;
   cudaStream_t s2 = nullptr;     // the second stream, and the events that fork / chain / join it
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chain = nullptr;
   void *noalloc_scratch = nullptr;   // device address of the fixed scratch of flf_backward_noalloc
@@ -468,11 +470,45 @@ int build_group(flf_ctx *ctx, Group &G, int fp64, int dir, cudaStream_t s) {
 int build_direction(flf_ctx *ctx, int dir, cudaStream_t s) {
   for (int z = 0; z < ctx->nz; z++)
     if (!ctx->dH[dir][z])
-      return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, dir);
+      return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded%s", z, dir,
+                  ctx->psf_released ? " (the PSFs were released after the last precompute: upload them again "
+                                      "to build transfer matrices for another image shape)" : "");
+  ctx->psf_released = false;
   for (Group &g : ctx->geo.groups)
     if (!g.built[dir])
       if (int rc = build_group(ctx, g, ctx->geo.fp64, dir, s)) return rc;
   return FLF_OK;
+}
+
+// Every PSF of the directions in dmask (bit d) is uploaded, or they were
+// released after a precompute (a rebuild then fails with that explanation).
+int check_psfs(flf_ctx *ctx, int dmask) {
+  for (int d = 0; d < 2; d++)
+    if ((dmask >> d) & 1)
+      for (int z = 0; z < ctx->nz; z++)
+        if (!ctx->dH[d][z] && !ctx->psf_released)
+          return fail(ctx, FLF_E_STATE, "%s PSF for plane %d was not uploaded", d ? "backward" : "forward", z);
+  return FLF_OK;
+}
+
+// With the option "release_psf", free the uploaded PSF quadrants once both
+// directions' transfer matrices of the current image shape exist (they are
+// only read by the precompute); the sizes are kept.
+void maybe_release_psfs(flf_ctx *ctx) {
+  if (!ctx->opt_release_psf || !ctx->geo.built(FLF_DIR_FORWARD) || !ctx->geo.built(FLF_DIR_BACKWARD)) return;
+  bool any = false;
+  for (int d = 0; d < 2; d++)
+    for (float *&p : ctx->dH[d])
+      if (p) {
+        if (!any) cudaDeviceSynchronize();
+        cudaFree(p);
+        p = nullptr;
+        any = true;
+      }
+  if (any) {
+    ctx->psf_released = true;
+    ctx->mem_epoch++;
+  }
 }
 
 int smooth_at_least(int n) {
@@ -663,13 +699,10 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
   int rc = prepare(ctx, Y, X, f_req, ctx->req_fp64);
   if (rc != FLF_OK) return rc;
   if (!ctx->geo.built(dir)) rc = build_direction(ctx, dir, s);
+  if (rc == FLF_OK) maybe_release_psfs(ctx);
   return rc;
 }
 
-// Planes per CTA of the multiply-accumulate: enough CTAs for about 32 per SM
-// (a few waves at the kernel's occupancy), as few plane groups as that allows.
-// Planes per multiply-accumulate CTA: enough CTAs for 32 per SM, at most
-// kMacMaxZgroup planes each.
 // Planes per multiply-accumulate CTA: enough plane groups to give about 16
 // CTAs per SM over the nquads frequency quads.
 int zgroup_for(const flf_ctx *ctx, int nz, int nquads) {
@@ -1073,13 +1106,16 @@ int flf_prepare(flf_ctx *ctx, int Y, int X, int fft_size, int fp64) {
   cudaSetDevice(ctx->device);
   for (int d = 0; d < 2; d++)
     for (int z = 0; z < ctx->nz; z++)
-      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+      if (!ctx->dH[d][z] && !(ctx->psf_released && ctx->geo.valid && ctx->geo.Y == Y && ctx->geo.X == X))
+        return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded%s", z, d,
+                    ctx->psf_released ? " (released after the last precompute)" : "");
   int rc = prepare(ctx, Y, X, fft_size, fp64);
   if (rc != FLF_OK) return rc;
   ctx->req_f = fft_size;
   ctx->req_fp64 = fp64;
   for (int d = 0; d < 2 && rc == FLF_OK; d++)
     if (!ctx->geo.built(d)) rc = build_direction(ctx, d, 0);
+  if (rc == FLF_OK) maybe_release_psfs(ctx);
   return rc;
 }
 
@@ -1089,8 +1125,7 @@ int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y
   if (!vol_dev || !img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
   cudaSetDevice(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  for (int z = 0; z < ctx->nz; z++)
-    if (!ctx->dH[FLF_DIR_FORWARD][z]) return fail(ctx, FLF_E_STATE, "forward PSF for plane %d was not uploaded", z);
+  if (int rc0 = check_psfs(ctx, 1 << FLF_DIR_FORWARD)) return rc0;
   int rc = check_planes_arg(ctx, planes, nplanes);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
   PlaneSet ps;
@@ -1118,8 +1153,7 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
   if (!vol_dev || !img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
   cudaSetDevice(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  for (int z = 0; z < ctx->nz; z++)
-    if (!ctx->dH[FLF_DIR_BACKWARD][z]) return fail(ctx, FLF_E_STATE, "backward PSF for plane %d was not uploaded", z);
+  if (int rc0 = check_psfs(ctx, 1 << FLF_DIR_BACKWARD)) return rc0;
   int rc = check_planes_arg(ctx, planes, nplanes);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   PlaneSet ps;
@@ -1220,9 +1254,7 @@ int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int 
   if (variant != FLF_RL_PREVEDEL && variant != FLF_RL_STANDARD)
     return fail(ctx, FLF_E_ARG, "unknown RL variant %d", variant);
   if (iters < 0) return fail(ctx, FLF_E_ARG, "iters must be >= 0");
-  for (int d = 0; d < 2; d++)
-    for (int z = 0; z < ctx->nz; z++)
-      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+  if (int rc0 = check_psfs(ctx, 3)) return rc0;
   int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   if (rc != FLF_OK) return rc;
@@ -1454,6 +1486,12 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     }
     return FLF_OK;
   }
+  if (!strcmp(name, "release_psf")) {
+    if (value != 0 && value != 1) return fail(ctx, FLF_E_ARG, "release_psf must be 0 or 1");
+    ctx->opt_release_psf = (int)value;
+    if (value) maybe_release_psfs(ctx);
+    return FLF_OK;
+  }
   if (!strcmp(name, "geometry_cache")) {
     if (value < 0 || value > 16) return fail(ctx, FLF_E_ARG, "geometry_cache must be in [0, 16]");
     ctx->opt_geometry_cache = (int)value;
@@ -1500,9 +1538,7 @@ int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream) {
   if (!ctx || !out4) return FLF_E_ARG;
   cudaSetDevice(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  for (int d = 0; d < 2; d++)
-    for (int z = 0; z < ctx->nz; z++)
-      if (!ctx->dH[d][z]) return fail(ctx, FLF_E_STATE, "PSF for plane %d direction %d was not uploaded", z, d);
+  if (int rc0 = check_psfs(ctx, 3)) return rc0;
   int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   PlaneSet ps;

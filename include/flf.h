@@ -169,15 +169,19 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
  * stages of the multiply-accumulate, 2..16), "mac_chunk_rows" (stored rows
  * per stage, even, 2..64, both directions; "mac_chunk_rows_forward" and
  * "mac_chunk_rows_backward" set one), "mac_split" (threads sharing an orbit's rows,
- * 1..4), "plane_transform_sizes" (1: each plane uses the smallest
+ * 1..4; the CTA has two such groups, one per frequency pair of a quad, of at
+ * most 256 threads in all), "plane_transform_sizes" (1: each plane uses the smallest
  * transform its PSF allows, planes grouped by size - the default; 0: one
  * size for all planes) and "geometry_cache" (0..16, default 2: how many
  * transfer-matrix sets of other image shapes stay resident, most recent
  * first, so that a series alternating image sizes does not rebuild them) and
  * "streams" (1 or 2, default 2: the transform groups of a projection
  * alternate over this many streams, so one group's transforms overlap the
- * next group's multiply-accumulate).  Results agree to rounding whatever the
- * values. */
+ * next group's multiply-accumulate) and "release_psf" (0 or 1, default 0:
+ * free the uploaded PSF quadrants once both directions' transfer matrices of
+ * the current image shape are built, for PSF sets whose quadrants and
+ * matrices do not both fit; another image shape then needs the PSFs uploaded
+ * again).  Results agree to rounding whatever the values. */
 int flf_set_option(flf_ctx *ctx, const char *name, long long value);
 
 /* Wait for `stream` and report any failure of earlier launches, including a

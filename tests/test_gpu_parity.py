@@ -297,6 +297,41 @@ def test_geometry_cache_across_image_shapes(mods):
     assert ctx.memory_usage() < mem[4]
 
 
+def test_released_psfs_keep_projections_and_refuse_new_shapes(mods):
+    """With release_psf the PSF quadrants are freed after the precompute: the
+    projections of that image shape are unchanged, the memory count drops by the
+    PSF bytes, and another shape is refused until the PSFs are uploaded again."""
+    projector, lfdeconv, psfmatrix = mods
+    import _flf
+    import synthetic
+    N = 5
+    H, Ht = synthetic.random_psf(N, [21, 11, 31], seed=9)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(4)
+    img = rng.random((2, 40, 35)).astype(np.float32)
+    want_b = projector.Projector_gb300().BackwardProjectACC(hm, img, None)
+    want_f = projector.Projector_gb300().ForwardProjectACC(hm, want_b, None)
+    p = projector.Projector_gb300()
+    p.BackwardProjectACC(hm, img, None)
+    ctx = p.context(hm)
+    before = ctx.memory_usage()
+    ctx.set_option("release_psf", 1)
+    psf_bytes = 2 * sum(h.nbytes for h in H)
+    assert ctx.memory_usage() == before - psf_bytes
+    assert np.array_equal(p.BackwardProjectACC(hm, img, None), want_b)
+    assert np.array_equal(p.ForwardProjectACC(hm, want_b, None), want_f)
+    small = img[:, :30, :30].copy()
+    with pytest.raises(_flf.FlfError) as e:
+        p.BackwardProjectACC(hm, small, None)
+    assert e.value.code == -4 and "released" in str(e.value)
+    for z in range(len(H)):
+        ctx.upload_psf(z, _flf.FLF_DIR_FORWARD, H[z])
+        ctx.upload_psf(z, _flf.FLF_DIR_BACKWARD, Ht[z])
+    p._shape_key = None
+    assert rel(p.BackwardProjectACC(hm, small, None),
+               projector.Projector_gb300().BackwardProjectACC(hm, small, None)) == 0.0
+
+
 def test_autotune_keeps_results_and_caches(mods, tmp_path):
     """flf_autotune picks a launch shape per image shape; results do not change
     beyond rounding, and a cache file brings the choice back without timing."""
