@@ -557,8 +557,11 @@ def run_timeseries(args):
     """Mixed-size time series on one device (32 frames of each size by
     default): per size, T frames back projected and deconvolved together (x0 = Htf,
     as the time-series driver does), the multiply-accumulate launch shape autotuned
-    per size and the RL iterations replayed from one CUDA graph per size; one step =
-    every frame of every size.  The geometries of all sizes stay resident."""
+    per size; each size's whole deconvolution (back projection, x0 = Htf, RL
+    iterations) is captured as a graph and the three are combined into one graph,
+    so one step (every frame of every size) is one graph launch.  The geometries of
+    all sizes stay resident.  With T frames per launch the multiply-accumulate is
+    FP32-bound: its roofline is reported against the nominal FP32 rate."""
     import torch
     import projector
     import psfmatrix
@@ -616,15 +619,12 @@ def run_timeseries(args):
     graphs = []
     for (Y, X, img), (htf, x) in zip(data, bufs):
         p._prepare(ctx, Y, X, hm)
-        graphs.append(ctx.rl_graph(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X))
+        graphs.append(ctx.deconv_graph(img, htf, x, args.iters, T, Y, X))
+    whole = ctx.combine_graphs(graphs)
     setup_s = time.time() - t_setup
 
     def step():
-        for (Y, X, img), (htf, x), g in zip(data, bufs, graphs):
-            p._prepare(ctx, Y, X, hm)
-            ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
-            x.copy_(htf)
-            g.launch(s.cuda_stream)
+        whole.launch(s.cuda_stream)
 
     for _ in range(max(args.warmup, 1)):
         step()
@@ -641,18 +641,52 @@ def run_timeseries(args):
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
     nvol = T * len(data)
+    # per-kernel times: the same work launched directly between CUDA events on one
+    # stream; FP32 roofline of the multiply-accumulate from the reference's count of
+    # 8 N^2 F_z (F_z / 2 + 1) flops per plane, frame and projection
+    hs = [int(hm.PSFShape(c)[-1]) for c in range(Z)]
+    ctx.set_option("streams", 1)
+    ctx.profile(True)
+    flops = 0.0
+    for (Y, X, img), (htf, x) in zip(data, bufs):
+        p._prepare(ctx, Y, X, hm)
+        ctx.backward(img, htf, T, Y, X, None, stream=s.cuda_stream)
+        x.copy_(htf)
+        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, args.iters, T, Y, X, stream=s.cuda_stream)
+        for h in hs:
+            F = N * (-(-(max(Y, X) + h - 1) // N))
+            flops += (1 + 2 * args.iters) * T * 8.0 * N * N * F * (F // 2 + 1)
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    ctx.set_option("streams", 2)
+    mac = {k: v for k, v in prof.items() if k.startswith("k_mac")}
+    mac_ms = sum(v["ms"] for v in mac.values())
+    n_mac = max(1, sum(v["launches"] for v in mac.values()))
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    tot = sum(v["ms"] for v in prof.values()) or 1.0
+    roof = {"bound": "fp32", "kernel": "k_mac_fwd+k_mac_bwd", "unit": "TFLOP/s",
+            "achieved": round(flops / (mac_ms / 1000.0) / 1e12, 2), "peak": round(fp32_peak, 1),
+            "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 flop x 2.07 GHz); MEASURED_PEAKS.json "
+                           "has no FP32 figure",
+            "frac": round(flops / (mac_ms / 1000.0) / 1e12 / fp32_peak, 4), "launches": n_mac,
+            "avg_launch_ms": mac_ms / n_mac, "flops_per_launch": flops / n_mac,
+            "kernel_share": {k: round(v["ms"] / tot, 4) for k, v in prof.items()}}
     line = {"metric": "volumes/s, mixed-size time series (8 plain-RL iterations from x0 = Htf), 1 GB300",
             "value": nvol / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": wl["label"], "frames_per_size": T, "sizes_px": [Y for Y, _, _ in data],
                        "planes": Z, "nnum": N, "rl_iterations": args.iters, "volumes_per_step": nvol,
-                       "rl_launch": "one CUDA graph per size (%s kernels)" % [g.kernels for g in graphs],
+                       "rl_launch": "one CUDA graph for all sizes (%d kernels: back projection, x0 = Htf and "
+                                    "the RL iterations of each size)" % whole.kernels,
                        "autotuned": tuned, "device_gb": round(ctx.memory_usage() / 1e9, 2),
                        "setup_s": round(setup_s, 1),
                        "l2": "inputs larger than L2 (transfer matrices of three geometries)"},
-            "rl_iterations_per_s": nvol * args.iters / (ms / 1000.0), "clocks": clk}
+            "rl_iterations_per_s": nvol * args.iters / (ms / 1000.0), "roofline": roof,
+            "gpu_launches": int(whole.kernels), "clocks": clk}
     print(json.dumps(line), flush=True)
+    whole.close()
     for g in graphs:
         g.close()
 

@@ -49,6 +49,8 @@ _SIGS = {
     "flf_autotune": (_I, [_P, _I, _I, _I, ctypes.POINTER(ctypes.c_int), _P]),
     "flf_rl_graph_create": (_I, [_P, ctypes.POINTER(_P), _P, _P, _P, _I, _I, _I, _I, _I]),
     "flf_graph_launch": (_I, [_P, _P]),
+    "flf_deconv_graph_create": (_I, [_P, ctypes.POINTER(_P), _P, _P, _P, _I, _I, _I, _I]),
+    "flf_graph_combine": (_I, [ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "flf_graph_kernels": (_I, [_P]),
     "flf_graph_destroy": (_I, [_P]),
     "flf_set_tuned": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_int)]),
@@ -451,6 +453,21 @@ class Context:
         self._check(self._lib.flf_rl_graph_create(self._h, ctypes.byref(h), _ptr(x), _ptr(ref), _ptr(norm),
                                                   int(variant), int(iters), int(T), int(Y), int(X)))
         return RLGraph(self, h, (x, ref, norm))
+
+    def deconv_graph(self, img, htf, x, iters, T, Y, X):
+        """RLGraph of the whole deconvolution of T frames (flf_deconv_graph_create):
+        Htf = back projection of img, x = Htf, then `iters` Prevedel iterations."""
+        h = _P()
+        self._check(self._lib.flf_deconv_graph_create(self._h, ctypes.byref(h), _ptr(img), _ptr(htf), _ptr(x),
+                                                      int(iters), int(T), int(Y), int(X)))
+        return RLGraph(self, h, (img, htf, x))
+
+    def combine_graphs(self, graphs):
+        """One RLGraph running `graphs` (of this context) in order (flf_graph_combine)."""
+        arr = (_P * len(graphs))(*[g._h for g in graphs])
+        h = _P()
+        self._check(self._lib.flf_graph_combine(ctypes.byref(h), arr, len(graphs)))
+        return RLGraph(self, h, tuple(graphs))
 
     def autotune(self, T, Y, X, stream=None):
         """Launch shape of the multiply-accumulate for T frames of Y x X images:

@@ -92,6 +92,8 @@ struct flf_ctx {
   unsigned long long mem_epoch = 0;   // bumped whenever a workspace or geometry buffer is freed
   int opt_streams = 2;           // transform groups alternate over this many streams (1 or 2)
   int opt_release_psf = 0;       // free the PSF quadrants after the precompute of both directions
+  long long opt_wait_us = 1000000;   // limit of the multiply-accumulate's waits for a ring slot
+  int opt_drop_chunk = -1;       // test of the bounded waits: a chunk the first CTA never issues
   bool psf_released = false;
   cudaStream_t s2 = nullptr;     // the second stream, and the events that fork / chain / join it
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chain = nullptr;
@@ -783,6 +785,8 @@ MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   const int ntp = (ctx->L.nthr + 31) / 32 * 32;
   while (mp.split > 1 && 2 * mp.split * ntp > 256) mp.split--;   // at most 256 threads per block
   mp.err = ctx->d_err;
+  mp.wait_ns = (unsigned long long)ctx->opt_wait_us * 1000ull;
+  mp.drop_chunk = ctx->opt_drop_chunk;
   return mp;
 }
 
@@ -996,6 +1000,9 @@ int noalloc_scratch_lookup(flf_ctx *ctx) {
   return FLF_OK;
 }
 
+int backward_run(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X, const PlaneSet &ps,
+                 cudaStream_t s);
+
 }  // namespace
 
 // ============================================================================
@@ -1159,18 +1166,9 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
   PlaneSet ps;
   if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
-  const int TF = mac_max_frames();
-  const long long YX = (long long)Y * X;
-  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, TF));
-  float *cimg = (float *)ctx->wsCimg.p;
-  for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
-    const int nt = std::min(TF, T - t0);
-    SplitParams sp = split_params(ctx, img_dev + t0 * YX, 0, YX, nullptr, 1, nt, cimg);
-    LAUNCH(ctx, "k_split", chan_bytes(ctx, nt) + 4.0 * YX * nt, s, launch_split(sp, s));
-    const Strided out{vol_dev + t0 * YX, (long long)T * YX, YX};
-    rc = backward_chunk(ctx, cimg, ps, nt, out, Strided{nullptr, 0, 0}, Strided{nullptr, 0, 0}, EPI_STORE, s);
-  }
-  return rc;
+  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, mac_max_frames()));
+  if (rc != FLF_OK) return rc;
+  return backward_run(ctx, img_dev, vol_dev, T, Y, X, ps, s);
 }
 
 int flf_backward_noalloc(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X,
@@ -1275,6 +1273,24 @@ int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int 
   return rc;
 }
 
+// Back projection of T frames into vol_dev over the plane set ps (workspaces
+// sized beforehand).
+int backward_run(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X, const PlaneSet &ps,
+                 cudaStream_t s) {
+  const int TF = mac_max_frames();
+  const long long YX = (long long)Y * X;
+  float *cimg = (float *)ctx->wsCimg.p;
+  int rc = FLF_OK;
+  for (int t0 = 0; t0 < T && rc == FLF_OK; t0 += TF) {
+    const int nt = std::min(TF, T - t0);
+    SplitParams sp = split_params(ctx, img_dev + t0 * YX, 0, YX, nullptr, 1, nt, cimg);
+    LAUNCH(ctx, "k_split", chan_bytes(ctx, nt) + 4.0 * YX * nt, s, launch_split(sp, s));
+    const Strided out{vol_dev + t0 * YX, (long long)T * YX, YX};
+    rc = backward_chunk(ctx, cimg, ps, nt, out, Strided{nullptr, 0, 0}, Strided{nullptr, 0, 0}, EPI_STORE, s);
+  }
+  return rc;
+}
+
 // The RL loop on stream s (after rl_setup).
 int rl_run(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev, int variant, int iters, int T,
            int Y, int X, const PlaneSet &ps, cudaStream_t s) {
@@ -1332,14 +1348,14 @@ int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float
   return rl_run(ctx, x_dev, ref_dev, norm_dev, variant, iters, T, Y, X, ps, s);
 }
 
-int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float *ref_dev, const float *norm_dev,
-                        int variant, int iters, int T, int Y, int X) {
-  if (!ctx || !out) return FLF_E_ARG;
-  *out = nullptr;
-  cudaSetDevice(ctx->device);
-  PlaneSet ps;
-  int rc = rl_setup(ctx, x_dev, ref_dev, variant, iters, T, Y, X, nullptr, ps);
-  if (rc != FLF_OK) return rc;
+}  // extern "C"
+
+namespace {
+
+// Capture `body(stream)` (launches only: every buffer exists already) into a
+// new graph of this context.
+template <typename Body>
+int capture_graph(flf_ctx *ctx, flf_graph **out, const char *what, Body body) {
   CUDA_TRY(ctx, cudaDeviceSynchronize());
   cudaStream_t cs = nullptr;
   CUDA_TRY(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -1348,7 +1364,8 @@ int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float
   long long before = 0;
   for (auto &kv : ctx->kstats) before += kv.second.launches;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
-  if (e == cudaSuccess) rc = rl_run(ctx, x_dev, ref_dev, norm_dev, variant, iters, T, Y, X, ps, cs);
+  int rc = FLF_OK;
+  if (e == cudaSuccess) rc = body(cs);
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(cs, &g) : e;
   ctx->profiling = prof;
@@ -1359,14 +1376,13 @@ int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
     if (rc != FLF_OK) return rc;
-    return fail(ctx, FLF_E_CUDA, "capture of the RL loop failed: %s",
-                cudaGetErrorString(e != cudaSuccess ? e : e2));
+    return fail(ctx, FLF_E_CUDA, "capture of the %s failed: %s", what, cudaGetErrorString(e != cudaSuccess ? e : e2));
   }
   cudaGraphExec_t ex = nullptr;
   e = cudaGraphInstantiate(&ex, g, 0);
   if (e != cudaSuccess) {
     cudaGraphDestroy(g);
-    return fail(ctx, FLF_E_CUDA, "instantiating the RL graph failed: %s", cudaGetErrorString(e));
+    return fail(ctx, FLF_E_CUDA, "instantiating the %s graph failed: %s", what, cudaGetErrorString(e));
   }
   flf_graph *gr = new flf_graph;
   gr->ctx = ctx; gr->graph = g; gr->exec = ex; gr->launches = (int)(after - before);
@@ -1374,6 +1390,78 @@ int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float
   gr->device = ctx->device;
   *out = gr;
   return FLF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flf_deconv_graph_create(flf_ctx *ctx, flf_graph **out, const float *img_dev, float *htf_dev, float *x_dev,
+                            int iters, int T, int Y, int X) {
+  if (!ctx || !out) return FLF_E_ARG;
+  *out = nullptr;
+  if (!img_dev) return fail(ctx, FLF_E_ARG, "NULL array pointer");
+  cudaSetDevice(ctx->device);
+  PlaneSet ps;
+  int rc = rl_setup(ctx, x_dev, htf_dev, FLF_RL_PREVEDEL, iters, T, Y, X, nullptr, ps);
+  if (rc != FLF_OK) return rc;
+  const size_t vbytes = sizeof(float) * (size_t)ctx->nz * T * Y * X;
+  return capture_graph(ctx, out, "deconvolution", [&](cudaStream_t cs) {
+    int r = backward_run(ctx, img_dev, htf_dev, T, Y, X, ps, cs);
+    if (r != FLF_OK) return r;
+    if (cudaMemcpyAsync(x_dev, htf_dev, vbytes, cudaMemcpyDeviceToDevice, cs) != cudaSuccess)
+      return fail(ctx, FLF_E_CUDA, "copy of Htf into the start volume failed");
+    return rl_run(ctx, x_dev, htf_dev, nullptr, FLF_RL_PREVEDEL, iters, T, Y, X, ps, cs);
+  });
+}
+
+int flf_graph_combine(flf_graph **out, flf_graph *const *parts, int n) {
+  if (!out || !parts || n <= 0) return FLF_E_ARG;
+  *out = nullptr;
+  flf_ctx *ctx = parts[0] ? parts[0]->ctx : nullptr;
+  if (!ctx) return FLF_E_ARG;
+  for (int i = 0; i < n; i++) {
+    if (!parts[i] || parts[i]->ctx != ctx) return fail(ctx, FLF_E_ARG, "graphs to combine must share one context");
+    if (parts[i]->epoch != ctx->mem_epoch)
+      return fail(ctx, FLF_E_STATE, "graph %d refers to buffers freed since its capture: create it again", i);
+  }
+  cudaSetDevice(ctx->device);
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
+  cudaGraphNode_t prev = nullptr;
+  int launches = 0;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddChildGraphNode(&node, g, prev ? &prev : nullptr, prev ? 1 : 0, parts[i]->graph);
+    prev = node;
+    launches += parts[i]->launches;
+  }
+  cudaGraphExec_t ex = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ctx, FLF_E_CUDA, "combining graphs failed: %s", cudaGetErrorString(e));
+  }
+  flf_graph *gr = new flf_graph;
+  gr->ctx = ctx; gr->graph = g; gr->exec = ex; gr->launches = launches;
+  gr->epoch = ctx->mem_epoch;
+  gr->device = ctx->device;
+  *out = gr;
+  return FLF_OK;
+}
+
+int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float *ref_dev, const float *norm_dev,
+                        int variant, int iters, int T, int Y, int X) {
+  if (!ctx || !out) return FLF_E_ARG;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  PlaneSet ps;
+  int rc = rl_setup(ctx, x_dev, ref_dev, variant, iters, T, Y, X, nullptr, ps);
+  if (rc != FLF_OK) return rc;
+  return capture_graph(ctx, out, "RL loop", [&](cudaStream_t cs) {
+    return rl_run(ctx, x_dev, ref_dev, norm_dev, variant, iters, T, Y, X, ps, cs);
+  });
 }
 
 int flf_graph_launch(flf_graph *g, void *stream) {
@@ -1484,6 +1572,16 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
       cudaDeviceSynchronize();
       free_all_geometries(ctx);   // rebuilt on the next call
     }
+    return FLF_OK;
+  }
+  if (!strcmp(name, "mac_wait_limit_us")) {
+    if (value < 100 || value > 10000000) return fail(ctx, FLF_E_ARG, "mac_wait_limit_us must be in [100, 1e7]");
+    ctx->opt_wait_us = value;
+    return FLF_OK;
+  }
+  if (!strcmp(name, "test_drop_chunk")) {
+    if (value < -1 || value > 1000000) return fail(ctx, FLF_E_ARG, "test_drop_chunk must be -1 or a chunk index");
+    ctx->opt_drop_chunk = (int)value;
     return FLF_OK;
   }
   if (!strcmp(name, "release_psf")) {

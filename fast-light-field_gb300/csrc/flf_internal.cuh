@@ -214,6 +214,8 @@ struct MacParams {
   int chunk_rows;           // stored rows per stage (even)
   int split;                // threads sharing one orbit's rows (1..4)
   int *err;                 // set nonzero when a bounded wait gives up
+  unsigned long long wait_ns;   // limit of each wait for a ring slot (1 s)
+  int drop_chunk;           // test of the bounded waits: chunk the first CTA never issues (-1: none)
 };
 
 struct BuildKParams {       // lenslet-grid kernels K_iq for the precompute

@@ -557,7 +557,11 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   // that, the warp that releases a slot last (each warp counts itself out
   // once it has finished its rows of the chunk) refills it at once with chunk
   // g + NST, so no thread ever waits for a slot to drain.
+  // p.drop_chunk >= 0 (a test of the bounded waits only): the first CTA never
+  // issues that chunk, so the waits on its slot run out after p.wait_ns
+  const int drop = blockIdx.x == 0 && blockIdx.y == 0 ? p.drop_chunk : -1;
   auto issue = [&](int gn) {
+    if (gn == drop) return;
     const int zl_n = gn / cpb, ch_n = gn - zl_n * cpb, sl = gn % NST;
     const int r0 = ch_n * CH;
     const int nr = min(CH, nrq - r0);
@@ -587,7 +591,7 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
       if (zi + 1 < z1) stage_comb(scratch + ((zl + 1) & 1) * combStride, p, TF, zi + 1, uy, ux);
     }
     if (*abortf) dead = true;
-    if (!dead && !mbar_wait(full + slot, round & 1, kWaitLimitNs)) {
+    if (!dead && !mbar_wait(full + slot, round & 1, p.wait_ns)) {
       dead = true;
       *abortf = 1;
       atomicExch(p.err, 2);
@@ -746,7 +750,8 @@ __global__ void __launch_bounds__(MacOcc<TF, WIDE>::threads, MacOcc<TF, WIDE>::v
   __syncthreads();
   if (tid == 0 && *abortf) {
     const int issued = s_issued;
-    for (int g = max(0, issued - NST); g < issued; g++) mbar_wait(full + (g % NST), (g / NST) & 1, kWaitLimitNs / 10);
+    for (int g = max(0, issued - NST); g < issued; g++)
+      if (g != drop) mbar_wait(full + (g % NST), (g / NST) & 1, kWaitLimitNs / 10);
   }
   cp_async_wait_all();
 }

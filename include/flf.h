@@ -181,7 +181,15 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
  * free the uploaded PSF quadrants once both directions' transfer matrices of
  * the current image shape are built, for PSF sets whose quadrants and
  * matrices do not both fit; another image shape then needs the PSFs uploaded
- * again).  Results agree to rounding whatever the values. */
+ * again).  Results agree to rounding whatever the values.
+ * Two options exist to test the bounded waits of the multiply-accumulate:
+ * "mac_wait_limit_us" (100..1e7, default 1e6: how long a wait for a ring
+ * slot may last before the kernel gives up, sets the error flag that the next
+ * flf_synchronize reports as FLF_E_TIMEOUT, and returns) and
+ * "test_drop_chunk" (-1 default; k >= 0: the first CTA of each
+ * multiply-accumulate launch never issues its k-th bulk copy, so its wait
+ * for that slot runs out).  Neither faults or hangs the GPU; results of a
+ * launch that gave up are incomplete. */
 int flf_set_option(flf_ctx *ctx, const char *name, long long value);
 
 /* Wait for `stream` and report any failure of earlier launches, including a
@@ -326,6 +334,18 @@ int flf_ws_head(const void *d, const void *w, float bias, float floor_, const fl
 typedef struct flf_graph flf_graph;
 int flf_rl_graph_create(flf_ctx *ctx, flf_graph **out, float *x_dev, const float *ref_dev,
                         const float *norm_dev, int variant, int iters, int T, int Y, int X);
+/* The whole deconvolution of T frames as one graph: the back projection of
+ * img_dev [T][Y][X] into htf_dev [Z][T][Y][X], the start volume x = Htf (as
+ * the reference's time-series driver starts, deconvolve_time_series.py:28) and
+ * `iters` Prevedel iterations on x_dev, with these pointers baked in. */
+int flf_deconv_graph_create(flf_ctx *ctx, flf_graph **out, const float *img_dev, float *htf_dev, float *x_dev,
+                            int iters, int T, int Y, int X);
+/* One graph that runs `parts` (graphs of one context, e.g. the deconvolution
+ * graphs of several image sizes, whose transfer matrices the geometry cache
+ * keeps resident) in order: one flf_graph_launch for all of them.  The parts
+ * stay owned by the caller; destroy the combined graph with
+ * flf_graph_destroy. */
+int flf_graph_combine(flf_graph **out, flf_graph *const *parts, int n);
 int flf_graph_launch(flf_graph *graph, void *stream);
 int flf_graph_kernels(const flf_graph *graph);   /* kernels per replay */
 int flf_graph_destroy(flf_graph *graph);

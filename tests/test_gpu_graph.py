@@ -95,3 +95,47 @@ def test_graph_refuses_after_buffers_freed(env):
     p.ClearCache()
     with pytest.raises(_flf.FlfError):
         g.launch()
+
+
+def test_combined_deconvolution_graph_of_two_sizes(env):
+    """flf_deconv_graph_create (back projection, x0 = Htf, Prevedel iterations) for
+    two image sizes of one context, combined by flf_graph_combine into one graph:
+    one launch gives the volumes of the direct calls, bit for bit."""
+    torch, _flf, projector, psfmatrix, synthetic = env
+    N, iters, T = 5, 3, 2
+    H, Ht = synthetic.random_psf(N, [21, 11, 31], seed=13)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(8)
+    sizes = [(40, 35), (55, 50)]
+    imgs = [torch.tensor(rng.random((T,) + sz) * 100 + 10, dtype=torch.float32, device="cuda") for sz in sizes]
+    p = projector.Projector_gb300()
+    ctx = p.context(hm)
+    ctx.set_option("geometry_cache", 2)
+    s = torch.cuda.current_stream().cuda_stream
+    want, bufs = [], []
+    for (Y, X), img in zip(sizes, imgs):
+        p._prepare(ctx, Y, X, hm)
+        htf = torch.empty((3, T, Y, X), device="cuda")
+        x = torch.empty_like(htf)
+        ctx.backward(img, htf, T, Y, X, None, stream=s)
+        x.copy_(htf)
+        ctx.rl_iterate(x, htf, None, _flf.FLF_RL_PREVEDEL, iters, T, Y, X, stream=s)
+        want.append(x.clone())
+        bufs.append((torch.empty_like(htf), torch.zeros_like(htf)))
+    torch.cuda.synchronize()
+    graphs = []
+    for (Y, X), img, (htf, x) in zip(sizes, imgs, bufs):
+        p._prepare(ctx, Y, X, hm)
+        graphs.append(ctx.deconv_graph(img, htf, x, iters, T, Y, X))
+    whole = ctx.combine_graphs(graphs)
+    assert whole.kernels == sum(g.kernels for g in graphs) > 0
+    for _ in range(2):
+        for _, x in bufs:
+            x.zero_()
+        whole.launch(s)
+        ctx.synchronize(s)
+        for w, (_, x) in zip(want, bufs):
+            assert torch.equal(x, w)
+    whole.close()
+    for g in graphs:
+        g.close()

@@ -366,3 +366,38 @@ def test_autotune_keeps_results_and_caches(mods, tmp_path):
     q = projector.Projector_gb300()
     assert q.autotune(hm, 2, 56, 63, cache_path=cache) == d[k]
     assert rel(q.BackwardProjectACC(hm, img, None), bk0) < PROJ_TOL
+
+
+def test_bounded_wait_gives_up_and_context_recovers(mods):
+    """A bulk copy that never arrives (test option test_drop_chunk) makes the
+    multiply-accumulate's wait for that ring slot run out after a short limit:
+    the kernel sets the error flag and returns, the next synchronize reports
+    FLF_E_TIMEOUT, and the context then projects correctly again."""
+    projector, lfdeconv, psfmatrix = mods
+    import _flf
+    import synthetic
+    import torch
+    N = 5
+    H, Ht = synthetic.random_psf(N, [21, 11], seed=12)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    rng = np.random.default_rng(6)
+    img = rng.random((1, 40, 35)).astype(np.float32)
+    want = projector.Projector_gb300().BackwardProjectACC(hm, img, None)
+    p = projector.Projector_gb300()
+    p.BackwardProjectACC(hm, img, None)
+    ctx = p.context(hm)
+    ctx.set_option("mac_wait_limit_us", 2000)
+    ctx.set_option("test_drop_chunk", 0)
+    img_d = torch.as_tensor(img, device="cuda")
+    vol = torch.zeros((2, 1, 40, 35), device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    ctx.backward(img_d, vol, 1, 40, 35, None, stream=s)
+    with pytest.raises(_flf.FlfError) as e:
+        ctx.synchronize(s)
+    assert e.value.code == -5
+    ctx.set_option("test_drop_chunk", -1)
+    ctx.set_option("mac_wait_limit_us", 1000000)
+    ctx.synchronize(s)
+    assert np.array_equal(p.BackwardProjectACC(hm, img, None), want)
+    with pytest.raises(_flf.FlfError):
+        ctx.set_option("mac_wait_limit_us", 10)
