@@ -58,7 +58,8 @@ _SIGS = {
     "flf_psf_lf_input": (_I, [_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_lf_bin": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "flf_psf_ht": (_I, [_P, _P, _I, _I, _I, _I, _P]),
-    "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
+    "flf_conv3d": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P, _P]),
+    "flf_net_conv_wide_tcgen05": (_I, [_I]),
     "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
     "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
@@ -182,15 +183,22 @@ def _vshape(t):
     return B, Z, Y, X, C
 
 
-def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None):
+def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None, wt=None):
     """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16;
-    ws: optional float32 workspace for split-K layers (one B*Z*Y*X*Co slice per split, at least two)."""
+    ws: optional float32 workspace for split-K layers (one B*Z*Y*X*Co slice per split, at least two);
+    wt: optional flipped weights [27,Co,Ci] (conv3d_flip of w), with which the wide layers run on tcgen05."""
     lib = load_library()
     B, Z, Y, X, Ci = _vshape(x)
     Co = int(y.shape[-1])
     _check_global(lib.flf_conv3d(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X, Ci, Co,
-                                 int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0,
+                                 int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0, _ptr(wt),
                                  _ptr(stream)))
+
+
+def conv_wide_tcgen05(on):
+    """Run the wide layers (64 / 128 channels) on tcgen05 (True, the default) or mma.sync;
+    returns the previous setting."""
+    return bool(load_library().flf_net_conv_wide_tcgen05(int(bool(on))))
 
 
 def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):

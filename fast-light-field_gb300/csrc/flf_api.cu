@@ -1819,15 +1819,16 @@ static int net_shape(int B, int Z, int Y, int X, int C) {
   } while (0)
 
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, float *ws, long long ws_elems, void *stream) {
+               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wt, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
   if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
   if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
     return fail(nullptr, FLF_E_ARG, "volumes and weights must be 16-byte aligned");
   if (ws && !aligned16(ws)) return fail(nullptr, FLF_E_ARG, "workspace must be 16-byte aligned");
+  if (wt && !aligned16(wt)) return fail(nullptr, FLF_E_ARG, "flipped weights must be 16-byte aligned");
   ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
-               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0, ws, 1};
+               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0, ws, 1, (const __nv_bfloat16 *)wt};
   NET_CHECK(launch_conv3d(p, ws ? ws_elems : 0, (cudaStream_t)stream));
   return FLF_OK;
 }
@@ -1852,6 +1853,8 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
 int flf_net_conv16_tcgen05(int mode) { return net_set_conv16_tcgen05(mode); }
 
 long long flf_net_launches(void) { return net_launches(); }
+
+int flf_net_conv_wide_tcgen05(int on) { return net_set_conv_wide_tcgen05(on); }
 
 int flf_net_status(void) {
   const int v = net_status_read_and_clear();

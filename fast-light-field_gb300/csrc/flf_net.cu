@@ -1623,6 +1623,202 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Wide layers (32..128 channels in and out, at least one side 64 or more) on
+// tcgen05: an implicit GEMM whose CTA owns M = 128 consecutive voxels and all
+// N = CO output channels (one TMEM accumulator of CO columns), K = 27 taps x
+// CI input channels.  One pipeline stage holds one tap: the A tile (the 128
+// voxels' neighbours at that tap, CI channels each, zero outside the volume)
+// and the B tile (that tap's CO x CI weights), both in the canonical
+// no-swizzle K-major layout (8-row x 16-byte core matrices; K-adjacent core
+// matrices LBO apart, row-adjacent ones 128 bytes apart), written by cp.async
+// from all threads, S taps ahead.  Thread 0 issues the tap's CI / 16 MMAs
+// (M 128 x N CO x K 16) and commits them to the stage's mbarrier, which frees
+// the stage.  B comes from the flipped weights (wt[26 - tap] is the tap's
+// [co][ci] matrix, as flf_conv3d_flip writes it).  Epilogue: each warp reads
+// its 32 TMEM lanes (voxels) x CO columns, adds the bias, ReLU / mask, and
+// stores BF16.  Every wait is bounded (g_net_err).
+// ---------------------------------------------------------------------------
+template <int CI, int CO, int S>
+__global__ void __launch_bounds__(128, 1) k_conv3d_umma(ConvParams p) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  constexpr uint32_t ABYTES = 128u * CI * 2u, BBYTES = (uint32_t)CO * CI * 2u;
+  constexpr uint32_t LBO_A = 16u * 128u, LBO_B = (CO / 8) * 128u;   // K-adjacent core matrices
+  constexpr uint32_t TCOLS = CO < 32 ? 32 : CO;
+  unsigned char *stA = smem;
+  unsigned char *stB = smem + S * ABYTES;
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(stB + S * BBYTES);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + S + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  const long long m0 = (long long)blockIdx.x * 128;
+  const long long mrow = m0 + tid;
+  const bool rowok = mrow < M;
+  const Vox v = decode(rowok ? mrow : 0, p.Z, p.Y, p.X);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0)
+    for (int i = 0; i < S; i++) net_mbar_init(su32(bars + i), 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(CO >> 3) << 17) | ((128u >> 4) << 24);
+
+  // stage `st` <- tap t: A row tid (its CI channels, 16-byte chunks j at core
+  // matrix (j, tid / 8), row tid % 8) and this thread's share of B
+  auto load = [&](int t, int st) {
+    const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+    const int z = v.z + dz, y = v.y + dy, x = v.x + dx;
+    const bool ok = rowok && z >= 0 && z < p.Z && y >= 0 && y < p.Y && x >= 0 && x < p.X;
+    const bf16 *src = ok ? p.x + ((((long long)v.b * p.Z + z) * p.Y + y) * p.X + x) * CI : p.x;
+    const uint32_t a = su32(stA + st * ABYTES) + (tid >> 3) * 128 + (tid & 7) * 16;
+#pragma unroll
+    for (int j = 0; j < CI / 8; j++) cp16(a + j * LBO_A, ok ? src + 8 * j : p.x, ok);
+    const bf16 *wsrc = p.wt + (long long)(26 - t) * CO * CI;   // [co][ci]
+    const uint32_t b = su32(stB + st * BBYTES);
+    for (int i = tid; i < CO * CI / 8; i += 128) {
+      const int co = i / (CI / 8), j = i - co * (CI / 8);
+      cp16(b + j * LBO_B + (co >> 3) * 128 + (co & 7) * 16, wsrc + (long long)co * CI + 8 * j, true);
+    }
+  };
+
+  bool ok = true;
+  int committed = 0;   // taps whose MMAs were issued and committed
+  // taps 0 .. S-2 in flight before the first MMA
+#pragma unroll
+  for (int t = 0; t < S - 1; t++) {
+    load(t, t);
+    cp_commit();
+  }
+  for (int t = 0; t < 27; t++) {
+    const int st = t % S;
+    // refill the stage of tap t-1 with tap t+S-1 once tap t-1's MMAs are done
+    const int tn = t + S - 1;
+    if (tn < 27) {
+      if (t >= 1) {
+        const int late = net_mbar_wait(su32(bars + (t - 1) % S), ((t - 1) / S) & 1, 1000000000ULL) ? 0 : 1;
+        if (__syncthreads_or(late)) {
+          if (tid == 0) atomicExch(&g_net_err, 12);
+          ok = false;
+          break;
+        }
+      }
+      load(tn, tn % S);
+    }
+    cp_commit();
+    cp_wait<S - 1>();                        // tap t's copies are in shared memory
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a0 = su32(stA + st * ABYTES), b0 = su32(stB + st * BBYTES);
+#pragma unroll
+      for (int k = 0; k < CI / 16; k++) {
+        const uint64_t ad = umma_desc(a0 + 2 * k * LBO_A, LBO_A, 128);
+        const uint64_t bd = umma_desc(b0 + 2 * k * LBO_B, LBO_B, 128);
+        umma_f16(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
+      }
+      umma_commit(su32(bars + st));
+    }
+    committed = t + 1;
+  }
+  cp_wait<0>();
+  // the taps whose stage was not waited for in the loop: every MMA is done
+  // (and every commit has arrived) before TMEM and shared memory are released
+  int late = 0;
+  for (int t = committed > S ? committed - S : 0; t < committed; t++)
+    if (!net_mbar_wait(su32(bars + t % S), (t / S) & 1, 1000000000ULL)) late = 1;
+  if (__syncthreads_or(late)) {
+    if (tid == 0) atomicExch(&g_net_err, 13);
+    ok = false;
+  }
+  tc_fence_after();
+  if (ok) {
+    const long long row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < CO; c0 += 16) {
+      float d[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, d);
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < M) {
+        const long long o = row * CO + c0;
+        uint4 mk[2];
+        if (p.mask) {
+          mk[0] = *reinterpret_cast<const uint4 *>(p.mask + o);
+          mk[1] = *reinterpret_cast<const uint4 *>(p.mask + o + 8);
+        }
+        const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
+        uint4 outv[2];
+        __nv_bfloat162 *hh = reinterpret_cast<__nv_bfloat162 *>(outv);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          float v0 = d[2 * k] + (p.bias ? p.bias[c0 + 2 * k] : 0.f);
+          float v1 = d[2 * k + 1] + (p.bias ? p.bias[c0 + 2 * k + 1] : 0.f);
+          if (p.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          if (p.mask) {
+            const float2 mf = __bfloat1622float2(m2[k]);
+            if (!(mf.x > 0.f)) v0 = 0.f;
+            if (!(mf.y > 0.f)) v1 = 0.f;
+          }
+          hh[k] = __floats2bfloat162_rn(v0, v1);
+        }
+        *reinterpret_cast<uint4 *>(p.y + o) = outv[0];
+        *reinterpret_cast<uint4 *>(p.y + o + 8) = outv[1];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+  }
+}
+
+template <int CI, int CO>
+static cudaError_t launch_umma(const ConvParams &p, cudaStream_t s) {
+  constexpr int S = (CI * 256 + CO * CI * 2) <= 48 * 1024 ? 4 : 3;
+  constexpr size_t SMEM = (size_t)S * (128 * CI * 2 + CO * CI * 2) + 8 * (S + 1) + 16;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_umma<CI, CO, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const long long M = (long long)p.B * p.Z * p.Y * p.X;
+  FLF_NET_LAUNCH(k_conv3d_umma<CI, CO, S><<<(unsigned)((M + 127) / 128), 128, SMEM, s>>>(p));
+  return cudaGetLastError();
+}
+
+// the wide layers (a side of 64 or 128 channels) on tcgen05 when the flipped
+// weights are given: 1 (default) or 0 (mma.sync)
+static int g_conv_wide_tc = 1;
+
+int net_set_conv_wide_tcgen05(int on) {
+  const int old = g_conv_wide_tc;
+  g_conv_wide_tc = on ? 1 : 0;
+  return old;
+}
+
+static cudaError_t launch_wide_umma(const ConvParams &p, cudaStream_t s, bool &done) {
+  done = true;
+#define FLF_UM(a, b) if (p.Ci == a && p.Co == b) return launch_umma<a, b>(p, s);
+  FLF_UM(32, 64) FLF_UM(64, 32) FLF_UM(64, 64) FLF_UM(64, 128) FLF_UM(128, 64) FLF_UM(128, 128)
+  FLF_UM(32, 128) FLF_UM(128, 32)
+#undef FLF_UM
+  done = false;
+  return cudaSuccess;
+}
+
 // kernels of the 16 / 32-channel convolutions: 0 = mma.sync tiles; 1 = tcgen05 with TMA staging
 // for 16 -> 16, mma.sync for the 32-channel layers; 2 (default) = tcgen05 for all of them
 static int g_conv16_tc = 2;
@@ -1650,6 +1846,11 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
     return g_conv16_tc == 2 ? launch_tma16<32, 16, 2, 4, false, true>(p, HeadOut{}, s) : launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32)
     return g_conv16_tc == 2 ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
+  if (p.wt && g_conv_wide_tc) {
+    bool done = false;
+    const cudaError_t e = launch_wide_umma(p, s, done);
+    if (done) return e;
+  }
   const int BN = p.Co >= 64 ? 64 : p.Co;
   const long long ctas = (M + 127) / 128 * (p.Co / BN);
   const int KT = 27 * (p.Ci / 16);

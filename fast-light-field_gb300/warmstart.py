@@ -105,7 +105,8 @@ class UNet3D:
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
         _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,
-                    stream=torch.cuda.current_stream(self.dev).cuda_stream, ws=self._ws)
+                    stream=torch.cuda.current_stream(self.dev).cuda_stream, ws=self._ws,
+                    wt=q["wb"] if flip else q["wf"])
         return y
 
     def _pool(self, x):

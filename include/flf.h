@@ -247,7 +247,10 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   or NULL) lets layers with few output tiles split their K loop across
  *   CTAs, each split into its own B Z Y X Co slice (as many splits as fit,
  *   at least 2), summed in split order; it must not be shared by concurrent
- *   calls.
+ *   calls.  wt (or NULL): the same weights as flf_conv3d_flip writes them
+ *   (wt[26 - tap][co][ci] = w[tap][ci][co]); with it the layers of 32 to 128
+ *   channels with a side of 64 or more run on the tcgen05 tensor cores
+ *   (flf_net_conv_wide_tcgen05(0) selects the mma.sync kernel instead).
  * flf_conv3d_wgrad: dw [27][Ci][Co] float += sum_v x[v + tap][ci] dy[v][co].
  *   The voxels are cut into chunks whose partial gradients go to ws (float,
  *   27 Ci Co per chunk; as many chunks as ws holds, one without ws) and are
@@ -276,7 +279,7 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   fixed-point integers, so the result does not depend on the order of
  *   arrival (per-voxel totals below 2^31); without it, FP32 atomics. */
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, float *ws, long long ws_elems, void *stream);
+               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wt, void *stream);
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      float *ws, long long ws_elems, void *stream);
 /* flf_conv3d_tc: flf_conv3d for 16 -> 16 channels on the tcgen05 tensor cores
@@ -298,6 +301,9 @@ int flf_net_conv16_tcgen05(int mode);
 /* Number of kernel launches the network entry points above have made since
  * the library was loaded (all threads). */
 long long flf_net_launches(void);
+/* Wide layers (a side of 64 or 128 channels) on tcgen05 when flf_conv3d gets
+ * the flipped weights: 1 (default) or 0 (mma.sync); returns the previous value. */
+int flf_net_conv_wide_tcgen05(int on);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
 int flf_bias_grad(const void *g, float *db, long long M, int C, float *ws, long long ws_elems, void *stream);
 int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);

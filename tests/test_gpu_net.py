@@ -43,6 +43,9 @@ def _close(torch, got, ref, rel=1e-2, absf=1e-3):
     ((1, 2, 3, 5), 16, 16, True), ((2, 6, 24, 40), 16, 16, False),
     # few output tiles and a long K loop: split across CTAs through the workspace
     ((1, 3, 6, 6), 128, 64, True), ((1, 2, 5, 7), 64, 128, False), ((2, 3, 9, 9), 64, 32, True),
+    # more than one 128-voxel tile with a ragged last one (the tcgen05 kernel of the wide layers)
+    ((2, 6, 12, 23), 64, 64, True), ((1, 5, 11, 17), 128, 128, False), ((1, 4, 9, 30), 32, 128, True),
+    ((1, 4, 9, 30), 128, 32, False),
 ])
 def test_conv3d_forward(env, shape, Ci, Co, relu):
     torch, _flf = env
@@ -52,18 +55,25 @@ def test_conv3d_forward(env, shape, Ci, Co, relu):
     b = torch.randn(Co, generator=g).float()
     y = torch.empty(shape + (Co,), dtype=torch.bfloat16, device="cuda")
     ws = torch.empty(4 * int(np.prod(shape)) * Co, device="cuda")    # room for 4 K slices
-    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws)
     ref = _ref_conv(torch, x.double(), w.double(), b.double())
     if relu:
         ref = ref.clamp_min(0)
-    _close(torch, y, ref)
-    # split layers add their K slices in a fixed order: the same bits again
-    y2 = torch.empty_like(y)
-    _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y2, relu=relu, ws=ws)
-    assert torch.equal(y, y2)
+    # without and with the flipped weights (with them the wide layers run on tcgen05)
+    wt = torch.empty((27, Co, Ci), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d_flip(w.cuda(), wt)
+    for flipped in (None, wt):
+        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws, wt=flipped)
+        _close(torch, y, ref)
+        # split layers add their K slices in a fixed order: the same bits again
+        y2 = torch.empty_like(y)
+        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y2, relu=relu, ws=ws, wt=flipped)
+        assert torch.equal(y, y2)
+    torch.cuda.synchronize()
+    _flf.net_status()
 
 
-@pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 32, 16), ((1, 3, 6, 6), 64, 128)])
+@pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 32, 16), ((1, 3, 6, 6), 64, 128), ((2, 5, 9, 13), 128, 64),
+                                         ((1, 4, 7, 11), 32, 64)])
 def test_conv3d_mask_and_data_gradient(env, shape, Ci, Co):
     torch, _flf = env
     g = torch.Generator().manual_seed(3)
@@ -79,6 +89,9 @@ def test_conv3d_mask_and_data_gradient(env, shape, Ci, Co):
     dx = torch.empty(shape + (Ci,), dtype=torch.bfloat16, device="cuda")
     ws = torch.empty(4 * int(np.prod(shape)) * Ci, device="cuda")
     _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws)
+    _close(torch, dx, ref)
+    # the data gradient on tcgen05: the flipped weights of w2 are w itself
+    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws, wt=w.cuda())
     _close(torch, dx, ref)
 
 
