@@ -519,10 +519,13 @@ int smooth_at_least(int n) {
   return f;
 }
 
+// Kernel radius of plane z in lenslets.  Released PSFs keep their sizes, so
+// the radius (and with it the geometry of every image shape) stays the one the
+// transfer matrices were built with.
 int plane_radius(const flf_ctx *ctx, int z) {
   int R = 0;
   for (int d = 0; d < 2; d++)
-    if (ctx->dH[d][z]) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
+    if (ctx->dH[d][z] || ctx->psf_released) R = std::max(R, kernel_radius(ctx, ctx->h[d][z]));
   return R;
 }
 
