@@ -776,17 +776,40 @@ int join_streams(flf_ctx *ctx, cudaStream_t s) {
   return FLF_OK;
 }
 
+// Launch shape of the multiply-accumulate in direction dir: the image shape's
+// tuned shape where one was set, else the options.
+void mac_shape(const flf_ctx *ctx, int dir, int &stages, int &chunk_rows, int &split) {
+  const int *tn = ctx->geo.tuned;
+  stages = tn[0] ? tn[0] : ctx->opt_stages;
+  chunk_rows = tn[1 + dir] ? tn[1 + dir] : ctx->opt_chunk_rows[dir];
+  split = tn[3] ? tn[3] : ctx->opt_split;
+  const int ntp = (ctx->L.nthr + 31) / 32 * 32;
+  while (split > 1 && 2 * split * ntp > 256) split--;   // at most 256 threads per block
+}
+
+// Frames one multiply-accumulate pass takes: mac_max_frames(), or fewer where
+// the ring, the staged spectra and the operand tables of that many frames do
+// not fit shared memory with the current launch shape (Nnum 19 at 12 rows per
+// stage: 2 frames).
+int frames_per_pass(const flf_ctx *ctx) {
+  for (int tf = mac_max_frames(); tf > 1; tf /= 2) {
+    bool fits = true;
+    for (int d = 0; d < 2; d++) {
+      int st, cr, sp;
+      mac_shape(ctx, d, st, cr, sp);
+      if (mac_smem_bytes(ctx->L, tf, st, cr, sp, d == FLF_DIR_FORWARD) > kMacSmemMax) fits = false;
+    }
+    if (fits) return tf;
+  }
+  return 1;
+}
+
 MacParams mac_params(const flf_ctx *ctx, const Group &G, int dir, int nt) {
   MacParams mp{};
   mp.L = ctx->L; mp.f = G.f; mp.fh = G.fh; mp.fq = G.fq; mp.nkp = G.nkp; mp.nquads = G.nquads; mp.T = nt;
   mp.P = G.P[dir];
   mp.rowS = ctx->d_rowS; mp.rowF = ctx->d_rowF; mp.oslots = ctx->d_oslots; mp.slotcol = ctx->d_slotcol;
-  const int *tn = ctx->geo.tuned;
-  mp.stages = tn[0] ? tn[0] : ctx->opt_stages;
-  mp.chunk_rows = tn[1 + dir] ? tn[1 + dir] : ctx->opt_chunk_rows[dir];
-  mp.split = tn[3] ? tn[3] : ctx->opt_split;
-  const int ntp = (ctx->L.nthr + 31) / 32 * 32;
-  while (mp.split > 1 && 2 * mp.split * ntp > 256) mp.split--;   // at most 256 threads per block
+  mac_shape(ctx, dir, mp.stages, mp.chunk_rows, mp.split);
   mp.err = ctx->d_err;
   mp.wait_ns = (unsigned long long)ctx->opt_wait_us * 1000ull;
   mp.drop_chunk = ctx->opt_drop_chunk;
@@ -1141,7 +1164,7 @@ int flf_forward(flf_ctx *ctx, const float *vol_dev, float *img_dev, int T, int Y
   PlaneSet ps;
   if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
-  const int TF = mac_max_frames();
+  const int TF = frames_per_pass(ctx);
   const long long vol_sz = (long long)T * Y * X;
   rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, TF));
   float *cimg = (float *)ctx->wsCimg.p;
@@ -1169,7 +1192,7 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
   PlaneSet ps;
   if (rc == FLF_OK) rc = make_plane_set(ctx, planes, nplanes, s, ps);
   if (rc != FLF_OK) return rc;
-  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, mac_max_frames()));
+  rc = ensure_ws(ctx, ctx->wsCimg, sizeof(float) * chan_set_floats(ctx) * std::min(T, frames_per_pass(ctx)));
   if (rc != FLF_OK) return rc;
   return backward_run(ctx, img_dev, vol_dev, T, Y, X, ps, s);
 }
@@ -1259,7 +1282,7 @@ int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int 
   int rc = check_ready(ctx, T, Y, X, FLF_DIR_FORWARD, s);
   if (rc == FLF_OK) rc = check_ready(ctx, T, Y, X, FLF_DIR_BACKWARD, s);
   if (rc != FLF_OK) return rc;
-  const int nt = std::min(T, mac_max_frames());
+  const int nt = std::min(T, frames_per_pass(ctx));
   const size_t cset = sizeof(float) * chan_set_floats(ctx) * nt;
   rc = ensure_ws(ctx, ctx->wsCimg, cset);
   if (rc == FLF_OK && variant == FLF_RL_STANDARD) rc = ensure_ws(ctx, ctx->wsCy, cset);
@@ -1280,7 +1303,7 @@ int rl_setup(flf_ctx *ctx, float *x_dev, const float *ref_dev, int variant, int 
 // sized beforehand).
 int backward_run(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int Y, int X, const PlaneSet &ps,
                  cudaStream_t s) {
-  const int TF = mac_max_frames();
+  const int TF = frames_per_pass(ctx);
   const long long YX = (long long)Y * X;
   float *cimg = (float *)ctx->wsCimg.p;
   int rc = FLF_OK;
@@ -1297,7 +1320,7 @@ int backward_run(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
 // The RL loop on stream s (after rl_setup).
 int rl_run(flf_ctx *ctx, float *x_dev, const float *ref_dev, const float *norm_dev, int variant, int iters, int T,
            int Y, int X, const PlaneSet &ps, cudaStream_t s) {
-  const int TF = mac_max_frames();
+  const int TF = frames_per_pass(ctx);
   const long long YX = (long long)Y * X;
   float *cimg = (float *)ctx->wsCimg.p;
   float *cy = (float *)ctx->wsCy.p;
@@ -1624,7 +1647,7 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
       return fail(ctx, FLF_E_ARG, "mac_split must be in [1, 4] with at most 256 threads per block "
                                   "(2 frequency pairs x split x %d orbit threads)", ntp);
     for (int cr : {crf, crb})
-      if (mac_smem_bytes(ctx->L, mac_max_frames(), st, cr, sp, true) > 227 * 1024)
+      if (mac_smem_bytes(ctx->L, 1, st, cr, sp, true) > kMacSmemMax)
         return fail(ctx, FLF_E_ARG, "pipeline of %d stages x %d rows exceeds shared memory", st, cr);
     ctx->opt_stages = st;
     ctx->opt_chunk_rows[FLF_DIR_FORWARD] = crf;
@@ -1646,7 +1669,7 @@ int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream) {
   if (rc == FLF_OK) rc = make_plane_set(ctx, nullptr, ctx->nz, s, ps);
   if (rc != FLF_OK) return rc;
   Geometry &Gm = ctx->geo;
-  const int nt = std::min(T, mac_max_frames());
+  const int nt = std::min(T, frames_per_pass(ctx));
   size_t sSf, sOf, sCf, sSb, sOb, sCb;
   ws_needs(ctx, ps, nt, true, sSf, sOf, sCf);
   ws_needs(ctx, ps, nt, false, sSb, sOb, sCb);
@@ -1680,7 +1703,8 @@ int flf_autotune(flf_ctx *ctx, int T, int Y, int X, int *out4, void *stream) {
       for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         if (2 * split_c[b] * ntp > 256) continue;
         for (int ch : chunk_c) {
-          if (mac_smem_bytes(ctx->L, mac_max_frames(), stages_c[a], ch, split_c[b], true) > 227 * 1024) continue;
+          if (mac_smem_bytes(ctx->L, nt <= 1 ? 1 : (nt <= 2 ? 2 : 4), stages_c[a], ch, split_c[b], true) > kMacSmemMax)
+            continue;
           e = mac_group_launch(ctx, gi, d, nt, ps, stages_c[a], ch, split_c[b], s);   // warm-up
           if (e == cudaSuccess) e = cudaEventRecord(e0, s);
           for (int k = 0; k < 3 && e == cudaSuccess; k++) e = mac_group_launch(ctx, gi, d, nt, ps, stages_c[a], ch, split_c[b], s);
@@ -1723,7 +1747,7 @@ int flf_set_tuned(flf_ctx *ctx, int Y, int X, const int *in4) {
     return fail(ctx, FLF_E_ARG, "invalid launch shape");
   for (int d = 1; d <= 2; d++)
     if (in4[d] < 2 || in4[d] > 64 || (in4[d] & 1) ||
-        mac_smem_bytes(ctx->L, mac_max_frames(), in4[0], in4[d], in4[3], true) > 227 * 1024)
+        mac_smem_bytes(ctx->L, 1, in4[0], in4[d], in4[3], true) > kMacSmemMax)
       return fail(ctx, FLF_E_ARG, "invalid rows per chunk %d", in4[d]);
   for (int i = 0; i < 4; i++) Gm.tuned[i] = in4[i];
   return FLF_OK;

@@ -350,6 +350,8 @@ cudaError_t launch_build_k(const BuildKParams &p, int nimg, cudaStream_t s);
 cudaError_t launch_pack(const PackParams &p, cudaStream_t s);
 size_t rfft2_smem_bytes(int f, int imgs, int fp64);
 int mac_max_frames();
+// Shared memory one CTA may opt in to (sm_100 family).
+constexpr size_t kMacSmemMax = 227 * 1024;
 size_t mac_smem_bytes(const Layout &L, int TF, int stages, int chunk_rows, int split, bool fwd);
 
 }  // namespace flf

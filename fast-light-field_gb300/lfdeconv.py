@@ -70,7 +70,7 @@ def ForwardProjectACC(hMatrix, realspace, planes=None, progress=None, logPrint=T
 
 
 def DeconvRL(hMatrix, Htf, maxIter, Xguess, logPrint=True, numjobs=None, projector=None, im=None,
-             progress=None, prevedel=True, trustMask=None):
+             progress=None, prevedel=True, trustMask=None, out=None):
     """Richardson-Lucy deconvolution (lfdeconv.py:72-202).
 
     Htf       the initial back projection of the camera image (or None, with ``im``)
@@ -78,6 +78,8 @@ def DeconvRL(hMatrix, Htf, maxIter, Xguess, logPrint=True, numjobs=None, project
     prevedel  True: ``x <- x * Htf / Ht(H x)`` (the default of the reference);
               False: ``x <- x * Ht(im / H x)``, divided by ``Ht(trustMask)``
               when a trust mask is given.  NaN results are set to 0.
+    out       optional float32 numpy array ``[Z, T, Y, X]`` (e.g. a view of pinned host
+              memory) that receives the volume; it is then the return value.
     Returns the volume as a numpy array ``[Z, T, Y, X]``.
     """
     projector = _projector(projector)
@@ -123,10 +125,13 @@ def DeconvRL(hMatrix, Htf, maxIter, Xguess, logPrint=True, numjobs=None, project
                     projector.storeVolumesOnGPU = saved
         if maxIter > 0:
             projector.RichardsonLucy(hMatrix, x, ref, maxIter, prevedel=prevedel, norm=norm)
-        result = projector.asnumpy(x)
+        result = projector.asnumpy(x, out=out)
     else:
         result = _deconv_rl_generic(hMatrix, Htf, maxIter, Xguess, numjobs, projector, im, prevedel,
                                     trustMask)
+        if out is not None:
+            out[...] = result
+            result = out
     if logPrint:
         print("Deconvolution elapsed wallclock time %f" % (time.time() - t1))
     return result

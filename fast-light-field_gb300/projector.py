@@ -39,7 +39,10 @@ class Projector_base(object):
     def asnative(self, m):
         return np.asarray(m)
 
-    def asnumpy(self, m):
+    def asnumpy(self, m, out=None):
+        if out is not None:
+            out[...] = m
+            return out
         return np.asarray(m)
 
     def nativeZeros(self, shape, dtype=float):
@@ -105,7 +108,15 @@ class Projector_gb300(Projector_base):
             return m.to(device=self._dev(), dtype=torch.float32).contiguous()
         return torch.as_tensor(np.ascontiguousarray(m, dtype=np.float32), device=self._dev())
 
-    def asnumpy(self, m):
+    def asnumpy(self, m, out=None):
+        """A host copy of m; with ``out`` (a float32 numpy array of m's shape, e.g.
+        a view of pinned memory) the copy lands there and ``out`` is returned."""
+        if out is not None:
+            if not isinstance(out, np.ndarray) or out.dtype != np.float32 or tuple(out.shape) != tuple(m.shape) \
+                    or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float32 numpy array of shape %s" % (tuple(m.shape),))
+            torch.from_numpy(out).copy_(m if isinstance(m, torch.Tensor) else torch.as_tensor(np.asarray(m)))
+            return out
         if isinstance(m, torch.Tensor):
             return m.detach().to("cpu").numpy()
         return np.asarray(m)

@@ -466,10 +466,11 @@ class WarmStart:
             return tuple(int(v) for v in f["meta.shape"])
 
 
-def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):
+def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None, out=None):
     """RL from the network's start volume: back projection, warm start, ``maxIter``
     Prevedel iterations (the reference's default update), on the device; returns the
-    volume [Z, T, Y, X] as a device tensor."""
+    volume [Z, T, Y, X] as a device tensor, or, with ``out`` (a float32 numpy array of
+    that shape, e.g. a view of pinned host memory), copied into ``out``."""
     p = projector or warm.proj
     img = p.asnative(im)
     T, Y, X = img.shape
@@ -478,6 +479,8 @@ def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None):
     x = warm.initial_volume(htf)
     if maxIter > 0:
         p.RichardsonLucy(warm.hm, x, htf if prevedel else img, maxIter, prevedel=prevedel)
+    if out is not None:
+        return p.asnumpy(x, out=out)
     return x
 
 

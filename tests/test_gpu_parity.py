@@ -77,6 +77,7 @@ def test_rl_matches_reference_vectors(mods, name):
     (7, [43, 15], 6, 49, 56),         # T > 4 exercises frame chunking
     (15, [61, 91], 2, 150, 120),
     (19, [77], 1, 95, 114),
+    (19, [77, 39], 5, 95, 114),       # Nnum 19 runs 2 frames per pass (shared memory): 2 + 2 + 1
 ])
 def test_projection_matches_fp64_oracle(mods, N, hs, T, Y, X):
     projector, lfdeconv, psfmatrix = mods
@@ -148,6 +149,26 @@ def test_zero_image_rl_gives_zero(mods):
     img = np.zeros_like(c["img"])
     r = lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=img)
     assert np.all(r == 0)
+
+
+def test_rl_into_pinned_host_array(mods):
+    """DeconvRL with ``out`` (a view of pinned host memory) writes the volume of the
+    plain call there and returns that array; a wrong shape or type is refused."""
+    import torch
+    projector, lfdeconv, psfmatrix = mods
+    c = case_inputs("rl_prevedel")
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    p = projector.Projector_gb300()
+    want = lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=c["img"])
+    img = torch.empty(c["img"].shape, dtype=torch.float32, pin_memory=True).numpy()
+    img[...] = c["img"]
+    out = torch.empty(want.shape, dtype=torch.float32, pin_memory=True).numpy()
+    r = lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=img, out=out)
+    assert r is out and np.array_equal(out, want)
+    with pytest.raises(ValueError):
+        lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=img, out=out[:, :, 1:])
+    with pytest.raises(ValueError):
+        lfdeconv.DeconvRL(hm, None, 2, None, logPrint=False, projector=p, im=img, out=out.astype(np.float64))
 
 
 def test_full_size_linearity_and_adjointness(mods):

@@ -135,6 +135,17 @@ def test_rl_driver_generic_path_matches_reference(name):
     assert rel(r, g) < 1e-5
 
 
+def test_rl_driver_writes_into_out():
+    import lfdeconv
+    import psfmatrix
+    c = case_inputs("rl_prevedel")
+    hm = psfmatrix.HMatrixArrays(c["H"], c["Ht"])
+    want = lfdeconv.DeconvRL(hm, None, 1, None, logPrint=False, projector=OracleProjector(), im=c["img"])
+    out = np.empty_like(want)
+    r = lfdeconv.DeconvRL(hm, None, 1, None, logPrint=False, projector=OracleProjector(), im=c["img"], out=out)
+    assert r is out and np.array_equal(out, want)
+
+
 def test_rl_driver_rejects_trust_mask_with_prevedel():
     import lfdeconv
     import psfmatrix
