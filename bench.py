@@ -137,6 +137,9 @@ def parse():
                     choices=["tcgen05", "tcgen05-all", "tcgen05-noswizzle", "mma.sync"],
                     help="conv16 / unet: tcgen05 = the 16->16 layers on tcgen05; tcgen05-all (the default) = "
                          "the 32-channel layers too")
+    ap.add_argument("--wide", type=int, default=1, choices=range(6),
+                    help="unet: kernel of the 64/128-channel layers (0 mma.sync, 1 tcgen05, 2..5 tcgen05 with "
+                         "1..4 M tiles per work item)")
     ap.add_argument("--planes", default=None,
                     help="comma-separated z indices of the workload to keep (smaller cases for profiling)")
     return ap.parse_args()
@@ -1242,6 +1245,7 @@ def run_network_case(args):
     build_lib.build()
     _flf.load_library()
     _flf.conv16_tcgen05({"mma.sync": 0, "tcgen05-all": 2}.get(args.kernel, 1))
+    _flf.conv_wide_tcgen05(args.wide)
     Z, Y, X = args.shape
     g = torch.Generator(device="cuda").manual_seed(0)
     if args.workload == "conv16":
@@ -1276,7 +1280,8 @@ def run_network_case(args):
             "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulation)",
             "data": "synthetic", "config": {"workload": WORKLOADS[args.workload]["label"], "shape": [Z, Y, X],
-                                            "kernel": args.kernel, "l2": "activations larger than L2"}}
+                                            "kernel": args.kernel, "wide_kernel": args.wide,
+                                            "l2": "activations larger than L2"}}
     if flop:
         line["tflops"] = flop / ms / 1e9
     print(json.dumps(line), flush=True)

@@ -65,6 +65,7 @@ _SIGS = {
     "flf_net_status": (_I, []),
     "flf_net_conv16_tcgen05": (_I, [_I]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
+    "flf_conv3d_pack": (_I, [_P, _P, _I, _I, _P]),
     "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P, ctypes.c_longlong, _P]),
     "flf_pool2": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_pool2_bwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
@@ -183,22 +184,29 @@ def _vshape(t):
     return B, Z, Y, X, C
 
 
-def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None, wt=None):
+def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None, wp=None):
     """y = [relu](conv3x3x3(x, w) + bias) [* (mask > 0)]; x [B,Z,Y,X,Ci], w [27,Ci,Co], y [B,Z,Y,X,Co] bf16;
     ws: optional float32 workspace for split-K layers (one B*Z*Y*X*Co slice per split, at least two);
-    wt: optional flipped weights [27,Co,Ci] (conv3d_flip of w), with which the wide layers run on tcgen05."""
+    wp: optional packed weights (conv3d_pack of w), with which the wide layers run on tcgen05."""
     lib = load_library()
     B, Z, Y, X, Ci = _vshape(x)
     Co = int(y.shape[-1])
     _check_global(lib.flf_conv3d(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X, Ci, Co,
-                                 int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0, _ptr(wt),
+                                 int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0, _ptr(wp),
                                  _ptr(stream)))
 
 
-def conv_wide_tcgen05(on):
-    """Run the wide layers (64 / 128 channels) on tcgen05 (True, the default) or mma.sync;
-    returns the previous setting."""
-    return bool(load_library().flf_net_conv_wide_tcgen05(int(bool(on))))
+def conv_wide_tcgen05(mode):
+    """Kernel of the wide layers (64 / 128 channels) when packed weights are given:
+    0 / False = mma.sync, 1 / True (the default) = tcgen05, 2..5 = tcgen05 with 1..4
+    M tiles per work item; returns the previous setting."""
+    return int(load_library().flf_net_conv_wide_tcgen05(int(mode)))
+
+
+def conv3d_pack(w, wp, stream=None):
+    """wp = w [27, Ci, Co] bf16 packed as the tcgen05 wide-layer kernel's B blocks (same size)."""
+    _, Ci, Co = w.shape
+    _check_global(load_library().flf_conv3d_pack(_ptr(w), _ptr(wp), int(Ci), int(Co), _ptr(stream)))
 
 
 def conv3d_tc(x, w, bias, y, relu=False, mask=None, stream=None, rows=4):

@@ -1846,16 +1846,16 @@ static int net_shape(int B, int Z, int Y, int X, int C) {
   } while (0)
 
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wt, void *stream) {
+               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wp, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = net_shape(B, Z, Y, X, Ci)) return rc;
   if (int rc = net_shape(B, Z, Y, X, Co)) return rc;
   if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
     return fail(nullptr, FLF_E_ARG, "volumes and weights must be 16-byte aligned");
   if (ws && !aligned16(ws)) return fail(nullptr, FLF_E_ARG, "workspace must be 16-byte aligned");
-  if (wt && !aligned16(wt)) return fail(nullptr, FLF_E_ARG, "flipped weights must be 16-byte aligned");
+  if (wp && !aligned16(wp)) return fail(nullptr, FLF_E_ARG, "packed weights must be 16-byte aligned");
   ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, (const __nv_bfloat16 *)mask,
-               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0, ws, 1, (const __nv_bfloat16 *)wt};
+               (__nv_bfloat16 *)y, B, Z, Y, X, Ci, Co, relu ? 1 : 0, ws, 1, (const __nv_bfloat16 *)wp};
   NET_CHECK(launch_conv3d(p, ws ? ws_elems : 0, (cudaStream_t)stream));
   return FLF_OK;
 }
@@ -1881,7 +1881,7 @@ int flf_net_conv16_tcgen05(int mode) { return net_set_conv16_tcgen05(mode); }
 
 long long flf_net_launches(void) { return net_launches(); }
 
-int flf_net_conv_wide_tcgen05(int on) { return net_set_conv_wide_tcgen05(on); }
+int flf_net_conv_wide_tcgen05(int mode) { return net_set_conv_wide_tcgen05(mode); }
 
 int flf_net_status(void) {
   const int v = net_status_read_and_clear();
@@ -1905,6 +1905,14 @@ int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream) {
   if (!w || !w2 || Ci <= 0 || Co <= 0) return fail(nullptr, FLF_E_ARG, "invalid weight flip arguments");
   NET_CHECK(launch_conv3d_flip(w, w2, Ci, Co, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
+int flf_conv3d_pack(const void *w, void *wp, int Ci, int Co, void *stream) {
+  if (!w || !wp || Ci <= 0 || Co <= 0 || Ci % 16 || Co % 8)
+    return fail(nullptr, FLF_E_ARG, "invalid weight packing arguments (Ci a multiple of 16, Co of 8)");
+  if (!aligned16(wp)) return fail(nullptr, FLF_E_ARG, "packed weights must be 16-byte aligned");
+  NET_CHECK(launch_conv3d_pack(w, wp, Ci, Co, (cudaStream_t)stream));
   return FLF_OK;
 }
 

@@ -290,8 +290,9 @@ struct ConvParams {          // y = act(conv3x3x3(x, w) + bias) (* (mask > 0))
   int B, Z, Y, X, Ci, Co, relu;
   float *ws;                 // [splits][M][Co] FP32 partial sums when the K loop is split (splits > 1)
   int splits;
-  const __nv_bfloat16 *wt;   // or null: the same weights flipped, wt[26 - tap][co][ci] = w[tap][ci][co]
-                             // (K-major per tap, what the tcgen05 kernel of the wide layers reads)
+  const __nv_bfloat16 *wp;   // or null: the same weights packed by k_conv3d_pack_weights (per tap
+                             // and 16 input channels one [2][Co][8] block), what the tcgen05
+                             // kernel of the wide layers reads
 };
 struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co]
   const __nv_bfloat16 *x;
@@ -303,7 +304,8 @@ struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co
 };
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
 long long net_launches();
-int net_set_conv_wide_tcgen05(int on);
+int net_set_conv_wide_tcgen05(int mode);
+cudaError_t launch_conv3d_pack(const void *w, void *wp, int Ci, int Co, cudaStream_t s);
 cudaError_t launch_conv3d_wgrad(WgradParams p, long long ws_elems, cudaStream_t s, int num_sms);
 cudaError_t launch_conv3d_tc16(const ConvParams &p, cudaStream_t s);
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32);

@@ -19,6 +19,10 @@
 //                     epilogue roles, TMA-staged input slabs, the z taps
 //                     folded into N and summed from a TMEM accumulator ring.
 //   k_conv3d_tc16     the first single-role tcgen05 16 -> 16 kernel.
+//   k_conv3d_wide     32..128 -> 32..128 channels (a side of 64 or more) on
+//                     tcgen05: padded-row implicit GEMM over TMA-staged input
+//                     slabs, packed weights streamed by bulk copies, persistent
+//                     CTAs with two TMEM accumulator buffers.
 //   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
 //                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
 //                     split-K over its 4 warps, FP32 atomics into dW.
@@ -1625,197 +1629,417 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 
 // ---------------------------------------------------------------------------
 // Wide layers (32..128 channels in and out, at least one side 64 or more) on
-// tcgen05: an implicit GEMM whose CTA owns M = 128 consecutive voxels and all
-// N = CO output channels (one TMEM accumulator of CO columns), K = 27 taps x
-// CI input channels.  One pipeline stage holds one tap: the A tile (the 128
-// voxels' neighbours at that tap, CI channels each, zero outside the volume)
-// and the B tile (that tap's CO x CI weights), both in the canonical
-// no-swizzle K-major layout (8-row x 16-byte core matrices; K-adjacent core
-// matrices LBO apart, row-adjacent ones 128 bytes apart), written by cp.async
-// from all threads, S taps ahead.  Thread 0 issues the tap's CI / 16 MMAs
-// (M 128 x N CO x K 16) and commits them to the stage's mbarrier, which frees
-// the stage.  B comes from the flipped weights (wt[26 - tap] is the tap's
-// [co][ci] matrix, as flf_conv3d_flip writes it).  Epilogue: each warp reads
-// its 32 TMEM lanes (voxels) x CO columns, adds the bias, ReLU / mask, and
-// stores BF16.  Every wait is bounded (g_net_err).
+// tcgen05, as an implicit GEMM over "padded rows".  A work item is one output
+// plane z of one volume b and a block of R rows y0 .. y0+R-1.  Input slabs
+// (R+2 rows x Xp = X+2 voxels, the halo included, zeros outside the volume)
+// arrive by TMA in the canonical no-swizzle K-major layout: one 16-byte row
+// per voxel and 8 channels, the 8-channel groups LBO apart.  In such a slab
+// the voxel at (row r, column c) is row r*Xp + c, so for output position
+// q = r*Xp + x (x < Xp) the tap (dy, dx) is slab row q + dy*Xp + dx: every
+// tap's A operand is the slab seen from another start row, a legal operand
+// address (16-byte aligned).  An item's M = nM x 128 positions q cover its R
+// rows (positions with x >= X or beyond the R rows are computed and dropped).
+//   chunk = one input plane z+dz x KC (<= 64) input channels: KC/8 TMA loads
+//           into one of 2 slab slots;
+//   B     = one (tap, 16 input channels) block of the packed weights
+//           (flf_conv3d_pack: [2 k8][CO][8] BF16), by 1-D bulk copy into a
+//           ring of 8;
+//   MMA   = M 128 x N CO x K 16, nM per B block, into one of 2 TMEM
+//           accumulator buffers (nM x CO <= 256 columns each).
+//   warp 0      slab producer (one thread);
+//   warp 1      MMA issuer (one thread), TMEM allocation;
+//   warp 2      B producer (one thread);
+//   warps 4-7   epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 of every
+//               M tile, adds the bias, ReLU / mask, stores BF16.
+// Items are dealt round-robin to persistent CTAs (one per SM); the epilogue of
+// an item overlaps the MMAs of the next.  Every mbarrier wait is bounded; a
+// give-up sets g_net_err and a shared abort flag, and the CTA drains its copies
+// and MMAs before TMEM is released.
 // ---------------------------------------------------------------------------
-template <int CI, int CO, int S>
-__global__ void __launch_bounds__(128, 1) k_conv3d_umma(ConvParams p) {
+struct WideGrid {
+  int Xp, R, nM, nyb;   // padded row, rows per item, M tiles per item, y blocks
+  int slab_rows;        // rows of one 8-channel group of a slab slot (LBO / 16)
+  long long items;      // B * Z * nyb
+};
+
+constexpr int WIDE_SB = 8;           // B block ring
+constexpr int WIDE_ACC_COLS = 256;   // columns of one TMEM accumulator buffer
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(256, 1)
+    k_conv3d_wide(const __grid_constant__ CUtensorMap tx, ConvParams p, const bf16 *__restrict__ wp, WideGrid g) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  constexpr uint32_t ABYTES = 128u * CI * 2u, BBYTES = (uint32_t)CO * CI * 2u;
-  constexpr uint32_t LBO_A = 16u * 128u, LBO_B = (CO / 8) * 128u;   // K-adjacent core matrices
-  constexpr uint32_t TCOLS = CO < 32 ? 32 : CO;
-  unsigned char *stA = smem;
-  unsigned char *stB = smem + S * ABYTES;
-  unsigned long long *bars = reinterpret_cast<unsigned long long *>(stB + S * BBYTES);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + S + 1);
+  constexpr int KC = CI < 64 ? CI : 64;   // input channels of one chunk
+  constexpr int NCG = CI / KC;            // chunks per input plane
+  constexpr int G8 = KC / 8;              // TMA loads (8-channel groups) per chunk
+  constexpr int KS = KC / 16;             // K steps per chunk
+  constexpr uint32_t BBLK = 32u * CO;     // one packed B block
+  static_assert(CI % 32 == 0 && CO % 32 == 0 && CO <= 128 && CI <= 128, "32..128 channels");
+  const uint32_t LBO = (uint32_t)g.slab_rows * 16u;   // between 8-channel groups of a slab
+  const uint32_t SLOT = G8 * LBO;
+  const uint32_t box_tx = 16u * (uint32_t)g.Xp * (uint32_t)(g.R + 2);
+  // layout: [2 slab slots][B ring][mbarriers][tmem address][abort flag]
+  const uint32_t smem_s = su32(smem);
+  const uint32_t slab_s = smem_s, bring_s = smem_s + 2 * SLOT;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + WIDE_SB * BBLK);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4 + 2 * WIDE_SB + 4 + 1);
+  volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint32_t bar_s = su32(bars);
+  auto sfull = [&](uint32_t k) { return bar_s + 8u * k; };                           // slab slot loaded
+  auto sempty = [&](uint32_t k) { return bar_s + 8u * (2 + k); };                    // slab slot read
+  auto bfull = [&](uint32_t k) { return bar_s + 8u * (4 + k); };                     // B block loaded
+  auto bempty = [&](uint32_t k) { return bar_s + 8u * (4 + WIDE_SB + k); };          // B block read
+  auto afull = [&](uint32_t k) { return bar_s + 8u * (4 + 2 * WIDE_SB + k); };       // accumulator done
+  auto aempty = [&](uint32_t k) { return bar_s + 8u * (6 + 2 * WIDE_SB + k); };      // accumulator read
+  const uint32_t fin = bar_s + 8u * (8 + 2 * WIDE_SB);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long M = (long long)p.B * p.Z * p.Y * p.X;
-  const long long m0 = (long long)blockIdx.x * 128;
-  const long long mrow = m0 + tid;
-  const bool rowok = mrow < M;
-  const Vox v = decode(rowok ? mrow : 0, p.Z, p.Y, p.X);
-  if (warp == 0) {
+
+  if (tid == 0) {
+    for (int k = 0; k < 2; k++) {
+      net_mbar_init(sfull(k), 1);
+      net_mbar_init(sempty(k), 1);
+      net_mbar_init(afull(k), 1);
+      net_mbar_init(aempty(k), 4);
+    }
+    for (int k = 0; k < WIDE_SB; k++) {
+      net_mbar_init(bfull(k), 1);
+      net_mbar_init(bempty(k), 1);
+    }
+    net_mbar_init(fin, 1);
+    *abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");   // visible to TMA and the MMAs
+  }
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
-                 "r"(TCOLS)
+                 "r"(2 * WIDE_ACC_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
-  if (tid == 0)
-    for (int i = 0; i < S; i++) net_mbar_init(su32(bars + i), 1);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(CO >> 3) << 17) | ((128u >> 4) << 24);
 
-  // stage `st` <- tap t: A row tid (its CI channels, 16-byte chunks j at core
-  // matrix (j, tid / 8), row tid % 8) and this thread's share of B
-  auto load = [&](int t, int st) {
-    const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
-    const int z = v.z + dz, y = v.y + dy, x = v.x + dx;
-    const bool ok = rowok && z >= 0 && z < p.Z && y >= 0 && y < p.Y && x >= 0 && x < p.X;
-    const bf16 *src = ok ? p.x + ((((long long)v.b * p.Z + z) * p.Y + y) * p.X + x) * CI : p.x;
-    const uint32_t a = su32(stA + st * ABYTES) + (tid >> 3) * 128 + (tid & 7) * 16;
-#pragma unroll
-    for (int j = 0; j < CI / 8; j++) cp16(a + j * LBO_A, ok ? src + 8 * j : p.x, ok);
-    const bf16 *wsrc = p.wt + (long long)(26 - t) * CO * CI;   // [co][ci]
-    const uint32_t b = su32(stB + st * BBYTES);
-    for (int i = tid; i < CO * CI / 8; i += 128) {
-      const int co = i / (CI / 8), j = i - co * (CI / 8);
-      cp16(b + j * LBO_B + (co >> 3) * 128 + (co & 7) * 16, wsrc + (long long)co * CI + 8 * j, true);
-    }
+  auto decode = [&](long long it, int &b, int &z, int &y0) {
+    const int yb = (int)(it % g.nyb);
+    const long long q = it / g.nyb;
+    z = (int)(q % p.Z);
+    b = (int)(q / p.Z);
+    y0 = yb * g.R;
   };
 
-  bool ok = true;
-  int committed = 0;   // taps whose MMAs were issued and committed
-  // taps 0 .. S-2 in flight before the first MMA
-#pragma unroll
-  for (int t = 0; t < S - 1; t++) {
-    load(t, t);
-    cp_commit();
-  }
-  for (int t = 0; t < 27; t++) {
-    const int st = t % S;
-    // refill the stage of tap t-1 with tap t+S-1 once tap t-1's MMAs are done
-    const int tn = t + S - 1;
-    if (tn < 27) {
-      if (t >= 1) {
-        const int late = net_mbar_wait(su32(bars + (t - 1) % S), ((t - 1) / S) & 1, 1000000000ULL) ? 0 : 1;
-        if (__syncthreads_or(late)) {
-          if (tid == 0) atomicExch(&g_net_err, 12);
+  uint32_t nslab = 0, nbb = 0;   // slab chunks / B blocks issued (producers)
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- slab producer ----
+      for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
+        int b, z, y0;
+        decode(it, b, z, y0);
+        bool ok = true;
+        for (int dz = -1; dz <= 1 && ok; dz++) {
+          if (z + dz < 0 || z + dz >= p.Z) continue;
+          for (int cg = 0; cg < NCG; cg++) {
+            const uint32_t sl = nslab & 1;
+            if (nslab >= 2 && !role_wait(sempty(sl), ((nslab >> 1) - 1) & 1, abort_s, 21)) {
+              ok = false;
+              break;
+            }
+            net_expect_tx(sfull(sl), G8 * box_tx);
+            for (int k = 0; k < G8; k++)
+              tma_load_5d(slab_s + sl * SLOT + k * LBO, &tx, cg * KC + 8 * k, -1, y0 - 1, z + dz, b, sfull(sl));
+            nslab++;
+          }
+        }
+        if (!ok) break;
+      }
+    }
+  } else if (warp == 2) {
+    if (lane == 0) {
+      // ---- B producer: the blocks in the issuer's order ----
+      for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
+        int b, z, y0;
+        decode(it, b, z, y0);
+        bool ok = true;
+        for (int dz = -1; dz <= 1 && ok; dz++) {
+          if (z + dz < 0 || z + dz >= p.Z) continue;
+          for (int cg = 0; cg < NCG && ok; cg++)
+            for (int t9 = 0; t9 < 9 && ok; t9++)
+              for (int ks = 0; ks < KS; ks++) {
+                const uint32_t sl = nbb % WIDE_SB;
+                if (nbb >= WIDE_SB && !role_wait(bempty(sl), ((nbb / WIDE_SB) - 1) & 1, abort_s, 22)) {
+                  ok = false;
+                  break;
+                }
+                const int tap = (dz + 1) * 9 + t9;
+                const bf16 *src = wp + ((long long)tap * (CI / 16) + cg * KS + ks) * (BBLK / 2);
+                net_expect_tx(bfull(sl), BBLK);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                        bring_s + sl * BBLK),
+                    "l"(src), "r"(BBLK), "r"(bfull(sl))
+                    : "memory");
+                nbb++;
+              }
+        }
+        if (!ok) break;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = CO, M = 128
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(CO >> 3) << 17) | ((128u >> 4) << 24);
+      uint32_t ns = 0, nb = 0, li = 0;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x, li++) {
+        int b, z, y0;
+        decode(it, b, z, y0);
+        const uint32_t ab = li & 1;
+        if (li >= 2 && !role_wait(aempty(ab), ((li >> 1) - 1) & 1, abort_s, 23)) {
           ok = false;
           break;
         }
+        tc_fence_after();
+        const uint32_t dcol = tmem + ab * WIDE_ACC_COLS;
+        bool first = true;
+        for (int dz = -1; dz <= 1 && ok; dz++) {
+          if (z + dz < 0 || z + dz >= p.Z) continue;
+          for (int cg = 0; cg < NCG && ok; cg++) {
+            const uint32_t sl = ns & 1;
+            if (!role_wait(sfull(sl), (ns >> 1) & 1, abort_s, 24)) {
+              ok = false;
+              break;
+            }
+            const uint32_t a0 = slab_s + sl * SLOT;
+            for (int t9 = 0; t9 < 9 && ok; t9++) {
+              const int dy = t9 / 3, dx = t9 % 3;
+              for (int ks = 0; ks < KS; ks++) {
+                const uint32_t bs = nb % WIDE_SB;
+                if (!role_wait(bfull(bs), (nb / WIDE_SB) & 1, abort_s, 25)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint64_t bd = umma_desc(bring_s + bs * BBLK, 16u * CO, 128);
+                for (int m = 0; m < g.nM; m++) {
+                  const uint32_t row = (uint32_t)(m * 128 + dy * g.Xp + dx);
+                  const uint64_t ad = umma_desc(a0 + 2u * ks * LBO + row * 16u, LBO, 128);
+                  umma_f16(dcol + m * CO, ad, bd, idesc, first ? 0u : 1u);
+                }
+                first = false;
+                umma_commit(bempty(bs));   // the B block is free once these MMAs complete
+                nb++;
+              }
+            }
+            if (!ok) break;
+            umma_commit(sempty(sl));       // the slab slot likewise
+            ns++;
+          }
+        }
+        if (!ok) break;
+        umma_commit(afull(ab));
       }
-      load(tn, tn % S);
     }
-    cp_commit();
-    cp_wait<S - 1>();                        // tap t's copies are in shared memory
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+  } else if (warp >= 4) {
+    // ---- epilogue ----
+    const int qd = warp & 3;
+    const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
+    uint32_t li = 0;
+    for (long long it = blockIdx.x; it < g.items; it += gridDim.x, li++) {
+      int b, z, y0;
+      decode(it, b, z, y0);
+      const uint32_t ab = li & 1;
+      // tcgen05.ld is .sync.aligned: the whole warp takes one decision
+      if (!__all_sync(0xffffffffu, role_wait(afull(ab), (li >> 1) & 1, abort_s, 26) ? 1 : 0)) break;
       tc_fence_after();
-      const uint32_t a0 = su32(stA + st * ABYTES), b0 = su32(stB + st * BBYTES);
-#pragma unroll
-      for (int k = 0; k < CI / 16; k++) {
-        const uint64_t ad = umma_desc(a0 + 2 * k * LBO_A, LBO_A, 128);
-        const uint64_t bd = umma_desc(b0 + 2 * k * LBO_B, LBO_B, 128);
-        umma_f16(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
-      }
-      umma_commit(su32(bars + st));
-    }
-    committed = t + 1;
-  }
-  cp_wait<0>();
-  // the taps whose stage was not waited for in the loop: every MMA is done
-  // (and every commit has arrived) before TMEM and shared memory are released
-  int late = 0;
-  for (int t = committed > S ? committed - S : 0; t < committed; t++)
-    if (!net_mbar_wait(su32(bars + t % S), (t / S) & 1, 1000000000ULL)) late = 1;
-  if (__syncthreads_or(late)) {
-    if (tid == 0) atomicExch(&g_net_err, 13);
-    ok = false;
-  }
-  tc_fence_after();
-  if (ok) {
-    const long long row = m0 + warp * 32 + lane;
+      for (int m = 0; m < g.nM; m++) {
+        const int q = m * 128 + qd * 32 + lane;
+        const int yl = q / g.Xp, x = q - yl * g.Xp;
+        const int y = y0 + yl;
+        const bool valid = yl < g.R && y < p.Y && x < p.X;
+        const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO;
 #pragma unroll 1
-    for (int c0 = 0; c0 < CO; c0 += 16) {
-      float d[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, d);
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      if (row < M) {
-        const long long o = row * CO + c0;
-        uint4 mk[2];
-        if (p.mask) {
-          mk[0] = *reinterpret_cast<const uint4 *>(p.mask + o);
-          mk[1] = *reinterpret_cast<const uint4 *>(p.mask + o + 8);
-        }
-        const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
-        uint4 outv[2];
-        __nv_bfloat162 *hh = reinterpret_cast<__nv_bfloat162 *>(outv);
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-          float v0 = d[2 * k] + (p.bias ? p.bias[c0 + 2 * k] : 0.f);
-          float v1 = d[2 * k + 1] + (p.bias ? p.bias[c0 + 2 * k + 1] : 0.f);
-          if (p.relu) {
-            v0 = fmaxf(v0, 0.f);
-            v1 = fmaxf(v1, 0.f);
-          }
+        for (int c0 = 0; c0 < CO; c0 += 16) {
+          float d[16];
+          tmem_ld16(tmem + lane_base + ab * WIDE_ACC_COLS + m * CO + c0, d);
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          if (!valid) continue;
+          uint4 mk[2];
           if (p.mask) {
-            const float2 mf = __bfloat1622float2(m2[k]);
-            if (!(mf.x > 0.f)) v0 = 0.f;
-            if (!(mf.y > 0.f)) v1 = 0.f;
+            mk[0] = *reinterpret_cast<const uint4 *>(p.mask + off + c0);
+            mk[1] = *reinterpret_cast<const uint4 *>(p.mask + off + c0 + 8);
           }
-          hh[k] = __floats2bfloat162_rn(v0, v1);
+          const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
+          uint4 outv[2];
+          __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(outv);
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            float v0 = d[2 * k] + (p.bias ? p.bias[c0 + 2 * k] : 0.f);
+            float v1 = d[2 * k + 1] + (p.bias ? p.bias[c0 + 2 * k + 1] : 0.f);
+            if (p.relu) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            if (p.mask) {
+              const float2 mf = __bfloat1622float2(m2[k]);
+              if (!(mf.x > 0.f)) v0 = 0.f;
+              if (!(mf.y > 0.f)) v1 = 0.f;
+            }
+            hv[k] = __floats2bfloat162_rn(v0, v1);
+          }
+          *reinterpret_cast<uint4 *>(p.y + off + c0) = outv[0];
+          *reinterpret_cast<uint4 *>(p.y + off + c0 + 8) = outv[1];
         }
-        *reinterpret_cast<uint4 *>(p.y + o) = outv[0];
-        *reinterpret_cast<uint4 *>(p.y + o + 8) = outv[1];
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) net_arrive(aempty(ab));
     }
+  }
+
+  __syncthreads();   // every role has left its loop (normally, or on an abort)
+  if (*abort_s) {
+    // copies still in flight land before the CTA exits: wait for the last load of every slot
+    if (warp == 0 && lane == 0)
+      for (uint32_t sl = 0; sl < 2 && sl < nslab; sl++) {
+        const uint32_t last = sl + ((nslab - 1 - sl) / 2) * 2;
+        if (!net_mbar_wait(sfull(sl), (last >> 1) & 1, 1000000000ULL)) atomicExch(&g_net_err, 27);
+      }
+    if (warp == 2 && lane == 0)
+      for (uint32_t sl = 0; sl < (uint32_t)WIDE_SB && sl < nbb; sl++) {
+        const uint32_t last = sl + ((nbb - 1 - sl) / WIDE_SB) * WIDE_SB;
+        if (!net_mbar_wait(bfull(sl), (last / WIDE_SB) & 1, 1000000000ULL)) atomicExch(&g_net_err, 28);
+      }
+  }
+  if (warp == 1 && lane == 0) {
+    // every MMA issued has completed before the accumulators are released
+    umma_commit(fin);
+    if (!net_mbar_wait(fin, 0, 1000000000ULL)) atomicExch(&g_net_err, 29);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * WIDE_ACC_COLS)
+                 : "memory");
   }
 }
 
-template <int CI, int CO>
-static cudaError_t launch_umma(const ConvParams &p, cudaStream_t s) {
-  constexpr int S = (CI * 256 + CO * CI * 2) <= 48 * 1024 ? 4 : 3;
-  constexpr size_t SMEM = (size_t)S * (128 * CI * 2 + CO * CI * 2) + 8 * (S + 1) + 16;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_umma<CI, CO, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM);
-    if (e != cudaSuccess) return e;
-    attr = true;
+// Packed B blocks of the wide kernel: wp[((tap * Ci/16 + ks) * 2 + k8) * Co + co][j]
+// = w[tap][ci = 16 ks + 8 k8 + j][co], i.e. per (tap, 16 input channels) one
+// [2][Co][8] block, the canonical no-swizzle K-major layout of an N = Co x
+// K = 16 operand (K-adjacent core matrices 16 Co bytes apart).
+__global__ void k_conv3d_pack_weights(const bf16 *w, bf16 *wp, int Ci, int Co) {
+  const long long n = 27LL * Ci * Co;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int co = (int)(i % Co);
+    const long long t = i / Co;
+    const int ci = (int)(t % Ci), tap = (int)(t / Ci);
+    const int ks = ci >> 4, k8 = (ci >> 3) & 1, j = ci & 7;
+    wp[((((long long)tap * (Ci / 16) + ks) * 2 + k8) * Co + co) * 8 + j] = w[i];
   }
-  const long long M = (long long)p.B * p.Z * p.Y * p.X;
-  FLF_NET_LAUNCH(k_conv3d_umma<CI, CO, S><<<(unsigned)((M + 127) / 128), 128, SMEM, s>>>(p));
-  return cudaGetLastError();
 }
 
-// the wide layers (a side of 64 or 128 channels) on tcgen05 when the flipped
-// weights are given: 1 (default) or 0 (mma.sync)
+// 0: the wide layers on mma.sync; 1 (default): on k_conv3d_wide with the rows
+// per item chosen from the shape; 2..5: k_conv3d_wide with 1..4 M tiles per
+// item (a sweep of the choice)
 static int g_conv_wide_tc = 1;
 
-int net_set_conv_wide_tcgen05(int on) {
+int net_set_conv_wide_tcgen05(int mode) {
   const int old = g_conv_wide_tc;
-  g_conv_wide_tc = on ? 1 : 0;
+  g_conv_wide_tc = mode < 0 ? 0 : (mode > 5 ? 5 : mode);
   return old;
 }
 
-static cudaError_t launch_wide_umma(const ConvParams &p, cudaStream_t s, bool &done) {
-  done = true;
-#define FLF_UM(a, b) if (p.Ci == a && p.Co == b) return launch_umma<a, b>(p, s);
-  FLF_UM(32, 64) FLF_UM(64, 32) FLF_UM(64, 64) FLF_UM(64, 128) FLF_UM(128, 64) FLF_UM(128, 128)
-  FLF_UM(32, 128) FLF_UM(128, 32)
-#undef FLF_UM
+// Shared memory of k_conv3d_wide for a slab of slab_rows rows per 8-channel group.
+static size_t wide_smem(int CI, int CO, int slab_rows) {
+  const int KC = CI < 64 ? CI : 64;
+  return (size_t)2 * (KC / 8) * slab_rows * 16 + (size_t)WIDE_SB * 32 * CO + 8 * (8 + 2 * WIDE_SB + 1) + 16;
+}
+
+// The item shape for nM M tiles: rows per item R (balanced over the y blocks),
+// its slab rows and shared memory; false when nM tiles hold no full row or the
+// slab does not fit.
+static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t &smem) {
+  g.Xp = X + 2;
+  const int rmax = nM * 128 / g.Xp;
+  if (rmax < 1 || g.Xp > 256 || nM * CO > WIDE_ACC_COLS) return false;
+  g.nyb = (Y + rmax - 1) / rmax;
+  g.R = (Y + g.nyb - 1) / g.nyb;
+  if (g.R + 2 > 256) return false;
+  g.nM = (g.R * g.Xp + 127) / 128;
+  g.slab_rows = (g.nM * 128 + 2 * g.Xp + 2 + 7) / 8 * 8;
+  smem = wide_smem(CI, CO, g.slab_rows);
+  return smem <= 227 * 1024;
+}
+
+template <int CI, int CO>
+static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) {
   done = false;
+  if (!p.wp) return cudaSuccess;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 1;
+  }
+  // item shape: forced (modes 2..5), else the one with the least estimated time
+  // (waves of items x their MMA count, plus a fixed cost per item)
+  WideGrid g{};
+  size_t smem = 0;
+  bool found = false;
+  double best = 0;
+  for (int nM = 1; nM <= 4; nM++) {
+    if (g_conv_wide_tc >= 2 && nM != g_conv_wide_tc - 1) continue;
+    WideGrid c{};
+    size_t sm = 0;
+    if (!wide_shape(CI, CO, p.Y, p.X, nM, c, sm)) continue;
+    c.items = (long long)p.B * p.Z * c.nyb;
+    const double waves = (double)((c.items + sms - 1) / sms);
+    const double cost = waves * (c.nM + 0.5);
+    if (!found || cost < best) {
+      found = true;
+      best = cost;
+      g = c;
+      smem = sm;
+    }
+  }
+  if (!found) return cudaSuccess;   // the mma.sync kernel takes this shape
+  done = true;
+  if (reinterpret_cast<uintptr_t>(p.x) % 16 || reinterpret_cast<uintptr_t>(p.wp) % 16) return cudaErrorMisalignedAddress;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  CUtensorMap map;
+  const cuuint64_t vb = 2ull * CI;   // bytes per voxel
+  const cuuint64_t dims[5] = {(cuuint64_t)CI, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
+  const cuuint64_t strides[4] = {vb, vb * p.X, vb * p.X * p.Y, vb * p.X * p.Y * p.Z};
+  const cuuint32_t box[5] = {8u, (cuuint32_t)g.Xp, (cuuint32_t)(g.R + 2), 1, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(p.x), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  // one CTA per SM (its 512 TMEM columns): ask for at least half the shared memory
+  const size_t sm_launch = smem < 116 * 1024 ? 116 * 1024 : smem;
+  static size_t attr = 0;
+  if (attr < sm_launch) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_wide<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(227 * 1024));
+    if (e != cudaSuccess) return e;
+    attr = 227 * 1024;
+  }
+  const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
+  FLF_NET_LAUNCH(k_conv3d_wide<CI, CO><<<grid, 256, sm_launch, s>>>(map, p, p.wp, g));
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_wide_tc(const ConvParams &p, cudaStream_t s, bool &done) {
+  done = false;
+#define FLF_WD(a, b) if (p.Ci == a && p.Co == b) return launch_wide<a, b>(p, s, done);
+  FLF_WD(32, 64) FLF_WD(64, 32) FLF_WD(64, 64) FLF_WD(64, 128) FLF_WD(128, 64) FLF_WD(128, 128)
+  FLF_WD(32, 128) FLF_WD(128, 32)
+#undef FLF_WD
   return cudaSuccess;
 }
 
@@ -1846,9 +2070,9 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
     return g_conv16_tc == 2 ? launch_tma16<32, 16, 2, 4, false, true>(p, HeadOut{}, s) : launch_tiled<32, 16>(p, s);
   if (p.Ci == 32 && p.Co == 32)
     return g_conv16_tc == 2 ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
-  if (p.wt && g_conv_wide_tc) {
+  if (p.wp && g_conv_wide_tc) {
     bool done = false;
-    const cudaError_t e = launch_wide_umma(p, s, done);
+    const cudaError_t e = launch_wide_tc(p, s, done);
     if (done) return e;
   }
   const int BN = p.Co >= 64 ? 64 : p.Co;
@@ -1952,6 +2176,12 @@ int net_status_read_and_clear() {
 
 cudaError_t launch_conv3d_flip(const void *w, void *w2, int Ci, int Co, cudaStream_t s) {
   FLF_NET_LAUNCH(k_conv3d_flip_weights<<<grid_for(27LL * Ci * Co, 256), 256, 0, s>>>((const bf16 *)w, (bf16 *)w2, Ci, Co));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv3d_pack(const void *w, void *wp, int Ci, int Co, cudaStream_t s) {
+  FLF_NET_LAUNCH(k_conv3d_pack_weights<<<grid_for(27LL * Ci * Co, 256), 256, 0, s>>>((const bf16 *)w, (bf16 *)wp, Ci,
+                                                                                      Co));
   return cudaGetLastError();
 }
 

@@ -79,6 +79,9 @@ class UNet3D:
         for q in self.p.values():
             q["wb"] = _bf(q["w"].shape, self.dev)
             q["wf"] = _bf((27, q["co"], q["ci"]), self.dev)
+            if max(q["ci"], q["co"]) >= 64:   # the wide layers' tcgen05 kernel reads packed weights
+                q["wp"] = _bf(q["w"].shape, self.dev)
+                q["wfp"] = _bf((27, q["co"], q["ci"]), self.dev)
             for k in ("gw", "mw", "vw"):
                 q[k] = torch.zeros_like(q["w"])
             for k in ("gb", "mb", "vb"):
@@ -89,7 +92,16 @@ class UNet3D:
         s = torch.cuda.current_stream(self.dev).cuda_stream
         for q in self.p.values():
             q["wb"].copy_(q["w"])
-            _flf.conv3d_flip(q["wb"], q["wf"], s)
+            self._derive(q, s)
+
+    @staticmethod
+    def _derive(q, s):
+        """The flipped weights of the data gradient and, for the wide layers, both
+        weight sets packed for the tcgen05 kernel, from the BF16 weights."""
+        _flf.conv3d_flip(q["wb"], q["wf"], s)
+        if "wp" in q:
+            _flf.conv3d_pack(q["wb"], q["wp"], s)
+            _flf.conv3d_pack(q["wf"], q["wfp"], s)
 
     def num_parameters(self):
         return int(sum(q["w"].numel() + q["b"].numel() for q in self.p.values()))
@@ -106,7 +118,7 @@ class UNet3D:
             self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
         _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,
                     stream=torch.cuda.current_stream(self.dev).cuda_stream, ws=self._ws,
-                    wt=q["wb"] if flip else q["wf"])
+                    wp=q.get("wfp") if flip else q.get("wp"))
         return y
 
     def _pool(self, x):
@@ -216,7 +228,7 @@ class UNet3D:
                 q["gw"][:, :, 1:] = 0
             _flf.adam(q["w"], q["gw"], q["mw"], q["vw"], q["wb"], lr, b1, b2, eps, c1, c2, wd, s)
             _flf.adam(q["b"], q["gb"], q["mb"], q["vb"], None, lr, b1, b2, eps, c1, c2, 0.0, s)
-            _flf.conv3d_flip(q["wb"], q["wf"], s)
+            self._derive(q, s)
 
     def state_dict(self):
         return {"%s.%s" % (n, k): q[k].cpu().numpy() for n, q in self.p.items() for k in ("w", "b")}

@@ -247,10 +247,10 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   or NULL) lets layers with few output tiles split their K loop across
  *   CTAs, each split into its own B Z Y X Co slice (as many splits as fit,
  *   at least 2), summed in split order; it must not be shared by concurrent
- *   calls.  wt (or NULL): the same weights as flf_conv3d_flip writes them
- *   (wt[26 - tap][co][ci] = w[tap][ci][co]); with it the layers of 32 to 128
- *   channels with a side of 64 or more run on the tcgen05 tensor cores
- *   (flf_net_conv_wide_tcgen05(0) selects the mma.sync kernel instead).
+ *   calls.  wp (or NULL): the same weights as flf_conv3d_pack writes them;
+ *   with it the layers of 32 to 128 channels with a side of 64 or more (and
+ *   X <= 254) run on the tcgen05 tensor cores (flf_net_conv_wide_tcgen05(0)
+ *   selects the mma.sync kernel instead).
  * flf_conv3d_wgrad: dw [27][Ci][Co] float += sum_v x[v + tap][ci] dy[v][co].
  *   The voxels are cut into chunks whose partial gradients go to ws (float,
  *   27 Ci Co per chunk; as many chunks as ws holds, one without ws) and are
@@ -260,6 +260,9 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   value of flf_mse_grad alone is summed with atomics.
  * flf_conv3d_flip: w2[26 - tap][co][ci] = w[tap][ci][co]; conv3d with w2 is
  *   the data gradient.
+ * flf_conv3d_pack: wp = w [27][Ci][Co] (Ci a multiple of 16) as the B operand
+ *   blocks of the tcgen05 wide-layer kernel: per tap and 16 input channels
+ *   one [2][Co][8] block (27 Ci Co bf16 in all, 16-byte aligned).
  * flf_bias_grad: db[c] += sum over the M rows of g[M][C] (C <= 128); row
  *   blocks of 2048 have their sums in ws (float, C per block; as many blocks as
  *   ws holds, one without ws), added in block order.
@@ -279,7 +282,7 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   fixed-point integers, so the result does not depend on the order of
  *   arrival (per-voxel totals below 2^31); without it, FP32 atomics. */
 int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y, int X,
-               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wt, void *stream);
+               int Ci, int Co, int relu, float *ws, long long ws_elems, const void *wp, void *stream);
 int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int Y, int X, int Ci, int Co,
                      float *ws, long long ws_elems, void *stream);
 /* flf_conv3d_tc: flf_conv3d for 16 -> 16 channels on the tcgen05 tensor cores
@@ -301,10 +304,14 @@ int flf_net_conv16_tcgen05(int mode);
 /* Number of kernel launches the network entry points above have made since
  * the library was loaded (all threads). */
 long long flf_net_launches(void);
-/* Wide layers (a side of 64 or 128 channels) on tcgen05 when flf_conv3d gets
- * the flipped weights: 1 (default) or 0 (mma.sync); returns the previous value. */
-int flf_net_conv_wide_tcgen05(int on);
+/* Wide layers (a side of 64 or 128 channels) when flf_conv3d gets packed
+ * weights: 0 = the mma.sync kernel; 1 (default) = the tcgen05 kernel with the
+ * rows per work item chosen from the shape; 2..5 = the tcgen05 kernel with
+ * 1..4 tiles of 128 padded-row positions per work item.  Returns the previous
+ * value. */
+int flf_net_conv_wide_tcgen05(int mode);
 int flf_conv3d_flip(const void *w, void *w2, int Ci, int Co, void *stream);
+int flf_conv3d_pack(const void *w, void *wp, int Ci, int Co, void *stream);
 int flf_bias_grad(const void *g, float *db, long long M, int C, float *ws, long long ws_elems, void *stream);
 int flf_pool2(const void *in, void *out, int B, int Z, int Y, int X, int C, void *stream);
 int flf_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *gin, int B, int Z, int Y, int X, int C,

@@ -58,16 +58,26 @@ def test_conv3d_forward(env, shape, Ci, Co, relu):
     ref = _ref_conv(torch, x.double(), w.double(), b.double())
     if relu:
         ref = ref.clamp_min(0)
-    # without and with the flipped weights (with them the wide layers run on tcgen05)
-    wt = torch.empty((27, Co, Ci), dtype=torch.bfloat16, device="cuda")
-    _flf.conv3d_flip(w.cuda(), wt)
-    for flipped in (None, wt):
-        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws, wt=flipped)
+    # without and with the packed weights (with them the wide layers run on tcgen05)
+    wp = torch.empty((27, Ci, Co), dtype=torch.bfloat16, device="cuda")
+    _flf.conv3d_pack(w.cuda(), wp)
+    for packed in (None, wp):
+        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws, wp=packed)
         _close(torch, y, ref)
         # split layers add their K slices in a fixed order: the same bits again
         y2 = torch.empty_like(y)
-        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y2, relu=relu, ws=ws, wt=flipped)
+        _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y2, relu=relu, ws=ws, wp=packed)
         assert torch.equal(y, y2)
+    if max(Ci, Co) >= 64:
+        # every work-item shape of the tcgen05 kernel (1..4 M tiles of 128 padded-row positions)
+        try:
+            for mode in (2, 3, 4, 5):
+                _flf.conv_wide_tcgen05(mode)
+                y.zero_()
+                _flf.conv3d(x.cuda(), w.cuda(), b.cuda(), y, relu=relu, ws=ws, wp=wp)
+                _close(torch, y, ref)
+        finally:
+            _flf.conv_wide_tcgen05(1)
     torch.cuda.synchronize()
     _flf.net_status()
 
@@ -90,9 +100,66 @@ def test_conv3d_mask_and_data_gradient(env, shape, Ci, Co):
     ws = torch.empty(4 * int(np.prod(shape)) * Ci, device="cuda")
     _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws)
     _close(torch, dx, ref)
-    # the data gradient on tcgen05: the flipped weights of w2 are w itself
-    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws, wt=w.cuda())
+    # the data gradient on tcgen05 (packed flipped weights)
+    w2p = torch.empty_like(w2)
+    _flf.conv3d_pack(w2, w2p)
+    dx.zero_()
+    _flf.conv3d(dy.cuda(), w2, None, dx, mask=act.cuda(), ws=ws, wp=w2p)
     _close(torch, dx, ref)
+
+
+@pytest.mark.parametrize("shape,Ci,Co,relu,masked", [
+    # the network's wide layers at inference (24 x 456 x 456 volume: levels 2 and 3)
+    ((1, 6, 114, 114), 32, 64, True, False), ((1, 6, 114, 114), 64, 64, True, False),
+    ((1, 6, 114, 114), 64, 32, True, False), ((1, 3, 57, 57), 64, 128, True, False),
+    ((1, 3, 57, 57), 128, 128, True, False), ((1, 3, 57, 57), 128, 64, True, False),
+    # training crops (4 x 24 x 128 x 128) with the ReLU mask of a data gradient
+    ((4, 6, 32, 32), 64, 64, False, True), ((4, 3, 16, 16), 128, 128, False, True),
+    ((4, 6, 32, 32), 64, 32, False, True), ((4, 3, 16, 16), 64, 128, False, True),
+    # the widest padded row a TMA box takes (254 + 2), and a wider one (mma.sync)
+    ((1, 2, 9, 254), 64, 64, True, False), ((1, 2, 5, 300), 64, 64, True, False),
+])
+def test_wide_layers_against_fp32_conv(env, shape, Ci, Co, relu, masked):
+    """The wide layers at the network's own shapes, against torch's FP32 conv3d on the
+    same BF16 inputs (TF32 off), both kernels and every tcgen05 work-item shape."""
+    torch, _flf = env
+    g = torch.Generator().manual_seed(Ci + 7 * Co + shape[-1])
+    x = torch.randn(shape + (Ci,), generator=g).bfloat16().cuda()
+    w = (torch.randn((27, Ci, Co), generator=g) / np.sqrt(27 * Ci)).bfloat16().cuda()
+    b = None if masked else torch.randn(Co, generator=g).float().cuda()
+    mask = torch.randn(shape + (Co,), generator=g).bfloat16().cuda() if masked else None
+    old = torch.backends.cudnn.allow_tf32
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        wr = w.float().reshape(3, 3, 3, Ci, Co).permute(4, 3, 0, 1, 2).contiguous()
+        ref = torch.nn.functional.conv3d(x.float().permute(0, 4, 1, 2, 3), wr, bias=b, padding=1)
+        ref = ref.permute(0, 2, 3, 4, 1).double().cpu()
+    finally:
+        torch.backends.cudnn.allow_tf32 = old
+    if relu:
+        ref = ref.clamp_min(0)
+    if masked:
+        ref = ref * (mask.double().cpu() > 0)
+    wp = torch.empty_like(w)
+    _flf.conv3d_pack(w, wp)
+    y = torch.empty(shape + (Co,), dtype=torch.bfloat16, device="cuda")
+    ws = torch.empty(4 * int(np.prod(shape)) * Co, device="cuda")
+    first = None
+    try:
+        for mode in (0, 1, 2, 3, 4, 5):
+            _flf.conv_wide_tcgen05(mode)
+            y.zero_()
+            _flf.conv3d(x, w, b, y, relu=relu, mask=mask, ws=ws, wp=wp)
+            _close(torch, y, ref)
+            if mode == 1:
+                first = y.clone()
+        _flf.conv_wide_tcgen05(1)
+        _flf.conv3d(x, w, b, y, relu=relu, mask=mask, ws=ws, wp=wp)
+        assert torch.equal(y, first)      # the same bits on a second run
+    finally:
+        _flf.conv_wide_tcgen05(1)
+    torch.cuda.synchronize()
+    _flf.net_status()
 
 
 @pytest.mark.parametrize("shape,Ci,Co", [((2, 4, 6, 10), 16, 16), ((1, 6, 9, 11), 32, 64), ((2, 3, 8, 8), 128, 128),
