@@ -165,6 +165,29 @@ def test_training_and_warm_started_rl(env):
     assert need is not None and need < 8, need
 
 
+def test_training_repeats_bit_for_bit(env):
+    """No reduction of training uses floating-point atomics (weight and bias
+    gradients add their partial sums in a fixed order, the training volumes are
+    rendered with fixed-point sums), so two runs with the same seeds give the
+    same weights, bit for bit."""
+    torch, ws_mod = env
+    import projector
+    import psfmatrix
+    import synthetic
+    N = 5
+    H, Ht = synthetic.synthetic_psf(N, np.arange(-4, 5, 2), 3)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    runs = []
+    for _ in range(2):
+        p = projector.Projector_gb300()
+        ws = ws_mod.WarmStart(p, hm, 60, 60, beads=30, filaments=2)
+        ws.train(steps=30, batch=2, crop=32, volumes_per_refresh=4, refresh_every=10, target_iters=4)
+        runs.append({k: v.copy() for k, v in ws.net.state_dict().items()})
+    assert runs[0].keys() == runs[1].keys()
+    for k in runs[0]:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
 @pytest.mark.parametrize("tcgen05", [False, True])
 def test_fused_input_and_head_kernels(env, tcgen05):
     """flf_ws_input / flf_ws_head against their torch formulas (head on the
