@@ -1075,6 +1075,8 @@ def run_warmstart(args):
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
                        "conv_kernels": "tcgen05 for the 16/32-channel layers, mma.sync for 64/128 channels",
                        "target_iters": args.target_iters, "residual_finetune_steps": args.tune_steps,
+                       "residual_finetune_loss_first_last": ([ws.tune_losses[0][1], ws.tune_losses[-1][1]]
+                                                             if ws.tune_losses else None),
                        "finetune_s": round(tune_s, 1),
                        "train_loss_mean_last_100": float(np.mean(losses[-100:])) if losses else None,
                        "train_loss_mean_first_100": float(np.mean(losses[:100])) if losses else None,

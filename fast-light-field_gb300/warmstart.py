@@ -303,7 +303,8 @@ class WarmStart:
         self.hth1.clamp_(min=1e-12)
         self.c2 = float(1.0 / self.hth1.mean())
         self.c3 = float(1.0 / self.ht1.mean())
-        self.losses = []
+        self.losses = []         # (step, loss) of train()
+        self.tune_losses = []    # (step, residual loss) of finetune_residual()
 
     @property
     def ctx(self):
@@ -425,7 +426,7 @@ class WarmStart:
             self.net.backward(cache, dout)
             self.net.adam_step(lr)
             if log_every and (step % log_every == 0 or step == steps - 1):
-                self.losses.append(("residual", step, loss))
+                self.tune_losses.append((step, loss))
             del cache, out
         torch.cuda.synchronize(self.dev)
         _flf.net_status()   # raise if a bounded wait in a tensor-core convolution gave up
