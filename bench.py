@@ -42,11 +42,11 @@ for _p in (ROOT, PKG):
 
 METRIC = "volumes/s to plain-RL(8 it) accuracy: learned warm-start vs plain RL, 1 GB300"
 
-# DRAM bytes (read + write) per k_mac launch over its algorithmic bytes, from one
-# ncu --set full capture of the full-field f = 96 launches (4 planes, 2401
-# frequency pairs: 1.001 forward, 1.005 back projection).  The matrices dominate
+# DRAM bytes (read + write) per k_mac launch over the bytes it streams, from one
+# ncu --set full capture of the full-field f = 96 launches (4 planes, 1225
+# frequency quads: 1.022 forward, 1.016 back projection).  The matrices dominate
 # both, so the traffic of a launch scales with the bytes it streams.
-MAC_TRAFFIC_RATIO = 1.003
+MAC_TRAFFIC_RATIO = 1.02
 UNIT = "volumes/s"
 
 WORKLOADS = {
@@ -95,6 +95,17 @@ WORKLOADS = {
 }
 
 
+def set_mac_shape(ctx, spec):
+    """--mac STAGES,ROWS_FWD,ROWS_BWD,SPLIT: the multiply-accumulate launch shape (a sweep)."""
+    if not spec:
+        return
+    st, rf, rb, sp = (int(v) for v in spec.split(","))
+    ctx.set_option("mac_stages", st)
+    ctx.set_option("mac_chunk_rows_forward", rf)
+    ctx.set_option("mac_chunk_rows_backward", rb)
+    ctx.set_option("mac_split", sp)
+
+
 def pinned_empty(shape):
     """A float32 numpy array backed by page-locked host memory."""
     import torch
@@ -140,6 +151,8 @@ def parse():
     ap.add_argument("--wide", type=int, default=1, choices=range(6),
                     help="unet: kernel of the 64/128-channel layers (0 mma.sync, 1 tcgen05, 2..5 tcgen05 with "
                          "1..4 M tiles per work item)")
+    ap.add_argument("--mac", default=None, metavar="STAGES,ROWS_FWD,ROWS_BWD,SPLIT",
+                    help="projection workloads: the multiply-accumulate launch shape (default: the library's)")
     ap.add_argument("--planes", default=None,
                     help="comma-separated z indices of the workload to keep (smaller cases for profiling)")
     return ap.parse_args()
@@ -444,6 +457,7 @@ def run_gb300(args, rank, world, local):
     gen = torch.Generator(device="cpu").manual_seed(99 + rank)
     img_h = torch.poisson((clean.cpu().double() + 100.0).clamp_min(0), generator=gen).float().numpy()
     ctx = p.context(hm)
+    set_mac_shape(ctx, args.mac)
     geo = ctx.geometry()
     setup_s = time.time() - t_setup
     stream = torch.cuda.current_stream(dev)
@@ -921,6 +935,7 @@ def run_warmstart(args):
     rng = np.random.default_rng(2024)
     nseed = args.held_out if args.held_out > 0 else (256 if Y * X * Z < 10_000_000 else 16)
     ctx = ws.ctx
+    set_mac_shape(ctx, args.mac)
 
     def resid(x, img):
         T = img.shape[0]
@@ -995,11 +1010,29 @@ def run_warmstart(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / args.steps
 
+    # each arm's step replays one CUDA graph (back projection, network, RL iterations);
+    # the direct launches are timed beside it
+    saved = p.useGraphs
+    p.useGraphs = False
+    plain_step()
+    torch.cuda.synchronize()
+    g_plain = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_plain, capture_error_mode="relaxed"):
+        plain_step()
+    p.useGraphs = saved
+    g_warm = None
+    if k_warm is not None:
+        g_warm = warmstart.WarmStartGraph(ws, 1, k_warm)
+        g_warm.img.copy_(img1)
+    torch.cuda.synchronize()
+
     clocks = ClockSampler(0)
     clocks.start()
-    ms_plain = timed(plain_step)
-    ms_warm = timed(warm_step) if k_warm is not None else None
+    ms_plain = timed(g_plain.replay)
+    ms_warm = timed(g_warm.replay) if g_warm is not None else None
     clk = clocks.stop()
+    ms_plain_direct = timed(plain_step)
+    ms_warm_direct = timed(warm_step) if k_warm is not None else None
     net_ms = timed(lambda: ws.initial_volume(htf1))
 
     # kernel launches of one warm-start step: the projection kernels (launch
@@ -1054,12 +1087,12 @@ def run_warmstart(args):
     # end to end through the public API: host image in, host volume out (pinned host buffers)
     img_h = pinned_like(img1)
     out = pinned_empty((Z, 1, Y, X))
-    warmstart.DeconvRLWarm(ws, img_h, k_warm or 0, out=out)
+    warmstart.DeconvRLWarm(ws, img_h, k_warm or 0, out=out, graph=True)
     torch.cuda.synchronize()
     ne = max(5, args.steps)
     t0 = time.perf_counter()
     for _ in range(ne):
-        warmstart.DeconvRLWarm(ws, img_h, k_warm or 0, out=out)
+        warmstart.DeconvRLWarm(ws, img_h, k_warm or 0, out=out, graph=True)
     e2e_s = (time.perf_counter() - t0) / ne
     fp64 = fp64_accuracy(wl["fp64_case"]) if wl.get("fp64_case") else None
 
@@ -1085,10 +1118,12 @@ def run_warmstart(args):
                        "device_gb": round(ctx.memory_usage() / 1e9, 2),
                        "l2": "transfer matrices (%.2f GB per projection) and volumes larger than L2"
                              % (roof["own_bytes_per_launch"] * roof["launches"] / args.steps / 17 / 1e9)},
+            "step_launch": "one CUDA graph per volume for each arm (ms_direct: the same kernels launched one by one)",
             "plain_rl": {"volumes_per_s": 1000.0 / ms_plain, "ms_per_volume": ms_plain, "iterations": 8,
+                         "ms_direct": ms_plain_direct,
                          "residual_rel_l2_mean": float(r_plain.mean()),
                          "truth_rel_l2_scaled_mean": float(t_plain.mean())},
-            "warm_start": {"rl_iterations_needed": k_warm, "network_ms": net_ms,
+            "warm_start": {"rl_iterations_needed": k_warm, "network_ms": net_ms, "ms_direct": ms_warm_direct,
                            "residual_after_k_mean": [round(v, 5) for v in curve],
                            "truth_rel_l2_scaled_mean_after_k": [round(float(v), 5) for v in tcurves.mean(axis=1)],
                            "truth_rel_l2_scaled_mean": float(tcurves[k_use].mean()),
@@ -1098,7 +1133,7 @@ def run_warmstart(args):
                          "residual_rel_l2_warm_mean": float(curves[k_use].mean()), "reductions": "f64"},
             "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(img_h.nbytes),
                     "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": e2e_s * 1000.0,
-                    "path": "warmstart.DeconvRLWarm on a host image, volume copied back"},
+                    "path": "warmstart.DeconvRLWarm(graph=True) on a pinned host image, volume copied to pinned host memory"},
             "gpu_launches": int(round(launches_warm)), "roofline": roof, "roofline_network": roof_net,
             "cpu_baseline": cb, "clocks": clk}
     print(json.dumps(line), flush=True)

@@ -37,6 +37,7 @@ _SIGS = {
     "flf_backward": (_I, [_P, _P, _P, _I, _I, _I, _P, _I, _P]),
     "flf_rl_iterate": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_memory_usage": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "flf_memory_epoch": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong)]),
     "flf_clear_cache": (_I, [_P]),
     "flf_geometry": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "flf_version": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
@@ -439,6 +440,13 @@ class Context:
     def memory_usage(self):
         v = ctypes.c_size_t(0)
         self._check(self._lib.flf_memory_usage(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def memory_epoch(self):
+        """Bumped whenever the context frees a buffer: a graph captured around library
+        calls stays valid while it is unchanged."""
+        v = ctypes.c_ulonglong(0)
+        self._check(self._lib.flf_memory_epoch(self._h, ctypes.byref(v)))
         return int(v.value)
 
     def clear_cache(self):

@@ -1512,6 +1512,12 @@ int flf_graph_destroy(flf_graph *g) {
   return FLF_OK;
 }
 
+int flf_memory_epoch(const flf_ctx *ctx, unsigned long long *epoch) {
+  if (!ctx || !epoch) return FLF_E_ARG;
+  *epoch = ctx->mem_epoch;
+  return FLF_OK;
+}
+
 int flf_memory_usage(const flf_ctx *ctx, size_t *bytes) {
   if (!ctx || !bytes) return FLF_E_ARG;
   size_t b = 0;

@@ -42,7 +42,7 @@ try:
 except ImportError:  # torch is needed for device arrays
     torch = None
 
-__all__ = ["UNet3D", "WarmStart", "synthetic_volume_points", "DeconvRLWarm"]
+__all__ = ["UNet3D", "WarmStart", "WarmStartGraph", "synthetic_volume_points", "DeconvRLWarm"]
 
 CIN = 16
 # (name, input channels, output channels, ReLU)
@@ -479,11 +479,78 @@ class WarmStart:
             return tuple(int(v) for v in f["meta.shape"])
 
 
-def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None, out=None):
+class WarmStartGraph:
+    """The whole warm-started deconvolution of T frames of the trained size as one
+    CUDA graph: back projection, network input, network, head and ``maxIter`` RL
+    iterations, on static device buffers (``img`` [T, Y, X] in, ``x`` [Z, T, Y, X]
+    out).  One direct run first sizes every workspace and builds the transfer
+    matrices; the capture then records the same launches (the RL iterations as
+    direct launches, not as a nested graph).  ``replay`` copies a new image in
+    (host or device), replays, and copies the volume to ``out`` when given."""
+
+    def __init__(self, warm, T, maxIter=0, prevedel=True):
+        self.warm, self.T, self.maxIter, self.prevedel = warm, int(T), int(maxIter), bool(prevedel)
+        p = warm.proj
+        self.img = torch.zeros((self.T, warm.Y, warm.X), dtype=torch.float32, device=warm.dev)
+        self.htf = torch.empty((warm.Z, self.T, warm.Y, warm.X), dtype=torch.float32, device=warm.dev)
+        saved = p.useGraphs
+        p.useGraphs = False
+        try:
+            self._run()                          # sizes workspaces, builds matrices, sets kernel attributes
+            torch.cuda.synchronize(warm.dev)
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
+                self.x = self._run()
+        finally:
+            p.useGraphs = saved
+        torch.cuda.synchronize(warm.dev)
+        # the graph holds the context's buffers (valid while the epoch stands) and the
+        # head bias as a value (valid while the weights are those of the capture)
+        self.key = (warm.ctx.memory_epoch(), warm.net.adam_t, warm.net.loads)
+
+    def valid(self):
+        w = self.warm
+        return self.key == (w.ctx.memory_epoch(), w.net.adam_t, w.net.loads)
+
+    def _run(self):
+        w = self.warm
+        w.ctx.backward(self.img, self.htf, self.T, w.Y, w.X, None, stream=w._s())
+        x = w.initial_volume(self.htf)
+        if self.maxIter > 0:
+            w.proj.RichardsonLucy(w.hm, x, self.htf if self.prevedel else self.img, self.maxIter,
+                                  prevedel=self.prevedel)
+        return x
+
+    def replay(self, im=None, out=None):
+        """Deconvolve ``im`` ([T, Y, X], host or device; None: the image already in
+        ``self.img``); returns ``self.x``, or ``out`` (a float32 host array) filled."""
+        if not self.valid():
+            raise _flf.FlfError(-4, "the warm-start graph refers to freed buffers or earlier weights: capture it again")
+        if im is not None:
+            src = im if isinstance(im, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(im, np.float32))
+            self.img.copy_(src.reshape(self.img.shape))
+        self.graph.replay()
+        if out is not None:
+            return self.warm.proj.asnumpy(self.x, out=out)
+        return self.x
+
+
+def DeconvRLWarm(warm, im, maxIter, prevedel=True, projector=None, out=None, graph=False):
     """RL from the network's start volume: back projection, warm start, ``maxIter``
     Prevedel iterations (the reference's default update), on the device; returns the
     volume [Z, T, Y, X] as a device tensor, or, with ``out`` (a float32 numpy array of
-    that shape, e.g. a view of pinned host memory), copied into ``out``."""
+    that shape, e.g. a view of pinned host memory), copied into ``out``.  With
+    ``graph`` the whole deconvolution replays one CUDA graph (WarmStartGraph, kept
+    per frame count, iteration count and update; the returned tensor is the graph's
+    own output buffer, overwritten by the next call)."""
+    if graph and projector is None:
+        T = int(np.shape(im)[0])
+        key = (T, int(maxIter), bool(prevedel))
+        cache = warm.__dict__.setdefault("_step_graphs", {})
+        if key not in cache or not cache[key].valid():
+            cache.pop(key, None)
+            cache[key] = WarmStartGraph(warm, T, maxIter, prevedel)
+        return cache[key].replay(im, out=out)
     p = projector or warm.proj
     img = p.asnative(im)
     T, Y, X = img.shape

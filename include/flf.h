@@ -143,6 +143,12 @@ int flf_rl_iterate(flf_ctx *ctx, float *x_dev, const float *ref_dev,
  * workspaces).  Counterpart of gMemoryUsage (py_light_field.cpp:654-670). */
 int flf_memory_usage(const flf_ctx *ctx, size_t *bytes);
 
+/* A count the context bumps whenever it frees a workspace, transfer matrix or
+ * PSF buffer.  A CUDA graph a caller captured around calls of this library
+ * (rather than through flf_rl_graph_create) refers to the context's buffers
+ * only while the count is unchanged: compare before each replay. */
+int flf_memory_epoch(const flf_ctx *ctx, unsigned long long *epoch);
+
 /* Drop the transfer matrices and workspaces (keeps the uploaded PSFs).
  * Counterpart of ClearFHCache (py_light_field.cpp:1370-1385). */
 int flf_clear_cache(flf_ctx *ctx);

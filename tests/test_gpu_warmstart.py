@@ -188,6 +188,35 @@ def test_training_repeats_bit_for_bit(env):
         assert np.array_equal(runs[0][k], runs[1][k]), k
 
 
+def test_warm_start_graph_matches_direct(env):
+    """WarmStartGraph (back projection, network, head and RL iterations as one CUDA
+    graph) gives the direct launches' volume bit for bit; a graph whose context
+    buffers were freed refuses to replay, and DeconvRLWarm(graph=True) captures
+    again."""
+    torch, ws_mod = env
+    import _flf
+    import projector
+    import psfmatrix
+    import synthetic
+    N = 5
+    H, Ht = synthetic.synthetic_psf(N, np.arange(-4, 5, 2), 3)
+    hm = psfmatrix.HMatrixArrays(H, Ht)
+    p = projector.Projector_gb300()
+    ws = ws_mod.WarmStart(p, hm, 60, 60, beads=30)
+    _, img, _ = ws.make_batch(2, np.random.default_rng(3))
+    direct = ws_mod.DeconvRLWarm(ws, img, 2).clone()
+    g = ws_mod.WarmStartGraph(ws, 2, 2)
+    assert torch.equal(g.replay(img), direct)
+    out = torch.empty(tuple(direct.shape), dtype=torch.float32, pin_memory=True).numpy()
+    r = ws_mod.DeconvRLWarm(ws, img.cpu().numpy(), 2, out=out, graph=True)
+    assert r is out and np.array_equal(out, direct.cpu().numpy())
+    ws.ctx.clear_cache()
+    with pytest.raises(_flf.FlfError, match="FLF_E_STATE"):
+        g.replay(img)
+    again = ws_mod.DeconvRLWarm(ws, img, 2, graph=True)
+    assert torch.equal(again, direct)
+
+
 @pytest.mark.parametrize("tcgen05", [False, True])
 def test_fused_input_and_head_kernels(env, tcgen05):
     """flf_ws_input / flf_ws_head against their torch formulas (head on the
