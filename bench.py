@@ -136,8 +136,9 @@ def parse():
                     help="held-out volumes of the warm-start evaluation (0: 256 at 450 x 450, 16 at full field)")
     ap.add_argument("--target-iters", type=int, default=32,
                     help="plain-RL iterations the warm-start network learns to reach")
-    ap.add_argument("--tune-steps", type=int, default=0,
-                    help="warm-start fine-tuning steps on the data-fit residual (whole volumes)")
+    ap.add_argument("--tune-steps", type=int, default=-1,
+                    help="warm-start fine-tuning steps on the data-fit residual (whole volumes) after training "
+                         "(default: 300 at 450 x 450, none at full field)")
     ap.add_argument("--streams", type=int, default=2, choices=[1, 2],
                     help="streams the transform groups alternate over (config4)")
     ap.add_argument("--no-graph", action="store_true", help="launch the RL kernels one by one instead of replaying a CUDA graph")
@@ -929,6 +930,8 @@ def run_warmstart(args):
     refresh = 8 if Y * X * Z < 10_000_000 else 16
     train_s = ws.train(steps=args.train_steps, batch=4, crop=128, target_iters=args.target_iters, log_every=1,
                        refresh_every=refresh)
+    if args.tune_steps < 0:
+        args.tune_steps = 300 if args.workload == "warmstart" else 0
     tune_s = ws.finetune_residual(steps=args.tune_steps, log_every=50) if args.tune_steps > 0 else 0.0
     dev = ws.dev
     s = torch.cuda.current_stream(dev)

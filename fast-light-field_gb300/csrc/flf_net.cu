@@ -1643,7 +1643,9 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 //           into one of 2 slab slots;
 //   B     = one (tap, 16 input channels) block of the packed weights
 //           (flf_conv3d_pack: [2 k8][CO][8] BF16), by 1-D bulk copy into a
-//           ring of 8;
+//           ring that fills the shared memory the slabs leave (every item
+//           streams all 27 x CI x CO weights, so the bytes in flight set the
+//           rate);
 //   MMA   = M 128 x N CO x K 16, nM per B block, into one of 2 TMEM
 //           accumulator buffers (nM x CO <= 256 columns each).
 //   warp 0      slab producer (one thread);
@@ -1659,10 +1661,11 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 struct WideGrid {
   int Xp, R, nM, nyb;   // padded row, rows per item, M tiles per item, y blocks
   int slab_rows;        // rows of one 8-channel group of a slab slot (LBO / 16)
+  int sb;               // B blocks in the ring (the shared memory the slabs leave)
   long long items;      // B * Z * nyb
 };
 
-constexpr int WIDE_SB = 8;           // B block ring
+constexpr int WIDE_SB_MAX = 64;      // B block ring: at most this many blocks in flight
 constexpr int WIDE_ACC_COLS = 256;   // columns of one TMEM accumulator buffer
 
 template <int CI, int CO>
@@ -1681,17 +1684,18 @@ __global__ void __launch_bounds__(256, 1)
   // layout: [2 slab slots][B ring][mbarriers][tmem address][abort flag]
   const uint32_t smem_s = su32(smem);
   const uint32_t slab_s = smem_s, bring_s = smem_s + 2 * SLOT;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + WIDE_SB * BBLK);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4 + 2 * WIDE_SB + 4 + 1);
+  const uint32_t SB = (uint32_t)g.sb;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + SB * BBLK);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4 + 2 * WIDE_SB_MAX + 4 + 1);
   volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const uint32_t bar_s = su32(bars);
   auto sfull = [&](uint32_t k) { return bar_s + 8u * k; };                           // slab slot loaded
   auto sempty = [&](uint32_t k) { return bar_s + 8u * (2 + k); };                    // slab slot read
   auto bfull = [&](uint32_t k) { return bar_s + 8u * (4 + k); };                     // B block loaded
-  auto bempty = [&](uint32_t k) { return bar_s + 8u * (4 + WIDE_SB + k); };          // B block read
-  auto afull = [&](uint32_t k) { return bar_s + 8u * (4 + 2 * WIDE_SB + k); };       // accumulator done
-  auto aempty = [&](uint32_t k) { return bar_s + 8u * (6 + 2 * WIDE_SB + k); };      // accumulator read
-  const uint32_t fin = bar_s + 8u * (8 + 2 * WIDE_SB);
+  auto bempty = [&](uint32_t k) { return bar_s + 8u * (4 + WIDE_SB_MAX + k); };      // B block read
+  auto afull = [&](uint32_t k) { return bar_s + 8u * (4 + 2 * WIDE_SB_MAX + k); };   // accumulator done
+  auto aempty = [&](uint32_t k) { return bar_s + 8u * (6 + 2 * WIDE_SB_MAX + k); };  // accumulator read
+  const uint32_t fin = bar_s + 8u * (8 + 2 * WIDE_SB_MAX);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
@@ -1701,7 +1705,7 @@ __global__ void __launch_bounds__(256, 1)
       net_mbar_init(afull(k), 1);
       net_mbar_init(aempty(k), 4);
     }
-    for (int k = 0; k < WIDE_SB; k++) {
+    for (uint32_t k = 0; k < SB; k++) {
       net_mbar_init(bfull(k), 1);
       net_mbar_init(bempty(k), 1);
     }
@@ -1765,8 +1769,8 @@ __global__ void __launch_bounds__(256, 1)
           for (int cg = 0; cg < NCG && ok; cg++)
             for (int t9 = 0; t9 < 9 && ok; t9++)
               for (int ks = 0; ks < KS; ks++) {
-                const uint32_t sl = nbb % WIDE_SB;
-                if (nbb >= WIDE_SB && !role_wait(bempty(sl), ((nbb / WIDE_SB) - 1) & 1, abort_s, 22)) {
+                const uint32_t sl = nbb % SB;
+                if (nbb >= SB && !role_wait(bempty(sl), ((nbb / SB) - 1) & 1, abort_s, 22)) {
                   ok = false;
                   break;
                 }
@@ -1814,8 +1818,8 @@ __global__ void __launch_bounds__(256, 1)
             for (int t9 = 0; t9 < 9 && ok; t9++) {
               const int dy = t9 / 3, dx = t9 % 3;
               for (int ks = 0; ks < KS; ks++) {
-                const uint32_t bs = nb % WIDE_SB;
-                if (!role_wait(bfull(bs), (nb / WIDE_SB) & 1, abort_s, 25)) {
+                const uint32_t bs = nb % SB;
+                if (!role_wait(bfull(bs), (nb / SB) & 1, abort_s, 25)) {
                   ok = false;
                   break;
                 }
@@ -1906,9 +1910,9 @@ __global__ void __launch_bounds__(256, 1)
         if (!net_mbar_wait(sfull(sl), (last >> 1) & 1, 1000000000ULL)) atomicExch(&g_net_err, 27);
       }
     if (warp == 2 && lane == 0)
-      for (uint32_t sl = 0; sl < (uint32_t)WIDE_SB && sl < nbb; sl++) {
-        const uint32_t last = sl + ((nbb - 1 - sl) / WIDE_SB) * WIDE_SB;
-        if (!net_mbar_wait(bfull(sl), (last / WIDE_SB) & 1, 1000000000ULL)) atomicExch(&g_net_err, 28);
+      for (uint32_t sl = 0; sl < SB && sl < nbb; sl++) {
+        const uint32_t last = sl + ((nbb - 1 - sl) / SB) * SB;
+        if (!net_mbar_wait(bfull(sl), (last / SB) & 1, 1000000000ULL)) atomicExch(&g_net_err, 28);
       }
   }
   if (warp == 1 && lane == 0) {
@@ -1951,15 +1955,17 @@ int net_set_conv_wide_tcgen05(int mode) {
   return old;
 }
 
-// Shared memory of k_conv3d_wide for a slab of slab_rows rows per 8-channel group.
-static size_t wide_smem(int CI, int CO, int slab_rows) {
+// Shared memory of k_conv3d_wide: the two slab slots of slab_rows rows per
+// 8-channel group, sb B blocks, the mbarriers, the TMEM address and abort flag.
+static size_t wide_smem(int CI, int CO, int slab_rows, int sb) {
   const int KC = CI < 64 ? CI : 64;
-  return (size_t)2 * (KC / 8) * slab_rows * 16 + (size_t)WIDE_SB * 32 * CO + 8 * (8 + 2 * WIDE_SB + 1) + 16;
+  return (size_t)2 * (KC / 8) * slab_rows * 16 + (size_t)sb * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
 }
 
 // The item shape for nM M tiles: rows per item R (balanced over the y blocks),
-// its slab rows and shared memory; false when nM tiles hold no full row or the
-// slab does not fit.
+// its slab rows, the B blocks the rest of the shared memory holds, and the
+// shared memory; false when nM tiles hold no full row or fewer than 8 B blocks
+// fit beside the slabs.
 static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t &smem) {
   g.Xp = X + 2;
   const int rmax = nM * 128 / g.Xp;
@@ -1969,8 +1975,12 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
   if (g.R + 2 > 256) return false;
   g.nM = (g.R * g.Xp + 127) / 128;
   g.slab_rows = (g.nM * 128 + 2 * g.Xp + 2 + 7) / 8 * 8;
-  smem = wide_smem(CI, CO, g.slab_rows);
-  return smem <= 227 * 1024;
+  const size_t fixed = wide_smem(CI, CO, g.slab_rows, 0);
+  if (fixed + 8 * 32 * (size_t)CO > 227 * 1024) return false;
+  g.sb = (int)((227 * 1024 - fixed) / (32 * (size_t)CO));
+  if (g.sb > WIDE_SB_MAX) g.sb = WIDE_SB_MAX;
+  smem = wide_smem(CI, CO, g.slab_rows, g.sb);
+  return true;
 }
 
 template <int CI, int CO>
@@ -1984,8 +1994,11 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     sms = n > 0 ? n : 1;
   }
-  // item shape: forced (modes 2..5), else the one with the least estimated time
-  // (waves of items x their MMA count, plus a fixed cost per item)
+  // item shape: forced (modes 2..5), else the one with the least estimated time:
+  // waves of items x (the slower of the item's MMAs and its weight stream, plus a
+  // fixed cost), in cycles: an M 128 x N CO x K 16 MMA ~48 (N 64) or ~64 (N 128)
+  // cycles; each of the item's 27 CI/16 weight blocks a ~2000-cycle round trip,
+  // sb of them in flight
   WideGrid g{};
   size_t smem = 0;
   bool found = false;
@@ -1997,7 +2010,9 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     if (!wide_shape(CI, CO, p.Y, p.X, nM, c, sm)) continue;
     c.items = (long long)p.B * p.Z * c.nyb;
     const double waves = (double)((c.items + sms - 1) / sms);
-    const double cost = waves * (c.nM + 0.5);
+    const double t_mma = 27.0 * (CI / 16) * c.nM * (CO <= 64 ? 48.0 : 64.0);
+    const double t_b = 27.0 * (CI / 16) * 2000.0 / c.sb;
+    const double cost = waves * ((t_mma > t_b ? t_mma : t_b) + 3000.0);
     if (!found || cost < best) {
       found = true;
       best = cost;
