@@ -1665,7 +1665,8 @@ struct WideGrid {
   long long items;      // B * Z * nyb
 };
 
-constexpr int WIDE_SB_MAX = 64;      // B block ring: at most this many blocks in flight
+constexpr int WIDE_SB_MAX = 64;      // B block ring: barriers for at most this many blocks
+constexpr int WIDE_SB = 16;          // B blocks in flight (deeper rings measured slower)
 constexpr int WIDE_ACC_COLS = 256;   // columns of one TMEM accumulator buffer
 
 template <int CI, int CO>
@@ -1674,13 +1675,16 @@ __global__ void __launch_bounds__(256, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   constexpr int KC = CI < 64 ? CI : 64;   // input channels of one chunk
   constexpr int NCG = CI / KC;            // chunks per input plane
-  constexpr int G8 = KC / 8;              // TMA loads (8-channel groups) per chunk
+  constexpr bool SW = KC == 64;           // 128-byte rows, 128-byte swizzle (else 8-channel groups)
+  constexpr int NBOX = SW ? 1 : KC / 8;   // TMA loads per chunk
   constexpr int KS = KC / 16;             // K steps per chunk
   constexpr uint32_t BBLK = 32u * CO;     // one packed B block
   static_assert(CI % 32 == 0 && CO % 32 == 0 && CO <= 128 && CI <= 128, "32..128 channels");
-  const uint32_t LBO = (uint32_t)g.slab_rows * 16u;   // between 8-channel groups of a slab
-  const uint32_t SLOT = G8 * LBO;
-  const uint32_t box_tx = 16u * (uint32_t)g.Xp * (uint32_t)(g.R + 2);
+  // SW: a slab slot is slab_rows rows of 128 bytes (64 channels), written by one TMA load with the
+  // 128-byte swizzle; otherwise KC/8 groups of slab_rows 16-byte rows, LBO apart
+  const uint32_t LBO = (uint32_t)g.slab_rows * 16u;
+  const uint32_t SLOT = SW ? (uint32_t)g.slab_rows * 128u : (uint32_t)(KC / 8) * LBO;
+  const uint32_t box_tx = (SW ? 128u : 16u) * (uint32_t)g.Xp * (uint32_t)(g.R + 2);
   // layout: [2 slab slots][B ring][mbarriers][tmem address][abort flag]
   const uint32_t smem_s = su32(smem);
   const uint32_t slab_s = smem_s, bring_s = smem_s + 2 * SLOT;
@@ -1748,8 +1752,8 @@ __global__ void __launch_bounds__(256, 1)
               ok = false;
               break;
             }
-            net_expect_tx(sfull(sl), G8 * box_tx);
-            for (int k = 0; k < G8; k++)
+            net_expect_tx(sfull(sl), NBOX * box_tx);
+            for (int k = 0; k < NBOX; k++)
               tma_load_5d(slab_s + sl * SLOT + k * LBO, &tx, cg * KC + 8 * k, -1, y0 - 1, z + dz, b, sfull(sl));
             nslab++;
           }
@@ -1827,7 +1831,11 @@ __global__ void __launch_bounds__(256, 1)
                 const uint64_t bd = umma_desc(bring_s + bs * BBLK, 16u * CO, 128);
                 for (int m = 0; m < g.nM; m++) {
                   const uint32_t row = (uint32_t)(m * 128 + dy * g.Xp + dx);
-                  const uint64_t ad = umma_desc(a0 + 2u * ks * LBO + row * 16u, LBO, 128);
+                  // SW: K-major with the 128-byte swizzle (layout type 2 in bits 61-63), 8-row
+                  // groups 1024 bytes apart, the K step 32 bytes into the row; the swizzle acts
+                  // on absolute address bits, as the TMA load wrote it, so any start row works
+                  const uint64_t ad = SW ? (umma_desc(a0 + row * 128u + ks * 32u, 16, 1024) | (2ull << 61))
+                                         : umma_desc(a0 + 2u * ks * LBO + row * 16u, LBO, 128);
                   umma_f16(dcol + m * CO, ad, bd, idesc, first ? 0u : 1u);
                 }
                 first = false;
@@ -1955,11 +1963,11 @@ int net_set_conv_wide_tcgen05(int mode) {
   return old;
 }
 
-// Shared memory of k_conv3d_wide: the two slab slots of slab_rows rows per
-// 8-channel group, sb B blocks, the mbarriers, the TMEM address and abort flag.
+// Shared memory of k_conv3d_wide: the two slab slots of slab_rows rows of KC
+// channels, sb B blocks, the mbarriers, the TMEM address and abort flag.
 static size_t wide_smem(int CI, int CO, int slab_rows, int sb) {
   const int KC = CI < 64 ? CI : 64;
-  return (size_t)2 * (KC / 8) * slab_rows * 16 + (size_t)sb * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
+  return (size_t)2 * KC * 2 * slab_rows + (size_t)sb * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
 }
 
 // The item shape for nM M tiles: rows per item R (balanced over the y blocks),
@@ -1978,7 +1986,7 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
   const size_t fixed = wide_smem(CI, CO, g.slab_rows, 0);
   if (fixed + 8 * 32 * (size_t)CO > 227 * 1024) return false;
   g.sb = (int)((227 * 1024 - fixed) / (32 * (size_t)CO));
-  if (g.sb > WIDE_SB_MAX) g.sb = WIDE_SB_MAX;
+  if (g.sb > WIDE_SB) g.sb = WIDE_SB;
   smem = wide_smem(CI, CO, g.slab_rows, g.sb);
   return true;
 }
@@ -2029,11 +2037,13 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
   const cuuint64_t vb = 2ull * CI;   // bytes per voxel
   const cuuint64_t dims[5] = {(cuuint64_t)CI, (cuuint64_t)p.X, (cuuint64_t)p.Y, (cuuint64_t)p.Z, (cuuint64_t)p.B};
   const cuuint64_t strides[4] = {vb, vb * p.X, vb * p.X * p.Y, vb * p.X * p.Y * p.Z};
-  const cuuint32_t box[5] = {8u, (cuuint32_t)g.Xp, (cuuint32_t)(g.R + 2), 1, 1};
+  // 64-channel chunks: one box of 64 channels (128-byte rows, 128-byte swizzle); 32: 8-channel boxes
+  constexpr bool SW = CI >= 64;
+  const cuuint32_t box[5] = {SW ? 64u : 8u, (cuuint32_t)g.Xp, (cuuint32_t)(g.R + 2), 1, 1};
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(p.x), dims, strides, box, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+          CU_TENSOR_MAP_INTERLEAVE_NONE, SW ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return cudaErrorInvalidValue;
   // one CTA per SM (its 512 TMEM columns): ask for at least half the shared memory
   const size_t sm_launch = smem < 116 * 1024 ? 116 * 1024 : smem;
