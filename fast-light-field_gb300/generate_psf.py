@@ -257,13 +257,15 @@ def GeneratePSFArrays(M, NA, MLPitch, Nnum, OSR, n, fml, lam, zmin, zmax, zspaci
 
 def GeneratePSF(M, NA, MLPitch, Nnum, OSR, n, fml, lam, zmin, zmax, zspacing, normalisePSF=True,
                 reproduceMaxBug=False, matrixSaveDir="PSFmatrix", verbose=False, maxPSFLenslets=20, device=0,
-                matPath=None):
+                matPath=None, saveMat=False):
     """Generate and save the PSF matrices (generate_psf.py:63-737); returns the matrix path.
 
     The files go to ``<matrixSaveDir>/<prefix>PSFmatrix_<parameters>/`` in the
     memmap layout, where ``<prefix>`` is ``fdnorm`` (normalised), ``reducedBuggy``
     or ``reduced``, as in the reference (or to the folder of ``matPath``);
     ``psfmatrix.LoadMatrix`` opens the returned ``.mat`` path through that folder.
+    With ``saveMat`` the ``.mat`` file itself is written too, in the reference's
+    HDF5 layout (``psfmatrix.SaveRawMatrixData``), as the reference always does.
     """
     r = GeneratePSFArrays(M, NA, MLPitch, Nnum, OSR, n, fml, lam, zmin, zmax, zspacing, normalisePSF,
                           reproduceMaxBug, maxPSFLenslets, device, verbose)
@@ -280,6 +282,9 @@ def GeneratePSF(M, NA, MLPitch, Nnum, OSR, n, fml, lam, zmin, zmax, zspacing, no
                 IMGSIZE_REF=r["IMGSIZE_REF"])
     with open(os.path.join(mmapPath, "PSFInfo.json"), "w") as f:
         json.dump(info, f, indent=1)
+    if saveMat:
+        scalars = {k: v for k, v in info.items() if k not in ("CAindex", "ReducedMatrix", "IMGSIZE_REF")}
+        psfmatrix.SaveRawMatrixData(matPath, r["H"], r["Ht"], r["CAindex"], scalars)
     if verbose:
         print("PSF matrices written to %s (%.1f s)" % (mmapPath, r["timings"]["total_s"]))
     return matPath

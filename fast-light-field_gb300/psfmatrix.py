@@ -14,7 +14,7 @@ import warnings
 
 import numpy as np
 
-__all__ = ["HMatrix", "HMatrixArrays", "GetPathFormats", "LoadRawMatrixData", "LoadMatrix",
+__all__ = ["HMatrix", "HMatrixArrays", "GetPathFormats", "LoadRawMatrixData", "SaveRawMatrixData", "LoadMatrix",
            "SaveReducedMatrices"]
 
 
@@ -119,20 +119,51 @@ def SaveReducedMatrices(mmapPath, H, Ht):
     np.save(os.path.join(mmapPath, "HtReducedShape.npy"), np.array(shapes))
 
 
+def SaveRawMatrixData(matPath, H, Ht, CAindex, params=None):
+    """Write a PSF .mat (HDF5) file in the reference's layout (generate_psf.py:739-785,
+    ``SaveMatrices``): the per-plane quadrants H[z] / Ht[z] ([nh][nh][h][h]) placed at
+    their CAindex window (1-based, [2][Z]) in full [Z][nh][nh][L][L] arrays, CAindex
+    stored as [Z][2], ``ReducedMatrix`` True, ``Nnum`` and the other scalars of
+    ``params``.  LoadRawMatrixData reads it back to the same quadrants.  Written with
+    hdf5lite (contiguous datasets, as h5py lays them out by default)."""
+    import hdf5lite
+    CA = np.asarray(CAindex, dtype=np.int64)
+    nz = len(H)
+    nh = np.asarray(H[0]).shape[0]
+    L = int(CA[1].max())
+    items = dict(params or {})
+    items["CAindex"] = CA.T.copy()
+    items["ReducedMatrix"] = True
+    for key, planes in (("H", H), ("Ht", Ht)):
+        full = np.zeros((nz, nh, nh, L, L), np.float32)
+        for cc in range(nz):
+            a, b = int(CA[0, cc]) - 1, int(CA[1, cc])
+            full[cc, :, :, a:b, a:b] = planes[cc]
+        items[key] = full
+    if "Nnum" not in items:
+        items["Nnum"] = np.int64(2 * nh - 1)
+    hdf5lite.write(matPath, items)
+
+
 def LoadRawMatrixData(matPath, expectedNnum=None, createPSF=True):
     """Convert a reference PSF .mat (HDF5) file into the memmap layout (psfmatrix.py:100-167).
 
-    Needs h5py.  Keys read: ``CAindex``, ``Nnum``, ``ReducedMatrix``, ``H``, ``Ht``.
+    Keys read: ``CAindex``, ``Nnum``, ``ReducedMatrix``, ``H``, ``Ht``.  The file is
+    opened with h5py where it is installed, else with this package's own HDF5
+    reader (hdf5lite: contiguous, compact and chunked/deflate datasets, as h5py
+    and MATLAB write them).
     """
     try:
-        import h5py  # noqa: F401
-    except ImportError as e:
-        raise ImportError("reading PSF .mat files needs h5py, which is not installed") from e
+        import h5py
+        opener = h5py.File
+    except ImportError:
+        import hdf5lite
+        opener = hdf5lite.File
     if not os.path.exists(matPath):
         raise FileNotFoundError("%s does not exist (LoadMatrix(..., createPSF=True) generates it)" % matPath)
     mmapPath, hPathFormat, htPathFormat = GetPathFormats(matPath)
     os.makedirs(mmapPath, exist_ok=True)
-    with h5py.File(matPath, "r") as f:
+    with opener(matPath, "r") as f:
         CA = f["CAindex"][()].astype("int")
         if CA.shape[1] == 2:
             CA = CA.T

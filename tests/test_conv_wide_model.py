@@ -14,7 +14,9 @@ row window (M = nM x 128 positions) with the packed weight block of
 
 Positions with x >= X or yl >= R are computed and dropped.  The rows a slab
 load does not write hold stale data (NaN here); only dropped positions read
-them.  The item shapes follow the launcher (rows per item balanced over the y
+them.  (On the device a 64-channel chunk is one TMA load of 128-byte rows with
+the 128-byte swizzle, which the operand descriptors undo; the logical rows, and
+so this model, are the same.)  The item shapes follow the launcher (rows per item balanced over the y
 blocks, nM = ceil(R*Xp / 128)), and the weights the packing kernel's layout.
 """
 
