@@ -1641,13 +1641,12 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 // rows (positions with x >= X or beyond the R rows are computed and dropped).
 //   chunk = one input plane z+dz x KC (<= 64) input channels: KC/8 TMA loads
 //           into one of 2 slab slots;
-//   B     = one (tap, 16 input channels) block of the packed weights
-//           (flf_conv3d_pack: [2 k8][CO][8] BF16), by 1-D bulk copy into a
-//           ring that fills the shared memory the slabs leave (every item
-//           streams all 27 x CI x CO weights, so the bytes in flight set the
-//           rate);
+//   B     = the KC/16 blocks of one (tap, chunk) of the packed weights
+//           (flf_conv3d_pack: per 16 input channels a [2 k8][CO][8] BF16
+//           block), one 1-D bulk copy per ring slot;
 //   MMA   = M 128 x N CO x K 16, nM per B block, into one of 2 TMEM
-//           accumulator buffers (nM x CO <= 256 columns each).
+//           accumulator buffers (nM x CO <= 256 columns each); the issuing
+//           thread moves only the start-address words of the descriptors.
 //   warp 0      slab producer (one thread);
 //   warp 1      MMA issuer (one thread), TMEM allocation;
 //   warp 2      B producer (one thread);
@@ -1666,7 +1665,7 @@ struct WideGrid {
 };
 
 constexpr int WIDE_SB_MAX = 64;      // B block ring: barriers for at most this many blocks
-constexpr int WIDE_SB = 16;          // B blocks in flight (deeper rings measured slower)
+constexpr int WIDE_SB = 12;          // taps of B blocks in flight at most
 constexpr int WIDE_ACC_COLS = 256;   // columns of one TMEM accumulator buffer
 
 template <int CI, int CO>
@@ -1688,8 +1687,9 @@ __global__ void __launch_bounds__(256, 1)
   // layout: [2 slab slots][B ring][mbarriers][tmem address][abort flag]
   const uint32_t smem_s = su32(smem);
   const uint32_t slab_s = smem_s, bring_s = smem_s + 2 * SLOT;
-  const uint32_t SB = (uint32_t)g.sb;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + SB * BBLK);
+  const uint32_t SB = (uint32_t)g.sb;          // taps in the B ring
+  constexpr uint32_t TB = KS * BBLK;            // one tap's B blocks (KC input channels)
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + SB * TB);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4 + 2 * WIDE_SB_MAX + 4 + 1);
   volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const uint32_t bar_s = su32(bars);
@@ -1763,7 +1763,7 @@ __global__ void __launch_bounds__(256, 1)
     }
   } else if (warp == 2) {
     if (lane == 0) {
-      // ---- B producer: the blocks in the issuer's order ----
+      // ---- B producer: one tap's KS blocks per ring slot, in the issuer's order ----
       for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
         int b, z, y0;
         decode(it, b, z, y0);
@@ -1771,23 +1771,22 @@ __global__ void __launch_bounds__(256, 1)
         for (int dz = -1; dz <= 1 && ok; dz++) {
           if (z + dz < 0 || z + dz >= p.Z) continue;
           for (int cg = 0; cg < NCG && ok; cg++)
-            for (int t9 = 0; t9 < 9 && ok; t9++)
-              for (int ks = 0; ks < KS; ks++) {
-                const uint32_t sl = nbb % SB;
-                if (nbb >= SB && !role_wait(bempty(sl), ((nbb / SB) - 1) & 1, abort_s, 22)) {
-                  ok = false;
-                  break;
-                }
-                const int tap = (dz + 1) * 9 + t9;
-                const bf16 *src = wp + ((long long)tap * (CI / 16) + cg * KS + ks) * (BBLK / 2);
-                net_expect_tx(bfull(sl), BBLK);
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                        bring_s + sl * BBLK),
-                    "l"(src), "r"(BBLK), "r"(bfull(sl))
-                    : "memory");
-                nbb++;
+            for (int t9 = 0; t9 < 9; t9++) {
+              const uint32_t sl = nbb % SB;
+              if (nbb >= SB && !role_wait(bempty(sl), ((nbb / SB) - 1) & 1, abort_s, 22)) {
+                ok = false;
+                break;
               }
+              const int tap = (dz + 1) * 9 + t9;
+              const bf16 *src = wp + ((long long)tap * (CI / 16) + cg * KS) * (BBLK / 2);
+              net_expect_tx(bfull(sl), TB);
+              asm volatile(
+                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                      bring_s + sl * TB),
+                  "l"(src), "r"(TB), "r"(bfull(sl))
+                  : "memory");
+              nbb++;
+            }
         }
         if (!ok) break;
       }
@@ -1797,6 +1796,17 @@ __global__ void __launch_bounds__(256, 1)
       // ---- MMA issuer ----
       // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = CO, M = 128
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(CO >> 3) << 17) | ((128u >> 4) << 24);
+      // operand descriptors: only the start-address field (low word, 16-byte units) moves.
+      // A (SW): 128-byte swizzle, 8-row groups 1024 bytes apart, a row 8 units, a K step 2 units;
+      // A (otherwise): 8-channel groups LBO apart, a row 1 unit, a K step 2 LBO; B: N-adjacent
+      // core matrices 128 bytes apart, K-adjacent ones 16 CO bytes apart, a K step 2 CO units
+      const uint64_t a0d = SW ? (umma_desc(slab_s, 16, 1024) | (2ull << 61)) : umma_desc(slab_s, LBO, 128);
+      const uint64_t b0d = umma_desc(bring_s, 16u * CO, 128);
+      const uint32_t a_lo0 = (uint32_t)a0d, a_hi = (uint32_t)(a0d >> 32);
+      const uint32_t b_lo0 = (uint32_t)b0d, b_hi = (uint32_t)(b0d >> 32);
+      const uint32_t a_row = SW ? 8u : 1u, a_ks = SW ? 2u : 2u * (LBO >> 4), a_slot = SLOT >> 4;
+      const uint32_t a_m = 128u * a_row, b_ks = (2u * CO * 16u) >> 4, b_slot = TB >> 4;
+      const int nM = g.nM;
       uint32_t ns = 0, nb = 0, li = 0;
       bool ok = true;
       for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x, li++) {
@@ -1809,7 +1819,7 @@ __global__ void __launch_bounds__(256, 1)
         }
         tc_fence_after();
         const uint32_t dcol = tmem + ab * WIDE_ACC_COLS;
-        bool first = true;
+        uint32_t acc = 0;   // the item's first MMA of each tile overwrites
         for (int dz = -1; dz <= 1 && ok; dz++) {
           if (z + dz < 0 || z + dz >= p.Z) continue;
           for (int cg = 0; cg < NCG && ok; cg++) {
@@ -1818,33 +1828,30 @@ __global__ void __launch_bounds__(256, 1)
               ok = false;
               break;
             }
-            const uint32_t a0 = slab_s + sl * SLOT;
-            for (int t9 = 0; t9 < 9 && ok; t9++) {
-              const int dy = t9 / 3, dx = t9 % 3;
-              for (int ks = 0; ks < KS; ks++) {
-                const uint32_t bs = nb % SB;
-                if (!role_wait(bfull(bs), (nb / SB) & 1, abort_s, 25)) {
-                  ok = false;
-                  break;
-                }
-                tc_fence_after();
-                const uint64_t bd = umma_desc(bring_s + bs * BBLK, 16u * CO, 128);
-                for (int m = 0; m < g.nM; m++) {
-                  const uint32_t row = (uint32_t)(m * 128 + dy * g.Xp + dx);
-                  // SW: K-major with the 128-byte swizzle (layout type 2 in bits 61-63), 8-row
-                  // groups 1024 bytes apart, the K step 32 bytes into the row; the swizzle acts
-                  // on absolute address bits, as the TMA load wrote it, so any start row works
-                  const uint64_t ad = SW ? (umma_desc(a0 + row * 128u + ks * 32u, 16, 1024) | (2ull << 61))
-                                         : umma_desc(a0 + 2u * ks * LBO + row * 16u, LBO, 128);
-                  umma_f16(dcol + m * CO, ad, bd, idesc, first ? 0u : 1u);
-                }
-                first = false;
-                umma_commit(bempty(bs));   // the B block is free once these MMAs complete
-                nb++;
+            const uint32_t a_c = a_lo0 + sl * a_slot;
+            for (int t9 = 0; t9 < 9; t9++) {
+              const uint32_t bs = nb % SB;
+              if (!role_wait(bfull(bs), (nb / SB) & 1, abort_s, 25)) {
+                ok = false;
+                break;
               }
+              tc_fence_after();
+              const uint32_t a_t = a_c + (uint32_t)((t9 / 3) * g.Xp + (t9 % 3)) * a_row;
+              const uint32_t b_t = b_lo0 + bs * b_slot;
+#pragma unroll
+              for (int ks = 0; ks < KS; ks++) {
+                const uint64_t bd = ((uint64_t)b_hi << 32) | (b_t + ks * b_ks);
+#pragma unroll
+                for (int m = 0; m < 4; m++)
+                  if (m < nM)
+                    umma_f16(dcol + m * CO, ((uint64_t)a_hi << 32) | (a_t + ks * a_ks + m * a_m), bd, idesc, acc);
+                acc = 1;
+              }
+              umma_commit(bempty(bs));   // the tap's B blocks are free once these MMAs complete
+              nb++;
             }
             if (!ok) break;
-            umma_commit(sempty(sl));       // the slab slot likewise
+            umma_commit(sempty(sl));     // the slab slot likewise
             ns++;
           }
         }
@@ -1967,12 +1974,12 @@ int net_set_conv_wide_tcgen05(int mode) {
 // channels, sb B blocks, the mbarriers, the TMEM address and abort flag.
 static size_t wide_smem(int CI, int CO, int slab_rows, int sb) {
   const int KC = CI < 64 ? CI : 64;
-  return (size_t)2 * KC * 2 * slab_rows + (size_t)sb * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
+  return (size_t)2 * KC * 2 * slab_rows + (size_t)sb * (KC / 16) * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
 }
 
 // The item shape for nM M tiles: rows per item R (balanced over the y blocks),
-// its slab rows, the B blocks the rest of the shared memory holds, and the
-// shared memory; false when nM tiles hold no full row or fewer than 8 B blocks
+// its slab rows, the taps of B blocks the rest of the shared memory holds, and
+// the shared memory; false when nM tiles hold no full row or fewer than 3 taps
 // fit beside the slabs.
 static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t &smem) {
   g.Xp = X + 2;
@@ -1984,8 +1991,9 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
   g.nM = (g.R * g.Xp + 127) / 128;
   g.slab_rows = (g.nM * 128 + 2 * g.Xp + 2 + 7) / 8 * 8;
   const size_t fixed = wide_smem(CI, CO, g.slab_rows, 0);
-  if (fixed + 8 * 32 * (size_t)CO > 227 * 1024) return false;
-  g.sb = (int)((227 * 1024 - fixed) / (32 * (size_t)CO));
+  const size_t tb = (size_t)((CI < 64 ? CI : 64) / 16) * 32 * CO;   // one tap's B blocks
+  if (fixed + 3 * tb > 227 * 1024) return false;
+  g.sb = (int)((227 * 1024 - fixed) / tb);
   if (g.sb > WIDE_SB) g.sb = WIDE_SB;
   smem = wide_smem(CI, CO, g.slab_rows, g.sb);
   return true;
@@ -2005,8 +2013,8 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
   // item shape: forced (modes 2..5), else the one with the least estimated time:
   // waves of items x (the slower of the item's MMAs and its weight stream, plus a
   // fixed cost), in cycles: an M 128 x N CO x K 16 MMA ~48 (N 64) or ~64 (N 128)
-  // cycles; each of the item's 27 CI/16 weight blocks a ~2000-cycle round trip,
-  // sb of them in flight
+  // cycles; each of the item's 27 CI/KC taps of weight blocks a ~2000-cycle round
+  // trip, sb of them in flight
   WideGrid g{};
   size_t smem = 0;
   bool found = false;
@@ -2019,7 +2027,7 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     c.items = (long long)p.B * p.Z * c.nyb;
     const double waves = (double)((c.items + sms - 1) / sms);
     const double t_mma = 27.0 * (CI / 16) * c.nM * (CO <= 64 ? 48.0 : 64.0);
-    const double t_b = 27.0 * (CI / 16) * 2000.0 / c.sb;
+    const double t_b = 27.0 * (CI < 64 ? 1 : CI / 64) * 2000.0 / c.sb;
     const double cost = waves * ((t_mma > t_b ? t_mma : t_b) + 3000.0);
     if (!found || cost < best) {
       found = true;
