@@ -1644,12 +1644,9 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 //   B     = the KC/16 blocks of one (tap, chunk) of the packed weights
 //           (flf_conv3d_pack: per 16 input channels a [2 k8][CO][8] BF16
 //           block), one 1-D bulk copy per ring slot;
-//   MMA   = M 128 x N CO x K 16, nM per B block.  Consecutive MMAs into one
-//           accumulator wait for each other, so an item's MMAs are dealt over
-//           nM x nk independent accumulators (M tile x K step modulo nk), in
-//           one of nbuf TMEM buffers; the epilogue adds the nk partials.  The
-//           issuing thread moves only the start-address words of the
-//           descriptors.
+//   MMA   = M 128 x N CO x K 16, nM per B block, into one of 2 TMEM
+//           accumulator buffers (nM x CO <= 256 columns each); the issuing
+//           thread moves only the start-address words of the descriptors.
 //   warp 0      slab producer (one thread);
 //   warp 1      MMA issuer (one thread), TMEM allocation;
 //   warp 2      B producer (one thread);
@@ -1663,15 +1660,13 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 struct WideGrid {
   int Xp, R, nM, nyb;   // padded row, rows per item, M tiles per item, y blocks
   int slab_rows;        // rows of one 8-channel group of a slab slot (LBO / 16)
-  int sb;               // taps of B blocks in the ring (the shared memory the slabs leave)
-  int nk;               // partial accumulators per M tile (K steps dealt round-robin)
-  int nbuf;             // accumulator buffers (2: an item's epilogue overlaps the next item)
+  int sb;               // B blocks in the ring (the shared memory the slabs leave)
   long long items;      // B * Z * nyb
 };
 
 constexpr int WIDE_SB_MAX = 64;      // B block ring: barriers for at most this many blocks
 constexpr int WIDE_SB = 12;          // taps of B blocks in flight at most
-constexpr int WIDE_TMEM_COLS = 512;  // all of TMEM (one CTA per SM)
+constexpr int WIDE_ACC_COLS = 256;   // columns of one TMEM accumulator buffer
 
 template <int CI, int CO>
 __global__ void __launch_bounds__(256, 1)
@@ -1724,7 +1719,7 @@ __global__ void __launch_bounds__(256, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
-                 "r"(WIDE_TMEM_COLS)
+                 "r"(2 * WIDE_ACC_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
@@ -1732,8 +1727,6 @@ __global__ void __launch_bounds__(256, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t acols = (uint32_t)(g.nM * g.nk * CO);   // one accumulator buffer
-  const uint32_t nbuf = (uint32_t)g.nbuf;
 
   auto decode = [&](long long it, int &b, int &z, int &y0) {
     const int yb = (int)(it % g.nyb);
@@ -1819,15 +1812,14 @@ __global__ void __launch_bounds__(256, 1)
       for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x, li++) {
         int b, z, y0;
         decode(it, b, z, y0);
-        const uint32_t ab = li % nbuf, use = li / nbuf;
-        if (use >= 1 && !role_wait(aempty(ab), (use - 1) & 1, abort_s, 23)) {
+        const uint32_t ab = li & 1;
+        if (li >= 2 && !role_wait(aempty(ab), ((li >> 1) - 1) & 1, abort_s, 23)) {
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t dcol = tmem + ab * acols;
-        const int nk = g.nk;
-        bool first = true;   // the item's first tap: each partial accumulator's first MMA overwrites
+        const uint32_t dcol = tmem + ab * WIDE_ACC_COLS;
+        uint32_t acc = 0;   // the item's first MMA of each tile overwrites
         for (int dz = -1; dz <= 1 && ok; dz++) {
           if (z + dz < 0 || z + dz >= p.Z) continue;
           for (int cg = 0; cg < NCG && ok; cg++) {
@@ -1849,15 +1841,12 @@ __global__ void __launch_bounds__(256, 1)
 #pragma unroll
               for (int ks = 0; ks < KS; ks++) {
                 const uint64_t bd = ((uint64_t)b_hi << 32) | (b_t + ks * b_ks);
-                const uint32_t acc = (first && ks < nk) ? 0u : 1u;
-                const uint32_t kcol = (uint32_t)((ks & (nk - 1)) * CO);
 #pragma unroll
                 for (int m = 0; m < 4; m++)
                   if (m < nM)
-                    umma_f16(dcol + (uint32_t)(m * nk * CO) + kcol,
-                             ((uint64_t)a_hi << 32) | (a_t + ks * a_ks + m * a_m), bd, idesc, acc);
+                    umma_f16(dcol + m * CO, ((uint64_t)a_hi << 32) | (a_t + ks * a_ks + m * a_m), bd, idesc, acc);
+                acc = 1;
               }
-              first = false;
               umma_commit(bempty(bs));   // the tap's B blocks are free once these MMAs complete
               nb++;
             }
@@ -1878,9 +1867,9 @@ __global__ void __launch_bounds__(256, 1)
     for (long long it = blockIdx.x; it < g.items; it += gridDim.x, li++) {
       int b, z, y0;
       decode(it, b, z, y0);
-      const uint32_t ab = li % nbuf, use = li / nbuf;
+      const uint32_t ab = li & 1;
       // tcgen05.ld is .sync.aligned: the whole warp takes one decision
-      if (!__all_sync(0xffffffffu, role_wait(afull(ab), use & 1, abort_s, 26) ? 1 : 0)) break;
+      if (!__all_sync(0xffffffffu, role_wait(afull(ab), (li >> 1) & 1, abort_s, 26) ? 1 : 0)) break;
       tc_fence_after();
       for (int m = 0; m < g.nM; m++) {
         const int q = m * 128 + qd * 32 + lane;
@@ -1891,15 +1880,7 @@ __global__ void __launch_bounds__(256, 1)
 #pragma unroll 1
         for (int c0 = 0; c0 < CO; c0 += 16) {
           float d[16];
-          const uint32_t tcol = tmem + lane_base + ab * acols + (uint32_t)(m * g.nk * CO + c0);
-          tmem_ld16(tcol, d);
-          for (int j = 1; j < g.nk; j++) {   // the K partials of this tile
-            float e[16];
-            tmem_ld16(tcol + (uint32_t)(j * CO), e);
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-            for (int k = 0; k < 16; k++) d[k] += e[k];
-          }
+          tmem_ld16(tmem + lane_base + ab * WIDE_ACC_COLS + m * CO + c0, d);
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
           if (!valid) continue;
           uint4 mk[2];
@@ -1958,7 +1939,7 @@ __global__ void __launch_bounds__(256, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(WIDE_TMEM_COLS)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * WIDE_ACC_COLS)
                  : "memory");
   }
 }
@@ -2003,7 +1984,7 @@ static size_t wide_smem(int CI, int CO, int slab_rows, int sb) {
 static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t &smem) {
   g.Xp = X + 2;
   const int rmax = nM * 128 / g.Xp;
-  if (rmax < 1 || g.Xp > 256 || nM * CO > WIDE_TMEM_COLS) return false;
+  if (rmax < 1 || g.Xp > 256 || nM * CO > WIDE_ACC_COLS) return false;
   g.nyb = (Y + rmax - 1) / rmax;
   g.R = (Y + g.nyb - 1) / g.nyb;
   if (g.R + 2 > 256) return false;
@@ -2015,12 +1996,6 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
   g.sb = (int)((227 * 1024 - fixed) / tb);
   if (g.sb > WIDE_SB) g.sb = WIDE_SB;
   smem = wide_smem(CI, CO, g.slab_rows, g.sb);
-  // independent accumulators: at least 4 (M tiles x K partials) where TMEM holds them,
-  // K partials at most the K steps of a chunk; two buffers where both fit
-  const int ks = (CI < 64 ? CI : 64) / 16;
-  g.nk = 1;
-  while (g.nM * g.nk < 4 && g.nk * 2 <= ks && g.nM * g.nk * 2 * CO <= WIDE_TMEM_COLS) g.nk *= 2;
-  g.nbuf = 2 * g.nM * g.nk * CO <= WIDE_TMEM_COLS ? 2 : 1;
   return true;
 }
 
@@ -2037,12 +2012,9 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
   }
   // item shape: forced (modes 2..5), else the one with the least estimated time:
   // waves of items x (the slower of the item's MMAs and its weight stream, plus a
-  // fixed cost and, with one accumulator buffer, the unhidden epilogue), in
-  // cycles.  An M 128 x N CO x K 16 MMA reads 4 KB of A and 32 CO bytes of B from
-  // shared memory (~70 bytes per cycle) and waits ~450 cycles for the previous
-  // MMA into the same accumulator, so its cost is the larger of the operand time
-  // and 450 / (independent accumulators); the weights stream at ~23 bytes per
-  // cycle (measured with the MMAs removed).
+  // fixed cost), in cycles: an M 128 x N CO x K 16 MMA ~48 (N 64) or ~64 (N 128)
+  // cycles; each of the item's 27 CI/KC taps of weight blocks a ~2000-cycle round
+  // trip, sb of them in flight
   WideGrid g{};
   size_t smem = 0;
   bool found = false;
@@ -2054,10 +2026,9 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     if (!wide_shape(CI, CO, p.Y, p.X, nM, c, sm)) continue;
     c.items = (long long)p.B * p.Z * c.nyb;
     const double waves = (double)((c.items + sms - 1) / sms);
-    const double t_op = (4096.0 + 32.0 * CO) / 70.0, t_lat = 450.0 / (c.nM * c.nk);
-    const double t_mma = 27.0 * (CI / 16) * c.nM * (t_op > t_lat ? t_op : t_lat);
-    const double t_b = 27.0 * CI * CO * 2.0 / 23.0;
-    const double cost = waves * ((t_mma > t_b ? t_mma : t_b) + 3000.0 + (c.nbuf == 1 ? 1500.0 : 0.0));
+    const double t_mma = 27.0 * (CI / 16) * c.nM * (CO <= 64 ? 48.0 : 64.0);
+    const double t_b = 27.0 * (CI < 64 ? 1 : CI / 64) * 2000.0 / c.sb;
+    const double cost = waves * ((t_mma > t_b ? t_mma : t_b) + 3000.0);
     if (!found || cost < best) {
       found = true;
       best = cost;

@@ -54,7 +54,7 @@ def item_shape(Y, X, CO, nM):
     """The launcher's wide_shape: (Xp, R, nM, nyb, slab_rows) or None."""
     Xp = X + 2
     rmax = nM * 128 // Xp
-    if rmax < 1 or Xp > 256 or nM * CO > 512:
+    if rmax < 1 or Xp > 256 or nM * CO > 256:
         return None
     nyb = -(-Y // rmax)
     R = -(-Y // nyb)
@@ -129,6 +129,6 @@ def test_item_shapes():
     assert item_shape(114, 114, 64, 3) == (116, 3, 3, 38, 624)
     assert item_shape(57, 57, 128, 1) == (59, 2, 1, 29, 248)
     assert item_shape(32, 32, 64, 2) == (34, 7, 2, 5, 328)
-    # no full padded row in the tiles, or accumulators beyond the 512 TMEM columns
+    # no full padded row in the tiles, or accumulators beyond 256 TMEM columns
     assert item_shape(10, 200, 64, 1) is None
-    assert item_shape(10, 20, 128, 5) is None
+    assert item_shape(10, 20, 128, 4) is None
