@@ -96,14 +96,16 @@ WORKLOADS = {
 
 
 def set_mac_shape(ctx, spec):
-    """--mac STAGES,ROWS_FWD,ROWS_BWD,SPLIT: the multiply-accumulate launch shape (a sweep)."""
+    """--mac STAGES,ROWS_FWD,ROWS_BWD,SPLIT[,CTAS_PER_SM]: the multiply-accumulate launch shape (a sweep)."""
     if not spec:
         return
-    st, rf, rb, sp = (int(v) for v in spec.split(","))
-    ctx.set_option("mac_stages", st)
-    ctx.set_option("mac_chunk_rows_forward", rf)
-    ctx.set_option("mac_chunk_rows_backward", rb)
-    ctx.set_option("mac_split", sp)
+    v = [int(t) for t in spec.split(",")]
+    ctx.set_option("mac_stages", v[0])
+    ctx.set_option("mac_chunk_rows_forward", v[1])
+    ctx.set_option("mac_chunk_rows_backward", v[2])
+    ctx.set_option("mac_split", v[3])
+    if len(v) > 4:
+        ctx.set_option("mac_ctas_per_sm", v[4])
 
 
 def pinned_empty(shape):
@@ -152,7 +154,7 @@ def parse():
     ap.add_argument("--wide", type=int, default=1, choices=range(6),
                     help="unet: kernel of the 64/128-channel layers (0 mma.sync, 1 tcgen05, 2..5 tcgen05 with "
                          "1..4 M tiles per work item)")
-    ap.add_argument("--mac", default=None, metavar="STAGES,ROWS_FWD,ROWS_BWD,SPLIT",
+    ap.add_argument("--mac", default=None, metavar="STAGES,ROWS_FWD,ROWS_BWD,SPLIT[,CTAS_PER_SM]",
                     help="projection workloads: the multiply-accumulate launch shape (default: the library's)")
     ap.add_argument("--planes", default=None,
                     help="comma-separated z indices of the workload to keep (smaller cases for profiling)")

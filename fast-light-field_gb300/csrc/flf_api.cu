@@ -86,6 +86,7 @@ struct flf_ctx {
   int opt_stages = 2;            // tunable: MAC shared-memory pipeline stages
   int opt_chunk_rows[2] = {12, 12};   // tunable: stored rows per pipeline stage (forward, backward)
   int opt_split = 1;             // tunable: threads sharing one orbit's rows
+  int opt_ctas_per_sm = 16;      // tunable: multiply-accumulate CTAs per SM the plane grouping aims at
   int opt_plane_sizes = 1;       // 1: transform size per plane (grouped); 0: one size for all
   int opt_geometry_cache = 2;    // geometries of other image shapes kept resident (most recent first)
   std::vector<Geometry> parked;  // those geometries
@@ -708,10 +709,10 @@ int check_ready(flf_ctx *ctx, int T, int Y, int X, int dir, cudaStream_t s) {
   return rc;
 }
 
-// Planes per multiply-accumulate CTA: enough plane groups to give about 16
-// CTAs per SM over the nquads frequency quads.
+// Planes per multiply-accumulate CTA: enough plane groups to give about
+// opt_ctas_per_sm (16) CTAs per SM over the nquads frequency quads.
 int zgroup_for(const flf_ctx *ctx, int nz, int nquads) {
-  const int target = 16 * std::max(1, ctx->num_sms);
+  const int target = ctx->opt_ctas_per_sm * std::max(1, ctx->num_sms);
   const int nzg_needed = std::min(nz, std::max(1, (target + nquads - 1) / nquads));
   return std::min(kMacMaxZgroup, std::max(1, (nz + nzg_needed - 1) / nzg_needed));
 }
@@ -1620,6 +1621,11 @@ int flf_set_option(flf_ctx *ctx, const char *name, long long value) {
     if (value != 0 && value != 1) return fail(ctx, FLF_E_ARG, "release_psf must be 0 or 1");
     ctx->opt_release_psf = (int)value;
     if (value) maybe_release_psfs(ctx);
+    return FLF_OK;
+  }
+  if (!strcmp(name, "mac_ctas_per_sm")) {
+    if (value < 1 || value > 64) return fail(ctx, FLF_E_ARG, "mac_ctas_per_sm must be in [1, 64]");
+    ctx->opt_ctas_per_sm = (int)value;
     return FLF_OK;
   }
   if (!strcmp(name, "geometry_cache")) {

@@ -176,7 +176,9 @@ int flf_profile_read(flf_ctx *ctx, char *buf, size_t len);
  * per stage, even, 2..64, both directions; "mac_chunk_rows_forward" and
  * "mac_chunk_rows_backward" set one), "mac_split" (threads sharing an orbit's rows,
  * 1..4; the CTA has two such groups, one per frequency pair of a quad, of at
- * most 256 threads in all), "plane_transform_sizes" (1: each plane uses the smallest
+ * most 256 threads in all), "mac_ctas_per_sm" (1..64, default 16: the CTAs
+ * per SM the grouping of planes per CTA aims at; fewer CTAs stream more planes
+ * each), "plane_transform_sizes" (1: each plane uses the smallest
  * transform its PSF allows, planes grouped by size - the default; 0: one
  * size for all planes) and "geometry_cache" (0..16, default 2: how many
  * transfer-matrix sets of other image shapes stay resident, most recent
