@@ -714,6 +714,11 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 // accumulator slot is free after the last output plane that reads it.
 // Planes outside the volume contribute nothing: their MMAs are skipped and
 // the epilogue leaves their terms out.
+// The head (HEAD; only output channel 0 is used) folds (dz, dy) into N
+// instead: one MMA of N 16 (9 columns used) per input row ri of a slab and dx,
+//   D[z'][ri][x][dz*3 + dy] = sum over (dx, ci) of in[z'][y0-1+ri][x+dx-1][ci] w[dz*9 + dy*3 + dx][ci][0],
+// and out[z][y0+r][x] = sum over (dz, dy) of D[z-1+dz][r+dy][x][dz*3+dy], so a
+// slab of R+2 input rows costs 3 (R+2) MMAs for R output rows instead of 9 R.
 //   warp 0     producer: one thread issues the TMA loads;
 //   warps 1-2  MMA issuers: one thread each issues the 9 MMAs of half of the
 //              rows per slab, then commits to the slab's accumulator barrier
@@ -799,8 +804,11 @@ __global__ void __launch_bounds__(352, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   constexpr int PYH = R + 2, NACC = TMA16_NACC;
   constexpr int KS = CI / 16;                 // K steps of 16 input channels
-  constexpr int NN = 3 * CO;                  // N of one MMA: (dz, co)
-  constexpr int NISS = R % 2 == 0 ? 2 : 1;    // MMA-issuing threads (warps 1 .. NISS)
+  // N of one MMA: (dz, co); the head, whose only output channel is 0, folds (dz, dy) into N
+  // instead (9 of 16 columns) and issues one MMA per input row and dx
+  constexpr int NN = HEAD ? 16 : 3 * CO;
+  constexpr int NBLK = HEAD ? 3 : 9;          // B blocks per K step: (dy, dx), or dx for the head
+  constexpr int NISS = (HEAD ? PYH : R) % 2 == 0 ? 2 : 1;   // MMA-issuing threads (warps 1 .. NISS)
   constexpr int CH = CO / 2;                  // output channels per epilogue warp
   static_assert((CI == 16 || CI == 32) && (CO == 16 || CO == 32), "16 or 32 channels in and out");
   static_assert(SW32 || CI == 16, "the unswizzled slab layout is for 16 input channels");
@@ -814,8 +822,8 @@ __global__ void __launch_bounds__(352, 1)
   constexpr uint32_t LOADS = SW32 ? KS : 2;
   constexpr uint32_t SLOT = LOADS * PLANE;
   constexpr uint32_t BBLK = NN * 16 * 2;                     // B operand of one (dy, dx, K step)
-  constexpr uint32_t SLAB0 = (9 * KS * BBLK + 1023) / 1024 * 1024;
-  constexpr uint32_t ACOLS = R * NN;                         // one accumulator slot
+  constexpr uint32_t SLAB0 = (NBLK * KS * BBLK + 1023) / 1024 * 1024;
+  constexpr uint32_t ACOLS = (HEAD ? PYH : R) * NN;          // one accumulator slot (per output / input row)
   constexpr uint32_t TCOLS = NACC * ACOLS <= 256 ? 256 : 512;
   static_assert(NACC * ACOLS <= 512, "the accumulator slots fit the 512 TMEM columns");
   // layout: [B operands][S slots][mbarriers][tmem address][abort flag]
@@ -832,18 +840,20 @@ __global__ void __launch_bounds__(352, 1)
   const uint32_t fin = bar_s + 8u * (2 * S + 2 * NACC);
 
   // B operands: block (dy, dx, K step kh) holds B[n = dz*CO + co][k = ci - 16 kh] =
-  // w[tap = dz*9 + dy*3 + dx][ci][co]; core matrix (n/8, k/8) at (n/8)*256 + (k/8)*128, row n%8 at
-  // 16 B, element k%8 at 2 B
-  for (int i = tid; i < 9 * KS * NN; i += blockDim.x) {
+  // w[tap = dz*9 + dy*3 + dx][ci][co]; for the head, block (dx, kh) holds B[n = dz*3 + dy][k] =
+  // w[tap = dz*9 + dy*3 + dx][ci][0] (n < 9, zero above); core matrix (n/8, k/8) at
+  // (n/8)*256 + (k/8)*128, row n%8 at 16 B, element k%8 at 2 B
+  for (int i = tid; i < NBLK * KS * NN; i += blockDim.x) {
     const int bk = i / NN, n = i % NN;
     const int blk = bk / KS, kh = bk % KS;
-    const int tap = (n / CO) * 9 + blk, co = n % CO;
+    const bool used = !HEAD || n < 9;
+    const int tap = HEAD ? (n / 3) * 9 + (n % 3) * 3 + blk : (n / CO) * 9 + blk, co = HEAD ? 0 : n % CO;
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       const int ci = kh * 16 + 2 * c;
-      const unsigned short lo = __bfloat16_as_ushort(p.w[((long long)tap * CI + ci) * CO + co]);
-      const unsigned short hi = __bfloat16_as_ushort(p.w[((long long)tap * CI + ci + 1) * CO + co]);
+      const unsigned short lo = used ? __bfloat16_as_ushort(p.w[((long long)tap * CI + ci) * CO + co]) : 0;
+      const unsigned short hi = used ? __bfloat16_as_ushort(p.w[((long long)tap * CI + ci + 1) * CO + co]) : 0;
       pk[c] = (uint32_t)lo | ((uint32_t)hi << 16);
     }
     unsigned char *row = Wb + bk * BBLK + (n >> 3) * 256 + (n & 7) * 16;
@@ -906,8 +916,9 @@ __global__ void __launch_bounds__(352, 1)
     }
   } else if (warp <= 2) {
     if (lane == 0 && warp <= NISS) {
-      // ---- MMA issuers: warp 1 + j takes rows j*R/NISS .. (j+1)*R/NISS - 1 ----
-      constexpr int RI = R / NISS;
+      // ---- MMA issuers: warp 1 + j takes rows j*RR/NISS .. (j+1)*RR/NISS - 1 (output rows, or for
+      // the head input rows) ----
+      constexpr int RI = (HEAD ? PYH : R) / NISS;
       const int r0 = (warp - 1) * RI;
       // instruction descriptor: F32 accumulate, BF16 A and B, both K-major, N = 3 CO, M = 128
       const uint32_t idesc =
@@ -938,8 +949,9 @@ __global__ void __launch_bounds__(352, 1)
             const uint32_t al = a_lo + (n % S) * (SLOT >> 4);
             const uint32_t dcol = tmem + acc * ACOLS;
 #pragma unroll
-            for (int blk = 0; blk < 9; blk++) {
-              const int dy = blk / 3, dx = blk % 3;
+            for (int blk = 0; blk < NBLK; blk++) {
+              // head: block dx, slab row = the input row; otherwise block (dy, dx), slab row r + dy
+              const int dy = HEAD ? 0 : blk / 3, dx = HEAD ? blk : blk % 3;
 #pragma unroll
               for (int kh = 0; kh < KS; kh++) {
                 const uint64_t bd = ((uint64_t)b_hi << 32) | (uint64_t)(b_lo + (blk * KS + kh) * (BBLK >> 4));
@@ -982,58 +994,85 @@ __global__ void __launch_bounds__(352, 1)
         }
         tc_fence_after();
         const int z = zlo + i;
-        float d[R][3][CH];
-#pragma unroll
-        for (int r = 0; r < R; r++)
-#pragma unroll
-          for (int dz = 0; dz < 3; dz++) {
-            const uint32_t a = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + r * NN + dz * CO + hf * CH;
-            if constexpr (CH == 16) tmem_ld16(a, d[r][dz]);
-            else tmem_ld8(a, d[r][dz]);
-          }
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        tc_fence_before();
-        net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
         const bool lo_in = z > 0, hi_in = z + 1 < p.Z;
+        if constexpr (HEAD) {
+          // out[z][y0 + r] = sum over (dz, dy) of column dz*3 + dy of input row r + dy of slab z-1+dz
+          float o[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-          const int y = y0 + r;
-          float o[CH];
+          for (int r = 0; r < R; r++) o[r] = 0.f;
+          if (hf == 0) {   // warp-uniform: the first channel half's warps hold the single output channel
+#pragma unroll 1
+            for (int dz = 0; dz < 3; dz++) {
+              // planes outside the volume had no MMAs: their slot holds stale values, selected away
+              const bool in = !((dz == 0 && !lo_in) || (dz == 2 && !hi_in));
+              const uint32_t slot = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS;
 #pragma unroll
-          for (int c = 0; c < CH; c++)
-            o[c] = (lo_in ? d[r][0][c] : 0.f) + d[r][1][c] + (hi_in ? d[r][2][c] : 0.f);
-          if (HEAD) {
-            if (hf == 0 && b < h.T && z < h.Zr && y < h.Yr && x < h.Xr) {
-              const float sc = h.sum_x1[b] / h.count;
-              h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[0] + h.bias, h.floor) * sc;
+              for (int ri = 0; ri < PYH; ri++) {
+                float v[16];
+                tmem_ld16(slot + ri * NN, v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                for (int dy = 0; dy < 3; dy++)
+                  if (ri - dy >= 0 && ri - dy < R) o[ri - dy] += in ? v[dz * 3 + dy] : 0.f;
+              }
             }
-            continue;
           }
-          if (x >= p.X || y >= p.Y) continue;
-          const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO + hf * CH;
+          tc_fence_before();
+          net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
+          if (hf == 0 && b < h.T && z < h.Zr && x < h.Xr) {
+            const float sc = h.sum_x1[b] / h.count;
 #pragma unroll
-          for (int v = 0; v < CH / 8; v++) {
-            uint4 mk;
-            if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + off + v * 8);
-            uint4 outv;
-            __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(&outv);
-            const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-              float v0 = o[v * 8 + 2 * k] + bias[v * 8 + 2 * k];
-              float v1 = o[v * 8 + 2 * k + 1] + bias[v * 8 + 2 * k + 1];
-              if (p.relu) {
-                v0 = fmaxf(v0, 0.f);
-                v1 = fmaxf(v1, 0.f);
-              }
-              if (p.mask) {
-                const float2 mf = __bfloat1622float2(m2[k]);
-                if (!(mf.x > 0.f)) v0 = 0.f;
-                if (!(mf.y > 0.f)) v1 = 0.f;
-              }
-              hv[k] = __floats2bfloat162_rn(v0, v1);
+            for (int r = 0; r < R; r++) {
+              const int y = y0 + r;
+              if (y < h.Yr) h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[r] + h.bias, h.floor) * sc;
             }
-            *reinterpret_cast<uint4 *>(p.y + off + v * 8) = outv;
+          }
+        } else {
+          float d[R][3][CH];
+#pragma unroll
+          for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int dz = 0; dz < 3; dz++) {
+              const uint32_t a = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + r * NN + dz * CO + hf * CH;
+              if constexpr (CH == 16) tmem_ld16(a, d[r][dz]);
+              else tmem_ld8(a, d[r][dz]);
+            }
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          tc_fence_before();
+          net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            const int y = y0 + r;
+            float o[CH];
+#pragma unroll
+            for (int c = 0; c < CH; c++)
+              o[c] = (lo_in ? d[r][0][c] : 0.f) + d[r][1][c] + (hi_in ? d[r][2][c] : 0.f);
+            if (x >= p.X || y >= p.Y) continue;
+            const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO + hf * CH;
+#pragma unroll
+            for (int v = 0; v < CH / 8; v++) {
+              uint4 mk;
+              if (p.mask) mk = *reinterpret_cast<const uint4 *>(p.mask + off + v * 8);
+              uint4 outv;
+              __nv_bfloat162 *hv = reinterpret_cast<__nv_bfloat162 *>(&outv);
+              const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&mk);
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                float v0 = o[v * 8 + 2 * k] + bias[v * 8 + 2 * k];
+                float v1 = o[v * 8 + 2 * k + 1] + bias[v * 8 + 2 * k + 1];
+                if (p.relu) {
+                  v0 = fmaxf(v0, 0.f);
+                  v1 = fmaxf(v1, 0.f);
+                }
+                if (p.mask) {
+                  const float2 mf = __bfloat1622float2(m2[k]);
+                  if (!(mf.x > 0.f)) v0 = 0.f;
+                  if (!(mf.y > 0.f)) v1 = 0.f;
+                }
+                hv[k] = __floats2bfloat162_rn(v0, v1);
+              }
+              *reinterpret_cast<uint4 *>(p.y + off + v * 8) = outv;
+            }
           }
         }
       }
@@ -2289,7 +2328,7 @@ cudaError_t launch_ws_head(const void *d, const void *w, float bias, float floor
                            int T, int Z, int Y, int X, int Zp, int Yp, int Xp, cudaStream_t s) {
   ConvParams p{(const bf16 *)d, (const bf16 *)w, nullptr, nullptr, nullptr, T, Zp, Yp, Xp, 16, 16, 0, nullptr, 1};
   HeadOut h{x0, sum_x1, (float)Z * Y * X, bias, floor_, T, Z, Y, X};
-  return g_conv16_tc ? launch_tma16<16, 16, 2, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
+  return g_conv16_tc ? launch_tma16<16, 16, 4, 8, true, true>(p, h, s) : launch_t16<true>(p, h, s);
 }
 
 cudaError_t launch_render_blobs(float *vol, void *acc, int Z, int Y, int X, const float *pts, int npts, float sigma,

@@ -111,3 +111,66 @@ def test_fold_model_matches_direct_convolution(ci, co, R, shape, W, zc):
     got = fold_model(x, w, R, W, zc)
     assert not np.isnan(got).any()                       # every output voxel written once
     np.testing.assert_allclose(got, direct_conv(x, w), rtol=1e-12, atol=1e-12)
+
+
+def head_model(x, w, R, W, zc):
+    """The head variant (output channel 0 only): B block dx holds B[n = dz*3 + dy][ci] =
+    w[dz*9 + dy*3 + dx][ci][0] (n < 9, zero above); one MMA per slab input row and dx
+    accumulates D[z'][ri][x][n]; out[z][y0 + r][x] = sum over (dz, dy) of
+    D[z - 1 + dz][r + dy][x][dz*3 + dy], planes outside the volume left out."""
+    B, Z, Y, X, CI = x.shape
+    KS = CI // 16
+    blocks = np.zeros((3 * KS, 16, 16))
+    for dx in range(3):
+        for kh in range(KS):
+            for n in range(9):
+                dz, dy = divmod(n, 3)
+                blocks[dx * KS + kh, n, :] = w[dz * 9 + dy * 3 + dx, kh * 16:(kh + 1) * 16, 0]
+    out = np.full((B, Z, Y, X), np.nan)
+    for b in range(B):
+        for zlo in range(0, Z, zc):
+            nz = min(Z - zlo, zc)
+            for y0 in range(0, Y, R):
+                for x0 in range(0, X, W):
+                    D = {}
+                    for k in range(nz + 2):
+                        zin = zlo - 1 + k
+                        if not 0 <= zin < Z:
+                            continue
+                        slab = np.zeros((R + 2, W + 2, CI))
+                        for j in range(R + 2):
+                            yy = y0 - 1 + j
+                            if not 0 <= yy < Y:
+                                continue
+                            lo, hi = max(x0 - 1, 0), min(x0 - 1 + W + 2, X)
+                            slab[j, lo - (x0 - 1):hi - (x0 - 1)] = x[b, zin, yy, lo:hi]
+                        acc = np.zeros((R + 2, W, 16))
+                        for ri in range(R + 2):
+                            for dx in range(3):
+                                for kh in range(KS):
+                                    acc[ri] += slab[ri, dx:dx + W, kh * 16:(kh + 1) * 16] @ blocks[dx * KS + kh].T
+                        D[zin] = acc
+                    for i in range(nz):
+                        z = zlo + i
+                        o = np.zeros((R, W))
+                        for dz in range(3):
+                            if (z - 1 + dz) not in D:
+                                continue
+                            for r in range(R):
+                                for dy in range(3):
+                                    o[r] += D[z - 1 + dz][r + dy, :, dz * 3 + dy]
+                        for r in range(R):
+                            if y0 + r < Y:
+                                n = min(W, X - x0)
+                                out[b, z, y0 + r, x0:x0 + n] = o[r, :n]
+    return out
+
+
+@pytest.mark.parametrize("shape,W,zc", [((1, 5, 9, 13), 8, 5), ((2, 6, 6, 9), 4, 2), ((1, 7, 3, 6), 16, 3)])
+def test_head_fold_model_matches_direct_convolution(shape, W, zc):
+    rng = np.random.default_rng(sum(shape) + W)
+    x = rng.standard_normal(shape + (16,))
+    w = rng.standard_normal((27, 16, 16)) / np.sqrt(27 * 16)
+    got = head_model(x, w, 4, W, zc)
+    assert not np.isnan(got).any()
+    np.testing.assert_allclose(got, direct_conv(x, w)[..., 0], rtol=1e-12, atol=1e-12)
