@@ -798,6 +798,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t addr, float *v) {
 
 }  // namespace
 
+// Head epilogue: add column dz*3 + dy of input row r + dy (dy = 0..2) to output row r.
+template <int RH, int DZ>
+__device__ __forceinline__ void head_rows(float (&o)[RH], const float (&v)[RH + 2][16], bool in) {
+#pragma unroll
+  for (int r = 0; r < RH; r++)
+#pragma unroll
+    for (int dy = 0; dy < 3; dy++) o[r] += in ? v[r + dy][DZ * 3 + dy] : 0.f;
+}
+
 template <int CI, int CO, int R, int S, bool HEAD, bool SW32>
 __global__ void __launch_bounds__(352, 1)
     k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
@@ -996,34 +1005,36 @@ __global__ void __launch_bounds__(352, 1)
         const int z = zlo + i;
         const bool lo_in = z > 0, hi_in = z + 1 < p.Z;
         if constexpr (HEAD) {
-          // out[z][y0 + r] = sum over (dz, dy) of column dz*3 + dy of input row r + dy of slab z-1+dz
-          float o[R];
+          // out[z][y0 + r] = sum over (dz, dy) of column dz*3 + dy of input row r + dy of slab z-1+dz.
+          // Channel half hf takes output rows hf*R/2 .. : input rows hf*R/2 .. hf*R/2 + R/2 + 1
+          constexpr int RH = R / 2;
+          static_assert(!HEAD || R % 2 == 0, "the head's rows split between the two warp halves");
+          float o[RH];
 #pragma unroll
-          for (int r = 0; r < R; r++) o[r] = 0.f;
-          if (hf == 0) {   // warp-uniform: the first channel half's warps hold the single output channel
-#pragma unroll 1
-            for (int dz = 0; dz < 3; dz++) {
-              // planes outside the volume had no MMAs: their slot holds stale values, selected away
-              const bool in = !((dz == 0 && !lo_in) || (dz == 2 && !hi_in));
-              const uint32_t slot = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS;
+          for (int r = 0; r < RH; r++) o[r] = 0.f;
+          const int rb = hf * RH;
+          // one plane's rows at a time (planes outside the volume had no MMAs: their slot holds
+          // stale values, selected away); the column index is a constant in each call
+          float v[RH + 2][16];
+          auto rows = [&](int dz) {
+            const uint32_t slot = tmem + lane_base + ((n + i + dz) % NACC) * ACOLS + rb * NN;
 #pragma unroll
-              for (int ri = 0; ri < PYH; ri++) {
-                float v[16];
-                tmem_ld16(slot + ri * NN, v);
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-                for (int dy = 0; dy < 3; dy++)
-                  if (ri - dy >= 0 && ri - dy < R) o[ri - dy] += in ? v[dz * 3 + dy] : 0.f;
-              }
-            }
-          }
+            for (int j = 0; j < RH + 2; j++) tmem_ld16(slot + j * NN, v[j]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          };
+          rows(0);
+          head_rows<RH, 0>(o, v, lo_in);
+          rows(1);
+          head_rows<RH, 1>(o, v, true);
+          rows(2);
+          head_rows<RH, 2>(o, v, hi_in);
           tc_fence_before();
           net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
-          if (hf == 0 && b < h.T && z < h.Zr && x < h.Xr) {
+          if (b < h.T && z < h.Zr && x < h.Xr) {
             const float sc = h.sum_x1[b] / h.count;
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-              const int y = y0 + r;
+            for (int r = 0; r < RH; r++) {
+              const int y = y0 + rb + r;
               if (y < h.Yr) h.x0[(((long long)z * h.T + b) * h.Yr + y) * h.Xr + x] = fmaxf(o[r] + h.bias, h.floor) * sc;
             }
           }
