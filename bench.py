@@ -126,7 +126,9 @@ def pinned_like(a):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 for the warm-start workload, whose steps take ~1.5 ms, "
+                         "so the clock sampler sees the timed region; 10 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="warmstart", choices=sorted(WORKLOADS))
@@ -158,7 +160,10 @@ def parse():
                     help="projection workloads: the multiply-accumulate launch shape (default: the library's)")
     ap.add_argument("--planes", default=None,
                     help="comma-separated z indices of the workload to keep (smaller cases for profiling)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 200 if args.workload == "warmstart" and args.impl == "gb300" else 10
+    return args
 
 
 def dist_env():
@@ -188,7 +193,10 @@ def build_problem(wl, seed=1234, keep=None):
 
 
 class ClockSampler:
-    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples (every 50 ms) of SM clock and throttle reasons.  A reader
+    thread stamps each sample with the host time it arrives; mark() brackets the
+    timed region, and stop() keeps the samples inside it (the first one after it
+    when the region is shorter than the sampling interval)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -197,27 +205,48 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
+        import threading
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                self.lines.append((time.time(), line))
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def mark(self, begin):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
 
     def stop(self):
         if self.proc is None:
             return None
         self.proc.terminate()
         try:
-            out, _ = self.proc.communicate(timeout=5)
+            self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-            out, _ = self.proc.communicate()
+        self.thread.join(timeout=5)
+        rows = self.lines
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for r in rows if self.t0 <= r[0] <= self.t1 + 0.06]
+            after = [r for r in rows if r[0] >= self.t0]
+            rows = inside if inside else after[:1]
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in out.strip().splitlines():
+        for _, line in rows:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -498,7 +527,9 @@ def run_gb300(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
+    clocks.mark(True)
     ms = timed(direct=False)
+    clocks.mark(False)
     clk = clocks.stop()
     # per-kernel durations: the same steps again, launched directly on one
     # stream with CUDA events around every kernel (a graph replay has no
@@ -670,12 +701,14 @@ def run_timeseries(args):
     clocks = ClockSampler(0)
     clocks.start()
     time.sleep(0.3)
+    clocks.mark(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
     for _ in range(args.steps):
         step()
     e1.record(s)
     torch.cuda.synchronize()
+    clocks.mark(False)
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
     nvol = T * len(data)
@@ -814,6 +847,8 @@ def run_psf(args):
     steps = max(1, args.steps)
     clocks = ClockSampler(0)
     clocks.start()
+    time.sleep(0.3)
+    clocks.mark(True)
     t0 = time.perf_counter()
     tim = []
     for _ in range(steps):
@@ -821,6 +856,7 @@ def run_psf(args):
         tim.append(r["timings"])
     torch.cuda.synchronize()
     sec = (time.perf_counter() - t0) / steps
+    clocks.mark(False)
     clk = clocks.stop()
     with tempfile.TemporaryDirectory() as d:
         t0 = time.perf_counter()
@@ -1033,8 +1069,11 @@ def run_warmstart(args):
 
     clocks = ClockSampler(0)
     clocks.start()
+    time.sleep(0.3)   # nvidia-smi's first sample
+    clocks.mark(True)
     ms_plain = timed(g_plain.replay)
     ms_warm = timed(g_warm.replay) if g_warm is not None else None
+    clocks.mark(False)
     clk = clocks.stop()
     ms_plain_direct = timed(plain_step)
     ms_warm_direct = timed(warm_step) if k_warm is not None else None
@@ -1234,12 +1273,15 @@ def run_config4(args):
     free_b, total_b = torch.cuda.mem_get_info(dev)
     clocks = ClockSampler(0)
     clocks.start()
+    time.sleep(0.3)
+    clocks.mark(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
     for _ in range(args.steps):
         step()
     e1.record(s)
     torch.cuda.synchronize()
+    clocks.mark(False)
     clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
     ctx.synchronize(s.cuda_stream)
