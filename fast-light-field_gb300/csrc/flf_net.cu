@@ -1710,8 +1710,9 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 struct WideGrid {
   int Xp, R, nM, nyb;   // padded row, rows per item, M tiles per item, y blocks
   int slab_rows;        // rows of one 8-channel group of a slab slot (LBO / 16)
-  int sb;               // B blocks in the ring (the shared memory the slabs leave)
-  long long items;      // B * Z * nyb
+  int sb;               // taps of B blocks in the ring (the shared memory the slabs leave)
+  int splits;           // 1, or 3: work unit = (item, input plane z-1+s) writing FP32 partials to ws[s]
+  long long items;      // B * Z * nyb * splits (work units)
 };
 
 constexpr int WIDE_SB_MAX = 64;      // B block ring: barriers for at most this many blocks
@@ -1751,6 +1752,7 @@ __global__ void __launch_bounds__(256, 1)
   auto aempty = [&](uint32_t k) { return bar_s + 8u * (6 + 2 * WIDE_SB_MAX + k); };  // accumulator read
   const uint32_t fin = bar_s + 8u * (8 + 2 * WIDE_SB_MAX);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long Mv = (long long)p.B * p.Z * p.Y * p.X;   // voxels (the stride of a partial-sum slice)
 
   if (tid == 0) {
     for (int k = 0; k < 2; k++) {
@@ -1778,12 +1780,24 @@ __global__ void __launch_bounds__(256, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  auto decode = [&](long long it, int &b, int &z, int &y0) {
-    const int yb = (int)(it % g.nyb);
-    const long long q = it / g.nyb;
+  // work unit it -> volume b, output plane z, first row y0 and, with splits, the one input
+  // plane offset dz1 (-1..1) it covers (splits == 1: all three, dz1 = 2)
+  auto decode = [&](long long it, int &b, int &z, int &y0, int &dz1) {
+    long long q = it;
+    dz1 = 2;
+    if (g.splits > 1) {
+      dz1 = (int)(q % g.splits) - 1;
+      q /= g.splits;
+    }
+    const int yb = (int)(q % g.nyb);
+    q /= g.nyb;
     z = (int)(q % p.Z);
     b = (int)(q / p.Z);
     y0 = yb * g.R;
+  };
+  // the input planes a unit reads: in the volume, and its own with splits
+  auto plane_used = [&](int z, int dz, int dz1) {
+    return z + dz >= 0 && z + dz < p.Z && (dz1 == 2 || dz == dz1);
   };
 
   uint32_t nslab = 0, nbb = 0;   // slab chunks / B blocks issued (producers)
@@ -1791,11 +1805,11 @@ __global__ void __launch_bounds__(256, 1)
     if (lane == 0) {
       // ---- slab producer ----
       for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
-        int b, z, y0;
-        decode(it, b, z, y0);
+        int b, z, y0, dz1;
+        decode(it, b, z, y0, dz1);
         bool ok = true;
         for (int dz = -1; dz <= 1 && ok; dz++) {
-          if (z + dz < 0 || z + dz >= p.Z) continue;
+          if (!plane_used(z, dz, dz1)) continue;
           for (int cg = 0; cg < NCG; cg++) {
             const uint32_t sl = nslab & 1;
             if (nslab >= 2 && !role_wait(sempty(sl), ((nslab >> 1) - 1) & 1, abort_s, 21)) {
@@ -1815,11 +1829,11 @@ __global__ void __launch_bounds__(256, 1)
     if (lane == 0) {
       // ---- B producer: one tap's KS blocks per ring slot, in the issuer's order ----
       for (long long it = blockIdx.x; it < g.items && !*abort_s; it += gridDim.x) {
-        int b, z, y0;
-        decode(it, b, z, y0);
+        int b, z, y0, dz1;
+        decode(it, b, z, y0, dz1);
         bool ok = true;
         for (int dz = -1; dz <= 1 && ok; dz++) {
-          if (z + dz < 0 || z + dz >= p.Z) continue;
+          if (!plane_used(z, dz, dz1)) continue;
           for (int cg = 0; cg < NCG && ok; cg++)
             for (int t9 = 0; t9 < 9; t9++) {
               const uint32_t sl = nbb % SB;
@@ -1860,8 +1874,8 @@ __global__ void __launch_bounds__(256, 1)
       uint32_t ns = 0, nb = 0, li = 0;
       bool ok = true;
       for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x, li++) {
-        int b, z, y0;
-        decode(it, b, z, y0);
+        int b, z, y0, dz1;
+        decode(it, b, z, y0, dz1);
         const uint32_t ab = li & 1;
         if (li >= 2 && !role_wait(aempty(ab), ((li >> 1) - 1) & 1, abort_s, 23)) {
           ok = false;
@@ -1871,7 +1885,7 @@ __global__ void __launch_bounds__(256, 1)
         const uint32_t dcol = tmem + ab * WIDE_ACC_COLS;
         uint32_t acc = 0;   // the item's first MMA of each tile overwrites
         for (int dz = -1; dz <= 1 && ok; dz++) {
-          if (z + dz < 0 || z + dz >= p.Z) continue;
+          if (!plane_used(z, dz, dz1)) continue;
           for (int cg = 0; cg < NCG && ok; cg++) {
             const uint32_t sl = ns & 1;
             if (!role_wait(sfull(sl), (ns >> 1) & 1, abort_s, 24)) {
@@ -1915,24 +1929,35 @@ __global__ void __launch_bounds__(256, 1)
     const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
     uint32_t li = 0;
     for (long long it = blockIdx.x; it < g.items; it += gridDim.x, li++) {
-      int b, z, y0;
-      decode(it, b, z, y0);
+      int b, z, y0, dz1;
+      decode(it, b, z, y0, dz1);
       const uint32_t ab = li & 1;
       // tcgen05.ld is .sync.aligned: the whole warp takes one decision
       if (!__all_sync(0xffffffffu, role_wait(afull(ab), (li >> 1) & 1, abort_s, 26) ? 1 : 0)) break;
       tc_fence_after();
+      // with splits a unit whose input plane lies outside the volume issued no MMA: zeros
+      const bool none = g.splits > 1 && !plane_used(z, dz1, dz1);
       for (int m = 0; m < g.nM; m++) {
         const int q = m * 128 + qd * 32 + lane;
         const int yl = q / g.Xp, x = q - yl * g.Xp;
         const int y = y0 + yl;
         const bool valid = yl < g.R && y < p.Y && x < p.X;
-        const long long off = ((((long long)b * p.Z + z) * p.Y + y) * p.X + x) * CO;
+        const long long vox = (((long long)b * p.Z + z) * p.Y + y) * p.X + x;
+        const long long off = vox * CO;
 #pragma unroll 1
         for (int c0 = 0; c0 < CO; c0 += 16) {
           float d[16];
           tmem_ld16(tmem + lane_base + ab * WIDE_ACC_COLS + m * CO + c0, d);
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
           if (!valid) continue;
+          if (g.splits > 1) {   // FP32 partial sum of this input plane; bias, ReLU and mask come later
+            float *dst = p.ws + (long long)(dz1 + 1) * Mv * CO + off + c0;
+#pragma unroll
+            for (int k = 0; k < 16; k += 4)
+              *reinterpret_cast<float4 *>(dst + k) =
+                  none ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(d[k], d[k + 1], d[k + 2], d[k + 3]);
+            continue;
+          }
           uint4 mk[2];
           if (p.mask) {
             mk[0] = *reinterpret_cast<const uint4 *>(p.mask + off + c0);
@@ -2050,7 +2075,7 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
 }
 
 template <int CI, int CO>
-static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) {
+static cudaError_t launch_wide(ConvParams p, long long ws_elems, cudaStream_t s, bool &done) {
   done = false;
   if (!p.wp) return cudaSuccess;
   static int sms = 0;
@@ -2060,11 +2085,13 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     sms = n > 0 ? n : 1;
   }
-  // item shape: forced (modes 2..5), else the one with the least estimated time:
-  // waves of items x (the slower of the item's MMAs and its weight stream, plus a
-  // fixed cost), in cycles: an M 128 x N CO x K 16 MMA ~48 (N 64) or ~64 (N 128)
-  // cycles; each of the item's 27 CI/KC taps of weight blocks a ~2000-cycle round
-  // trip, sb of them in flight
+  const long long Mv = (long long)p.B * p.Z * p.Y * p.X;
+  const bool can_split = p.ws && ws_elems >= 3 * Mv * CO;
+  // work-unit shape: M tiles per item forced (modes 2..5) or chosen, and whether each item
+  // splits over its three input planes (FP32 partials in ws, summed by k_conv3d_finish): the
+  // least estimated time.  Measured: a unit's time follows its weight blocks (~320 cycles each,
+  // whatever the number of M tiles they feed), plus a fixed cost per unit; the finish kernel
+  // costs ~8000 cycles.
   WideGrid g{};
   size_t smem = 0;
   bool found = false;
@@ -2074,16 +2101,18 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     WideGrid c{};
     size_t sm = 0;
     if (!wide_shape(CI, CO, p.Y, p.X, nM, c, sm)) continue;
-    c.items = (long long)p.B * p.Z * c.nyb;
-    const double waves = (double)((c.items + sms - 1) / sms);
-    const double t_mma = 27.0 * (CI / 16) * c.nM * (CO <= 64 ? 48.0 : 64.0);
-    const double t_b = 27.0 * (CI < 64 ? 1 : CI / 64) * 2000.0 / c.sb;
-    const double cost = waves * ((t_mma > t_b ? t_mma : t_b) + 3000.0);
-    if (!found || cost < best) {
-      found = true;
-      best = cost;
-      g = c;
-      smem = sm;
+    for (int sp = 1; sp <= (can_split ? 3 : 1); sp += 2) {
+      c.splits = sp;
+      c.items = (long long)p.B * p.Z * c.nyb * sp;
+      const double waves = (double)((c.items + sms - 1) / sms);
+      const double blocks = 27.0 * (CI / 16) / sp;
+      const double cost = waves * (blocks * 320.0 + 3000.0) + (sp > 1 ? 8000.0 : 0.0);
+      if (!found || cost < best) {
+        found = true;
+        best = cost;
+        g = c;
+        smem = sm;
+      }
     }
   }
   if (!found) return cudaSuccess;   // the mma.sync kernel takes this shape
@@ -2113,13 +2142,15 @@ static cudaError_t launch_wide(const ConvParams &p, cudaStream_t s, bool &done) 
     attr = 227 * 1024;
   }
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
+  p.splits = g.splits;
   FLF_NET_LAUNCH(k_conv3d_wide<CI, CO><<<grid, 256, sm_launch, s>>>(map, p, p.wp, g));
+  if (g.splits > 1) FLF_NET_LAUNCH(k_conv3d_finish<<<grid_for(Mv * CO / 8, 256), 256, 0, s>>>(p, Mv));
   return cudaGetLastError();
 }
 
-static cudaError_t launch_wide_tc(const ConvParams &p, cudaStream_t s, bool &done) {
+static cudaError_t launch_wide_tc(const ConvParams &p, long long ws_elems, cudaStream_t s, bool &done) {
   done = false;
-#define FLF_WD(a, b) if (p.Ci == a && p.Co == b) return launch_wide<a, b>(p, s, done);
+#define FLF_WD(a, b) if (p.Ci == a && p.Co == b) return launch_wide<a, b>(p, ws_elems, s, done);
   FLF_WD(32, 64) FLF_WD(64, 32) FLF_WD(64, 64) FLF_WD(64, 128) FLF_WD(128, 64) FLF_WD(128, 128)
   FLF_WD(32, 128) FLF_WD(128, 32)
 #undef FLF_WD
@@ -2155,7 +2186,7 @@ cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s) {
     return g_conv16_tc == 2 ? launch_tma16<32, 32, 1, 5, false, true>(p, HeadOut{}, s) : launch_tiled<32, 32>(p, s);
   if (p.wp && g_conv_wide_tc) {
     bool done = false;
-    const cudaError_t e = launch_wide_tc(p, s, done);
+    const cudaError_t e = launch_wide_tc(p, ws_elems, s, done);
     if (done) return e;
   }
   const int BN = p.Co >= 64 ? 64 : p.Co;

@@ -113,7 +113,7 @@ class UNet3D:
         if relu is None:
             relu = q["relu"] and not flip       # a data gradient is linear
         # split-K layers (few output tiles: the coarse levels) write one slice per split
-        need = y.numel() * (4 if y.numel() < (1 << 22) else 1)
+        need = y.numel() * (4 if y.numel() < (1 << 23) else 1)
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.float32, device=self.dev)
         _flf.conv3d(x, q["wf"] if flip else q["wb"], None if flip else q["b"], y, relu=relu, mask=mask,

@@ -17,7 +17,9 @@ load does not write hold stale data (NaN here); only dropped positions read
 them.  (On the device a 64-channel chunk is one TMA load of 128-byte rows with
 the 128-byte swizzle, which the operand descriptors undo; the logical rows, and
 so this model, are the same.)  The item shapes follow the launcher (rows per item balanced over the y
-blocks, nM = ceil(R*Xp / 128)), and the weights the packing kernel's layout.
+blocks, nM = ceil(R*Xp / 128)), and the weights the packing kernel's layout.  With
+splits, each input plane z+dz of an item is its own work unit writing an FP32
+partial sum, and the three partials are added afterwards.
 """
 
 import numpy as np
@@ -63,7 +65,7 @@ def item_shape(Y, X, CO, nM):
     return Xp, R, nM, nyb, slab_rows
 
 
-def wide_conv(x, w, nM_req):
+def wide_conv(x, w, nM_req, splits=1):
     B, Z, Y, X, CI = x.shape
     CO = w.shape[2]
     shp = item_shape(Y, X, CO, nM_req)
@@ -77,8 +79,10 @@ def wide_conv(x, w, nM_req):
         yb, q = it % nyb, it // nyb
         z, b = q % Z, q // Z
         y0 = yb * R
-        D = np.zeros((nM * 128, CO))
+        # with splits each input plane's partial is its own unit's output, summed afterwards
+        parts = {}
         for dz in (-1, 0, 1):
+            D = parts.setdefault(dz if splits > 1 else 0, np.zeros((nM * 128, CO)))
             if not 0 <= z + dz < Z:
                 continue
             for cg in range(NCG):
@@ -102,6 +106,7 @@ def wide_conv(x, w, nM_req):
                             rows = m * 128 + np.arange(128) + dy * Xp + dx
                             A = np.concatenate([slab[2 * ks, rows], slab[2 * ks + 1, rows]], axis=1)
                             D[m * 128:(m + 1) * 128] += A @ Bm
+        D = sum(parts[k] for k in sorted(parts))
         for qq in range(nM * 128):
             yl, xx = qq // Xp, qq % Xp
             y = y0 + yl
@@ -114,11 +119,12 @@ def wide_conv(x, w, nM_req):
     ((1, 3, 7, 9), 32, 64, 1), ((1, 3, 7, 9), 32, 64, 3), ((2, 2, 5, 13), 64, 32, 1),
     ((1, 3, 11, 30), 128, 64, 2), ((1, 2, 4, 70), 64, 128, 2), ((1, 2, 3, 126), 64, 64, 1),
 ])
-def test_wide_decomposition_matches_direct_conv(shape, CI, CO, nM):
+@pytest.mark.parametrize("splits", [1, 3])
+def test_wide_decomposition_matches_direct_conv(shape, CI, CO, nM, splits):
     rng = np.random.default_rng(CI + CO + nM)
     x = rng.standard_normal(shape + (CI,))
     w = rng.standard_normal((27, CI, CO))
-    got = wide_conv(x, w, nM)
+    got = wide_conv(x, w, nM, splits)
     ref = direct_conv(x, w)
     assert np.isfinite(got).all()
     assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
