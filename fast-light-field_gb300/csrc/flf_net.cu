@@ -1710,7 +1710,8 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
 struct WideGrid {
   int Xp, R, nM, nyb;   // padded row, rows per item, M tiles per item, y blocks
   int slab_rows;        // rows of one 8-channel group of a slab slot (LBO / 16)
-  int sb;               // taps of B blocks in the ring (the shared memory the slabs leave)
+  int sb;               // B ring slots (the shared memory the slabs leave)
+  int tps;              // taps per B ring slot (3: a row of dx taps, one wait and one commit)
   int splits;           // 1, or 3: work unit = (item, input plane z-1+s) writing FP32 partials to ws[s]
   long long items;      // B * Z * nyb * splits (work units)
 };
@@ -1738,9 +1739,11 @@ __global__ void __launch_bounds__(256, 1)
   // layout: [2 slab slots][B ring][mbarriers][tmem address][abort flag]
   const uint32_t smem_s = su32(smem);
   const uint32_t slab_s = smem_s, bring_s = smem_s + 2 * SLOT;
-  const uint32_t SB = (uint32_t)g.sb;          // taps in the B ring
+  const uint32_t SB = (uint32_t)g.sb;          // B ring slots
   constexpr uint32_t TB = KS * BBLK;            // one tap's B blocks (KC input channels)
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + SB * TB);
+  const int TPS = g.tps;                        // taps per slot
+  const uint32_t SLOTB = (uint32_t)TPS * TB;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * SLOT + SB * SLOTB);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4 + 2 * WIDE_SB_MAX + 4 + 1);
   volatile int *abort_s = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const uint32_t bar_s = su32(bars);
@@ -1835,20 +1838,24 @@ __global__ void __launch_bounds__(256, 1)
         for (int dz = -1; dz <= 1 && ok; dz++) {
           if (!plane_used(z, dz, dz1)) continue;
           for (int cg = 0; cg < NCG && ok; cg++)
-            for (int t9 = 0; t9 < 9; t9++) {
+            for (int t9 = 0; t9 < 9; t9 += TPS) {
               const uint32_t sl = nbb % SB;
               if (nbb >= SB && !role_wait(bempty(sl), ((nbb / SB) - 1) & 1, abort_s, 22)) {
                 ok = false;
                 break;
               }
-              const int tap = (dz + 1) * 9 + t9;
-              const bf16 *src = wp + ((long long)tap * (CI / 16) + cg * KS) * (BBLK / 2);
-              net_expect_tx(bfull(sl), TB);
-              asm volatile(
-                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                      bring_s + sl * TB),
-                  "l"(src), "r"(TB), "r"(bfull(sl))
-                  : "memory");
+              net_expect_tx(bfull(sl), SLOTB);
+              // taps t9 .. t9+TPS-1 (contiguous in the packed weights when one chunk covers CI)
+              for (int u = 0; u < TPS; u += (NCG == 1 ? TPS : 1)) {
+                const int tap = (dz + 1) * 9 + t9 + u;
+                const bf16 *src = wp + ((long long)tap * (CI / 16) + cg * KS) * (BBLK / 2);
+                const uint32_t bytes = NCG == 1 ? SLOTB : TB;
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                        bring_s + sl * SLOTB + u * TB),
+                    "l"(src), "r"(bytes), "r"(bfull(sl))
+                    : "memory");
+              }
               nbb++;
             }
         }
@@ -1869,7 +1876,7 @@ __global__ void __launch_bounds__(256, 1)
       const uint32_t a_lo0 = (uint32_t)a0d, a_hi = (uint32_t)(a0d >> 32);
       const uint32_t b_lo0 = (uint32_t)b0d, b_hi = (uint32_t)(b0d >> 32);
       const uint32_t a_row = SW ? 8u : 1u, a_ks = SW ? 2u : 2u * (LBO >> 4), a_slot = SLOT >> 4;
-      const uint32_t a_m = 128u * a_row, b_ks = (2u * CO * 16u) >> 4, b_slot = TB >> 4;
+      const uint32_t a_m = 128u * a_row, b_ks = (2u * CO * 16u) >> 4, b_slot = SLOTB >> 4, b_tap = TB >> 4;
       const int nM = g.nM;
       uint32_t ns = 0, nb = 0, li = 0;
       bool ok = true;
@@ -1893,25 +1900,28 @@ __global__ void __launch_bounds__(256, 1)
               break;
             }
             const uint32_t a_c = a_lo0 + sl * a_slot;
-            for (int t9 = 0; t9 < 9; t9++) {
+            for (int t9 = 0; t9 < 9; t9 += TPS) {
               const uint32_t bs = nb % SB;
               if (!role_wait(bfull(bs), (nb / SB) & 1, abort_s, 25)) {
                 ok = false;
                 break;
               }
               tc_fence_after();
-              const uint32_t a_t = a_c + (uint32_t)((t9 / 3) * g.Xp + (t9 % 3)) * a_row;
-              const uint32_t b_t = b_lo0 + bs * b_slot;
+              for (int u = 0; u < TPS; u++) {
+                const int t = t9 + u;
+                const uint32_t a_t = a_c + (uint32_t)((t / 3) * g.Xp + (t % 3)) * a_row;
+                const uint32_t b_t = b_lo0 + bs * b_slot + u * b_tap;
 #pragma unroll
-              for (int ks = 0; ks < KS; ks++) {
-                const uint64_t bd = ((uint64_t)b_hi << 32) | (b_t + ks * b_ks);
+                for (int ks = 0; ks < KS; ks++) {
+                  const uint64_t bd = ((uint64_t)b_hi << 32) | (b_t + ks * b_ks);
 #pragma unroll
-                for (int m = 0; m < 4; m++)
-                  if (m < nM)
-                    umma_f16(dcol + m * CO, ((uint64_t)a_hi << 32) | (a_t + ks * a_ks + m * a_m), bd, idesc, acc);
-                acc = 1;
+                  for (int m = 0; m < 4; m++)
+                    if (m < nM)
+                      umma_f16(dcol + m * CO, ((uint64_t)a_hi << 32) | (a_t + ks * a_ks + m * a_m), bd, idesc, acc);
+                  acc = 1;
+                }
               }
-              umma_commit(bempty(bs));   // the tap's B blocks are free once these MMAs complete
+              umma_commit(bempty(bs));   // the slot's B blocks are free once these MMAs complete
               nb++;
             }
             if (!ok) break;
@@ -2047,9 +2057,10 @@ int net_set_conv_wide_tcgen05(int mode) {
 
 // Shared memory of k_conv3d_wide: the two slab slots of slab_rows rows of KC
 // channels, sb B blocks, the mbarriers, the TMEM address and abort flag.
-static size_t wide_smem(int CI, int CO, int slab_rows, int sb) {
+static size_t wide_smem(int CI, int CO, int slab_rows, int sb, int tps) {
   const int KC = CI < 64 ? CI : 64;
-  return (size_t)2 * KC * 2 * slab_rows + (size_t)sb * (KC / 16) * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) + 16;
+  return (size_t)2 * KC * 2 * slab_rows + (size_t)sb * tps * (KC / 16) * 32 * CO + 8 * (8 + 2 * WIDE_SB_MAX + 1) +
+         16;
 }
 
 // The item shape for nM M tiles: rows per item R (balanced over the y blocks),
@@ -2065,12 +2076,15 @@ static bool wide_shape(int CI, int CO, int Y, int X, int nM, WideGrid &g, size_t
   if (g.R + 2 > 256) return false;
   g.nM = (g.R * g.Xp + 127) / 128;
   g.slab_rows = (g.nM * 128 + 2 * g.Xp + 2 + 7) / 8 * 8;
-  const size_t fixed = wide_smem(CI, CO, g.slab_rows, 0);
+  const size_t fixed = wide_smem(CI, CO, g.slab_rows, 0, 1);
   const size_t tb = (size_t)((CI < 64 ? CI : 64) / 16) * 32 * CO;   // one tap's B blocks
+  // a row of 3 taps per ring slot where 2 such slots fit, else one tap per slot (3 slots at least)
+  g.tps = fixed + 2 * 3 * tb <= 227 * 1024 ? 3 : 1;
   if (fixed + 3 * tb > 227 * 1024) return false;
-  g.sb = (int)((227 * 1024 - fixed) / tb);
-  if (g.sb > WIDE_SB) g.sb = WIDE_SB;
-  smem = wide_smem(CI, CO, g.slab_rows, g.sb);
+  g.sb = (int)((227 * 1024 - fixed) / (g.tps * tb));
+  const int cap = g.tps == 3 ? WIDE_SB / 3 : WIDE_SB;
+  if (g.sb > cap) g.sb = cap;
+  smem = wide_smem(CI, CO, g.slab_rows, g.sb, g.tps);
   return true;
 }
 
