@@ -2104,9 +2104,9 @@ static cudaError_t launch_wide(ConvParams p, long long ws_elems, cudaStream_t s,
   // work-unit shape: M tiles per item forced (modes 2..5) or chosen, and whether each item
   // splits over its three input planes (FP32 partials in ws, summed by k_conv3d_finish): the
   // least estimated time, ties to more M tiles.  Measured: a unit's time follows its weight
-  // blocks (~320 cycles each, whatever the number of M tiles they feed), plus a fixed cost per
-  // unit; a split also writes and reads three FP32 partial sets (~3000 bytes per cycle) and
-  // launches the finish kernel.
+  // blocks (~320 cycles each, whatever the number of M tiles they feed; ~15 % less with three
+  // taps per ring slot), plus a fixed cost per unit; a split also writes and reads three FP32
+  // partial sets (~3000 bytes per cycle) and launches the finish kernel.
   WideGrid g{};
   size_t smem = 0;
   bool found = false;
@@ -2122,7 +2122,7 @@ static cudaError_t launch_wide(ConvParams p, long long ws_elems, cudaStream_t s,
       const double waves = (double)((c.items + sms - 1) / sms);
       const double blocks = 27.0 * (CI / 16) / sp;
       const double partials = sp > 1 ? 4000.0 + 2.0 * 3.0 * (double)Mv * CO * 4.0 / 3000.0 : 0.0;
-      const double cost = waves * (blocks * 320.0 + 3000.0) + partials;
+      const double cost = waves * (blocks * (c.tps == 3 ? 272.0 : 320.0) + 3000.0) + partials;
       if (!found || cost <= best) {
         found = true;
         best = cost;
