@@ -1959,6 +1959,8 @@ int flf_pool2_bwd(const void *gpool, const void *gskip, const void *act, void *g
 int flf_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C, void *stream) {
   if (!low || !out) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
   if (int rc = even_shape(B, Z, Y, X, C)) return rc;
+  if (C % 8 || ((C / 8) & (C / 8 - 1)))
+    return fail(nullptr, FLF_E_ARG, "upsampling needs C / 8 a power of two (got C = %d)", C);
   NET_CHECK(launch_up2_add(low, skip, out, B, Z, Y, X, C, (cudaStream_t)stream));
   return FLF_OK;
 }

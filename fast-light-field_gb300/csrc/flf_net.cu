@@ -1396,21 +1396,27 @@ __global__ void k_pool2_bwd(const bf16 *gpool, const bf16 *gskip, const bf16 *ac
 }
 
 // out[v] = low[v/2] + skip[v]  (nearest 2x2x2 upsampling; low has C channels)
+// One CTA per output row (b, z, y): the row's coordinates are decoded once and
+// the threads walk its X * C / 8 vectors of 8 channels (C / 8 a power of two),
+// so the per-vector index work is a shift and a mask.
 __global__ void k_up2_add(const bf16 *low, const bf16 *skip, bf16 *out, int B, int Z, int Y, int X, int C) {
-  const int G = C / 8;
-  const long long n = (long long)B * Z * Y * X * G;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(i % G);
-    const long long vox = i / G;
-    const Vox v = decode(vox, Z, Y, X);
+  const int G = C / 8, gsh = __ffs(G) - 1;
+  const long long row = blockIdx.x;                    // (b * Z + z) * Y + y
+  const int y = (int)(row % Y);
+  const long long bz = row / Y;
+  const int z = (int)(bz % Z), b = (int)(bz / Z);
+  const bf16 *lrow = low + ((((long long)b * (Z / 2) + z / 2) * (Y / 2) + y / 2) * (long long)(X / 2)) * C;
+  const long long o = row * X * C;
+  for (int i = threadIdx.x; i < X * G; i += blockDim.x) {
+    const int x = i >> gsh, g = i & (G - 1);
     V8 r, q;
-    r.load(low + half_index(v, Z, Y, X, C) + g * 8);
+    r.load(lrow + (long long)(x >> 1) * C + g * 8);
     if (skip) {
-      q.load(skip + vox * C + g * 8);
+      q.load(skip + o + (long long)i * 8);
 #pragma unroll
       for (int k = 0; k < 8; k++) r.v[k] += q.v[k];
     }
-    r.store(out + vox * C + g * 8);
+    r.store(out + o + (long long)i * 8);
   }
 }
 
@@ -2343,8 +2349,12 @@ cudaError_t launch_pool2_bwd(const void *gpool, const void *gskip, const void *a
 
 cudaError_t launch_up2_add(const void *low, const void *skip, void *out, int B, int Z, int Y, int X, int C,
                            cudaStream_t s) {
-  FLF_NET_LAUNCH(k_up2_add<<<grid_for((long long)B * Z * Y * X * C / 8, 256), 256, 0, s>>>((const bf16 *)low, (const bf16 *)skip,
-                                                                          (bf16 *)out, B, Z, Y, X, C));
+  if ((C / 8) & (C / 8 - 1)) return cudaErrorInvalidValue;   // C / 8 a power of two
+  const long long rows = (long long)B * Z * Y;
+  if (rows == 0 || X == 0) return cudaSuccess;
+  const int threads = X * (C / 8) >= 256 ? 256 : 128;
+  FLF_NET_LAUNCH(k_up2_add<<<(unsigned)rows, threads, 0, s>>>((const bf16 *)low, (const bf16 *)skip, (bf16 *)out, B, Z,
+                                                            Y, X, C));
   return cudaGetLastError();
 }
 

@@ -278,7 +278,7 @@ int flf_psf_ht(float *Ht_dev, const float *H_dev, int Z, int nh, int S, int N, v
  *   adjoint plus an optional second gradient gskip, times (act > 0) if act.
  * flf_up2_add / flf_up2_bwd: out = nearest 2x upsampling of low (+ skip);
  *   adjoint: 2x2x2 block sums times (act > 0) if act.  Shapes are those of
- *   the full-resolution tensor.
+ *   the full-resolution tensor; flf_up2_add takes C / 8 a power of two.
  * flf_mse_grad: loss += mean((y[:, 0] - target)^2), g = its gradient in
  *   channel 0 (other channels 0); M voxels, y / g [M][C] bf16.
  * flf_adam: Adam step on FP32 weights w with gradient g and moments m, v

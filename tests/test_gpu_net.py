@@ -186,10 +186,10 @@ def test_conv3d_weight_and_bias_gradient(env, shape, Ci, Co):
     assert torch.equal(runs[1][0], runs[2][0]) and torch.equal(runs[1][1], runs[2][1])
 
 
-def test_pool_upsample_and_their_adjoints(env):
+@pytest.mark.parametrize("B,Z,Y,X,C", [(2, 4, 6, 8, 16), (1, 2, 4, 130, 64), (1, 2, 2, 6, 128), (3, 2, 4, 2, 32)])
+def test_pool_upsample_and_their_adjoints(env, B, Z, Y, X, C):
     torch, _flf = env
-    g = torch.Generator().manual_seed(5)
-    B, Z, Y, X, C = 2, 4, 6, 8, 16
+    g = torch.Generator().manual_seed(5 + C)
     x = torch.randn((B, Z, Y, X, C), generator=g).bfloat16()
     p = torch.empty((B, Z // 2, Y // 2, X // 2, C), dtype=torch.bfloat16, device="cuda")
     _flf.pool2(x.cuda(), p)
@@ -201,6 +201,8 @@ def test_pool_upsample_and_their_adjoints(env):
     _flf.up2_add(low.cuda(), skip.cuda(), up)
     upr = low.double().repeat_interleave(2, 1).repeat_interleave(2, 2).repeat_interleave(2, 3) + skip.double()
     _close(torch, up, upr)
+    _flf.up2_add(low.cuda(), None, up)   # without the skip term
+    _close(torch, up, upr - skip.double())
     # adjoints: <pool(x), q> = <x, pool^T(q)>, <up(l), u> = <l, up^T(u)>, with masks
     gp = torch.empty((B, Z, Y, X, C), dtype=torch.bfloat16, device="cuda")
     act = torch.randn((B, Z, Y, X, C), generator=g).bfloat16()
