@@ -1512,11 +1512,11 @@ __global__ void __launch_bounds__(256) k_ws_sum(const float *htf, const float *h
                                                 long long V, long long YX) {
   __shared__ float red[8];
   const int t = blockIdx.y;
+  const int Z = (int)(V / YX);
   float part = 0.f;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const long long z = v / YX, yx = v - z * YX;
-    part += htf[(z * T + t) * YX + yx] / hth1[v];
-  }
+  // a thread owns pixels yx (strided over the grid) of every plane: no division per element
+  for (long long yx = (long long)blockIdx.x * blockDim.x + threadIdx.x; yx < YX; yx += (long long)gridDim.x * blockDim.x)
+    for (int z = 0; z < Z; z++) part += htf[((long long)z * T + t) * YX + yx] / hth1[(long long)z * YX + yx];
   for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
   __syncthreads();
@@ -1538,15 +1538,15 @@ __global__ void k_ws_sum_final(const float *part, float *sum, int T, int blocks)
 // Network input, channels-last [T][Zp][Yp][Xp][16] from Htf [Z][T][Y][X]:
 // channel 0 = Htf / HtH1 / m[t] (the first RL iterate over its frame mean m),
 // 1 = Htf / Ht1 / m[t], 2 = HtH1 * c2, 3 = Ht1 * c3, 4..15 = 0; zero in the padding.
+// One CTA per padded output row (t, z, y), its coordinates decoded once; the
+// threads walk x.
 __global__ void __launch_bounds__(256) k_ws_input(WsInputParams p) {
-  const long long n = (long long)p.T * p.Zp * p.Yp * p.Xp;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % p.Xp);
-    long long r = i / p.Xp;
-    const int y = (int)(r % p.Yp);
-    r /= p.Yp;
-    const int z = (int)(r % p.Zp);
-    const int t = (int)(r / p.Zp);
+  const long long row = blockIdx.x;                    // ((t * Zp) + z) * Yp + y
+  const int y = (int)(row % p.Yp);
+  const long long tz = row / p.Yp;
+  const int z = (int)(tz % p.Zp), t = (int)(tz / p.Zp);
+  for (int x = threadIdx.x; x < p.Xp; x += blockDim.x) {
+    const long long i = row * p.Xp + x;
     __nv_bfloat162 c[8];
     for (int k = 0; k < 8; k++) c[k] = __floats2bfloat162_rn(0.f, 0.f);
     if (z < p.Z && y < p.Y && x < p.X) {
@@ -2381,14 +2381,15 @@ cudaError_t launch_ws_input(const WsInputParams &p, cudaStream_t s) {
   const long long n = (long long)p.T * p.Zp * p.Yp * p.Xp;
   if (n == 0) return cudaSuccess;
   const long long V = (long long)p.Z * p.Y * p.X;
-  long long blocks = (V + 2047) / 2048;
+  const long long YX = (long long)p.Y * p.X;
+  long long blocks = (YX + 255) / 256;   // a thread per pixel of a plane, all planes in its loop
   if (blocks > 1024) blocks = 1024;
   // the per-block partial sums go to the start of `out` (T * blocks floats fit:
   // out holds 32 bytes per padded voxel), which k_ws_input overwrites afterwards
   float *part = reinterpret_cast<float *>(p.out);
   FLF_NET_LAUNCH(k_ws_sum<<<dim3((unsigned)blocks, (unsigned)p.T), 256, 0, s>>>(p.htf, p.hth1, part, p.T, V, (long long)p.Y * p.X));
   FLF_NET_LAUNCH(k_ws_sum_final<<<(p.T + 127) / 128, 128, 0, s>>>(part, p.sum_x1, p.T, (int)blocks));
-  FLF_NET_LAUNCH(k_ws_input<<<grid_for(n, 256), 256, 0, s>>>(p));
+  FLF_NET_LAUNCH(k_ws_input<<<(unsigned)((long long)p.T * p.Zp * p.Yp), p.Xp >= 256 ? 256 : 128, 0, s>>>(p));
   return cudaGetLastError();
 }
 
