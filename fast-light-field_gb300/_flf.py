@@ -63,6 +63,7 @@ _SIGS = {
     "flf_net_conv_wide_tcgen05": (_I, [_I]),
     "flf_conv3d_wgrad": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, ctypes.c_longlong, _P]),
     "flf_conv3d_tc": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "flf_conv3d_x1": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
     "flf_net_conv16_tcgen05": (_I, [_I]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
@@ -195,6 +196,15 @@ def conv3d(x, w, bias, y, relu=False, mask=None, stream=None, ws=None, wp=None):
     _check_global(lib.flf_conv3d(_ptr(x), _ptr(w), _ptr(bias), _ptr(mask), _ptr(y), B, Z, Y, X, Ci, Co,
                                  int(bool(relu)), _ptr(ws), int(ws.numel()) if ws is not None else 0, _ptr(wp),
                                  _ptr(stream)))
+
+
+def conv3d_x1(x, w, bias, y, relu=False, stream=None):
+    """y = [relu](3x3x1 convolution over (dz, dy) with the taps dx = 1 of w [27, 16, 16] + bias);
+    x, y [B, Z, Y, X, 16] bf16 (the first layer of the warm-start network, whose input
+    carries the x neighbours as channels)."""
+    lib = load_library()
+    B, Z, Y, X, _ = _vshape(x)
+    _check_global(lib.flf_conv3d_x1(_ptr(x), _ptr(w), _ptr(bias), _ptr(y), B, Z, Y, X, int(bool(relu)), _ptr(stream)))
 
 
 def conv_wide_tcgen05(mode):

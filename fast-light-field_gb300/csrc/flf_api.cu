@@ -1872,6 +1872,17 @@ int flf_conv3d(const void *x, const void *w, const float *bias, const void *mask
   return FLF_OK;
 }
 
+int flf_conv3d_x1(const void *x, const void *w, const float *bias, void *y, int B, int Z, int Y, int X, int relu,
+                  void *stream) {
+  if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = net_shape(B, Z, Y, X, 16)) return rc;
+  if (!aligned16(x) || !aligned16(y)) return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
+  ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, nullptr, (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16,
+               relu ? 1 : 0, nullptr, 1};
+  NET_CHECK(launch_conv3d_x1(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");

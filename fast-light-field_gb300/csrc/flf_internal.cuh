@@ -303,6 +303,7 @@ struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co
   float *part;               // [chunks][27][Ci][Co] partial gradients, reduced in chunk order (or null)
 };
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
+cudaError_t launch_conv3d_x1(const ConvParams &p, cudaStream_t s);
 long long net_launches();
 int net_set_conv_wide_tcgen05(int mode);
 cudaError_t launch_conv3d_pack(const void *w, void *wp, int Ci, int Co, cudaStream_t s);

@@ -807,7 +807,7 @@ __device__ __forceinline__ void head_rows(float (&o)[RH], const float (&v)[RH + 
     for (int dy = 0; dy < 3; dy++) o[r] += in ? v[r + dy][DZ * 3 + dy] : 0.f;
 }
 
-template <int CI, int CO, int R, int S, bool HEAD, bool SW32>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false>
 __global__ void __launch_bounds__(352, 1)
     k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -816,7 +816,10 @@ __global__ void __launch_bounds__(352, 1)
   // N of one MMA: (dz, co); the head, whose only output channel is 0, folds (dz, dy) into N
   // instead (9 of 16 columns) and issues one MMA per input row and dx
   constexpr int NN = HEAD ? 16 : 3 * CO;
-  constexpr int NBLK = HEAD ? 3 : 9;          // B blocks per K step: (dy, dx), or dx for the head
+  // B blocks per K step: (dy, dx); dx for the head; dy for X1, a 3x3x1 convolution (the taps
+  // dx != 1 of w are ignored: the first layer, whose input carries the x neighbours as channels)
+  constexpr int NBLK = (HEAD || X1) ? 3 : 9;
+  static_assert(!(HEAD && X1), "the head is a full 3x3x3 convolution");
   constexpr int NISS = (HEAD ? PYH : R) % 2 == 0 ? 2 : 1;   // MMA-issuing threads (warps 1 .. NISS)
   constexpr int CH = CO / 2;                  // output channels per epilogue warp
   static_assert((CI == 16 || CI == 32) && (CO == 16 || CO == 32), "16 or 32 channels in and out");
@@ -856,7 +859,8 @@ __global__ void __launch_bounds__(352, 1)
     const int bk = i / NN, n = i % NN;
     const int blk = bk / KS, kh = bk % KS;
     const bool used = !HEAD || n < 9;
-    const int tap = HEAD ? (n / 3) * 9 + (n % 3) * 3 + blk : (n / CO) * 9 + blk, co = HEAD ? 0 : n % CO;
+    const int tap = HEAD ? (n / 3) * 9 + (n % 3) * 3 + blk : (n / CO) * 9 + (X1 ? blk * 3 + 1 : blk);
+    const int co = HEAD ? 0 : n % CO;
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
@@ -959,8 +963,9 @@ __global__ void __launch_bounds__(352, 1)
             const uint32_t dcol = tmem + acc * ACOLS;
 #pragma unroll
             for (int blk = 0; blk < NBLK; blk++) {
-              // head: block dx, slab row = the input row; otherwise block (dy, dx), slab row r + dy
-              const int dy = HEAD ? 0 : blk / 3, dx = HEAD ? blk : blk % 3;
+              // head: block dx, slab row = the input row; X1: block dy, dx = 1; otherwise block
+              // (dy, dx), slab row r + dy
+              const int dy = HEAD ? 0 : (X1 ? blk : blk / 3), dx = HEAD ? blk : (X1 ? 1 : blk % 3);
 #pragma unroll
               for (int kh = 0; kh < KS; kh++) {
                 const uint64_t bd = ((uint64_t)b_hi << 32) | (uint64_t)(b_lo + (blk * KS + kh) * (BBLK >> 4));
@@ -1535,9 +1540,11 @@ __global__ void k_ws_sum_final(const float *part, float *sum, int T, int blocks)
   sum[t] = s;
 }
 
-// Network input, channels-last [T][Zp][Yp][Xp][16] from Htf [Z][T][Y][X]:
-// channel 0 = Htf / HtH1 / m[t] (the first RL iterate over its frame mean m),
-// 1 = Htf / Ht1 / m[t], 2 = HtH1 * c2, 3 = Ht1 * c3, 4..15 = 0; zero in the padding.
+// Network input, channels-last [T][Zp][Yp][Xp][16] from Htf [Z][T][Y][X]: with
+// the features f0 = Htf / HtH1 / m[t] (the first RL iterate over its frame
+// mean m), f1 = Htf / Ht1 / m[t], f2 = HtH1 * c2, f3 = Ht1 * c3, channel 4k + j
+// (k = 0..2) holds f_j at x + k - 1, so that the first layer's x taps are
+// channels and it runs as a 3x3x1 convolution; 12..15 = 0; zero in the padding.
 // One CTA per padded output row (t, z, y), its coordinates decoded once; the
 // threads walk x.
 __global__ void __launch_bounds__(256) k_ws_input(WsInputParams p) {
@@ -1549,13 +1556,18 @@ __global__ void __launch_bounds__(256) k_ws_input(WsInputParams p) {
     const long long i = row * p.Xp + x;
     __nv_bfloat162 c[8];
     for (int k = 0; k < 8; k++) c[k] = __floats2bfloat162_rn(0.f, 0.f);
-    if (z < p.Z && y < p.Y && x < p.X) {
-      const long long v = ((long long)z * p.Y + y) * p.X + x;
-      const float h = p.htf[(((long long)z * p.T + t) * p.Y + y) * p.X + x];
-      const float a = p.hth1[v], b = p.ht1[v];
+    if (z < p.Z && y < p.Y) {
       const float inv = p.count / fmaxf(p.sum_x1[t], 1e-30f);
-      c[0] = __floats2bfloat162_rn(h / a * inv, h / b * inv);
-      c[1] = __floats2bfloat162_rn(a * p.c2, b * p.c3);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int xs = x + k - 1;
+        if (xs < 0 || xs >= p.X) continue;
+        const long long v = ((long long)z * p.Y + y) * p.X + xs;
+        const float h = p.htf[(((long long)z * p.T + t) * p.Y + y) * p.X + xs];
+        const float a = p.hth1[v], b = p.ht1[v];
+        c[2 * k] = __floats2bfloat162_rn(h / a * inv, h / b * inv);
+        c[2 * k + 1] = __floats2bfloat162_rn(a * p.c2, b * p.c3);
+      }
     }
     uint4 *dst = reinterpret_cast<uint4 *>(p.out + i * 16);
     dst[0] = *reinterpret_cast<uint4 *>(&c[0]);
@@ -1625,7 +1637,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-template <int CI, int CO, int R, int S, bool HEAD, bool SW32>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false>
 static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
   constexpr int KS = CI / 16;
   constexpr size_t SLOT = SW32 ? KS * (((R + 2) * 136 * 32 + 1023) / 1024 * 1024)
@@ -1635,7 +1647,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
   static int sms = 0;
   if (!sms) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32>,
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, n = 0;
@@ -1679,7 +1691,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   g.zchunks = (p.Z + g.zc - 1) / g.zc;
   g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
-  FLF_NET_LAUNCH(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32><<<grid, 352, SMEM, s>>>(map, p, h, g));
+  FLF_NET_LAUNCH(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1><<<grid, 352, SMEM, s>>>(map, p, h, g));
   return cudaGetLastError();
 }
 
@@ -2187,6 +2199,13 @@ int net_set_conv16_tcgen05(int mode) {
   const int old = g_conv16_tc;
   g_conv16_tc = mode < 0 ? 0 : (mode > 2 ? 2 : mode);
   return old;
+}
+
+// 3x3x1 convolution (16 -> 16 channels; the taps dx != 1 of w ignored) on the
+// tcgen05 kernel, or the 3x3x3 mma.sync kernel (those taps must then be zero)
+cudaError_t launch_conv3d_x1(const ConvParams &p, cudaStream_t s) {
+  if (p.Ci != 16 || p.Co != 16) return cudaErrorInvalidValue;
+  return g_conv16_tc ? launch_tma16<16, 16, 2, 8, false, true, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
 }
 
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32) {

@@ -10,7 +10,9 @@ torch provides the tensors only.
 
 Architecture (channels-last [B][Z][Y][X][C], 3x3x3 convolutions, ReLU):
 four levels of 16-32-64-128 channels with two convolutions each on the way
-down (2x2x2 average pooling between levels), and on the way up a
+down (2x2x2 average pooling between levels; the input carries each voxel's x
+neighbours as channels, so the first convolution's x taps are channels and it
+runs as a 3x3x1 convolution), and on the way up a
 convolution that halves the channels at the coarse level, nearest 2x
 upsampling plus the encoder feature of that level (additive skip), and one
 convolution; a 16-channel head whose channel 0 is the prediction.  Volumes
@@ -52,6 +54,14 @@ LAYERS = [("e0a", CIN, 16, True), ("e0b", 16, 16, True), ("e1a", 16, 32, True), 
           ("u0", 32, 16, True), ("d0", 16, 16, True), ("head", 16, 16, False)]
 
 
+# The first layer is a 3x3x1 convolution (flf_conv3d_x1): the network input holds
+# the four features of x - 1, x and x + 1 as channels 0..11, so the layer's x taps
+# are channels and only the taps with dx = 1 (the centre) are kept.  Taps are
+# ordered dz*9 + dy*3 + dx.
+X1_LAYER = "e0a"
+_OFF_CENTRE_X = [t for t in range(27) if t % 3 != 1]
+
+
 def _bf(shape, dev):
     return torch.empty(shape, dtype=torch.bfloat16, device=dev)
 
@@ -71,6 +81,8 @@ class UNet3D:
             w = torch.randn((27, ci, co), generator=g) * std
             if name == "head":
                 w[:, :, 1:] = 0
+            if name == X1_LAYER:   # a 3x3x1 convolution: only the taps at the centre x offset
+                w[_OFF_CENTRE_X] = 0
             b = torch.zeros(co)
             self.p[name] = {"w": w.to(self.dev), "b": b.to(self.dev), "ci": ci, "co": co, "relu": relu}
         self.adam_t = 0
@@ -112,6 +124,9 @@ class UNet3D:
         y = out if out is not None else _bf(tuple(x.shape[:4]) + (co,), self.dev)
         if relu is None:
             relu = q["relu"] and not flip       # a data gradient is linear
+        if name == X1_LAYER and not flip and mask is None:
+            _flf.conv3d_x1(x, q["wb"], q["b"], y, relu=relu, stream=torch.cuda.current_stream(self.dev).cuda_stream)
+            return y
         # split-K layers (few output tiles: the coarse levels) write one slice per split
         need = y.numel() * (4 if y.numel() < (1 << 23) else 1)
         if self._ws is None or self._ws.numel() < need:
@@ -226,6 +241,8 @@ class UNet3D:
         for name, q in self.p.items():
             if name == "head":
                 q["gw"][:, :, 1:] = 0
+            if name == X1_LAYER:
+                q["gw"][_OFF_CENTRE_X] = 0
             _flf.adam(q["w"], q["gw"], q["mw"], q["vw"], q["wb"], lr, b1, b2, eps, c1, c2, wd, s)
             _flf.adam(q["b"], q["gb"], q["mb"], q["vb"], None, lr, b1, b2, eps, c1, c2, 0.0, s)
             self._derive(q, s)

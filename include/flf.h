@@ -307,6 +307,14 @@ int flf_conv3d_wgrad(const void *x, const void *dy, float *dw, int B, int Z, int
  * tcgen05 for all of them.  Returns the previous setting. */
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream);
+/* flf_conv3d_x1: the 3x3x1 convolution (the 9 taps (dz, dy) at the centre x
+ * offset, tap index dx = 1) of a 16 -> 16 channel layer whose input carries
+ * the x neighbours as channels (the warm start's first layer): y = act(conv +
+ * bias).  The taps with dx != 1 of w [27][16][16] are ignored by the tcgen05
+ * kernel and must be zero for the mma.sync kernel (flf_net_conv16_tcgen05(0)),
+ * which computes the full 3x3x3 sum. */
+int flf_conv3d_x1(const void *x, const void *w, const float *bias, void *y, int B, int Z, int Y, int X, int relu,
+                  void *stream);
 int flf_net_status(void);
 int flf_net_conv16_tcgen05(int mode);
 /* Number of kernel launches the network entry points above have made since
@@ -333,9 +341,11 @@ int flf_render_blobs(float *vol, int Z, int Y, int X, const float *pts, int npts
                      void *stream);
 /* Warm-start inference glue.  flf_ws_input: network input [T][Zp][Yp][Xp][16]
  * bf16 from Htf [Z][T][Y][X] float and the sensitivity maps HtH1, Ht1
- * [Z][Y][X]: channel 0 = Htf / HtH1 / m_t (m_t = frame mean of Htf / HtH1,
- * whose sums are left in sum_x1 [T]), 1 = Htf / Ht1 / m_t, 2 = HtH1 * c2,
- * 3 = Ht1 * c3, others and the padding 0.  flf_ws_head: the start volume
+ * [Z][Y][X]: with the features f0 = Htf / HtH1 / m_t (m_t = frame mean of
+ * Htf / HtH1, whose sums are left in sum_x1 [T]), f1 = Htf / Ht1 / m_t,
+ * f2 = HtH1 * c2, f3 = Ht1 * c3, channel 4k + j (k = 0..2) holds f_j at
+ * x + k - 1 (the x neighbours as channels, for the 3x3x1 first layer
+ * flf_conv3d_x1), channels 12..15 and the padding 0.  flf_ws_head: the start volume
  * x0 [Z][T][Y][X] = max(conv3x3x3(d, w)[0] + bias, floor) * m_t from the last
  * features d [T][Zp][Yp][Xp][16] and the head's BF16 weights w [27][16][16]
  * (output channel 0 is used). */

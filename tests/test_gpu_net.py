@@ -390,3 +390,29 @@ def test_conv3d_tcgen05_inference_level1_shape(env, ci, co):
     err = (out[2] - out[0]).abs()
     lim = 1e-2 * out[0].abs() + 1e-3 * float(out[0].abs().max())
     assert bool((err <= lim).all()), (float(err.max()), int((err > lim).sum()))
+
+
+@pytest.mark.parametrize("shape", [(1, 4, 6, 130), (2, 3, 9, 20), (1, 24, 40, 456)])
+@pytest.mark.parametrize("mode", [0, 2])
+def test_conv3d_x1(env, shape, mode):
+    """flf_conv3d_x1 (the first layer: a 3x3x1 convolution over the taps dx = 1) against
+    float64 conv3d with the other taps zero; the tcgen05 kernel ignores them, the
+    mma.sync kernel computes the full sum."""
+    torch, _flf = env
+    g = torch.Generator().manual_seed(sum(shape))
+    x = torch.randn(shape + (16,), generator=g).bfloat16()
+    w = (torch.randn((27, 16, 16), generator=g) / 12).bfloat16()
+    off = [t for t in range(27) if t % 3 != 1]
+    w0 = w.clone()
+    w0[off] = 0
+    b = torch.randn(16, generator=g).float()
+    ref = _ref_conv(torch, x.double(), w0.double(), b.double()).clamp_min(0)
+    y = torch.empty(shape + (16,), dtype=torch.bfloat16, device="cuda")
+    old = _flf.conv16_tcgen05(mode)
+    try:
+        _flf.conv3d_x1(x.cuda(), (w if mode else w0).cuda(), b.cuda(), y, relu=True)
+    finally:
+        _flf.conv16_tcgen05(old)
+    _close(torch, y, ref)
+    torch.cuda.synchronize()
+    _flf.net_status()

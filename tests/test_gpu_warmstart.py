@@ -246,11 +246,14 @@ def _input_and_head(torch, _flf):
     x1 = htf / hth1
     m = x1.reshape(Z, T, -1).mean(dim=(0, 2))
     assert float((sums / (Z * Y * X) - m).abs().max()) <= 1e-5 * float(m.abs().max())
+    feat = torch.zeros((T, Zp, Yp, Xp + 2, 4), device="cuda")   # the features, one zero column each side
+    feat[:, :Z, :Y, 1:X + 1, 0] = (x1 / m[None, :, None, None]).permute(1, 0, 2, 3)
+    feat[:, :Z, :Y, 1:X + 1, 1] = (htf / ht1 / m[None, :, None, None]).permute(1, 0, 2, 3)
+    feat[:, :Z, :Y, 1:X + 1, 2] = (hth1 * c2).expand(Z, T, Y, X).permute(1, 0, 2, 3)
+    feat[:, :Z, :Y, 1:X + 1, 3] = (ht1 * c3).expand(Z, T, Y, X).permute(1, 0, 2, 3)
     ref = torch.zeros((T, Zp, Yp, Xp, 16), device="cuda")
-    ref[:, :Z, :Y, :X, 0] = (x1 / m[None, :, None, None]).permute(1, 0, 2, 3)
-    ref[:, :Z, :Y, :X, 1] = (htf / ht1 / m[None, :, None, None]).permute(1, 0, 2, 3)
-    ref[:, :Z, :Y, :X, 2] = (hth1 * c2).permute(1, 0, 2, 3)
-    ref[:, :Z, :Y, :X, 3] = (ht1 * c3).permute(1, 0, 2, 3)
+    for k in range(3):   # channel 4k + j holds feature j at x + k - 1
+        ref[..., 4 * k:4 * k + 4] = feat[:, :, :, k:k + Xp]
     assert float((out.float() - ref).abs().max()) <= 1e-2 * float(ref.abs().max())
     d = torch.rand((T, Zp, Yp, Xp, 16), generator=g).bfloat16().cuda()
     wfull = torch.zeros((27, 16, 16))
