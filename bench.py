@@ -1150,7 +1150,7 @@ def run_warmstart(args):
             "config": {"workload": wl["label"], "image": [Y, X], "planes": Z, "nnum": N, "frames": 1,
                        "psf": psf_desc, "beads": wl["beads"], "filaments": wl.get("filaments", 0),
                        "train_steps": args.train_steps, "train_s": round(train_s, 1), "psf_s": round(psf_s, 1),
-                       "conv_kernels": "tcgen05 for the 16/32-channel layers, mma.sync for 64/128 channels",
+                       "conv_kernels": "tcgen05 for every layer, in training and inference",
                        "target_iters": args.target_iters, "residual_finetune_steps": args.tune_steps,
                        "residual_finetune_loss_first_last": ([ws.tune_losses[0][1], ws.tune_losses[-1][1]]
                                                              if ws.tune_losses else None),

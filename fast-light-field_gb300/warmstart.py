@@ -369,21 +369,30 @@ class WarmStart:
         return x
 
     def train(self, steps=1500, batch=4, crop=128, volumes_per_refresh=8, refresh_every=8, lr=1e-3, seed=1,
-              target_iters=32, log_every=0, kernels=None):
+              target_iters=32, log_every=0, kernels=None, warmup=None):
         """Train on crops of freshly generated synthetic volumes; returns seconds taken.
+
+        The learning rate rises linearly over the first ``warmup`` steps (default
+        steps / 16) and then follows a cosine from ``lr`` to zero over all
+        ``steps``.  Without the ramp, Adam's first full-size steps drive the loss
+        up by two orders of magnitude and leave most ReLUs dead, on a plateau of
+        about the target's variance.
 
         kernels selects the 16 / 32-channel convolution kernels used while training
         (forward and data gradients; a mode of _flf.conv16_tcgen05), None keeps the
         library's current choice."""
+        if warmup is None:
+            warmup = steps // 16
         old = _flf.conv16_tcgen05(kernels) if kernels is not None else None
         try:
             return self._train(steps, batch, crop, volumes_per_refresh, refresh_every, lr, seed, target_iters,
-                               log_every)
+                               log_every, warmup)
         finally:
             if old is not None:
                 _flf.conv16_tcgen05(old)
 
-    def _train(self, steps, batch, crop, volumes_per_refresh, refresh_every, lr, seed, target_iters, log_every):
+    def _train(self, steps, batch, crop, volumes_per_refresh, refresh_every, lr, seed, target_iters, log_every,
+               warmup):
         rng = np.random.default_rng(seed)
         t0 = time.time()
         cy, cx = min(crop, self.pad[1]), min(crop, self.pad[2])
@@ -408,7 +417,8 @@ class WarmStart:
             _flf.mse_grad(out, tb, dout, loss, self._s())
             self.net.backward(cache, dout)
             frac = step / max(steps - 1, 1)
-            self.net.adam_step(lr * 0.5 * (1 + np.cos(np.pi * frac)))
+            ramp = min(1.0, (step + 1) / warmup) if warmup > 0 else 1.0
+            self.net.adam_step(lr * ramp * 0.5 * (1 + np.cos(np.pi * frac)))
             if log_every and (step % log_every == 0 or step == steps - 1):
                 self.losses.append((step, float(loss)))
         torch.cuda.synchronize(self.dev)
