@@ -746,6 +746,16 @@ __device__ __forceinline__ void net_expect_tx(uint32_t bar, uint32_t bytes) {
 __device__ __forceinline__ void net_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
+// non-blocking test of a phase (1 = the phase with this parity has completed)
+__device__ __forceinline__ uint32_t mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok;
+}
 __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
                                             int c4, uint32_t bar) {
   asm volatile(
@@ -946,14 +956,25 @@ __global__ void __launch_bounds__(352, 1)
       constexpr uint32_t VOX = SW32 ? 2 : 1;   // one voxel in 16-byte units
       uint32_t n = 0;   // slabs consumed (= accumulator slots written)
       bool ok = true;
+      uint32_t pre_full = 0, pre_empty = 0;   // the next slab's barriers, tested ahead
       for (long long it = blockIdx.x; it < g.items && ok; it += gridDim.x) {
         int b, zlo, nz, y0, x0;
         decode(it, b, zlo, nz, y0, x0);
         for (int k = 0; k < nz + 2; k++, n++) {
           const uint32_t acc = n % NACC;
-          ok = role_wait(full(n % S), (n / S) & 1, abort_s, 5) &&
-               (n < NACC || role_wait(tempty(acc), ((n / NACC) - 1) & 1, abort_s, 6));
+          ok = (pre_full & pre_empty) ||
+               (role_wait(full(n % S), (n / S) & 1, abort_s, 5) &&
+                (n < NACC || role_wait(tempty(acc), ((n / NACC) - 1) & 1, abort_s, 6)));
           if (!ok) break;
+          {
+            // test slab n+1's barriers now, without blocking: the results are read at the next slab,
+            // so their latency overlaps this slab's MMAs (a blocking wait follows only if a phase
+            // was not yet complete).  A phase seen complete stays complete until this thread's own
+            // commits let the slot be refilled.
+            const uint32_t n1 = n + 1;
+            pre_full = mbar_test(full(n1 % S), (n1 / S) & 1);
+            pre_empty = n1 < NACC ? 1u : mbar_test(tempty(n1 % NACC), ((n1 / NACC) - 1) & 1);
+          }
           const int zin = zlo - 1 + k;
           if (zin >= 0 && zin < p.Z) {
             tc_fence_after();
