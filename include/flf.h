@@ -107,8 +107,8 @@ int flf_backward(flf_ctx *ctx, const float *img_dev, float *vol_dev, int T, int 
  *  - The intermediate spectra and channel images live in one fixed device
  *    array of FLF_NOALLOC_SCRATCH_BYTES (16 MiB) inside the library: one
  *    frame's channel images and spectra plus the output spectra and channel
- *    images of as many planes as fit.  Every GPU that loads the library holds
- *    this array until the process exits.  Geometries that need more
+ *    images of as many planes as fit.  A GPU holds this array from the first
+ *    flf_ctx_create on it until the process exits.  Geometries that need more
  *    (2 * (Nnum^2 * f * (f/2+1) * 8 + Nnum^2 * Ly * Lxp * 4) bytes, Lxp =
  *    ceil(X/Nnum) rounded up to 4; e.g. the 1005 x 1005 full field) are
  *    rejected with FLF_E_ARG; use flf_backward.
