@@ -66,6 +66,7 @@ _SIGS = {
     "flf_conv3d_x1": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_net_status": (_I, []),
     "flf_net_conv16_tcgen05": (_I, [_I]),
+    "flf_conv3d_pool": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "flf_conv3d_flip": (_I, [_P, _P, _I, _I, _P]),
     "flf_conv3d_pack": (_I, [_P, _P, _I, _I, _P]),
     "flf_bias_grad": (_I, [_P, _P, ctypes.c_longlong, _I, _P, ctypes.c_longlong, _P]),
@@ -205,6 +206,18 @@ def conv3d_x1(x, w, bias, y, relu=False, stream=None):
     lib = load_library()
     B, Z, Y, X, _ = _vshape(x)
     _check_global(lib.flf_conv3d_x1(_ptr(x), _ptr(w), _ptr(bias), _ptr(y), B, Z, Y, X, int(bool(relu)), _ptr(stream)))
+
+
+def conv3d_pool(x, w, bias, y, pooled, relu=False, stream=None):
+    """y = [relu](conv3d(x, w) + bias) for 16 -> 16 channels and pooled = pool2(y)
+    (2x2x2 average, [B, Z/2, Y/2, X/2, 16]) from the same launch; x, y [B, Z, Y, X, 16]
+    bf16 with Z, Y, X even."""
+    lib = load_library()
+    B, Z, Y, X, _ = _vshape(x)
+    if tuple(pooled.shape) != (B, Z // 2, Y // 2, X // 2, 16):
+        raise FlfError(-1, "pooled must be [B, Z/2, Y/2, X/2, 16], got %s" % (tuple(pooled.shape),))
+    _check_global(lib.flf_conv3d_pool(_ptr(x), _ptr(w), _ptr(bias), _ptr(y), _ptr(pooled), B, Z, Y, X,
+                                      int(bool(relu)), _ptr(stream)))
 
 
 def conv_wide_tcgen05(mode):

@@ -1883,6 +1883,20 @@ int flf_conv3d_x1(const void *x, const void *w, const float *bias, void *y, int 
   return FLF_OK;
 }
 
+int flf_conv3d_pool(const void *x, const void *w, const float *bias, void *y, void *pooled, int B, int Z, int Y,
+                    int X, int relu, void *stream) {
+  if (!x || !w || !y || !pooled) return fail(nullptr, FLF_E_ARG, "NULL array pointer");
+  if (int rc = net_shape(B, Z, Y, X, 16)) return rc;
+  if ((Z | Y | X) & 1) return fail(nullptr, FLF_E_ARG, "Z, Y and X must be even (%d x %d x %d)", Z, Y, X);
+  if (!aligned16(x) || !aligned16(y) || !aligned16(pooled))
+    return fail(nullptr, FLF_E_ARG, "volumes must be 16-byte aligned");
+  ConvParams p{(const __nv_bfloat16 *)x, (const __nv_bfloat16 *)w, bias, nullptr, (__nv_bfloat16 *)y, B, Z, Y, X, 16, 16,
+               relu ? 1 : 0, nullptr, 1};
+  p.pool = (__nv_bfloat16 *)pooled;
+  NET_CHECK(launch_conv3d_pool(p, (cudaStream_t)stream));
+  return FLF_OK;
+}
+
 int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *mask, void *y, int B, int Z, int Y,
                   int X, int relu, int rows, void *stream) {
   if (!x || !w || !y) return fail(nullptr, FLF_E_ARG, "NULL array pointer");

@@ -293,6 +293,8 @@ struct ConvParams {          // y = act(conv3x3x3(x, w) + bias) (* (mask > 0))
   const __nv_bfloat16 *wp;   // or null: the same weights packed by k_conv3d_pack_weights (per tap
                              // and 16 input channels one [2][Co][8] block), what the tcgen05
                              // kernel of the wide layers reads
+  __nv_bfloat16 *pool = nullptr;   // or [B][Z/2][Y/2][X/2][Co]: y's 2x2x2 average pooling as well
+                                   // (launch_conv3d_pool)
 };
 struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co]
   const __nv_bfloat16 *x;
@@ -303,6 +305,7 @@ struct WgradParams {         // dw[tap][ci][co] += sum_v x[v + tap][ci] dy[v][co
   float *part;               // [chunks][27][Ci][Co] partial gradients, reduced in chunk order (or null)
 };
 cudaError_t launch_conv3d(ConvParams p, long long ws_elems, cudaStream_t s);
+cudaError_t launch_conv3d_pool(const ConvParams &p, cudaStream_t s);
 cudaError_t launch_conv3d_x1(const ConvParams &p, cudaStream_t s);
 long long net_launches();
 int net_set_conv_wide_tcgen05(int mode);

@@ -817,7 +817,7 @@ __device__ __forceinline__ void head_rows(float (&o)[RH], const float (&v)[RH + 
     for (int dy = 0; dy < 3; dy++) o[r] += in ? v[r + dy][DZ * 3 + dy] : 0.f;
 }
 
-template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false, bool POOL = false>
 __global__ void __launch_bounds__(352, 1)
     k_conv3d_tma16(const __grid_constant__ CUtensorMap tx, ConvParams p, HeadOut h, Tma16Grid g) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -830,6 +830,8 @@ __global__ void __launch_bounds__(352, 1)
   // dx != 1 of w are ignored: the first layer, whose input carries the x neighbours as channels)
   constexpr int NBLK = (HEAD || X1) ? 3 : 9;
   static_assert(!(HEAD && X1), "the head is a full 3x3x3 convolution");
+  static_assert(!POOL || (CO == 16 && R == 2 && !HEAD && !X1),
+                "the pooled output is for 16 output channels and two rows per item");
   constexpr int NISS = (HEAD ? PYH : R) % 2 == 0 ? 2 : 1;   // MMA-issuing threads (warps 1 .. NISS)
   constexpr int CH = CO / 2;                  // output channels per epilogue warp
   static_assert((CI == 16 || CI == 32) && (CO == 16 || CO == 32), "16 or 32 channels in and out");
@@ -1018,6 +1020,7 @@ __global__ void __launch_bounds__(352, 1)
       int b, zlo, nz, y0, x0;
       decode(it, b, zlo, nz, y0, x0);
       const int x = x0 + qd * 32 + lane;
+      float pacc[POOL ? CH : 1];   // POOL: the 2x2x2 average of the output, summed over a plane pair
       for (int i = 0; i < nz; i++) {
         // output plane z = zlo + i reads slabs n+i (dz 0), n+i+1 (dz 1), n+i+2 (dz 2); each issuer's
         // commits complete in order, so slab n+i+2's barrier covers the other two
@@ -1077,6 +1080,11 @@ __global__ void __launch_bounds__(352, 1)
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
           tc_fence_before();
           net_arrive(tempty((n + i) % NACC));   // slab n+i has no later reader
+          uint4 kept[POOL ? R : 1];   // POOL: the BF16 outputs of this lane's rows
+          if constexpr (POOL) {
+#pragma unroll
+            for (int r = 0; r < R; r++) kept[r] = make_uint4(0u, 0u, 0u, 0u);
+          }
 #pragma unroll
           for (int r = 0; r < R; r++) {
             const int y = y0 + r;
@@ -1109,6 +1117,45 @@ __global__ void __launch_bounds__(352, 1)
                 hv[k] = __floats2bfloat162_rn(v0, v1);
               }
               *reinterpret_cast<uint4 *>(p.y + off + v * 8) = outv;
+              if constexpr (POOL) kept[r] = outv;
+            }
+          }
+          if constexpr (POOL) {
+            // k_pool2's sum in its order: (y0, x), (y0, x+1), (y0+1, x), (y0+1, x+1) of plane 2zp,
+            // then of plane 2zp+1, times 1/8; x+1 comes from the next lane (x0 and the item's first
+            // plane are even, so lane pairs and plane pairs are pooling pairs)
+            float pv[R][CH], nb[R][CH];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              const __nv_bfloat162 *k2 = reinterpret_cast<const __nv_bfloat162 *>(&kept[r]);
+#pragma unroll
+              for (int c = 0; c < CH / 2; c++) {
+                const float2 f = __bfloat1622float2(k2[c]);
+                pv[r][2 * c] = f.x;
+                pv[r][2 * c + 1] = f.y;
+              }
+#pragma unroll
+              for (int c = 0; c < CH; c++) nb[r][c] = __shfl_down_sync(0xffffffffu, pv[r][c], 1);
+            }
+            if ((i & 1) == 0) {
+#pragma unroll
+              for (int c = 0; c < CH; c++) pacc[c] = 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < CH; c++) {
+              pacc[c] += pv[0][c];
+              pacc[c] += nb[0][c];
+              pacc[c] += pv[1][c];
+              pacc[c] += nb[1][c];
+            }
+            if ((i & 1) && !(lane & 1) && x < p.X && y0 < p.Y) {
+              uint4 pw;
+              __nv_bfloat162 *h2 = reinterpret_cast<__nv_bfloat162 *>(&pw);
+#pragma unroll
+              for (int c = 0; c < CH / 2; c++) h2[c] = __floats2bfloat162_rn(pacc[2 * c] * 0.125f, pacc[2 * c + 1] * 0.125f);
+              const long long po =
+                  ((((long long)b * (p.Z / 2) + (z >> 1)) * (p.Y / 2) + (y0 >> 1)) * (p.X / 2) + (x >> 1)) * CO + hf * CH;
+              *reinterpret_cast<uint4 *>(p.pool + po) = pw;
             }
           }
         }
@@ -1658,7 +1705,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false>
+template <int CI, int CO, int R, int S, bool HEAD, bool SW32, bool X1 = false, bool POOL = false>
 static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStream_t s) {
   constexpr int KS = CI / 16;
   constexpr size_t SLOT = SW32 ? KS * (((R + 2) * 136 * 32 + 1023) / 1024 * 1024)
@@ -1668,7 +1715,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
   static int sms = 0;
   if (!sms) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1>,
+    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1, POOL>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, n = 0;
@@ -1700,7 +1747,8 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   long long best = -1;
   int zc_best = p.Z;
   for (int c = 1; c <= 8 && c <= p.Z; c++) {
-    const int zc = (p.Z + c - 1) / c;
+    int zc = (p.Z + c - 1) / c;
+    if (POOL) zc += zc & 1;   // plane pairs stay in one item
     const long long items = (long long)p.B * ((p.Z + zc - 1) / zc) * g.yblocks * g.xsegs;
     const long long cost = (items + sms - 1) / sms * (zc + 2);
     if (best < 0 || cost < best) {
@@ -1712,7 +1760,7 @@ static cudaError_t launch_tma16(const ConvParams &p, const HeadOut &h, cudaStrea
   g.zchunks = (p.Z + g.zc - 1) / g.zc;
   g.items = (long long)p.B * g.zchunks * g.yblocks * g.xsegs;
   const unsigned grid = (unsigned)(g.items < sms ? g.items : sms);
-  FLF_NET_LAUNCH(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1><<<grid, 352, SMEM, s>>>(map, p, h, g));
+  FLF_NET_LAUNCH(k_conv3d_tma16<CI, CO, R, S, HEAD, SW32, X1, POOL><<<grid, 352, SMEM, s>>>(map, p, h, g));
   return cudaGetLastError();
 }
 
@@ -2227,6 +2275,16 @@ int net_set_conv16_tcgen05(int mode) {
 cudaError_t launch_conv3d_x1(const ConvParams &p, cudaStream_t s) {
   if (p.Ci != 16 || p.Co != 16) return cudaErrorInvalidValue;
   return g_conv16_tc ? launch_tma16<16, 16, 2, 8, false, true, true>(p, HeadOut{}, s) : launch_t16<false>(p, HeadOut{}, s);
+}
+
+// 16 -> 16 channels with the output's 2x2x2 average pooling written as well (p.pool): the pooled
+// values come from the epilogue of the tcgen05 kernel, or from k_pool2 after the mma.sync kernel
+cudaError_t launch_conv3d_pool(const ConvParams &p, cudaStream_t s) {
+  if (p.Ci != 16 || p.Co != 16 || !p.pool || ((p.Z | p.Y | p.X) & 1)) return cudaErrorInvalidValue;
+  if (g_conv16_tc) return launch_tma16<16, 16, 2, 8, false, true, false, true>(p, HeadOut{}, s);
+  const cudaError_t e = launch_t16<false>(p, HeadOut{}, s);
+  if (e != cudaSuccess) return e;
+  return launch_pool2(p.y, p.pool, p.B, p.Z, p.Y, p.X, 16, s);
 }
 
 cudaError_t launch_conv3d_tma16(const ConvParams &p, cudaStream_t s, bool sw32) {

@@ -142,6 +142,16 @@ class UNet3D:
         _flf.pool2(x, y, torch.cuda.current_stream(self.dev).cuda_stream)
         return y
 
+    def _conv_pool(self, name, x):
+        """A 16 -> 16 layer and the 2x2x2 average pooling of its output, one launch."""
+        q = self.p[name]
+        B, Z, Y, X, _ = x.shape
+        y = _bf((B, Z, Y, X, q["co"]), self.dev)
+        pooled = _bf((B, Z // 2, Y // 2, X // 2, q["co"]), self.dev)
+        _flf.conv3d_pool(x, q["wb"], q["b"], y, pooled, relu=q["relu"],
+                         stream=torch.cuda.current_stream(self.dev).cuda_stream)
+        return y, pooled
+
     def _up_add(self, low, skip):
         y = _bf(tuple(skip.shape[:4]) + (low.shape[4],), self.dev)
         _flf.up2_add(low, skip, y, torch.cuda.current_stream(self.dev).cuda_stream)
@@ -152,8 +162,7 @@ class UNet3D:
         with head=False the last features d0 come back in place of out."""
         a = {"x": x}
         a["e0a"] = self._conv("e0a", x)
-        a["e0b"] = self._conv("e0b", a["e0a"])
-        a["p1"] = self._pool(a["e0b"])
+        a["e0b"], a["p1"] = self._conv_pool("e0b", a["e0a"])
         a["e1a"] = self._conv("e1a", a["p1"])
         a["e1b"] = self._conv("e1b", a["e1a"])
         a["p2"] = self._pool(a["e1b"])

@@ -315,6 +315,13 @@ int flf_conv3d_tc(const void *x, const void *w, const float *bias, const void *m
  * which computes the full 3x3x3 sum. */
 int flf_conv3d_x1(const void *x, const void *w, const float *bias, void *y, int B, int Z, int Y, int X, int relu,
                   void *stream);
+/* flf_conv3d_pool: y = act(conv3x3x3(x, w) + bias) for 16 -> 16 channels and
+ * pooled [B][Z/2][Y/2][X/2][16] = the 2x2x2 average pooling of y (flf_pool2 of
+ * y, the same bits), written from the convolution's epilogue on the tcgen05
+ * kernel (the encoder's last full-resolution layer and its pooling).  Z, Y, X
+ * even. */
+int flf_conv3d_pool(const void *x, const void *w, const float *bias, void *y, void *pooled, int B, int Z, int Y,
+                    int X, int relu, void *stream);
 int flf_net_status(void);
 int flf_net_conv16_tcgen05(int mode);
 /* Number of kernel launches the network entry points above have made since

@@ -392,6 +392,38 @@ def test_conv3d_tcgen05_inference_level1_shape(env, ci, co):
     assert bool((err <= lim).all()), (float(err.max()), int((err > lim).sum()))
 
 
+@pytest.mark.parametrize("shape", [(2, 4, 6, 10), (1, 2, 2, 2), (1, 6, 8, 140), (1, 10, 12, 258), (4, 24, 128, 128),
+                                   (1, 14, 40, 456)])
+@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("relu", [False, True])
+def test_conv3d_pool(env, shape, mode, relu):
+    """flf_conv3d_pool (the convolution with the 2x2x2 average pooling of its output
+    summed in the epilogue) gives the same bits as flf_conv3d followed by flf_pool2, for
+    one to several plane pairs per item, ragged x segments and the training crops."""
+    torch, _flf = env
+    B, Z, Y, X = shape
+    g = torch.Generator(device="cuda").manual_seed(B + 3 * Z + Y + X)
+    x = torch.randn(shape + (16,), generator=g, device="cuda").bfloat16()
+    w = (torch.randn((27, 16, 16), generator=g, device="cuda") / 12).bfloat16()
+    b = torch.randn(16, generator=g, device="cuda")
+    old = _flf.conv16_tcgen05(mode)
+    try:
+        ref = torch.full_like(x, float("nan"))
+        _flf.conv3d(x, w, b, ref, relu=relu)
+        pref = torch.full((B, Z // 2, Y // 2, X // 2, 16), float("nan"), dtype=torch.bfloat16, device="cuda")
+        _flf.pool2(ref, pref)
+        y = torch.full_like(x, float("nan"))
+        pooled = torch.full_like(pref, float("nan"))
+        _flf.conv3d_pool(x, w, b, y, pooled, relu=relu)
+        torch.cuda.synchronize()
+        _flf.net_status()
+    finally:
+        _flf.conv16_tcgen05(old)
+    assert bool(torch.isfinite(pref).all())
+    assert torch.equal(y, ref)
+    assert torch.equal(pooled, pref)
+
+
 @pytest.mark.parametrize("shape", [(1, 4, 6, 130), (2, 3, 9, 20), (1, 24, 40, 456)])
 @pytest.mark.parametrize("mode", [0, 2])
 def test_conv3d_x1(env, shape, mode):
