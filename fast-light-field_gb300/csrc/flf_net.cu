@@ -17,7 +17,10 @@
 //   k_conv3d_tma16    16 / 32 -> 16 / 32 channels on tcgen05 (the default for
 //                     these layers): warp-specialised producer / MMA /
 //                     epilogue roles, TMA-staged input slabs, the z taps
-//                     folded into N and summed from a TMEM accumulator ring.
+//                     folded into N and summed from a TMEM accumulator ring;
+//                     variants: the 3x3x1 first layer (X1), the folded head
+//                     (HEAD) and the output's 2x2x2 pooling from the epilogue
+//                     (POOL).
 //   k_conv3d_tc16     the first single-role tcgen05 16 -> 16 kernel.
 //   k_conv3d_wide     32..128 -> 32..128 channels (a side of 64 or more) on
 //                     tcgen05: padded-row implicit GEMM over TMA-staged input
@@ -722,11 +725,17 @@ __global__ void __launch_bounds__(128) k_conv3d_tc16(ConvParams p, int tiles_x, 
 //   warp 0     producer: one thread issues the TMA loads;
 //   warps 1-2  MMA issuers: one thread each issues the 9 MMAs of half of the
 //              rows per slab, then commits to the slab's accumulator barrier
-//              and to its shared-memory slot;
+//              and to its shared-memory slot; before a slab's MMAs it tests
+//              the next slab's barriers without blocking, so that test's
+//              latency overlaps the MMAs (a blocking wait follows only if a
+//              phase was not complete yet);
 //   warps 3-10 epilogue: warp w reads TMEM lane quarter w % 4 (tcgen05.ld)
 //              for 8 of the 16 output channels, sums the three z terms, then
 //              bias / ReLU / mask and BF16 stores, or with HEAD the clamped,
-//              scaled start volume from output channel 0.
+//              scaled start volume from output channel 0.  With POOL it also
+//              writes the 2x2x2 average of the stored outputs (x pairs from
+//              neighbouring lanes, row pairs of the item, plane pairs of
+//              consecutive planes; z chunks of even length).
 // Every mbarrier wait is bounded (1 s).  A wait that gives up sets g_net_err
 // and a shared abort flag that every role polls; the CTA then waits (bounded)
 // for its copies and MMAs in flight before TMEM is released.
