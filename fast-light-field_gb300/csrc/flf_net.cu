@@ -28,7 +28,9 @@
 //                     CTAs with two TMEM accumulator buffers.
 //   k_conv3d_wgrad    weight gradient dW[tap][ci][co] = sum_v x[v+tap][ci]
 //                     dy[v][co]: per (voxel chunk, tap, channel tile) one CTA,
-//                     split-K over its 4 warps, FP32 atomics into dW.
+//                     split-K over its 4 warps; each chunk writes a partial
+//                     sum and k_wgrad_reduce adds them in chunk order (no
+//                     atomics, so training repeats bit for bit).
 //   small kernels     bias gradient, 2x2x2 average pooling and its adjoint,
 //                     nearest 2x2x2 upsampling + skip and its adjoint with the
 //                     ReLU mask, MSE loss gradient, Adam, bead rendering.
