@@ -62,6 +62,14 @@ X1_LAYER = "e0a"
 _OFF_CENTRE_X = [t for t in range(27) if t % 3 != 1]
 
 
+def learning_rate(step, steps, lr, warmup):
+    """Training schedule: a linear ramp over the first ``warmup`` steps times a cosine
+    from ``lr`` at step 0 to zero at the last of ``steps`` steps."""
+    frac = step / max(steps - 1, 1)
+    ramp = min(1.0, (step + 1) / warmup) if warmup > 0 else 1.0
+    return lr * ramp * 0.5 * (1 + np.cos(np.pi * frac))
+
+
 def _bf(shape, dev):
     return torch.empty(shape, dtype=torch.bfloat16, device=dev)
 
@@ -425,9 +433,7 @@ class WarmStart:
             loss = torch.zeros(1, device=self.dev)
             _flf.mse_grad(out, tb, dout, loss, self._s())
             self.net.backward(cache, dout)
-            frac = step / max(steps - 1, 1)
-            ramp = min(1.0, (step + 1) / warmup) if warmup > 0 else 1.0
-            self.net.adam_step(lr * ramp * 0.5 * (1 + np.cos(np.pi * frac)))
+            self.net.adam_step(learning_rate(step, steps, lr, warmup))
             if log_every and (step % log_every == 0 or step == steps - 1):
                 self.losses.append((step, float(loss)))
         torch.cuda.synchronize(self.dev)

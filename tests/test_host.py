@@ -213,3 +213,17 @@ def test_frame_sharded_rl_two_gloo_ranks(tmp_path):
     sharded = np.load(out)
     assert sharded.shape == single.shape
     assert rel(sharded, single) < 1e-6
+
+
+def test_warm_start_learning_rate_schedule():
+    """The warm start's training schedule: linear ramp, then the cosine to zero."""
+    import warmstart
+    lr = warmstart.learning_rate
+    assert lr(0, 1600, 1e-3, 100) == pytest.approx(1e-5 * 0.5 * (1 + np.cos(0.0)))
+    assert lr(49, 1600, 1e-3, 100) == pytest.approx(0.5e-3 * 0.5 * (1 + np.cos(np.pi * 49 / 1599)))
+    assert lr(99, 1600, 1e-3, 100) == pytest.approx(1e-3 * 0.5 * (1 + np.cos(np.pi * 99 / 1599)))
+    assert lr(1599, 1600, 1e-3, 100) == pytest.approx(0.0, abs=1e-15)
+    assert lr(0, 10, 2e-3, 0) == pytest.approx(2e-3)
+    assert lr(0, 1, 2e-3, 0) == pytest.approx(2e-3)      # a single step: no division by zero
+    rates = [lr(k, 1600, 1e-3, 100) for k in range(1600)]
+    assert max(rates) <= 1e-3 and int(np.argmax(rates)) == 99
